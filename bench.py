@@ -1,0 +1,327 @@
+"""Throughput of the fused D3Q27 cumulant + Smagorinsky LES step on GB300 (GLUPS, % of HBM roofline).
+
+Workload (default): turbulent channel 512x256x256, periodic x/z, bounce-back walls, body force for
+Re_tau ~ 180, laminar profile + 5 % seeded noise; FP16-deviation population storage with FP32
+collision is the headline `value`; the plain FP32-storage kernel on the same case is reported beside
+it.  One "step" is one lattice time step over all 33.5 M cells.  The state (1.8 GB FP16, 3.6 GB
+FP32) is far larger than the 129 MB L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs one independent replica per GPU (the path does not shard in this build); value is the
+sum over ranks of cell updates divided by the slowest rank's time.  --impl reference times the CPU
+restatement of the reference's pass structure (oracle/, FP32, all host threads) on the same case.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_CELL = {"f64": 27 * 8 * 2 + 1, "f32": 27 * 4 * 2 + 1, "f16dev": 27 * 2 * 2 + 1}
+METRIC = "D3Q27 GLUPS, %HBM roofline: FP16-store+learned LES vs FP32 plain, equal error"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-cell DRAM bytes of the step kernels from the committed ncu summary (or None)."""
+    p = os.path.join(ROOT, "profiles", "step_kernel_traffic.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            return json.load(fh)
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return None, 0, 1, int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    import torch.distributed as dist
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend=backend)
+    return dist, dist.get_rank(), ws, local
+
+
+def dist_max(dist, x):
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_sum(dist, x):
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def channel_case(shape):
+    from lb_gb300 import cases
+    return cases.channel(*shape, re_tau=180.0, u_max=0.05, amp=0.05)
+
+
+def make_solver(shape, case, storage, device):
+    from lb_gb300.solver import CollisionCumD3Q27Turbulent2015, OmegaLES, Solver
+    s = Solver(shape, collision=CollisionCumD3Q27Turbulent2015, turbulence=OmegaLES, storage=storage,
+               nu=case["nu"], cles=0.17, periodic=case["periodic"], force=case["force"], device=device)
+    s.set_flags(case["flags"])
+    s.set_bc()
+    s.init_fields(case["rho"], case["u"])
+    return s
+
+
+def time_storage(shape, case, storage, steps, warmup, device, dist, with_clocks):
+    s = make_solver(shape, case, storage, device)
+    s.step(warmup)
+    s.synchronize()
+    barrier(dist)
+    sampler = ClockSampler(device) if with_clocks else None
+    if sampler:
+        sampler.__enter__()
+    ms = s.step_timed(steps)
+    if sampler:
+        sampler.__exit__()
+    barrier(dist)
+    d = s.reduce()
+    s.close()
+    return ms, d, (sampler.summary() if sampler else None)
+
+
+def e2e_run(shape, case, storage, steps, device):
+    """End to end through the public API with host buffers: upload flags + initial fields, then
+    every step lbm_step + the reference's per-step probe read-back (u, rho of one cell)."""
+    from lb_gb300.solver import CollisionCumD3Q27Turbulent2015, OmegaLES, Solver
+    s = Solver(shape, collision=CollisionCumD3Q27Turbulent2015, turbulence=OmegaLES, storage=storage,
+               nu=case["nu"], cles=0.17, periodic=case["periodic"], force=case["force"], device=device)
+    flags = np.ascontiguousarray(case["flags"], dtype=np.int32)
+    rho = np.ascontiguousarray(case["rho"], dtype=np.float64)
+    u = np.ascontiguousarray(case["u"], dtype=np.float64)
+    px, py, pz = shape[0] // 2, shape[1] // 2, shape[2] // 2
+    s.synchronize()
+    t0 = time.perf_counter()
+    s.set_flags(flags)
+    s.set_bc()
+    s.init_fields(rho, u)
+    for _ in range(steps):
+        s.step(1)
+        s.probe(px, py, pz)
+    s.synchronize()
+    dt = time.perf_counter() - t0
+    s.close()
+    h2d = flags.nbytes + rho.nbytes + u.nbytes
+    return dt, h2d, 32
+
+
+def cpu_reference(shape, case, steps, warmup, budget_s, threads=None):
+    """The oracle's reference-structured FP32 pipeline (separate omega, collision, A-B streaming,
+    boundary and moment passes) on the host cores; returns (seconds per step, steps timed, threads)."""
+    from lb_gb300 import capi
+    from oracle import oracle as O
+    if threads:
+        O.set_threads(threads)
+    nth = O.max_threads()
+    cfg = capi.make_config(*shape, periodic=case["periodic"], collision=capi.LBM_COLLISION_CUMULANT2015,
+                           closure=capi.LBM_CLOSURE_SMAGORINSKY, nu=case["nu"], cles=0.17, force=case["force"])
+    o = O.OracleSim(cfg, 32)
+    o.set_flags(case["flags"])
+    o.init_fields(case["rho"], case["u"])
+    for _ in range(warmup):
+        o.step(1)
+    t0 = time.perf_counter()
+    n = 0
+    while n < steps:
+        o.step(1)
+        n += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    o.close()
+    return dt / n, n, nth
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--shape", default="512,256,256")
+    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for the CPU arms")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    shape = tuple(int(v) for v in args.shape.split(","))
+    N = shape[0] * shape[1] * shape[2]
+    workload = f"turbulent channel {shape[0]}x{shape[1]}x{shape[2]}, D3Q27 cumulant-2015 + Smagorinsky (CLES 0.17), Re_tau 180"
+    dist, rank, ws, local = dist_setup()
+
+    if args.impl == "reference":
+        # the reference's own CPU path (restated, reference-structured passes) on the host cores
+        if rank != 0:
+            return
+        from oracle import build as obuild
+        obuild.build()
+        case = channel_case(shape)
+        sps, n, nth = cpu_reference(shape, case, args.steps, min(args.warmup, 1), budget_s=max(args.cpu_budget, 30.0))
+        glups = N / sps / 1e9
+        line = {"impl": "reference", "metric": METRIC, "value": glups, "unit": "GLUPS", "n_gpus": args.gpus,
+                "steps": n, "warmup": min(args.warmup, 1), "ms_per_step": sps * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": workload, "storage": "f32 (A-B, two population arrays)",
+                           "impl_detail": "CPU restatement of the reference's per-hook passes (oracle/), OpenMP"},
+                "cpu_baseline": {"value": glups, "unit": "GLUPS", "cores": nth, "kind": "port",
+                                 "sample": f"{n} steps of the full {shape[0]}x{shape[1]}x{shape[2]} lattice"},
+                "e2e": {"value": glups, "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    from lb_gb300 import build as lbuild
+    if rank == 0 or dist is None:
+        lbuild.build()
+    barrier(dist)
+    device = local
+    case = channel_case(shape)
+    hbm, peak_kind = peaks()
+    traffic = ncu_traffic()
+
+    ms16, d16, clk = time_storage(shape, case, "f16dev", args.steps, args.warmup, device, dist, rank == 0)
+    ms32, d32, _ = time_storage(shape, case, "f32", args.steps, args.warmup, device, dist, False)
+    ms16 = dist_max(dist, ms16)
+    ms32 = dist_max(dist, ms32)
+    cells = dist_sum(dist, float(N) * args.steps)
+    glups16 = cells / (ms16 * 1e-3) / 1e9
+    glups32 = cells / (ms32 * 1e-3) / 1e9
+
+    def roof(kind, ms):
+        per_launch = BYTES_PER_CELL[kind] * N
+        achieved = per_launch / (ms * 1e-3 / args.steps) / 1e9
+        t = traffic.get(kind)
+        return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "peak_kind": peak_kind, "traffic": (t["dram_bytes_per_cell"] * N) if t else None,
+                "algorithmic_bytes_per_launch": per_launch}
+
+    e2e = None
+    if not args.no_e2e:
+        k = min(args.steps, 200)
+        dt, h2d, d2h = e2e_run(shape, case, "f16dev", k, device)
+        dt = dist_max(dist, dt)
+        e2e = {"value": dist_sum(dist, float(N) * k) / dt / 1e9, "unit": "GLUPS",
+               "h2d_bytes_per_step": h2d / k, "d2h_bytes_per_step": d2h, "steps": k,
+               "includes": "lbm_set_flags + lbm_set_bc + lbm_init_fields from host buffers, then per step "
+                           "lbm_step + lbm_probe (device->host read of u, rho)"}
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        from oracle import build as obuild
+        obuild.build()
+        cshape = (256, 128, 128)
+        ccase = channel_case(cshape)
+        sps, n, nth = cpu_reference(cshape, ccase, 50, 1, budget_s=args.cpu_budget)
+        cpu = {"value": cshape[0] * cshape[1] * cshape[2] / sps / 1e9, "unit": "GLUPS", "cores": nth, "kind": "port",
+               "sample": f"{n} steps of the 256x128x128 channel, FP32, reference pass structure (oracle/)"}
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": glups16, "unit": "GLUPS", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms16 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload, "nx": shape[0], "ny": shape[1], "nz": shape[2],
+                       "storage": "f16dev (f - w rho0) * 2^10, FP32 collision", "closure": "smagorinsky",
+                       "learned_closure": "not in this measurement",
+                       "l2": "state 1.8 GB (f16) / 3.6 GB (f32) >> 129 MB L2; no flush needed",
+                       "parallelism": f"{ws} independent replica(s)"},
+            "roofline": roof("f16dev", ms16),
+            "fp32_plain": {"value": glups32, "ms_per_step": ms32 / args.steps, "roofline": roof("f32", ms32),
+                           "speedup_f16_over_f32": glups16 / glups32},
+            "gpu_launches": args.steps, "clocks": clk, "cpu_baseline": cpu, "e2e": e2e,
+            "check": {"f16_mass": d16.mass, "f32_mass": d32.mass, "nonfinite": d16.nonfinite + d32.nonfinite}}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,182 @@
+/*
+ * lbm.h - C ABI of the GB300 (sm_103a) D3Q27 lattice-Boltzmann solver core.
+ *
+ * Plain C types only: every buffer crossing this boundary is a host pointer plus
+ * sizes, owned by the caller and copied by the call.  One context owns one CUDA
+ * stream on one device; a context is not thread-safe (one host thread at a time).
+ * Every function returns lbm_status (0 = LBM_OK, negative = error); nothing throws
+ * across the boundary.  lbm_last_error() gives the message of the last failure.
+ *
+ * Reference interfaces replaced (stloufra/LB, paths inside that project):
+ *  - the compile-time policy hooks `static void hook(LBMDataPointer&, LBMConstantsPointer&)`
+ *    composed by SolverTurbulentLES (3D/simulation/src/solvers/SolverTurbulentLES.h:67-82);
+ *  - the data carriers LBMData / LBMConstants (3D/simulation/src/data/LBMData.h:3-77,
+ *    3D/simulation/src/data/LBMConstants.h:4-113);
+ *  - the boundary-condition records (3D/simulation/src/traits/LBMTraits.h:17-61);
+ *  - the OFF voxelizer (3D/preprocess/src/geometry/geometryMesherOFF.h:45-112 and
+ *    3D/preprocess/src/geometry/geometryHandlerOFF.h:63-182).
+ *
+ * Lattice: D3Q27 in the reference's velocity order (3D/simulation/src/solvers/models/
+ * D3Q27/D3Q27.h:81-111).  Scalar fields are (x,y,z) with x fastest; populations are
+ * SoA [v][z][y][x] (the reference NDArray layout, LBMTraits.h:84-85,177-180).
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBM_ABI_VERSION 1
+
+typedef int32_t lbm_status;
+#define LBM_OK                 0
+#define LBM_ERR_INVALID       -1  /* bad argument or inconsistent set-up */
+#define LBM_ERR_OOM           -2  /* device or host allocation failed */
+#define LBM_ERR_CUDA          -3  /* CUDA runtime error (message in lbm_last_error) */
+#define LBM_ERR_NONFINITE     -4  /* a population became NaN/Inf (reference: NaN break,
+                                     SolverTurbulentLES.h:233-239) */
+#define LBM_ERR_TIMEOUT       -5  /* a bounded device wait gave up */
+#define LBM_ERR_STATE         -6  /* call out of order (e.g. step before flags) */
+#define LBM_ERR_IO            -7  /* file could not be read or written */
+#define LBM_ERR_UNSUPPORTED   -8  /* configuration the kernels do not implement */
+
+/* collision operator (reference: solvers/collisions/) */
+#define LBM_COLLISION_SRT            0  /* CollisionSRTTurbulent.h:20-81 */
+#define LBM_COLLISION_CUMULANT2015   1  /* CollisionCumD3Q27Turbulent2015.h:19-537 */
+
+/* eddy-viscosity closure (reference: solvers/turbulence/) */
+#define LBM_CLOSURE_NONE         0  /* OmegaNo.h:25-48 : omega = 1/tau */
+#define LBM_CLOSURE_SMAGORINSKY  1  /* OmegaLES.h:25-137 */
+#define LBM_CLOSURE_MLP          2  /* learned closure; no reference counterpart */
+
+/* population storage in HBM; the collision always runs in FP32 (FP64 for F64) */
+#define LBM_STORAGE_F64     0
+#define LBM_STORAGE_F32     1
+#define LBM_STORAGE_F16DEV  2  /* half(h), f = w_v*rho0 + h*2^-s */
+
+/* what the reference's flag -1 nodes are (its INLETTYPE policy) */
+#define LBM_INLET_MOVING_WALL  0  /* Inlet/InletVelocityMovingWall.h:18-60 */
+#define LBM_INLET_EQUILIBRIUM  1  /* Inlet/InletVelocityEquilibrium.h:18-108 */
+
+typedef struct lbm_config {
+    int32_t nx, ny, nz;       /* lattice size */
+    int32_t periodic[3];      /* 1 = wrap this axis by index (replaces Periodic.h ghost planes) */
+    int32_t collision;        /* LBM_COLLISION_* */
+    int32_t closure;          /* LBM_CLOSURE_* */
+    int32_t storage;          /* LBM_STORAGE_* */
+    int32_t inlet_kind;       /* LBM_INLET_* */
+    double  nu;               /* lattice kinematic viscosity; tau = 3 nu + 1/2 */
+    double  tau;              /* if > 0, overrides the tau derived from nu */
+    double  cles;             /* Smagorinsky constant; coefficient 18*cles (OmegaLES.h:347) */
+    double  force[3];         /* body force density (lattice units); no reference counterpart */
+    double  rho0;             /* reference density of the FP16-deviation encoding */
+    int32_t f16_scale_log2;   /* s of the FP16-deviation encoding (10 => 2^10) */
+    int32_t device;           /* CUDA device ordinal */
+} lbm_config;
+
+/* boundary-condition records, mirroring LBMTraits.h:17-43 */
+typedef struct lbm_vertex { int32_t x, y, z; } lbm_vertex;
+
+typedef struct lbm_bc_inlet {       /* boundaryConditionInlet, LBMTraits.h:31-36 */
+    lbm_vertex vertex;
+    float normal[3];                /* outward normal */
+    float velocity[3];              /* lattice units */
+    int32_t regular;
+} lbm_bc_inlet;
+
+typedef struct lbm_bc_outlet {      /* boundaryConditionOutlet, LBMTraits.h:38-43 */
+    lbm_vertex vertex;
+    float normal[3];                /* outward normal, +-x only (as the reference) */
+    float density;                  /* lattice units */
+    int32_t regular;
+} lbm_bc_outlet;
+
+/* diagnostics of the current state, reduced in FP64 on the device */
+typedef struct lbm_diag {
+    double  mass;            /* sum of rho over stream-target cells */
+    double  momentum[3];     /* sum of rho*u over the same cells */
+    double  drag[3];         /* momentum exchange on solid links by the last completed step */
+    double  max_speed;       /* max |u| */
+    int64_t nonfinite;       /* cells whose populations are not all finite */
+    int64_t fluid_cells;     /* number of stream-target cells */
+    int64_t step;            /* time steps done */
+} lbm_diag;
+
+typedef struct lbm_ctx lbm_ctx;
+
+/* ---- lifecycle --------------------------------------------------------------- */
+lbm_status  lbm_create(const lbm_config* cfg, lbm_ctx** out);
+lbm_status  lbm_destroy(lbm_ctx* ctx);
+const char* lbm_status_string(lbm_status s);
+const char* lbm_last_error(const lbm_ctx* ctx);   /* ctx may be NULL: last global error */
+int32_t     lbm_abi_version(void);
+
+/* ---- set-up (replaces geometryMesherBoundary::arrayTransfer, geometryMesherBoundary.h:602-617) */
+/* flags: nx*ny*nz int32 in the reference encoding (geometryMesherBoundary.h:439-484,
+ * main.cu:95-97): 0 solid, >0 fluid, -1 inlet/moving wall, -2 outlet, -3 periodic
+ * (treated as fluid; periodicity comes from cfg.periodic). */
+lbm_status lbm_set_flags(lbm_ctx* ctx, const int32_t* flags);
+/* per-node records of the -1 and -2 nodes (compileBoundaryArrayInlets/Outlets). */
+lbm_status lbm_set_bc(lbm_ctx* ctx, const lbm_bc_inlet* inlets, int32_t n_inlets,
+                      const lbm_bc_outlet* outlets, int32_t n_outlets);
+
+/* ---- initialisation (InitializationEquilibriumConstVector.h:103-224) ---------- */
+lbm_status lbm_init_equilibrium(lbm_ctx* ctx, double rho0, const double u0[3]);
+/* rho: N doubles, u: 3*N doubles component-major (ux[N], uy[N], uz[N]) */
+lbm_status lbm_init_fields(lbm_ctx* ctx, const double* rho, const double* u);
+
+/* ---- time stepping (SolverTurbulentLES::runSimulation body, :186-226) ---------- */
+lbm_status lbm_step(lbm_ctx* ctx, int32_t nsteps);
+lbm_status lbm_synchronize(lbm_ctx* ctx);
+/* nsteps steps bracketed by CUDA events on the context's stream; *ms = elapsed device time */
+lbm_status lbm_step_timed(lbm_ctx* ctx, int32_t nsteps, double* ms);
+
+/* ---- read-back (host copies, caller-owned) ----------------------------------- */
+/* moments of the current pre-collision state (MomentDensityVelocityN27.h:27-83) */
+lbm_status lbm_get_moments(lbm_ctx* ctx, double* rho, double* u);
+/* the current pre-collision populations df[v][z][y][x] in reference velocity order */
+lbm_status lbm_get_populations(lbm_ctx* ctx, double* f);
+lbm_status lbm_set_populations(lbm_ctx* ctx, const double* f);
+lbm_status lbm_reduce(lbm_ctx* ctx, lbm_diag* out);
+/* u_x, u_y, u_z, rho of one cell (SolverTurbulentLES::probeWrite, SolverTurbulentLES.h:150-177) */
+lbm_status lbm_probe(lbm_ctx* ctx, int32_t x, int32_t y, int32_t z, double out[4]);
+
+/* relative velocity change since the previous call (ErrorQuadratic.h:19-91) */
+lbm_status lbm_error_evaluation(lbm_ctx* ctx, double* err);
+
+/* ---- time averaging (MomentTimeAvg.h:19-80, extended with <u_i u_j>) ------------ */
+lbm_status lbm_timeavg_begin(lbm_ctx* ctx);   /* zero accumulators, accumulate each step */
+lbm_status lbm_timeavg_end(lbm_ctx* ctx);     /* stop accumulating */
+/* means over the accumulated steps; uu: 6*N doubles (xx,yy,zz,xy,xz,yz); count may be NULL */
+lbm_status lbm_timeavg_get(lbm_ctx* ctx, double* rho_mean, double* u_mean,
+                           double* uu_mean, int64_t* count);
+
+/* ---- checkpoint / resume: bit-identical continuation ------------------------- */
+lbm_status lbm_checkpoint_save(lbm_ctx* ctx, const char* path);
+lbm_status lbm_checkpoint_load(lbm_ctx* ctx, const char* path);
+
+/* ---- host mesher (geometryMesherBoundary.h:439-484 wall pass) ---------------- */
+/* in place: every fluid cell (>0) gets 1 + number of solid cells in its 26-neighbourhood */
+lbm_status lbm_mesher_wall_pass(int32_t* flags, int32_t nx, int32_t ny, int32_t nz);
+
+/* ---- OFF voxelizer on the GPU (preprocess geometryMesherOFF.h:45-112) -------- */
+/* Reads an OFF/NOFF file; dims_out = ceil((BBmax-BBmin)*res + 2*add) per axis and bbox_out
+ * (xmin,ymin,zmin,xmax,ymax,zmax).  flags_out (nullable: query dims only) receives
+ * dims_out[0]*dims_out[1]*dims_out[2] int32, x fastest: 1 inside, 0 outside.
+ * `outside` is accepted for interface parity with polyhedronInside() and otherwise unused:
+ * the GPU casts +x rays. */
+lbm_status lbm_voxelize_off(const char* path, double res, double add, const double outside[3],
+                            int32_t* flags_out, int32_t dims_out[3], double bbox_out[6],
+                            int32_t device);
+/* the same on an in-memory triangle soup: verts 3*nv doubles, tris 3*nt int32 */
+lbm_status lbm_voxelize_mesh(const double* verts, int32_t nv, const int32_t* tris, int32_t nt,
+                             double res, double add, int32_t* flags_out, int32_t dims_out[3],
+                             double bbox_out[6], int32_t device);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LBM_GB300_H */

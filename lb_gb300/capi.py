@@ -1,0 +1,164 @@
+"""ctypes mirror of include/lbm.h and the loader of the in-tree CUDA library.
+
+The shared library lb_gb300/liblbm_gb300.so is built by lb_gb300.build (nvcc, sm_103a).
+Loading fails loudly when it is missing: there is no CPU fallback in the product path.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblbm_gb300.so")
+
+LBM_OK = 0
+LBM_ERR_INVALID = -1
+LBM_ERR_OOM = -2
+LBM_ERR_CUDA = -3
+LBM_ERR_NONFINITE = -4
+LBM_ERR_TIMEOUT = -5
+LBM_ERR_STATE = -6
+LBM_ERR_IO = -7
+LBM_ERR_UNSUPPORTED = -8
+
+LBM_COLLISION_SRT = 0
+LBM_COLLISION_CUMULANT2015 = 1
+LBM_CLOSURE_NONE = 0
+LBM_CLOSURE_SMAGORINSKY = 1
+LBM_CLOSURE_MLP = 2
+LBM_STORAGE_F64 = 0
+LBM_STORAGE_F32 = 1
+LBM_STORAGE_F16DEV = 2
+LBM_INLET_MOVING_WALL = 0
+LBM_INLET_EQUILIBRIUM = 1
+
+
+class LbmConfig(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+        ("periodic", C.c_int32 * 3),
+        ("collision", C.c_int32), ("closure", C.c_int32), ("storage", C.c_int32),
+        ("inlet_kind", C.c_int32),
+        ("nu", C.c_double), ("tau", C.c_double), ("cles", C.c_double),
+        ("force", C.c_double * 3),
+        ("rho0", C.c_double),
+        ("f16_scale_log2", C.c_int32),
+        ("device", C.c_int32),
+    ]
+
+
+class LbmVertex(C.Structure):
+    _fields_ = [("x", C.c_int32), ("y", C.c_int32), ("z", C.c_int32)]
+
+
+class LbmBcInlet(C.Structure):
+    _fields_ = [("vertex", LbmVertex), ("normal", C.c_float * 3), ("velocity", C.c_float * 3),
+                ("regular", C.c_int32)]
+
+
+class LbmBcOutlet(C.Structure):
+    _fields_ = [("vertex", LbmVertex), ("normal", C.c_float * 3), ("density", C.c_float),
+                ("regular", C.c_int32)]
+
+
+class LbmDiag(C.Structure):
+    _fields_ = [("mass", C.c_double), ("momentum", C.c_double * 3), ("drag", C.c_double * 3),
+                ("max_speed", C.c_double), ("nonfinite", C.c_int64), ("fluid_cells", C.c_int64),
+                ("step", C.c_int64)]
+
+
+def make_config(nx, ny, nz, periodic=(0, 0, 0), collision=LBM_COLLISION_CUMULANT2015,
+                closure=LBM_CLOSURE_NONE, storage=LBM_STORAGE_F32, inlet_kind=LBM_INLET_MOVING_WALL,
+                nu=1.0 / 6.0, tau=0.0, cles=0.173, force=(0.0, 0.0, 0.0), rho0=1.0,
+                f16_scale_log2=10, device=0):
+    c = LbmConfig()
+    c.nx, c.ny, c.nz = int(nx), int(ny), int(nz)
+    for a in range(3):
+        c.periodic[a] = int(periodic[a])
+        c.force[a] = float(force[a])
+    c.collision, c.closure, c.storage, c.inlet_kind = int(collision), int(closure), int(storage), int(inlet_kind)
+    c.nu, c.tau, c.cles, c.rho0 = float(nu), float(tau), float(cles), float(rho0)
+    c.f16_scale_log2, c.device = int(f16_scale_log2), int(device)
+    return c
+
+
+def make_inlet(x, y, z, normal, velocity, regular=1):
+    r = LbmBcInlet()
+    r.vertex = LbmVertex(int(x), int(y), int(z))
+    for a in range(3):
+        r.normal[a] = float(normal[a])
+        r.velocity[a] = float(velocity[a])
+    r.regular = int(regular)
+    return r
+
+
+def make_outlet(x, y, z, normal, density, regular=1):
+    r = LbmBcOutlet()
+    r.vertex = LbmVertex(int(x), int(y), int(z))
+    for a in range(3):
+        r.normal[a] = float(normal[a])
+    r.density = float(density)
+    r.regular = int(regular)
+    return r
+
+
+class LbmError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"lbm status {status}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def lib():
+    """Load liblbm_gb300.so; raises if the CUDA library has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with lb_gb300.build.build() "
+                          "(the solver has no CPU fallback)")
+    L = C.CDLL(LIB_PATH)
+    vp, i32, f64 = C.c_void_p, C.c_int32, C.c_double
+    dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int32)
+    sig = {
+        "lbm_create": ([C.POINTER(LbmConfig), C.POINTER(vp)], i32),
+        "lbm_destroy": ([vp], i32),
+        "lbm_status_string": ([i32], C.c_char_p),
+        "lbm_last_error": ([vp], C.c_char_p),
+        "lbm_abi_version": ([], i32),
+        "lbm_set_flags": ([vp, ip], i32),
+        "lbm_set_bc": ([vp, C.POINTER(LbmBcInlet), i32, C.POINTER(LbmBcOutlet), i32], i32),
+        "lbm_init_equilibrium": ([vp, f64, dp], i32),
+        "lbm_init_fields": ([vp, dp, dp], i32),
+        "lbm_step": ([vp, i32], i32),
+        "lbm_synchronize": ([vp], i32),
+        "lbm_step_timed": ([vp, i32, dp], i32),
+        "lbm_probe": ([vp, i32, i32, i32, dp], i32),
+        "lbm_get_moments": ([vp, dp, dp], i32),
+        "lbm_get_populations": ([vp, dp], i32),
+        "lbm_set_populations": ([vp, dp], i32),
+        "lbm_reduce": ([vp, C.POINTER(LbmDiag)], i32),
+        "lbm_error_evaluation": ([vp, dp], i32),
+        "lbm_timeavg_begin": ([vp], i32),
+        "lbm_timeavg_end": ([vp], i32),
+        "lbm_timeavg_get": ([vp, dp, dp, dp, C.POINTER(C.c_int64)], i32),
+        "lbm_checkpoint_save": ([vp, C.c_char_p], i32),
+        "lbm_checkpoint_load": ([vp, C.c_char_p], i32),
+        "lbm_mesher_wall_pass": ([ip, i32, i32, i32], i32),
+        "lbm_voxelize_off": ([C.c_char_p, f64, f64, dp, ip, ip, dp, i32], i32),
+        "lbm_voxelize_mesh": ([dp, i32, ip, i32, f64, f64, ip, ip, dp, i32], i32),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def check(status, ctx=None):
+    if status != LBM_OK:
+        L = lib()
+        msg = L.lbm_last_error(ctx)
+        raise LbmError(status, (msg or b"").decode() or L.lbm_status_string(status).decode())
+    return status

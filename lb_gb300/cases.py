@@ -1,0 +1,193 @@
+"""Seeded synthetic cases (lattice units) built on the reference's flag encoding.
+
+Flag fields are int32 [z, y, x] (x fastest in memory, as the reference's mesh matrix,
+postprocesors/outputerMesh.h:45-53): 0 solid, >0 fluid (after the wall pass, 1 + number of solid
+cells in the 26-neighbourhood, geometry/geometryMesherBoundary.h:439-484), -1 inlet / moving-wall
+node, -2 outlet node.  Random numbers come from a counter-based splitmix64 of (seed, cell, component)
+so any process reproduces them.
+"""
+import math
+
+import numpy as np
+
+from . import capi
+
+SEED = 0x5EED2026
+_M64 = (1 << 64) - 1
+
+
+def splitmix64(x):
+    """Vectorised splitmix64 finaliser on uint64 arrays."""
+    x = (x + np.uint64(0x9E3779B97F4A7C15)) & np.uint64(_M64)
+    z = x
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def uniform(seed, index, component):
+    """U[0,1) per (seed, index, component); index is an integer array."""
+    with np.errstate(over="ignore"):
+        key = np.uint64(seed) * np.uint64(0x100000001B3) + np.asarray(index, dtype=np.uint64) * np.uint64(8) + np.uint64(component)
+        r = splitmix64(splitmix64(key))
+    return (r >> np.uint64(11)).astype(np.float64) * (1.0 / (1 << 53))
+
+
+def wall_pass(flags):
+    """geometryMesherBoundary::meshingBoundaryWall via the C ABI (host code)."""
+    import ctypes as C
+    f = np.ascontiguousarray(flags, dtype=np.int32)
+    nz, ny, nx = f.shape
+    capi.check(capi.lib().lbm_mesher_wall_pass(f.ctypes.data_as(C.POINTER(C.c_int32)), nx, ny, nz))
+    return f
+
+
+def wall_pass_numpy(flags):
+    """Same count in numpy (no library needed): fluid cells get 1 + #solid 26-neighbours."""
+    f = np.asarray(flags, dtype=np.int32).copy()
+    solid = (f == 0)
+    pad = np.pad(solid, 1, constant_values=False)
+    cnt = np.zeros_like(f)
+    nz, ny, nx = f.shape
+    for dz in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                cnt += pad[1 + dz:1 + dz + nz, 1 + dy:1 + dy + ny, 1 + dx:1 + dx + nx]
+    m = f > 0
+    f[m] += cnt[m]
+    return f
+
+
+# ---- config 1: lid-driven cavity --------------------------------------------------------------------
+def cavity(n=64, u_lid=0.05, re=1000.0, wall=wall_pass_numpy):
+    """n^3 box: solid at x=0, x=n-1, y=0, z=0, z=n-1; the top plane y=n-1 (inside the side walls) is
+    moving-wall nodes (flag -1, normal +y, velocity (u_lid,0,0)); nu = u_lid * n / Re."""
+    f = np.ones((n, n, n), dtype=np.int32)
+    f[:, :, 0] = 0; f[:, :, -1] = 0
+    f[:, 0, :] = 0
+    f[0, :, :] = 0; f[-1, :, :] = 0
+    f[1:-1, -1, 1:-1] = -1
+    f = wall(f)
+    lid = [capi.make_inlet(i, n - 1, k, (0, 1, 0), (u_lid, 0, 0)) for k in range(1, n - 1) for i in range(1, n - 1)]
+    return {"flags": f, "inlets": lid, "outlets": [], "nu": u_lid * n / re, "periodic": (0, 0, 0)}
+
+
+# ---- configs 2/3: turbulent channel -------------------------------------------------------------------
+def channel(nx, ny, nz, re_tau=180.0, u_max=0.05, amp=0.05, seed=SEED, nu=None, wall=wall_pass_numpy):
+    """Periodic in x and z, bounce-back solid rows y=0 and y=ny-1 (walls at y=0.5 and ny-1.5, half
+    height h=(ny-2)/2).  Body force F_x = u_tau^2/h for Re_tau = u_tau h / nu.  nu (builder's
+    choice when not given): the turbulent centre-line velocity of a Re_tau = 180 channel is about
+    18.3 u_tau, so u_tau = u_max / 18.3 and nu = u_tau h / Re_tau (tau = 0.5058 at h = 127)."""
+    f = np.ones((nz, ny, nx), dtype=np.int32)
+    f[:, 0, :] = 0
+    f[:, -1, :] = 0
+    f = wall(f)
+    h = (ny - 2) / 2.0
+    if nu is None:
+        nu = (u_max / 18.3) * h / re_tau
+    u_tau = re_tau * nu / h
+    force = (u_tau * u_tau / h, 0.0, 0.0)
+    y = np.arange(ny, dtype=np.float64)
+    yc = (ny - 1) / 2.0
+    prof = u_max * (1.0 - ((y - yc) / h) ** 2)
+    prof[[0, -1]] = 0.0
+    N = nx * ny * nz
+    idx = np.arange(N, dtype=np.uint64)
+    u = np.zeros((3, N))
+    for a in range(3):
+        u[a] = (uniform(seed, idx, a) * 2.0 - 1.0) * amp * u_max
+    u[0] += np.broadcast_to(prof[None, :, None], (nz, ny, nx)).reshape(-1)
+    solid = f.reshape(-1) == 0
+    u[:, solid] = 0.0
+    rho = np.ones(N)
+    return {"flags": f, "inlets": [], "outlets": [], "nu": nu, "periodic": (1, 0, 1), "force": force,
+            "rho": rho, "u": u, "h": h, "u_tau": u_tau}
+
+
+# ---- config 4: flow past a seeded body ------------------------------------------------------------------
+def icosphere(subdiv):
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    v = [np.asarray(p, dtype=np.float64) / np.linalg.norm(p) for p in v]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+             (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+             (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    for _ in range(subdiv):
+        cache = {}
+        nf = []
+
+        def mid(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in cache:
+                p = v[a] + v[b]
+                v.append(p / np.linalg.norm(p))
+                cache[key] = len(v) - 1
+            return cache[key]
+
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    return np.asarray(v), np.asarray(faces, dtype=np.int32)
+
+
+def _real_sph_harm(l, m, theta, phi):
+    """Real spherical harmonic (unnormalised associated Legendre with Condon-Shortley phase)."""
+    from scipy.special import lpmv
+    x = np.cos(theta)
+    am = abs(m)
+    norm = math.sqrt((2 * l + 1) / (4 * math.pi) * math.factorial(l - am) / math.factorial(l + am))
+    p = lpmv(am, l, x)
+    if m > 0:
+        return math.sqrt(2) * norm * p * np.cos(am * phi)
+    if m < 0:
+        return math.sqrt(2) * norm * p * np.sin(am * phi)
+    return norm * p
+
+
+def perturbed_icosphere(radius=24.0, subdiv=5, lmax=6, amp=0.15, seed=SEED, center=(0.0, 0.0, 0.0)):
+    """Icosphere (20*4^subdiv faces) with r(theta,phi) = R (1 + s(theta,phi)), s = sum a_lm Y_lm over
+    1 <= l <= lmax with a_lm ~ U(-1,1) from the seed, scaled so max |s| over the vertices = amp."""
+    v, f = icosphere(subdiv)
+    theta = np.arccos(np.clip(v[:, 2], -1, 1))
+    phi = np.arctan2(v[:, 1], v[:, 0])
+    s = np.zeros(len(v))
+    k = 0
+    for l in range(1, lmax + 1):
+        for m in range(-l, l + 1):
+            a = uniform(seed, np.asarray([k]), 7)[0] * 2.0 - 1.0
+            s += a * _real_sph_harm(l, m, theta, phi)
+            k += 1
+    s *= amp / np.abs(s).max()
+    r = radius * (1.0 + s)
+    return v * r[:, None] + np.asarray(center)[None, :], f
+
+
+def write_off(path, verts, faces):
+    with open(path, "w") as fh:
+        fh.write("OFF\n%d %d 0\n" % (len(verts), len(faces)))
+        for p in verts:
+            fh.write("%.17g %.17g %.17g\n" % tuple(p))
+        for t in faces:
+            fh.write("3 %d %d %d\n" % tuple(t))
+
+
+def body_in_channel(nx=384, ny=192, nz=192, u_in=0.04, rho_out=1.0, nu=None, body_flags=None, center=None,
+                    wall=wall_pass_numpy):
+    """Inlet plane x=0 (-1 nodes, normal -x, u=(u_in,0,0)), outlet plane x=nx-1 (-2 nodes, normal +x,
+    rho_out), periodic y and z, solid body cells from `body_flags` (True = solid) placed with its
+    grid origin at `center` offset.  nu default: Re = u_in * D / nu = 200 with D = 48."""
+    f = np.ones((nz, ny, nx), dtype=np.int32)
+    if body_flags is not None:
+        bz, by, bx = body_flags.shape
+        ox, oy, oz = center
+        f[oz:oz + bz, oy:oy + by, ox:ox + bx][body_flags] = 0
+    f = wall(f)
+    f[:, :, 0] = -1
+    f[:, :, -1] = -2
+    inl = [capi.make_inlet(0, j, k, (-1, 0, 0), (u_in, 0, 0)) for k in range(nz) for j in range(ny)]
+    out = [capi.make_outlet(nx - 1, j, k, (1, 0, 0), rho_out) for k in range(nz) for j in range(ny)]
+    if nu is None:
+        nu = u_in * 48.0 / 200.0
+    return {"flags": f, "inlets": inl, "outlets": out, "nu": nu, "periodic": (0, 1, 1)}

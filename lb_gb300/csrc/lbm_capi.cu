@@ -1,0 +1,798 @@
+// lbm_capi.cu - C ABI of include/lbm.h: context, geometry classification, stepping, read-back.
+//
+// Host-side counterpart of the reference's set-up and driver code:
+//   geometryMesherBoundary (flag encoding, BC lists, arrayTransfer; geometryMesherBoundary.h),
+//   InitializationEquilibriumConstVector (initialisation), SolverTurbulentLES::runSimulation
+//   (the step loop), MomentTimeAvg / ErrorQuadratic (monitors).
+// Every call returns a status; CUDA errors and inconsistent set-ups are reported, never thrown.
+
+#include "../../include/lbm.h"
+#include "lbm_device.cuh"
+#include "lbm_aux.cuh"
+#include "lbm_launch.h"
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace lbm;
+
+struct lbm_ctx {
+    lbm_config cfg{};
+    cudaStream_t st = nullptr;
+    long long N = 0;
+    size_t esize = 0;  // bytes per stored population
+    void* d_f = nullptr;
+    uint8_t* d_cls = nullptr;
+    int32_t* d_aux = nullptr;
+    std::vector<int32_t> flags;
+    std::vector<lbm_bc_inlet> inlets;
+    std::vector<lbm_bc_outlet> outlets;
+    bool have_flags = false, have_geom = false, initialized = false;
+    // side tables
+    int n_lid = 0, n_in = 0, n_out = 0;
+    void* d_lid_state = nullptr;
+    float *d_lid_n = nullptr, *d_lid_u = nullptr;
+    void* d_in_probe = nullptr;
+    float* d_in_u = nullptr;
+    int32_t* d_in_dir = nullptr;
+    void* d_out_save = nullptr;
+    float* d_out_rho = nullptr;
+    int32_t* d_out_dir = nullptr;
+    long long m = 0;  // steps done
+    // monitors
+    double* d_acc = nullptr;
+    bool avg_on = false;
+    long long avg_begin = 0, avg_last = -1, avg_count = 0;
+    double* d_uerr = nullptr;
+    double* d_red = nullptr;
+    double *d_rho_out = nullptr, *d_u_out = nullptr, *d_f_out = nullptr;
+    double* d_probe = nullptr;
+    std::string err;
+};
+
+static std::string g_err;
+
+static lbm_status fail(lbm_ctx* c, lbm_status s, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    g_err = buf;
+    return s;
+}
+#define CU(ctx, call)                                                                                 \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                        \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? LBM_ERR_OOM : LBM_ERR_CUDA, "%s: %s (%s:%d)", \
+                        #call, cudaGetErrorString(e_), __FILE__, __LINE__);                           \
+    } while (0)
+
+static void dfree(void* p) { if (p) cudaFree(p); }
+
+static size_t real_size(const lbm_ctx* c) { return c->cfg.storage == LBM_STORAGE_F64 ? 8 : 4; }
+
+static Params make_params(const lbm_ctx* c) {
+    Params p;
+    std::memset(&p, 0, sizeof(p));
+    p.f = c->d_f; p.cls = c->d_cls; p.aux = c->d_aux;
+    p.nx = c->cfg.nx; p.ny = c->cfg.ny; p.nz = c->cfg.nz;
+    for (int a = 0; a < 3; a++) p.wrap[a] = c->cfg.periodic[a] ? 1 : 0;
+    p.N = c->N;
+    p.m = (int)c->m;
+    p.tau = c->cfg.tau > 0 ? c->cfg.tau : 3.0 * c->cfg.nu + 0.5;
+    p.cles18 = 18.0 * c->cfg.cles;
+    p.nu = c->cfg.nu;
+    for (int a = 0; a < 3; a++) p.F[a] = c->cfg.force[a];
+    p.rho0 = (float)c->cfg.rho0;
+    p.scale = std::ldexp(1.0f, c->cfg.f16_scale_log2);
+    p.inv_scale = std::ldexp(1.0f, -c->cfg.f16_scale_log2);
+    p.lid_state = c->d_lid_state; p.lid_n = c->d_lid_n; p.lid_u = c->d_lid_u; p.n_lid = c->n_lid;
+    p.in_probe = c->d_in_probe; p.in_u = c->d_in_u; p.in_dir = c->d_in_dir; p.n_in = c->n_in;
+    p.out_save = c->d_out_save; p.out_rho = c->d_out_rho; p.out_dir = c->d_out_dir; p.n_out = c->n_out;
+    p.acc = nullptr;
+    return p;
+}
+
+static cudaError_t do_step(lbm_ctx* c, const Params& p) {
+    switch (c->cfg.storage) {
+        case LBM_STORAGE_F64: return launch_step<StF64>(p, c->cfg.collision, c->cfg.closure, c->st);
+        case LBM_STORAGE_F32: return launch_step<StF32>(p, c->cfg.collision, c->cfg.closure, c->st);
+        default: return launch_step<StF16>(p, c->cfg.collision, c->cfg.closure, c->st);
+    }
+}
+static cudaError_t do_read(lbm_ctx* c, const Params& p, const ReadOut& o) {
+    switch (c->cfg.storage) {
+        case LBM_STORAGE_F64: return launch_read<StF64>(p, o, c->st);
+        case LBM_STORAGE_F32: return launch_read<StF32>(p, o, c->st);
+        default: return launch_read<StF16>(p, o, c->st);
+    }
+}
+static cudaError_t do_init(lbm_ctx* c, const Params& p, const double* r, const double* u, double r0, const double u0[3],
+                           const double* pops) {
+    switch (c->cfg.storage) {
+        case LBM_STORAGE_F64: return launch_init<StF64>(p, r, u, r0, u0, pops, c->st);
+        case LBM_STORAGE_F32: return launch_init<StF32>(p, r, u, r0, u0, pops, c->st);
+        default: return launch_init<StF16>(p, r, u, r0, u0, pops, c->st);
+    }
+}
+
+extern "C" {
+
+int32_t lbm_abi_version(void) { return LBM_ABI_VERSION; }
+
+const char* lbm_status_string(lbm_status s) {
+    switch (s) {
+        case LBM_OK: return "ok";
+        case LBM_ERR_INVALID: return "invalid argument";
+        case LBM_ERR_OOM: return "out of memory";
+        case LBM_ERR_CUDA: return "CUDA error";
+        case LBM_ERR_NONFINITE: return "non-finite populations";
+        case LBM_ERR_TIMEOUT: return "device wait timed out";
+        case LBM_ERR_STATE: return "call out of order";
+        case LBM_ERR_IO: return "I/O error";
+        case LBM_ERR_UNSUPPORTED: return "unsupported configuration";
+        default: return "unknown status";
+    }
+}
+
+const char* lbm_last_error(const lbm_ctx* c) { return c ? c->err.c_str() : g_err.c_str(); }
+
+lbm_status lbm_create(const lbm_config* cfg, lbm_ctx** out) {
+    if (!cfg || !out) return fail(nullptr, LBM_ERR_INVALID, "lbm_create: null argument");
+    *out = nullptr;
+    if (cfg->nx < 3 || cfg->ny < 3 || cfg->nz < 3)
+        return fail(nullptr, LBM_ERR_INVALID, "lattice must be at least 3 cells per axis (got %d %d %d)", cfg->nx, cfg->ny, cfg->nz);
+    long long N = (long long)cfg->nx * cfg->ny * cfg->nz;
+    if (27LL * N >= (1LL << 31) * 4LL)
+        return fail(nullptr, LBM_ERR_UNSUPPORTED, "lattice of %lld cells is too large", N);
+    if (cfg->collision != LBM_COLLISION_SRT && cfg->collision != LBM_COLLISION_CUMULANT2015)
+        return fail(nullptr, LBM_ERR_UNSUPPORTED, "collision %d not implemented", cfg->collision);
+    if (cfg->closure != LBM_CLOSURE_NONE && cfg->closure != LBM_CLOSURE_SMAGORINSKY)
+        return fail(nullptr, LBM_ERR_UNSUPPORTED, "closure %d not implemented", cfg->closure);
+    if (cfg->storage < LBM_STORAGE_F64 || cfg->storage > LBM_STORAGE_F16DEV)
+        return fail(nullptr, LBM_ERR_INVALID, "storage %d", cfg->storage);
+    double tau = cfg->tau > 0 ? cfg->tau : 3.0 * cfg->nu + 0.5;
+    if (!(tau > 0.5)) return fail(nullptr, LBM_ERR_INVALID, "tau = %g must exceed 1/2", tau);
+    if (cfg->storage == LBM_STORAGE_F16DEV && (cfg->f16_scale_log2 < 0 || cfg->f16_scale_log2 > 20))
+        return fail(nullptr, LBM_ERR_INVALID, "f16_scale_log2 = %d out of [0, 20]", cfg->f16_scale_log2);
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(nullptr, LBM_ERR_CUDA, "no CUDA device: %s", cudaGetErrorString(e));
+    if (cfg->device < 0 || cfg->device >= ndev) return fail(nullptr, LBM_ERR_INVALID, "device %d of %d", cfg->device, ndev);
+    lbm_ctx* c = new lbm_ctx;
+    c->cfg = *cfg;
+    c->N = N;
+    c->esize = cfg->storage == LBM_STORAGE_F64 ? 8 : cfg->storage == LBM_STORAGE_F32 ? 4 : 2;
+    lbm_status s = LBM_OK;
+    if ((e = cudaSetDevice(cfg->device)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaMalloc(&c->d_f, 27 * (size_t)N * c->esize)) != cudaSuccess ||
+        (e = cudaMalloc(&c->d_cls, (size_t)N)) != cudaSuccess ||
+        (e = cudaMalloc(&c->d_aux, (size_t)N * 4)) != cudaSuccess ||
+        (e = cudaMalloc(&c->d_red, RED_COUNT * sizeof(double))) != cudaSuccess) {
+        s = fail(nullptr, e == cudaErrorMemoryAllocation ? LBM_ERR_OOM : LBM_ERR_CUDA, "lbm_create: %s", cudaGetErrorString(e));
+        lbm_destroy(c);
+        return s;
+    }
+    // default geometry: every cell fluid
+    c->flags.assign((size_t)N, 1);
+    *out = c;
+    return LBM_OK;
+}
+
+static void free_side(lbm_ctx* c) {
+    dfree(c->d_lid_state); dfree(c->d_lid_n); dfree(c->d_lid_u);
+    dfree(c->d_in_probe); dfree(c->d_in_u); dfree(c->d_in_dir);
+    dfree(c->d_out_save); dfree(c->d_out_rho); dfree(c->d_out_dir);
+    c->d_lid_state = c->d_in_probe = c->d_out_save = nullptr;
+    c->d_lid_n = c->d_lid_u = c->d_in_u = c->d_out_rho = nullptr;
+    c->d_in_dir = c->d_out_dir = nullptr;
+    c->n_lid = c->n_in = c->n_out = 0;
+}
+
+lbm_status lbm_destroy(lbm_ctx* c) {
+    if (!c) return LBM_OK;
+    cudaSetDevice(c->cfg.device);
+    if (c->st) cudaStreamSynchronize(c->st);
+    dfree(c->d_f); dfree(c->d_cls); dfree(c->d_aux);
+    free_side(c);
+    dfree(c->d_acc); dfree(c->d_uerr); dfree(c->d_red);
+    dfree(c->d_rho_out); dfree(c->d_u_out); dfree(c->d_f_out); dfree(c->d_probe);
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+    return LBM_OK;
+}
+
+lbm_status lbm_set_flags(lbm_ctx* c, const int32_t* flags) {
+    if (!c || !flags) return fail(c, LBM_ERR_INVALID, "lbm_set_flags: null argument");
+    c->flags.assign(flags, flags + c->N);
+    c->have_flags = true;
+    c->have_geom = false;
+    c->initialized = false;
+    return LBM_OK;
+}
+
+lbm_status lbm_set_bc(lbm_ctx* c, const lbm_bc_inlet* in, int32_t nin, const lbm_bc_outlet* out, int32_t nout) {
+    if (!c || nin < 0 || nout < 0 || (nin && !in) || (nout && !out))
+        return fail(c, LBM_ERR_INVALID, "lbm_set_bc: bad argument");
+    c->inlets.assign(in, in + nin);
+    c->outlets.assign(out, out + nout);
+    c->have_geom = false;
+    c->initialized = false;
+    return LBM_OK;
+}
+
+// ---- geometry: reference flags + BC records -> class byte, side-table indices, validation -------
+static lbm_status build_geometry(lbm_ctx* c) {
+    const int nx = c->cfg.nx, ny = c->cfg.ny, nz = c->cfg.nz;
+    const long long N = c->N;
+    const int* wrap = c->cfg.periodic;
+    auto id = [&](int i, int j, int k) { return (long long)i + (long long)nx * ((long long)j + (long long)ny * k); };
+    auto wrapc = [&](int v, int n, int a, bool& ok) {
+        if (v < 0 || v >= n) { if (wrap[a]) v = (v + n) % n; else ok = false; }
+        return v;
+    };
+    std::vector<uint8_t> cls((size_t)N);
+    std::vector<int32_t> aux((size_t)N, -1);
+    const bool lid_kind = c->cfg.inlet_kind == LBM_INLET_MOVING_WALL;
+    for (long long q = 0; q < N; q++) {
+        int32_t f = c->flags[q];
+        uint8_t k;
+        if (f == 0) k = CLS_SOLID;
+        else if (f == -1) k = lid_kind ? CLS_LID : CLS_INLET;
+        else if (f == -2) k = CLS_OUTLET;
+        else if (f > 0 || f == -3) k = CLS_BULK;
+        else return fail(c, LBM_ERR_INVALID, "flag %d at cell %lld is not in the reference encoding", f, q);
+        cls[q] = k | (f == 1 ? BIT_REFBULK : 0);
+    }
+    // -1 records
+    std::vector<float> lid_n, lid_u, in_u;
+    std::vector<int32_t> in_dir, out_dir;
+    std::vector<float> out_rho;
+    int n_lid = 0, n_in = 0, n_out = 0;
+    for (const auto& r : c->inlets) {
+        int i = r.vertex.x, j = r.vertex.y, k = r.vertex.z;
+        if (i < 0 || j < 0 || k < 0 || i >= nx || j >= ny || k >= nz)
+            return fail(c, LBM_ERR_INVALID, "inlet record at (%d,%d,%d) is outside the lattice", i, j, k);
+        long long q = id(i, j, k);
+        if (c->flags[q] != -1) return fail(c, LBM_ERR_INVALID, "inlet record at (%d,%d,%d) is not a -1 cell", i, j, k);
+        if (aux[q] >= 0) return fail(c, LBM_ERR_INVALID, "two inlet records for (%d,%d,%d)", i, j, k);
+        if (lid_kind) {
+            aux[q] = n_lid++;
+            for (int a = 0; a < 3; a++) { lid_n.push_back(r.normal[a]); lid_u.push_back(r.velocity[a]); }
+        } else {
+            int s = (r.normal[0] == 1.f && r.normal[1] == 0.f && r.normal[2] == 0.f) ? 1
+                  : (r.normal[0] == -1.f && r.normal[1] == 0.f && r.normal[2] == 0.f) ? -1 : 0;
+            if (!s) return fail(c, LBM_ERR_UNSUPPORTED, "equilibrium inlet at (%d,%d,%d): only +-x normals (as the reference)", i, j, k);
+            aux[q] = n_in++;
+            in_dir.push_back(s);
+            for (int a = 0; a < 3; a++) in_u.push_back(r.velocity[a]);
+        }
+    }
+    for (const auto& r : c->outlets) {
+        int i = r.vertex.x, j = r.vertex.y, k = r.vertex.z;
+        if (i < 0 || j < 0 || k < 0 || i >= nx || j >= ny || k >= nz)
+            return fail(c, LBM_ERR_INVALID, "outlet record at (%d,%d,%d) is outside the lattice", i, j, k);
+        long long q = id(i, j, k);
+        if (c->flags[q] != -2) return fail(c, LBM_ERR_INVALID, "outlet record at (%d,%d,%d) is not a -2 cell", i, j, k);
+        if (aux[q] >= 0) return fail(c, LBM_ERR_INVALID, "two outlet records for (%d,%d,%d)", i, j, k);
+        int s = (r.normal[0] == 1.f && r.normal[1] == 0.f && r.normal[2] == 0.f) ? 1
+              : (r.normal[0] == -1.f && r.normal[1] == 0.f && r.normal[2] == 0.f) ? -1 : 0;
+        if (!s) return fail(c, LBM_ERR_UNSUPPORTED, "outlet at (%d,%d,%d): only +-x normals (as the reference)", i, j, k);
+        if (!(r.density > 0)) return fail(c, LBM_ERR_INVALID, "outlet density must be positive");
+        aux[q] = n_out++;
+        out_dir.push_back(s);
+        out_rho.push_back(r.density);
+    }
+    for (long long q = 0; q < N; q++) {
+        int k = cls[q] & CLS_MASK;
+        if ((k == CLS_LID || k == CLS_INLET || k == CLS_OUTLET) && aux[q] < 0)
+            return fail(c, LBM_ERR_INVALID, "cell %lld has flag %d but no boundary record", q, c->flags[q]);
+    }
+    // helper roles: probes of the equilibrium inlets, upstream cells of the outlets
+    auto set_role = [&](long long q, uint8_t bit, int node, const char* what) -> lbm_status {
+        int k = cls[q] & CLS_MASK;
+        if (k != CLS_BULK) return fail(c, LBM_ERR_UNSUPPORTED, "%s cell %lld must be a fluid cell", what, q);
+        if ((cls[q] & (BIT_PROBE1 | BIT_PROBE2 | BIT_OUTUP)) != 0)
+            return fail(c, LBM_ERR_UNSUPPORTED, "cell %lld would serve two boundary nodes", q);
+        cls[q] |= bit;
+        aux[q] = node;
+        return LBM_OK;
+    };
+    for (long long q = 0; q < N; q++) {
+        int k = cls[q] & CLS_MASK;
+        int i = (int)(q % nx), j = (int)((q / nx) % ny), kk = (int)(q / ((long long)nx * ny));
+        if (k == CLS_INLET) {
+            int s = in_dir[aux[q]];  // interior at -s
+            for (int d = 1; d <= 2; d++) {
+                bool ok = true;
+                int ii = wrapc(i - s * d, nx, 0, ok);
+                if (!ok) return fail(c, LBM_ERR_INVALID, "inlet at (%d,%d,%d) has no interior cell %d", i, j, kk, d);
+                lbm_status st = set_role(id(ii, j, kk), d == 1 ? BIT_PROBE1 : BIT_PROBE2, aux[q], "inlet probe");
+                if (st) return st;
+            }
+        } else if (k == CLS_OUTLET) {
+            int s = out_dir[aux[q]];
+            bool ok = true;
+            int ii = wrapc(i - s, nx, 0, ok);
+            if (!ok) return fail(c, LBM_ERR_INVALID, "outlet at (%d,%d,%d) has no upstream cell", i, j, kk);
+            lbm_status st = set_role(id(ii, j, kk), BIT_OUTUP, aux[q], "outlet upstream");
+            if (st) return st;
+        }
+    }
+    // BULK/EDGE split: fluid cells next to a solid, moving-wall or inlet node stream through
+    // per-link rules (visit the 26-neighbourhood of those nodes only)
+    for (long long q = 0; q < N; q++) {
+        int k = cls[q] & CLS_MASK;
+        if (k != CLS_SOLID && k != CLS_LID && k != CLS_INLET) continue;
+        int i = (int)(q % nx), j = (int)((q / nx) % ny), kk = (int)(q / ((long long)nx * ny));
+        for (int dz = -1; dz <= 1; dz++)
+            for (int dy = -1; dy <= 1; dy++)
+                for (int dx = -1; dx <= 1; dx++) {
+                    bool ok = true;
+                    int a = wrapc(i + dx, nx, 0, ok), b = wrapc(j + dy, ny, 1, ok), e = wrapc(kk + dz, nz, 2, ok);
+                    if (!ok) continue;
+                    long long r = id(a, b, e);
+                    if ((cls[r] & CLS_MASK) == CLS_BULK) cls[r] = (uint8_t)((cls[r] & ~CLS_MASK) | CLS_EDGE);
+                }
+    }
+    // stream targets on a face of a non-periodic axis would stream from outside the lattice;
+    // outlets may only do so on their interpolated links, and must not touch solid cells
+    auto check_links = [&](long long q) -> lbm_status {
+        int k = cls[q] & CLS_MASK;
+        if (k != CLS_BULK && k != CLS_EDGE && k != CLS_OUTLET) return LBM_OK;
+        int i = (int)(q % nx), j = (int)((q / nx) % ny), kk = (int)(q / ((long long)nx * ny));
+        for (int dz = -1; dz <= 1; dz++)
+            for (int dy = -1; dy <= 1; dy++)
+                for (int dx = -1; dx <= 1; dx++) {
+                    if (!dx && !dy && !dz) continue;
+                    bool ok = true;
+                    int a = wrapc(i + dx, nx, 0, ok), b = wrapc(j + dy, ny, 1, ok), e = wrapc(kk + dz, nz, 2, ok);
+                    bool interp = (k == CLS_OUTLET) && dx == out_dir[aux[q]];
+                    if (!ok) {
+                        if (interp) continue;
+                        return fail(c, LBM_ERR_UNSUPPORTED,
+                                    "cell (%d,%d,%d) streams from outside a non-periodic lattice: add a solid layer "
+                                    "(the reference's additional_factor >= 1) or make the axis periodic", i, j, kk);
+                    }
+                    if (k == CLS_OUTLET && (cls[id(a, b, e)] & CLS_MASK) == CLS_SOLID)
+                        return fail(c, LBM_ERR_UNSUPPORTED, "outlet cell (%d,%d,%d) touches a solid cell", i, j, kk);
+                }
+        return LBM_OK;
+    };
+    for (int axis = 0; axis < 3; axis++) {
+        if (wrap[axis]) continue;
+        int n0 = axis == 0 ? nx : axis == 1 ? ny : nz;
+        for (int face = 0; face < 2; face++) {
+            int fc = face ? n0 - 1 : 0;
+            int na = axis == 0 ? ny : nx, nb2 = axis == 2 ? ny : nz;
+            for (int u2 = 0; u2 < nb2; u2++)
+                for (int u1 = 0; u1 < na; u1++) {
+                    int i = axis == 0 ? fc : u1, j = axis == 1 ? fc : (axis == 0 ? u1 : u2), kk = axis == 2 ? fc : u2;
+                    lbm_status st = check_links(id(i, j, kk));
+                    if (st) return st;
+                }
+        }
+    }
+    for (long long q = 0; q < N; q++)
+        if ((cls[q] & CLS_MASK) == CLS_OUTLET) {
+            lbm_status st = check_links(q);
+            if (st) return st;
+        }
+    // upload
+    cudaSetDevice(c->cfg.device);
+    free_side(c);
+    CU(c, cudaMemcpyAsync(c->d_cls, cls.data(), (size_t)N, cudaMemcpyHostToDevice, c->st));
+    CU(c, cudaMemcpyAsync(c->d_aux, aux.data(), (size_t)N * 4, cudaMemcpyHostToDevice, c->st));
+    const size_t rs = real_size(c);
+    c->n_lid = n_lid; c->n_in = n_in; c->n_out = n_out;
+    if (n_lid) {
+        CU(c, cudaMalloc(&c->d_lid_state, 3 * 27 * (size_t)n_lid * rs));
+        CU(c, cudaMalloc(&c->d_lid_n, 3 * (size_t)n_lid * 4));
+        CU(c, cudaMalloc(&c->d_lid_u, 3 * (size_t)n_lid * 4));
+        std::vector<float> tn(3 * n_lid), tu(3 * n_lid);  // component-major
+        for (int e = 0; e < n_lid; e++)
+            for (int a = 0; a < 3; a++) { tn[a * n_lid + e] = lid_n[3 * e + a]; tu[a * n_lid + e] = lid_u[3 * e + a]; }
+        CU(c, cudaMemcpy(c->d_lid_n, tn.data(), tn.size() * 4, cudaMemcpyHostToDevice));
+        CU(c, cudaMemcpy(c->d_lid_u, tu.data(), tu.size() * 4, cudaMemcpyHostToDevice));
+    }
+    if (n_in) {
+        CU(c, cudaMalloc(&c->d_in_probe, 3 * 3 * (size_t)n_in * rs));
+        CU(c, cudaMemset(c->d_in_probe, 0, 3 * 3 * (size_t)n_in * rs));
+        CU(c, cudaMalloc(&c->d_in_u, 3 * (size_t)n_in * 4));
+        CU(c, cudaMalloc(&c->d_in_dir, (size_t)n_in * 4));
+        std::vector<float> tu(3 * n_in);
+        for (int e = 0; e < n_in; e++)
+            for (int a = 0; a < 3; a++) tu[a * n_in + e] = in_u[3 * e + a];
+        CU(c, cudaMemcpy(c->d_in_u, tu.data(), tu.size() * 4, cudaMemcpyHostToDevice));
+        CU(c, cudaMemcpy(c->d_in_dir, in_dir.data(), (size_t)n_in * 4, cudaMemcpyHostToDevice));
+    }
+    if (n_out) {
+        CU(c, cudaMalloc(&c->d_out_save, 2 * 18 * (size_t)n_out * rs));
+        CU(c, cudaMemset(c->d_out_save, 0, 2 * 18 * (size_t)n_out * rs));
+        CU(c, cudaMalloc(&c->d_out_rho, (size_t)n_out * 4));
+        CU(c, cudaMalloc(&c->d_out_dir, (size_t)n_out * 4));
+        CU(c, cudaMemcpy(c->d_out_rho, out_rho.data(), (size_t)n_out * 4, cudaMemcpyHostToDevice));
+        CU(c, cudaMemcpy(c->d_out_dir, out_dir.data(), (size_t)n_out * 4, cudaMemcpyHostToDevice));
+    }
+    CU(c, cudaStreamSynchronize(c->st));
+    c->have_geom = true;
+    return LBM_OK;
+}
+
+static lbm_status ensure_geometry(lbm_ctx* c) {
+    if (c->have_geom) return LBM_OK;
+    return build_geometry(c);
+}
+
+static lbm_status init_common(lbm_ctx* c, const double* rho, const double* u, double rho0, const double* u0,
+                              const double* pops) {
+    cudaSetDevice(c->cfg.device);
+    lbm_status s = ensure_geometry(c);
+    if (s) return s;
+    double *dr = nullptr, *du = nullptr, *dp = nullptr;
+    const size_t N = (size_t)c->N;
+    if (rho) {
+        CU(c, cudaMalloc(&dr, N * 8));
+        CU(c, cudaMalloc(&du, 3 * N * 8));
+        CU(c, cudaMemcpyAsync(dr, rho, N * 8, cudaMemcpyHostToDevice, c->st));
+        CU(c, cudaMemcpyAsync(du, u, 3 * N * 8, cudaMemcpyHostToDevice, c->st));
+    }
+    if (pops) {
+        CU(c, cudaMalloc(&dp, 27 * N * 8));
+        CU(c, cudaMemcpyAsync(dp, pops, 27 * N * 8, cudaMemcpyHostToDevice, c->st));
+    }
+    c->m = 0;
+    Params p = make_params(c);
+    double z3[3] = {0, 0, 0};
+    cudaError_t e = do_init(c, p, dr, du, rho0, u0 ? u0 : z3, dp);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    dfree(dr); dfree(du); dfree(dp);
+    if (e != cudaSuccess) return fail(c, LBM_ERR_CUDA, "init kernel: %s", cudaGetErrorString(e));
+    if (c->d_out_save) CU(c, cudaMemset(c->d_out_save, 0, 2 * 18 * (size_t)c->n_out * real_size(c)));
+    c->avg_on = false; c->avg_count = 0; c->avg_last = -1;
+    if (c->d_uerr) CU(c, cudaMemset(c->d_uerr, 0, 3 * N * 8));
+    c->initialized = true;
+    return LBM_OK;
+}
+
+lbm_status lbm_init_equilibrium(lbm_ctx* c, double rho0, const double u0[3]) {
+    if (!c || !u0) return fail(c, LBM_ERR_INVALID, "lbm_init_equilibrium: null argument");
+    if (!(rho0 > 0)) return fail(c, LBM_ERR_INVALID, "rho0 must be positive");
+    return init_common(c, nullptr, nullptr, rho0, u0, nullptr);
+}
+
+lbm_status lbm_init_fields(lbm_ctx* c, const double* rho, const double* u) {
+    if (!c || !rho || !u) return fail(c, LBM_ERR_INVALID, "lbm_init_fields: null argument");
+    return init_common(c, rho, u, 1.0, nullptr, nullptr);
+}
+
+lbm_status lbm_set_populations(lbm_ctx* c, const double* f) {
+    if (!c || !f) return fail(c, LBM_ERR_INVALID, "lbm_set_populations: null argument");
+    return init_common(c, nullptr, nullptr, 1.0, nullptr, f);
+}
+
+lbm_status lbm_step(lbm_ctx* c, int32_t n) {
+    if (!c || n < 0) return fail(c, LBM_ERR_INVALID, "lbm_step: bad argument");
+    if (!c->initialized) return fail(c, LBM_ERR_STATE, "lbm_step before initialisation");
+    cudaSetDevice(c->cfg.device);
+    for (int s = 0; s < n; s++) {
+        Params p = make_params(c);
+        if (c->avg_on && c->m > c->avg_begin && c->m > c->avg_last) {
+            p.acc = c->d_acc;
+            c->avg_last = c->m;
+            c->avg_count++;
+        }
+        cudaError_t e = do_step(c, p);
+        if (e != cudaSuccess) return fail(c, LBM_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));
+        c->m++;
+    }
+    return LBM_OK;
+}
+
+lbm_status lbm_step_timed(lbm_ctx* c, int32_t n, double* ms) {
+    if (!c || !ms || n < 0) return fail(c, LBM_ERR_INVALID, "lbm_step_timed: bad argument");
+    if (!c->initialized) return fail(c, LBM_ERR_STATE, "lbm_step_timed before initialisation");
+    cudaSetDevice(c->cfg.device);
+    cudaEvent_t e0, e1;
+    CU(c, cudaEventCreate(&e0));
+    CU(c, cudaEventCreate(&e1));
+    CU(c, cudaEventRecord(e0, c->st));
+    lbm_status s = lbm_step(c, n);
+    cudaError_t e = cudaEventRecord(e1, c->st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float f = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&f, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s) return s;
+    if (e != cudaSuccess) return fail(c, LBM_ERR_CUDA, "timing events: %s", cudaGetErrorString(e));
+    *ms = f;
+    return LBM_OK;
+}
+
+lbm_status lbm_probe(lbm_ctx* c, int32_t x, int32_t y, int32_t z, double out[4]) {
+    if (!c || !out) return fail(c, LBM_ERR_INVALID, "lbm_probe: null argument");
+    if (x < 0 || y < 0 || z < 0 || x >= c->cfg.nx || y >= c->cfg.ny || z >= c->cfg.nz)
+        return fail(c, LBM_ERR_INVALID, "probe (%d,%d,%d) outside the lattice", x, y, z);
+    if (!c->initialized) return fail(c, LBM_ERR_STATE, "lbm_probe before initialisation");
+    cudaSetDevice(c->cfg.device);
+    if (!c->d_probe) CU(c, cudaMalloc(&c->d_probe, 4 * sizeof(double)));
+    Params p = make_params(c);
+    cudaError_t e;
+    switch (c->cfg.storage) {
+        case LBM_STORAGE_F64: e = launch_probe<StF64>(p, x, y, z, c->d_probe, c->st); break;
+        case LBM_STORAGE_F32: e = launch_probe<StF32>(p, x, y, z, c->d_probe, c->st); break;
+        default: e = launch_probe<StF16>(p, x, y, z, c->d_probe, c->st); break;
+    }
+    if (e != cudaSuccess) return fail(c, LBM_ERR_CUDA, "probe kernel: %s", cudaGetErrorString(e));
+    CU(c, cudaMemcpyAsync(out, c->d_probe, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    return LBM_OK;
+}
+
+lbm_status lbm_synchronize(lbm_ctx* c) {
+    if (!c) return fail(c, LBM_ERR_INVALID, "null ctx");
+    cudaSetDevice(c->cfg.device);
+    CU(c, cudaStreamSynchronize(c->st));
+    return LBM_OK;
+}
+
+static lbm_status run_read(lbm_ctx* c, ReadOut& o) {
+    Params p = make_params(c);
+    if (o.mode & READ_ACC) p.acc = c->d_acc;
+    cudaError_t e = do_read(c, p, o);
+    if (e != cudaSuccess) return fail(c, LBM_ERR_CUDA, "read kernel: %s", cudaGetErrorString(e));
+    return LBM_OK;
+}
+
+lbm_status lbm_get_moments(lbm_ctx* c, double* rho, double* u) {
+    if (!c || (!rho && !u)) return fail(c, LBM_ERR_INVALID, "lbm_get_moments: null argument");
+    if (!c->initialized) return fail(c, LBM_ERR_STATE, "lbm_get_moments before initialisation");
+    cudaSetDevice(c->cfg.device);
+    const size_t N = (size_t)c->N;
+    if (!c->d_rho_out) CU(c, cudaMalloc(&c->d_rho_out, N * 8));
+    if (!c->d_u_out) CU(c, cudaMalloc(&c->d_u_out, 3 * N * 8));
+    ReadOut o{};
+    o.rho = c->d_rho_out; o.u = c->d_u_out; o.mode = READ_MOMENTS;
+    lbm_status s = run_read(c, o);
+    if (s) return s;
+    if (rho) CU(c, cudaMemcpyAsync(rho, c->d_rho_out, N * 8, cudaMemcpyDeviceToHost, c->st));
+    if (u) CU(c, cudaMemcpyAsync(u, c->d_u_out, 3 * N * 8, cudaMemcpyDeviceToHost, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    return LBM_OK;
+}
+
+lbm_status lbm_get_populations(lbm_ctx* c, double* f) {
+    if (!c || !f) return fail(c, LBM_ERR_INVALID, "lbm_get_populations: null argument");
+    if (!c->initialized) return fail(c, LBM_ERR_STATE, "lbm_get_populations before initialisation");
+    cudaSetDevice(c->cfg.device);
+    const size_t N = (size_t)c->N;
+    double* d = nullptr;
+    CU(c, cudaMalloc(&d, 27 * N * 8));
+    ReadOut o{};
+    o.f = d; o.mode = READ_POPS;
+    lbm_status s = run_read(c, o);
+    if (!s) {
+        cudaError_t e = cudaMemcpyAsync(f, d, 27 * N * 8, cudaMemcpyDeviceToHost, c->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+        if (e != cudaSuccess) s = fail(c, LBM_ERR_CUDA, "populations copy: %s", cudaGetErrorString(e));
+    }
+    cudaFree(d);
+    return s;
+}
+
+lbm_status lbm_reduce(lbm_ctx* c, lbm_diag* out) {
+    if (!c || !out) return fail(c, LBM_ERR_INVALID, "lbm_reduce: null argument");
+    if (!c->initialized) return fail(c, LBM_ERR_STATE, "lbm_reduce before initialisation");
+    cudaSetDevice(c->cfg.device);
+    CU(c, cudaMemsetAsync(c->d_red, 0, RED_COUNT * sizeof(double), c->st));
+    ReadOut o{};
+    o.red = c->d_red; o.mode = READ_DIAG;
+    lbm_status s = run_read(c, o);
+    if (s) return s;
+    double h[RED_COUNT];
+    CU(c, cudaMemcpyAsync(h, c->d_red, sizeof(h), cudaMemcpyDeviceToHost, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    out->mass = h[RED_MASS];
+    out->momentum[0] = h[RED_MX]; out->momentum[1] = h[RED_MY]; out->momentum[2] = h[RED_MZ];
+    out->drag[0] = h[RED_DX]; out->drag[1] = h[RED_DY]; out->drag[2] = h[RED_DZ];
+    out->max_speed = h[RED_VMAX];
+    out->nonfinite = (int64_t)h[RED_BAD];
+    out->fluid_cells = (int64_t)h[RED_FLUID];
+    out->step = c->m;
+    if (out->nonfinite > 0) return fail(c, LBM_ERR_NONFINITE, "%lld cells hold non-finite populations at step %lld",
+                                        (long long)out->nonfinite, (long long)c->m);
+    return LBM_OK;
+}
+
+lbm_status lbm_error_evaluation(lbm_ctx* c, double* err) {
+    if (!c || !err) return fail(c, LBM_ERR_INVALID, "lbm_error_evaluation: null argument");
+    if (!c->initialized) return fail(c, LBM_ERR_STATE, "lbm_error_evaluation before initialisation");
+    cudaSetDevice(c->cfg.device);
+    const size_t N = (size_t)c->N;
+    if (!c->d_uerr) {
+        CU(c, cudaMalloc(&c->d_uerr, 3 * N * 8));
+        CU(c, cudaMemsetAsync(c->d_uerr, 0, 3 * N * 8, c->st));
+    }
+    CU(c, cudaMemsetAsync(c->d_red, 0, RED_COUNT * sizeof(double), c->st));
+    ReadOut o{};
+    o.red = c->d_red; o.uerr = c->d_uerr; o.mode = READ_ERROR;
+    lbm_status s = run_read(c, o);
+    if (s) return s;
+    double h[RED_COUNT];
+    CU(c, cudaMemcpyAsync(h, c->d_red, sizeof(h), cudaMemcpyDeviceToHost, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    *err = std::sqrt(h[RED_ERR1]) / std::sqrt(h[RED_ERR2]);
+    if (std::isnan(*err)) return fail(c, LBM_ERR_NONFINITE, "error monitor is NaN at step %lld", (long long)c->m);
+    return LBM_OK;
+}
+
+lbm_status lbm_timeavg_begin(lbm_ctx* c) {
+    if (!c) return fail(c, LBM_ERR_INVALID, "null ctx");
+    if (!c->initialized) return fail(c, LBM_ERR_STATE, "lbm_timeavg_begin before initialisation");
+    cudaSetDevice(c->cfg.device);
+    const size_t N = (size_t)c->N;
+    if (!c->d_acc) CU(c, cudaMalloc(&c->d_acc, 10 * N * 8));
+    CU(c, cudaMemsetAsync(c->d_acc, 0, 10 * N * 8, c->st));
+    c->avg_on = true;
+    c->avg_begin = c->m;
+    c->avg_last = c->m;
+    c->avg_count = 0;
+    return LBM_OK;
+}
+
+// accumulate the current state if it was produced inside the window and not counted yet
+static lbm_status avg_flush(lbm_ctx* c) {
+    if (c->avg_on && c->m > c->avg_begin && c->m > c->avg_last) {
+        ReadOut o{};
+        o.mode = READ_ACC;
+        lbm_status s = run_read(c, o);
+        if (s) return s;
+        c->avg_last = c->m;
+        c->avg_count++;
+    }
+    return LBM_OK;
+}
+
+lbm_status lbm_timeavg_end(lbm_ctx* c) {
+    if (!c) return fail(c, LBM_ERR_INVALID, "null ctx");
+    cudaSetDevice(c->cfg.device);
+    lbm_status s = avg_flush(c);
+    if (s) return s;
+    c->avg_on = false;
+    return LBM_OK;
+}
+
+lbm_status lbm_timeavg_get(lbm_ctx* c, double* rho, double* u, double* uu, int64_t* count) {
+    if (!c) return fail(c, LBM_ERR_INVALID, "null ctx");
+    if (!c->d_acc) return fail(c, LBM_ERR_STATE, "lbm_timeavg_get without lbm_timeavg_begin");
+    cudaSetDevice(c->cfg.device);
+    lbm_status s = avg_flush(c);
+    if (s) return s;
+    const size_t N = (size_t)c->N;
+    std::vector<double> h(10 * N);
+    CU(c, cudaMemcpyAsync(h.data(), c->d_acc, 10 * N * 8, cudaMemcpyDeviceToHost, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    const double n = c->avg_count > 0 ? (double)c->avg_count : 1.0;
+    for (size_t q = 0; q < N; q++) {
+        if (rho) rho[q] = h[q] / n;
+        if (u) for (int a = 0; a < 3; a++) u[a * N + q] = h[(1 + a) * N + q] / n;
+        if (uu) for (int a = 0; a < 6; a++) uu[a * N + q] = h[(4 + a) * N + q] / n;
+    }
+    if (count) *count = c->avg_count;
+    return LBM_OK;
+}
+
+// ---- checkpoint: raw state in storage precision, bit-identical resume ------------------------
+static const char kMagic[8] = {'L', 'B', 'M', 'G', 'B', '3', '0', '0'};
+
+lbm_status lbm_checkpoint_save(lbm_ctx* c, const char* path) {
+    if (!c || !path) return fail(c, LBM_ERR_INVALID, "lbm_checkpoint_save: null argument");
+    if (!c->initialized) return fail(c, LBM_ERR_STATE, "nothing to save before initialisation");
+    cudaSetDevice(c->cfg.device);
+    CU(c, cudaStreamSynchronize(c->st));
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) return fail(c, LBM_ERR_IO, "cannot open %s", path);
+    const size_t N = (size_t)c->N, rs = real_size(c);
+    auto put = [&](const void* p, size_t n) { return std::fwrite(p, 1, n, fp) == n; };
+    auto put_dev = [&](const void* d, size_t n) -> bool {
+        if (!n) return true;
+        std::vector<char> h(n);
+        if (cudaMemcpy(h.data(), d, n, cudaMemcpyDeviceToHost) != cudaSuccess) return false;
+        return put(h.data(), n);
+    };
+    int32_t ver = LBM_ABI_VERSION;
+    int64_t m = c->m, nin = (int64_t)c->inlets.size(), nout = (int64_t)c->outlets.size();
+    bool ok = put(kMagic, 8) && put(&ver, 4) && put(&c->cfg, sizeof(c->cfg)) && put(&m, 8) &&
+              put(c->flags.data(), N * 4) && put(&nin, 8) && put(c->inlets.data(), nin * sizeof(lbm_bc_inlet)) &&
+              put(&nout, 8) && put(c->outlets.data(), nout * sizeof(lbm_bc_outlet)) &&
+              put_dev(c->d_f, 27 * N * c->esize) &&
+              put_dev(c->d_lid_state, 3 * 27 * (size_t)c->n_lid * rs) &&
+              put_dev(c->d_in_probe, 9 * (size_t)c->n_in * rs) &&
+              put_dev(c->d_out_save, 36 * (size_t)c->n_out * rs);
+    std::fclose(fp);
+    if (!ok) return fail(c, LBM_ERR_IO, "writing %s failed", path);
+    return LBM_OK;
+}
+
+lbm_status lbm_checkpoint_load(lbm_ctx* c, const char* path) {
+    if (!c || !path) return fail(c, LBM_ERR_INVALID, "lbm_checkpoint_load: null argument");
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) return fail(c, LBM_ERR_IO, "cannot open %s", path);
+    auto get = [&](void* p, size_t n) { return std::fread(p, 1, n, fp) == n; };
+    char mg[8];
+    int32_t ver = 0;
+    lbm_config cfg;
+    int64_t m = 0, nin = 0, nout = 0;
+    if (!get(mg, 8) || std::memcmp(mg, kMagic, 8) != 0 || !get(&ver, 4) || ver != LBM_ABI_VERSION ||
+        !get(&cfg, sizeof(cfg)) || !get(&m, 8)) {
+        std::fclose(fp);
+        return fail(c, LBM_ERR_IO, "%s is not a checkpoint of this library version", path);
+    }
+    if (cfg.nx != c->cfg.nx || cfg.ny != c->cfg.ny || cfg.nz != c->cfg.nz || cfg.storage != c->cfg.storage) {
+        std::fclose(fp);
+        return fail(c, LBM_ERR_INVALID, "checkpoint lattice/storage differ from this context");
+    }
+    const size_t N = (size_t)c->N;
+    std::vector<int32_t> fl(N);
+    bool ok = get(fl.data(), N * 4) && get(&nin, 8);
+    std::vector<lbm_bc_inlet> in(ok ? (size_t)nin : 0);
+    ok = ok && get(in.data(), nin * sizeof(lbm_bc_inlet)) && get(&nout, 8);
+    std::vector<lbm_bc_outlet> out(ok ? (size_t)nout : 0);
+    ok = ok && get(out.data(), nout * sizeof(lbm_bc_outlet));
+    if (!ok) { std::fclose(fp); return fail(c, LBM_ERR_IO, "truncated checkpoint %s", path); }
+    int dev = c->cfg.device;
+    c->cfg = cfg;
+    c->cfg.device = dev;
+    c->flags = fl; c->inlets = in; c->outlets = out;
+    c->have_flags = true; c->have_geom = false;
+    cudaSetDevice(dev);
+    lbm_status s = build_geometry(c);
+    if (s) { std::fclose(fp); return s; }
+    const size_t rs = real_size(c);
+    auto get_dev = [&](void* d, size_t n) -> bool {
+        if (!n) return true;
+        std::vector<char> h(n);
+        if (!get(h.data(), n)) return false;
+        return cudaMemcpy(d, h.data(), n, cudaMemcpyHostToDevice) == cudaSuccess;
+    };
+    ok = get_dev(c->d_f, 27 * N * c->esize) && get_dev(c->d_lid_state, 81 * (size_t)c->n_lid * rs) &&
+         get_dev(c->d_in_probe, 9 * (size_t)c->n_in * rs) && get_dev(c->d_out_save, 36 * (size_t)c->n_out * rs);
+    std::fclose(fp);
+    if (!ok) return fail(c, LBM_ERR_IO, "reading %s failed", path);
+    c->m = m;
+    c->initialized = true;
+    c->avg_on = false;
+    return LBM_OK;
+}
+
+// ---- host mesher: geometryMesherBoundary::meshingBoundaryWall (geometryMesherBoundary.h:439-484)
+lbm_status lbm_mesher_wall_pass(int32_t* fl, int32_t nx, int32_t ny, int32_t nz) {
+    if (!fl || nx <= 0 || ny <= 0 || nz <= 0) return fail(nullptr, LBM_ERR_INVALID, "lbm_mesher_wall_pass: bad argument");
+    auto at = [&](int i, int j, int k) -> int32_t& { return fl[(size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k)]; };
+    for (int k = 0; k < nz; k++)
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++) {
+                if (at(i, j, k) <= 0) continue;
+                int add = 0;
+                for (int n = -1; n <= 1; n++)
+                    for (int mm = -1; mm <= 1; mm++)
+                        for (int l = -1; l <= 1; l++) {
+                            int a = i + l, b = j + mm, e = k + n;
+                            if (a >= 0 && b >= 0 && e >= 0 && a < nx && b < ny && e < nz && at(a, b, e) == 0) add++;
+                        }
+                at(i, j, k) += add;
+            }
+    return LBM_OK;
+}
+
+}  // extern "C"

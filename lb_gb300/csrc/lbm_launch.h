@@ -1,0 +1,32 @@
+// lbm_launch.h - host-side launchers of the device kernels, one set per storage type.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace lbm {
+
+struct Params;
+struct ReadOut;
+
+// returns cudaSuccess or the launch error
+template <class S>
+cudaError_t launch_step(const Params& p, int collision, int closure, cudaStream_t st);
+template <class S>
+cudaError_t launch_read(const Params& p, const ReadOut& o, cudaStream_t st);
+template <class S>
+cudaError_t launch_init(const Params& p, const double* rho, const double* u, double rho0, const double u0[3],
+                        const double* pops, cudaStream_t st);
+
+template <class S>
+cudaError_t launch_probe(const Params& p, int x, int y, int z, double* out, cudaStream_t st);
+
+inline dim3 cell_block(int nx) {
+    int b = nx >= 128 ? 128 : ((nx + 31) / 32) * 32;
+    return dim3(b, 1, 1);
+}
+inline dim3 cell_grid(int nx, int ny, int nz) {
+    dim3 b = cell_block(nx);
+    return dim3((nx + b.x - 1) / b.x, ny, nz);
+}
+
+}  // namespace lbm

@@ -1,0 +1,226 @@
+// voxelizer.cu - GPU point-in-polyhedron voxelizer for OFF meshes (C ABI in include/lbm.h).
+//
+// Replaces the reference preprocessor (3D/preprocess/src/geometry/geometryMesherOFF.h:45-112 with
+// geometryHandlerOFF.h:63-182), which asks a CGAL AABB tree, cell by cell on one host thread, for
+// the distinct intersection points of the segment [cell centre, outside point] and marks the cell
+// inside when their number is odd.  Here one GPU thread owns one (y, z) column of cells and casts a
+// +x ray through it: it collects the x of every triangle whose (y, z) projection contains the
+// column, and a cell is inside when an odd number of crossings lie before its x.  For a closed
+// mesh and a cell not on the surface both counts have the same parity, so the flags agree with the
+// reference; the grid (dimensions, float-rounded bounding box and sample points) follows the
+// reference arithmetic exactly.  Ties (a column through an edge or a vertex of the projection) use
+// a half-open rule on canonically ordered edges, so a shared edge is counted by exactly one of the
+// triangles that cross there and by none or both at a silhouette; the reference instead merges
+// coincident intersection points (|d|^2 <= 1e-10, geometryHandlerOFF.h:174).
+#include "../../include/lbm.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+namespace {
+
+bool next_data_line(std::istream& in, std::string& line) {
+    while (std::getline(in, line)) {
+        size_t h = line.find('#');
+        if (h != std::string::npos) line.resize(h);
+        if (line.find_first_not_of(" \t\r\n") != std::string::npos) return true;
+    }
+    return false;
+}
+
+// OFF / NOFF / COFF: header word containing "OFF", counts (same or next line), vertex lines whose
+// first three numbers are the position, face lines "n i0 .. i(n-1) [colour]" (fan-triangulated)
+bool read_off(const char* path, std::vector<double>& V, std::vector<int32_t>& T) {
+    std::ifstream in(path);
+    if (!in) return false;
+    std::string line;
+    if (!next_data_line(in, line)) return false;
+    std::istringstream hs(line);
+    std::string head;
+    hs >> head;
+    if (head.find("OFF") == std::string::npos) return false;
+    long nv = -1, nf = -1;
+    if (!(hs >> nv >> nf)) {
+        if (!next_data_line(in, line)) return false;
+        std::istringstream cs(line);
+        if (!(cs >> nv >> nf)) return false;
+    }
+    if (nv <= 0 || nf <= 0) return false;
+    V.resize(3 * (size_t)nv);
+    for (long i = 0; i < nv; i++) {
+        if (!next_data_line(in, line)) return false;
+        std::istringstream vs(line);
+        if (!(vs >> V[3 * i] >> V[3 * i + 1] >> V[3 * i + 2])) return false;
+    }
+    for (long f = 0; f < nf; f++) {
+        if (!next_data_line(in, line)) return false;
+        std::istringstream fs(line);
+        int k;
+        if (!(fs >> k) || k < 3) return false;
+        std::vector<int32_t> idx(k);
+        for (int a = 0; a < k; a++)
+            if (!(fs >> idx[a]) || idx[a] < 0 || idx[a] >= nv) return false;
+        for (int a = 1; a + 1 < k; a++) { T.push_back(idx[0]); T.push_back(idx[a]); T.push_back(idx[a + 1]); }
+    }
+    return true;
+}
+
+// prepared triangle: projected (y, z) vertices ordered counter-clockwise, x of each vertex
+struct Tri {
+    double y[3], z[3], x[3];
+};
+
+constexpr int kMaxCross = 256;
+constexpr int kTile = 256;
+
+// edge function of p against the edge (a -> b), evaluated on the canonically ordered endpoints so
+// that the reversed edge gives exactly the negated value
+__device__ __forceinline__ double edge_fn(double ay, double az, double by, double bz, double py, double pz,
+                                          bool& incl) {
+    bool swap = (ay > by) || (ay == by && az > bz);
+    double sy = swap ? by : ay, sz = swap ? bz : az, ty = swap ? ay : by, tz = swap ? az : bz;
+    double e = (ty - sy) * (pz - sz) - (tz - sz) * (py - sy);
+    // half-open rule: a point on the edge belongs to the side the directed edge "includes";
+    // d and -d never both include it
+    double dy = by - ay, dz = bz - az;
+    incl = (dz > 0) || (dz == 0 && dy > 0);
+    return swap ? -e : e;
+}
+
+__global__ void k_columns(const Tri* tris, int nt, const float* ys, const float* zs, const float* xs, int nx,
+                          int ny, int nz, int32_t* flags, int* overflow) {
+    __shared__ Tri sh[kTile];
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = col < ny * nz;
+    const int j = live ? col % ny : 0, k = live ? col / ny : 0;
+    const double py = ys[j], pz = zs[k];
+    double cross[kMaxCross];
+    int nc = 0;
+    for (int base = 0; base < nt; base += kTile) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < kTile && base + t < nt; t += blockDim.x) sh[t] = tris[base + t];
+        __syncthreads();
+        const int cnt = min(kTile, nt - base);
+        if (!live) continue;
+        for (int t = 0; t < cnt; t++) {
+            const Tri& T = sh[t];
+            bool i0, i1, i2;
+            const double e0 = edge_fn(T.y[1], T.z[1], T.y[2], T.z[2], py, pz, i0);  // opposite vertex 0
+            const double e1 = edge_fn(T.y[2], T.z[2], T.y[0], T.z[0], py, pz, i1);  // opposite vertex 1
+            const double e2 = edge_fn(T.y[0], T.z[0], T.y[1], T.z[1], py, pz, i2);  // opposite vertex 2
+            const bool in = (e0 > 0 || (e0 == 0 && i0)) && (e1 > 0 || (e1 == 0 && i1)) && (e2 > 0 || (e2 == 0 && i2));
+            if (!in) continue;
+            const double area = e0 + e1 + e2;
+            if (!(area > 0)) continue;
+            const double xc = (e0 * T.x[0] + e1 * T.x[1] + e2 * T.x[2]) / area;
+            if (nc < kMaxCross) cross[nc++] = xc;
+            else atomicExch(overflow, 1);
+        }
+    }
+    if (!live) return;
+    // insertion sort of the crossings, then parity along the column
+    for (int a = 1; a < nc; a++) {
+        double v = cross[a];
+        int b = a - 1;
+        while (b >= 0 && cross[b] > v) { cross[b + 1] = cross[b]; b--; }
+        cross[b + 1] = v;
+    }
+    int32_t* row = flags + (size_t)nx * ((size_t)j + (size_t)ny * k);
+    int q = 0;
+    for (int i = 0; i < nx; i++) {
+        const double px = xs[i];
+        while (q < nc && cross[q] < px) q++;
+        row[i] = q & 1;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+lbm_status lbm_voxelize_mesh(const double* verts, int32_t nv, const int32_t* tris, int32_t nt, double res, double add,
+                             int32_t* flags_out, int32_t dims_out[3], double bbox_out[6], int32_t device) {
+    if (!verts || !tris || nv <= 0 || nt <= 0 || !dims_out || !(res > 0) || add < 0) return LBM_ERR_INVALID;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int i = 0; i < nv; i++)
+        for (int a = 0; a < 3; a++) { lo[a] = std::min(lo[a], verts[3 * i + a]); hi[a] = std::max(hi[a], verts[3 * i + a]); }
+    // the reference keeps BB, resolution and additional factor as float (LBMConstants.h:9-19)
+    const float resf = (float)res, addf = (float)add;
+    float blo[3], bhi[3];
+    for (int a = 0; a < 3; a++) { blo[a] = (float)lo[a]; bhi[a] = (float)hi[a]; }
+    for (int a = 0; a < 3; a++) dims_out[a] = (int32_t)std::ceil((bhi[a] - blo[a]) * resf + 2 * addf);
+    if (bbox_out) for (int a = 0; a < 3; a++) { bbox_out[a] = blo[a]; bbox_out[3 + a] = bhi[a]; }
+    if (!flags_out) return LBM_OK;
+    const int nx = dims_out[0], ny = dims_out[1], nz = dims_out[2];
+    if (nx <= 0 || ny <= 0 || nz <= 0) return LBM_ERR_INVALID;
+    // sample coordinates (geometryMesherOFF.h:94-96, stored in float `lookx`)
+    std::vector<float> s[3];
+    for (int a = 0; a < 3; a++) {
+        s[a].resize(dims_out[a]);
+        for (int i = 0; i < dims_out[a]; i++)
+            s[a][i] = (float)(((double)i + 0.5 - (double)addf) / (double)resf + (double)blo[a]);
+    }
+    // prepare triangles: drop index errors, orient projections counter-clockwise
+    std::vector<Tri> T;
+    T.reserve(nt);
+    for (int t = 0; t < nt; t++) {
+        int i0 = tris[3 * t], i1 = tris[3 * t + 1], i2 = tris[3 * t + 2];
+        if (i0 < 0 || i1 < 0 || i2 < 0 || i0 >= nv || i1 >= nv || i2 >= nv) return LBM_ERR_INVALID;
+        Tri r;
+        int id[3] = {i0, i1, i2};
+        for (int a = 0; a < 3; a++) { r.x[a] = verts[3 * id[a]]; r.y[a] = verts[3 * id[a] + 1]; r.z[a] = verts[3 * id[a] + 2]; }
+        double ar = (r.y[1] - r.y[0]) * (r.z[2] - r.z[0]) - (r.z[1] - r.z[0]) * (r.y[2] - r.y[0]);
+        if (ar == 0) continue;  // parallel to the rays: never crossed
+        if (ar < 0) { std::swap(r.x[1], r.x[2]); std::swap(r.y[1], r.y[2]); std::swap(r.z[1], r.z[2]); }
+        T.push_back(r);
+    }
+    if (cudaSetDevice(device) != cudaSuccess) return LBM_ERR_CUDA;
+    Tri* dT = nullptr;
+    float *dy = nullptr, *dz = nullptr, *dx = nullptr;
+    int32_t* dflags = nullptr;
+    int* dovf = nullptr;
+    const size_t ncell = (size_t)nx * ny * nz;
+    lbm_status st = LBM_OK;
+    if (cudaMalloc(&dT, std::max<size_t>(1, T.size()) * sizeof(Tri)) != cudaSuccess ||
+        cudaMalloc(&dx, nx * 4) != cudaSuccess || cudaMalloc(&dy, ny * 4) != cudaSuccess ||
+        cudaMalloc(&dz, nz * 4) != cudaSuccess || cudaMalloc(&dflags, ncell * 4) != cudaSuccess ||
+        cudaMalloc(&dovf, 4) != cudaSuccess) {
+        st = LBM_ERR_OOM;
+    } else {
+        cudaMemcpy(dT, T.data(), T.size() * sizeof(Tri), cudaMemcpyHostToDevice);
+        cudaMemcpy(dx, s[0].data(), nx * 4, cudaMemcpyHostToDevice);
+        cudaMemcpy(dy, s[1].data(), ny * 4, cudaMemcpyHostToDevice);
+        cudaMemcpy(dz, s[2].data(), nz * 4, cudaMemcpyHostToDevice);
+        cudaMemset(dovf, 0, 4);
+        const int cols = ny * nz, bs = 128;
+        k_columns<<<(cols + bs - 1) / bs, bs>>>(dT, (int)T.size(), dy, dz, dx, nx, ny, nz, dflags, dovf);
+        int ovf = 0;
+        if (cudaGetLastError() != cudaSuccess || cudaMemcpy(&ovf, dovf, 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(flags_out, dflags, ncell * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = LBM_ERR_CUDA;
+        else if (ovf)
+            st = LBM_ERR_UNSUPPORTED;  // more than kMaxCross crossings on one column
+    }
+    cudaFree(dT); cudaFree(dx); cudaFree(dy); cudaFree(dz); cudaFree(dflags); cudaFree(dovf);
+    return st;
+}
+
+lbm_status lbm_voxelize_off(const char* path, double res, double add, const double outside[3], int32_t* flags_out,
+                            int32_t dims_out[3], double bbox_out[6], int32_t device) {
+    (void)outside;
+    if (!path || !dims_out) return LBM_ERR_INVALID;
+    std::vector<double> V;
+    std::vector<int32_t> T;
+    if (!read_off(path, V, T)) return LBM_ERR_IO;
+    return lbm_voxelize_mesh(V.data(), (int32_t)(V.size() / 3), T.data(), (int32_t)(T.size() / 3), res, add, flags_out,
+                             dims_out, bbox_out, device);
+}
+
+}  // extern "C"

@@ -1,0 +1,316 @@
+"""Host-side mirror of the reference's solver/plugin interface over the C ABI (include/lbm.h).
+
+The reference composes a solver from compile-time policy structs
+(3D/simulation/src/solvers/SolverTurbulentLES.h:67-82, chosen in 3D/simulation/main.cu:37-52):
+
+    SolverTurbulentLES<Model, Initialisation, Collision, Streaming, BounceBackWall, Symmetry,
+                       Periodic, Inlet, Outlet, Moments, Turbulence, Error, NonDim, TimeAvg>
+
+Here the same policy names are tags that select the fused kernel's operator.  `Solver` is the
+thin object over one lbm_ctx; `SolverTurbulentLES` keeps the reference's method names
+(convertToLattice, initializeSimulation, runSimulation).  Every call goes to the CUDA library;
+there is no CPU fallback.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .capi import check, lib
+
+
+# ---- policy tags (reference names) ---------------------------------------------------------------
+class D3Q27:                                    # models/D3Q27/D3Q27.h
+    numberOfDiscreteVelocities = 27
+
+
+class CollisionCumD3Q27Turbulent2015:           # collisions/CollisionCumD3Q27Turbulent2015.h
+    code = capi.LBM_COLLISION_CUMULANT2015
+
+
+class CollisionSRTTurbulent:                    # collisions/CollisionSRTTurbulent.h
+    code = capi.LBM_COLLISION_SRT
+
+
+class CollisionSRTLaminar(CollisionSRTTurbulent):          # same update with a global omega
+    pass
+
+
+class CollisionCumD3Q27Laminar(CollisionCumD3Q27Turbulent2015):
+    pass
+
+
+class OmegaLES:                                 # turbulence/OmegaLES.h
+    code = capi.LBM_CLOSURE_SMAGORINSKY
+
+
+class OmegaNo:                                  # turbulence/OmegaNo.h
+    code = capi.LBM_CLOSURE_NONE
+
+
+class StreamingAB:                              # streamings/StreamingAB.h (AA in place here)
+    pass
+
+
+class BounceBackWallHalf:                       # boundaryConditions/Wall/BounceBackWallHalf.h
+    pass
+
+
+class NoSymmetry:                               # boundaryConditions/Symmetry/NoSymmetry.h
+    pass
+
+
+class Periodic:                                 # boundaryConditions/Periodic/Periodic.h (index wrap here)
+    pass
+
+
+class NoPeriodic:
+    pass
+
+
+class InletVelocityMovingWall:                  # boundaryConditions/Inlet/InletVelocityMovingWall.h
+    code = capi.LBM_INLET_MOVING_WALL
+
+
+class InletVelocityEquilibrium:                 # boundaryConditions/Inlet/InletVelocityEquilibrium.h
+    code = capi.LBM_INLET_EQUILIBRIUM
+
+
+class OutletDensityInterpolated:                # boundaryConditions/Outlet/OutletDensityInterpolated.h
+    pass
+
+
+class MomentDensityVelocityN27:                 # moments/MomentDensityVelocityN27.h
+    pass
+
+
+class ErrorQuadratic:                           # errorEvaluations/ErrorQuadratic.h
+    pass
+
+
+class MomentTimeAvg:                            # moments/MomentTimeAvg.h
+    pass
+
+
+class InitializationEquilibriumConstVector:     # initializations/InitializationEquilibriumConstVector.h
+    pass
+
+
+class NonDimensiolnaliseFactorsVelocity:        # nonDimensionalisions/NonDimensiolnaliseFactorsVelocity.h
+    """Physical -> lattice conversion (:20-131).  tau = 3 nu_lb + 1/2 here; the reference writes
+    nu_lb/3 + 1/2 (:66), which `reference_tau` reproduces for comparison."""
+
+    @staticmethod
+    def factors(L_phys, nx, u_phys, U_lb, nu_phys, rho_phys):
+        Cl = L_phys / nx
+        Cu = u_phys / U_lb
+        Ct = Cl / Cu
+        nu_lb = nu_phys * Ct / Cl / Cl
+        return {"Cl": Cl, "Cu": Cu, "Ct": Ct, "Cm": rho_phys * Cl ** 3, "nu": nu_lb, "tau": 3.0 * nu_lb + 0.5,
+                "Re": u_phys * L_phys / nu_phys}
+
+    @staticmethod
+    def reference_tau(nu_lb):
+        return nu_lb / 3.0 + 0.5
+
+
+STORAGE = {"f64": capi.LBM_STORAGE_F64, "f32": capi.LBM_STORAGE_F32, "f16dev": capi.LBM_STORAGE_F16DEV}
+
+
+class Diag:
+    def __init__(self, d):
+        self.mass = d.mass
+        self.momentum = tuple(d.momentum)
+        self.drag = tuple(d.drag)
+        self.max_speed = d.max_speed
+        self.nonfinite = d.nonfinite
+        self.fluid_cells = d.fluid_cells
+        self.step = d.step
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Solver:
+    """One lattice on one GPU (one lbm_ctx)."""
+
+    def __init__(self, shape, collision=CollisionCumD3Q27Turbulent2015, turbulence=OmegaNo,
+                 inlet=InletVelocityMovingWall, storage="f32", nu=1.0 / 6.0, tau=0.0, cles=0.173,
+                 periodic=(0, 0, 0), force=(0.0, 0.0, 0.0), rho0=1.0, f16_scale_log2=10, device=0):
+        nx, ny, nz = shape
+        self.shape = (int(nx), int(ny), int(nz))
+        self.N = nx * ny * nz
+        self.cfg = capi.make_config(nx, ny, nz, periodic=periodic, collision=collision.code,
+                                    closure=turbulence.code, storage=STORAGE[storage],
+                                    inlet_kind=inlet.code, nu=nu, tau=tau, cles=cles, force=force,
+                                    rho0=rho0, f16_scale_log2=f16_scale_log2, device=device)
+        self._ctx = C.c_void_p()
+        check(lib().lbm_create(C.byref(self.cfg), C.byref(self._ctx)))
+
+    # -- lifecycle
+    def close(self):
+        if self._ctx:
+            lib().lbm_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, s):
+        return check(s, self._ctx)
+
+    # -- set-up
+    def set_flags(self, flags):
+        """flags: int32 array [z, y, x] in the reference encoding (0 solid, >0 fluid, -1, -2, -3)."""
+        f = np.ascontiguousarray(flags, dtype=np.int32).reshape(-1)
+        assert f.size == self.N
+        self._check(lib().lbm_set_flags(self._ctx, f.ctypes.data_as(C.POINTER(C.c_int32))))
+
+    def set_bc(self, inlets=(), outlets=()):
+        ni, no = len(inlets), len(outlets)
+        ai = (capi.LbmBcInlet * max(ni, 1))(*inlets)
+        ao = (capi.LbmBcOutlet * max(no, 1))(*outlets)
+        self._check(lib().lbm_set_bc(self._ctx, ai, ni, ao, no))
+
+    def init_equilibrium(self, rho0=1.0, u0=(0.0, 0.0, 0.0)):
+        u = np.asarray(u0, dtype=np.float64)
+        self._check(lib().lbm_init_equilibrium(self._ctx, float(rho0), _dp(u)))
+
+    def init_fields(self, rho, u):
+        r = np.ascontiguousarray(rho, dtype=np.float64).reshape(-1)
+        uu = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
+        self._check(lib().lbm_init_fields(self._ctx, _dp(r), _dp(uu)))
+
+    def set_populations(self, f):
+        a = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        self._check(lib().lbm_set_populations(self._ctx, _dp(a)))
+
+    # -- stepping
+    def step(self, n=1):
+        self._check(lib().lbm_step(self._ctx, int(n)))
+
+    def step_timed(self, n):
+        """n steps timed with CUDA events on the context's stream; returns milliseconds."""
+        ms = C.c_double(0)
+        self._check(lib().lbm_step_timed(self._ctx, int(n), C.byref(ms)))
+        return ms.value
+
+    def probe(self, x, y, z):
+        """(u_x, u_y, u_z, rho) of one cell, copied to the host."""
+        out = np.empty(4)
+        self._check(lib().lbm_probe(self._ctx, int(x), int(y), int(z), _dp(out)))
+        return out
+
+    def synchronize(self):
+        self._check(lib().lbm_synchronize(self._ctx))
+
+    # -- read-back
+    def moments(self):
+        rho = np.empty(self.N)
+        u = np.empty(3 * self.N)
+        self._check(lib().lbm_get_moments(self._ctx, _dp(rho), _dp(u)))
+        return rho, u.reshape(3, self.N)
+
+    def populations(self):
+        f = np.empty(27 * self.N)
+        self._check(lib().lbm_get_populations(self._ctx, _dp(f)))
+        return f.reshape(27, self.N)
+
+    def reduce(self, allow_nonfinite=False):
+        d = capi.LbmDiag()
+        s = lib().lbm_reduce(self._ctx, C.byref(d))
+        if s == capi.LBM_ERR_NONFINITE and allow_nonfinite:
+            return Diag(d)
+        self._check(s)
+        return Diag(d)
+
+    def error_evaluation(self):
+        e = C.c_double(0)
+        self._check(lib().lbm_error_evaluation(self._ctx, C.byref(e)))
+        return e.value
+
+    def timeavg_begin(self):
+        self._check(lib().lbm_timeavg_begin(self._ctx))
+
+    def timeavg_end(self):
+        self._check(lib().lbm_timeavg_end(self._ctx))
+
+    def timeavg_get(self):
+        r = np.empty(self.N)
+        u = np.empty(3 * self.N)
+        uu = np.empty(6 * self.N)
+        cnt = C.c_int64(0)
+        self._check(lib().lbm_timeavg_get(self._ctx, _dp(r), _dp(u), _dp(uu), C.byref(cnt)))
+        return r, u.reshape(3, self.N), uu.reshape(6, self.N), cnt.value
+
+    def checkpoint_save(self, path):
+        self._check(lib().lbm_checkpoint_save(self._ctx, str(path).encode()))
+
+    def checkpoint_load(self, path):
+        self._check(lib().lbm_checkpoint_load(self._ctx, str(path).encode()))
+
+
+class SolverTurbulentLES:
+    """Reference-shaped driver: SolverTurbulentLES<...>(Constants, Data) with the same method names
+    (SolverTurbulentLES.h:106-324).  `constants` is a dict of lattice-unit parameters."""
+
+    def __init__(self, Model=D3Q27, Initialisation=InitializationEquilibriumConstVector,
+                 Collision=CollisionCumD3Q27Turbulent2015, Streaming=StreamingAB,
+                 BounceBackWall=BounceBackWallHalf, Symmetry=NoSymmetry, Periodic_=NoPeriodic,
+                 Inlet=InletVelocityMovingWall, Outlet=OutletDensityInterpolated,
+                 Moments=MomentDensityVelocityN27, Turbulence=OmegaLES, Error=ErrorQuadratic,
+                 NonDim=NonDimensiolnaliseFactorsVelocity, TimeAvg=MomentTimeAvg, *, constants, data):
+        if Model is not D3Q27:
+            raise NotImplementedError("only D3Q27 is implemented")
+        if Symmetry is not NoSymmetry:
+            raise NotImplementedError("symmetry boundaries are not implemented")
+        self.C = constants
+        self.data = data
+        self.policies = dict(Collision=Collision, Turbulence=Turbulence, Inlet=Inlet)
+        self.solver = None
+
+    def convertToLattice(self, verbose=False):
+        return None  # constants are given in lattice units
+
+    def initializeSimulation(self, verbose=False):
+        c, d = self.C, self.data
+        self.solver = Solver(d["flags"].shape[::-1], collision=self.policies["Collision"],
+                             turbulence=self.policies["Turbulence"], inlet=self.policies["Inlet"],
+                             storage=c.get("storage", "f32"), nu=c["nu"], cles=c.get("CLES", 0.173),
+                             periodic=c.get("periodic", (0, 0, 0)), force=c.get("force", (0.0, 0.0, 0.0)))
+        self.solver.set_flags(d["flags"])
+        self.solver.set_bc(d.get("inlets", ()), d.get("outlets", ()))
+        self.solver.init_equilibrium(c.get("rho0", 1.0), c.get("VelocityInit", (0.0, 0.0, 0.0)))
+
+    def runSimulation(self):
+        c = self.C
+        it = int(c["iterations"])
+        navg = int(c.get("iterationsMomentAvg", 0))
+        err_every = int(c.get("err_every_it", 0))
+        errors = []
+        k = 0
+        while k < it:
+            if navg and k == it - navg:
+                self.solver.timeavg_begin()
+            n = it - k
+            if err_every:
+                n = min(n, err_every - (k % err_every) if k % err_every else err_every)
+            if navg and k < it - navg:
+                n = min(n, it - navg - k)
+            self.solver.step(n)
+            k += n
+            if err_every and k % err_every == 0:
+                errors.append((k, self.solver.error_evaluation()))
+        if navg:
+            self.solver.timeavg_end()
+        return errors

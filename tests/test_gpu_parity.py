@@ -1,0 +1,275 @@
+"""GPU kernels (through the C ABI) against the CPU oracle on the same seeded inputs.
+
+Tolerances (stated per test): FP64 GPU vs FP64 oracle <= 1e-12 relative; FP32 GPU vs FP32 oracle
+per-cell |du| <= 1e-5 of the velocity scale after 100 steps; FP16-deviation storage against the
+FP64 oracle with a bound set by the 2^-10 storage quantum.  Moments are compared, never raw
+populations (the AA layout stores shifted slots on odd steps).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from lb_gb300 import capi, cases
+from lb_gb300.solver import (CollisionCumD3Q27Turbulent2015, CollisionSRTTurbulent, InletVelocityEquilibrium,
+                             InletVelocityMovingWall, OmegaLES, OmegaNo, Solver)
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+COLL = {"cum": CollisionCumD3Q27Turbulent2015, "srt": CollisionSRTTurbulent}
+CLOS = {"smag": OmegaLES, "none": OmegaNo}
+
+
+def pair(shape, case, coll, clos, storage, prec, inlet=InletVelocityMovingWall, periodic=None, force=(0, 0, 0)):
+    periodic = case.get("periodic", (0, 0, 0)) if periodic is None else periodic
+    g = Solver(shape, collision=COLL[coll], turbulence=CLOS[clos], inlet=inlet, storage=storage, nu=case["nu"],
+               cles=0.17, periodic=periodic, force=force)
+    g.set_flags(case["flags"])
+    g.set_bc(case["inlets"], case["outlets"])
+    cfg = capi.make_config(*shape, periodic=periodic, collision=COLL[coll].code, closure=CLOS[clos].code,
+                           inlet_kind=inlet.code, nu=case["nu"], cles=0.17, force=force)
+    o = O.OracleSim(cfg, prec)
+    o.set_flags(case["flags"])
+    o.set_bc(case["inlets"], case["outlets"])
+    return g, o
+
+
+def init_both(g, o, case, rho0=1.0, u0=(0, 0, 0)):
+    if "rho" in case:
+        g.init_fields(case["rho"], case["u"])
+        o.init_fields(case["rho"], case["u"])
+    else:
+        g.init_equilibrium(rho0, u0)
+        o.init_equilibrium(rho0, u0)
+
+
+def compare(g, o, uscale, tol_rho, tol_u, mask=None):
+    rg, ug = g.moments()
+    ro, uo = o.moments()
+    if mask is not None:
+        rg, ro, ug, uo = rg[mask], ro[mask], ug[:, mask], uo[:, mask]
+    dr = np.abs(rg - ro).max()
+    du = np.abs(ug - uo).max() / uscale
+    assert dr <= tol_rho, (dr, tol_rho)
+    assert du <= tol_u, (du, tol_u)
+    return dr, du
+
+
+@pytest.mark.parametrize("coll,clos", [("cum", "smag"), ("cum", "none"), ("srt", "smag"), ("srt", "none")])
+def test_cavity_fp64_matches_oracle(built_lib, oracle_lib, coll, clos):
+    n = 20
+    c = cases.cavity(n, u_lid=0.05, re=400.0)
+    g, o = pair((n, n, n), c, coll, clos, "f64", 64)
+    init_both(g, o, c)
+    for _ in range(4):
+        g.step(25)
+        o.step(25)
+        compare(g, o, 0.05, 1e-12, 1e-12)
+
+
+@pytest.mark.parametrize("coll", ["cum", "srt"])
+def test_cavity_fp32_matches_oracle_fp32(built_lib, oracle_lib, coll):
+    n = 24
+    c = cases.cavity(n, u_lid=0.05, re=1000.0)
+    g, o = pair((n, n, n), c, coll, "smag", "f32", 32)
+    init_both(g, o, c)
+    g.step(100)
+    o.step(100)
+    compare(g, o, 0.05, 1e-5, 1e-5)
+
+
+def test_channel_periodic_force_fp64(built_lib, oracle_lib):
+    nx, ny, nz = 24, 14, 12
+    c = cases.channel(nx, ny, nz, re_tau=180.0, u_max=0.05, nu=0.01)
+    g, o = pair((nx, ny, nz), c, "cum", "smag", "f64", 64, force=c["force"])
+    init_both(g, o, c)
+    for _ in range(3):
+        g.step(33)
+        o.step(33)
+        compare(g, o, 0.05, 1e-12, 1e-12)
+
+
+def test_channel_srt_force_fp64(built_lib, oracle_lib):
+    nx, ny, nz = 16, 12, 10
+    c = cases.channel(nx, ny, nz, re_tau=120.0, u_max=0.04, nu=0.02)
+    g, o = pair((nx, ny, nz), c, "srt", "none", "f64", 64, force=c["force"])
+    init_both(g, o, c)
+    g.step(60)
+    o.step(60)
+    compare(g, o, 0.04, 1e-12, 1e-12)
+
+
+def small_body_case(nx=40, ny=16, nz=14):
+    body = np.zeros((6, 6, 6), bool)
+    body[1:5, 1:5, 1:5] = True
+    body[0, 2:4, 2:4] = True
+    return cases.body_in_channel(nx, ny, nz, u_in=0.04, rho_out=1.0, nu=0.02, body_flags=body, center=(12, 5, 4))
+
+
+@pytest.mark.parametrize("coll,clos", [("cum", "smag"), ("srt", "none")])
+def test_inlet_outlet_body_fp64(built_lib, oracle_lib, coll, clos):
+    c = small_body_case()
+    shape = (40, 16, 14)
+    g, o = pair(shape, c, coll, clos, "f64", 64, inlet=InletVelocityEquilibrium)
+    init_both(g, o, c, 1.0, (0.04, 0, 0))
+    for _ in range(4):
+        g.step(20)
+        o.step(20)
+        compare(g, o, 0.04, 1e-12, 1e-12)
+    dg = g.reduce()
+    do = o.diag()
+    assert abs(dg.mass - do.mass) <= 1e-10 * do.mass
+    for a in range(3):
+        assert abs(dg.drag[a] - do.drag[a]) <= 1e-11 * (abs(do.drag[0]) + 1e-12)
+        assert abs(dg.momentum[a] - do.momentum[a]) <= 1e-10 * (abs(do.momentum[0]) + 1e-12)
+    assert dg.fluid_cells == do.fluid_cells
+
+
+def test_inlet_outlet_fp32(built_lib, oracle_lib):
+    c = small_body_case()
+    shape = (40, 16, 14)
+    g, o = pair(shape, c, "cum", "smag", "f32", 32, inlet=InletVelocityEquilibrium)
+    init_both(g, o, c, 1.0, (0.04, 0, 0))
+    g.step(100)
+    o.step(100)
+    compare(g, o, 0.04, 1e-5, 1e-5)
+
+
+def test_fp16_deviation_storage_tracks_fp64(built_lib, oracle_lib):
+    n = 20
+    c = cases.cavity(n, u_lid=0.05, re=400.0)
+    g, o = pair((n, n, n), c, "cum", "smag", "f16dev", 64)
+    init_both(g, o, c)
+    g.step(100)
+    o.step(100)
+    rg, ug = g.moments()
+    ro, uo = o.moments()
+    fl = c["flags"].reshape(-1) != 0
+    rel = np.linalg.norm(ug[:, fl] - uo[:, fl]) / np.linalg.norm(uo[:, fl])
+    assert rel < 2e-3, rel
+    assert np.abs(rg[fl] - ro[fl]).max() < 2e-3
+
+
+def test_populations_fp64_match_oracle(built_lib, oracle_lib):
+    c = small_body_case()
+    shape = (40, 16, 14)
+    g, o = pair(shape, c, "cum", "smag", "f64", 64, inlet=InletVelocityEquilibrium)
+    init_both(g, o, c, 1.0, (0.04, 0, 0))
+    for n in (7, 8):  # odd and even step counts
+        g.step(n)
+        o.step(n)
+        fg = g.populations()
+        fo = o.populations()
+        assert np.abs(fg - fo).max() < 1e-13
+
+
+def test_timeavg_and_error_monitor_match_oracle(built_lib, oracle_lib):
+    n = 16
+    c = cases.cavity(n, u_lid=0.05, re=200.0)
+    g, o = pair((n, n, n), c, "cum", "smag", "f64", 64)
+    init_both(g, o, c)
+    g.step(10); o.step(10)
+    g.timeavg_begin(); o.timeavg_begin()
+    g.step(13); o.step(13)
+    eg, eo = g.error_evaluation(), o.error()
+    assert abs(eg - eo) <= 1e-10 * abs(eo)
+    g.step(7); o.step(7)
+    g.timeavg_end(); o.timeavg_end()
+    rg, ug, uug, cg = g.timeavg_get()
+    ro, uo, uuo, co = o.timeavg_get()
+    assert cg == co == 20
+    assert np.abs(rg - ro).max() < 1e-12 and np.abs(ug - uo).max() < 1e-13 and np.abs(uug - uuo).max() < 1e-14
+    eg, eo = g.error_evaluation(), o.error()
+    assert abs(eg - eo) <= 1e-10 * abs(eo)
+
+
+def test_checkpoint_resume_is_bit_identical(built_lib, tmp_path):
+    c = small_body_case()
+    shape = (40, 16, 14)
+    a = Solver(shape, inlet=InletVelocityEquilibrium, turbulence=OmegaLES, storage="f16dev", nu=c["nu"],
+               periodic=c["periodic"])
+    a.set_flags(c["flags"]); a.set_bc(c["inlets"], c["outlets"]); a.init_equilibrium(1.0, (0.04, 0, 0))
+    a.step(11)
+    p = tmp_path / "state.lbm"
+    a.checkpoint_save(p)
+    a.step(9)
+    fa = a.populations()
+    b = Solver(shape, inlet=InletVelocityEquilibrium, turbulence=OmegaLES, storage="f16dev", nu=c["nu"],
+               periodic=c["periodic"])
+    b.checkpoint_load(p)
+    b.step(9)
+    assert np.array_equal(b.populations(), fa)
+
+
+def test_nonfinite_is_reported(built_lib):
+    n = 10
+    c = cases.cavity(n)
+    s = Solver((n, n, n), storage="f32", nu=c["nu"])
+    s.set_flags(c["flags"]); s.set_bc(c["inlets"], [])
+    s.init_equilibrium()
+    f = s.populations()
+    f[5, 5 + n * (5 + n * 5)] = np.nan
+    s.set_populations(f)
+    d = s.reduce(allow_nonfinite=True)
+    assert d.nonfinite >= 1
+    with pytest.raises(capi.LbmError) as e:
+        s.reduce()
+    assert e.value.status == capi.LBM_ERR_NONFINITE
+
+
+def test_mass_conserved_periodic_box_fp64(built_lib):
+    n = 16
+    rng = np.random.default_rng(5)
+    N = n ** 3
+    s = Solver((n, n, n), turbulence=OmegaLES, storage="f64", nu=0.005, periodic=(1, 1, 1))
+    s.set_flags(np.ones((n, n, n), np.int32))
+    s.set_bc()
+    s.init_fields(1 + 0.01 * rng.standard_normal(N), 0.03 * rng.standard_normal((3, N)))
+    d0 = s.reduce()
+    s.step(50)
+    d1 = s.reduce()
+    assert abs(d1.mass - d0.mass) < 1e-10 * d0.mass
+    assert max(abs(d1.momentum[a] - d0.momentum[a]) for a in range(3)) < 1e-10
+
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_gpu_voxelizer_matches_reference_golden(built_lib):
+    import ctypes as C
+    g = np.load(os.path.join(GOLD, "backward_step_laminar.npz"))
+    d = tuple(int(v) for v in g["dims"])
+    ref = np.unpackbits(g["packed"])[: d[0] * d[1] * d[2]].reshape(d[2], d[1], d[0]).astype(np.int32)
+    dims = np.zeros(3, np.int32)
+    bbox = np.zeros(6)
+    out = np.zeros(ref.size, np.int32)
+    o = np.array([-1.0, -1.0, -1.0])
+    L = capi.lib()
+    rc = L.lbm_voxelize_off(os.path.join(GOLD, "BackwardStepLaminar.off").encode(), float(g["resolution"]),
+                            float(g["additional"]), o.ctypes.data_as(C.POINTER(C.c_double)),
+                            out.ctypes.data_as(C.POINTER(C.c_int32)), dims.ctypes.data_as(C.POINTER(C.c_int32)),
+                            bbox.ctypes.data_as(C.POINTER(C.c_double)), 0)
+    assert rc == 0
+    assert tuple(dims) == d
+    assert np.array_equal(out.reshape(ref.shape), ref)
+
+
+def test_gpu_voxelizer_matches_oracle_on_seeded_body(built_lib, oracle_lib):
+    import ctypes as C
+    v, f = cases.perturbed_icosphere(radius=9.0, subdiv=3, lmax=6, amp=0.15)
+    dims = np.zeros(3, np.int32)
+    bbox = np.zeros(6)
+    L = capi.lib()
+    vv = np.ascontiguousarray(v)
+    ff = np.ascontiguousarray(f)
+    args = (vv.ctypes.data_as(C.POINTER(C.c_double)), len(vv), ff.ctypes.data_as(C.POINTER(C.c_int32)), len(ff),
+            1.0, 2.0)
+    assert L.lbm_voxelize_mesh(*args, None, dims.ctypes.data_as(C.POINTER(C.c_int32)),
+                               bbox.ctypes.data_as(C.POINTER(C.c_double)), 0) == 0
+    out = np.zeros(int(dims.prod()), np.int32)
+    assert L.lbm_voxelize_mesh(*args, out.ctypes.data_as(C.POINTER(C.c_int32)),
+                               dims.ctypes.data_as(C.POINTER(C.c_int32)), bbox.ctypes.data_as(C.POINTER(C.c_double)), 0) == 0
+    ref, _ = O.voxelize_mesh(v, f, 1.0, 2.0, (-100.0, -90.0, -80.0))
+    assert out.reshape(ref.shape).sum() > 100
+    assert np.array_equal(out.reshape(ref.shape), ref)

@@ -1,0 +1,164 @@
+"""CPU tests of the oracle: pinned against the reference's golden voxel matrix and checked on
+known-answer properties of the solver hooks."""
+import os
+
+import numpy as np
+import pytest
+
+from lb_gb300 import capi, cases
+from oracle import oracle as O
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def golden():
+    g = np.load(os.path.join(GOLD, "backward_step_laminar.npz"))
+    d = tuple(int(v) for v in g["dims"])
+    flags = np.unpackbits(g["packed"])[: d[0] * d[1] * d[2]].reshape(d[2], d[1], d[0]).astype(np.int32)
+    return g, d, flags
+
+
+def test_golden_fixture_counts():
+    g, d, flags = golden()
+    assert d == (377, 52, 52)
+    assert int(flags.sum()) == 843750 == int(g["count_inside"])
+
+
+def test_oracle_voxelizer_matches_reference_golden(oracle_lib):
+    g, d, ref = golden()
+    flags, bbox = O.voxelize_off(os.path.join(GOLD, "BackwardStepLaminar.off"), float(g["resolution"]),
+                                 float(g["additional"]), (-1.0, -1.0, -1.0))
+    assert flags.shape == ref.shape
+    assert np.array_equal(flags, ref)
+    assert np.allclose(bbox[:3], g["bbmin"]) and np.allclose(bbox[3:], g["bbmax"])
+
+
+def test_oracle_voxelizer_outside_point_independent(oracle_lib):
+    # a closed mesh: the parity must not depend on the outside reference point
+    g, d, ref = golden()
+    flags, _ = O.voxelize_off(os.path.join(GOLD, "BackwardStepLaminar.off"), float(g["resolution"]),
+                              float(g["additional"]), (-37.0, 251.0, -13.0))
+    assert np.array_equal(flags, ref)
+
+
+W = np.array([8 / 27] + [2 / 27] * 6 + [1 / 54] * 12 + [1 / 216] * 8)
+CV = np.array([[0, 0, 0], [1, 0, 0], [-1, 0, 0], [0, 0, -1], [0, 0, 1], [0, -1, 0], [0, 1, 0], [1, 0, -1],
+               [-1, 0, 1], [1, 0, 1], [-1, 0, -1], [-1, -1, 0], [1, 1, 0], [0, 1, -1], [0, -1, 1], [-1, 1, 0],
+               [1, -1, 0], [0, 1, 1], [0, -1, -1], [-1, 1, -1], [1, -1, 1], [-1, -1, 1], [1, 1, -1], [1, -1, -1],
+               [-1, 1, 1], [-1, -1, -1], [1, 1, 1]])
+
+
+def feq(r, u):
+    cu = CV @ u
+    return W * r * (1 + 3 * cu + 4.5 * cu * cu - 1.5 * u @ u)
+
+
+@pytest.mark.parametrize("coll", [capi.LBM_COLLISION_SRT, capi.LBM_COLLISION_CUMULANT2015])
+def test_collision_conserves_mass_and_momentum(oracle_lib, coll):
+    rng = np.random.default_rng(1)
+    for _ in range(5):
+        u = rng.uniform(-0.05, 0.05, 3)
+        f = feq(1 + rng.uniform(-0.02, 0.02), u) * (1 + 0.02 * rng.standard_normal(27))
+        r = f.sum()
+        uu = CV.T @ f / r
+        out = O.collide_cell(f, r, uu, rng.uniform(0.6, 1.9), coll)
+        assert abs(out.sum() - f.sum()) < 1e-14
+        assert np.abs(CV.T @ out - CV.T @ f).max() < 1e-14
+
+
+def test_srt_equilibrium_is_fixed_point(oracle_lib):
+    u = np.array([0.03, -0.02, 0.01])
+    f = feq(1.03, u)
+    assert np.abs(O.collide_cell(f, 1.03, u, 1.3, capi.LBM_COLLISION_SRT) - f).max() < 1e-15
+
+
+def test_cumulant_relaxes_shear_stress(oracle_lib):
+    # omega = 1 sets the off-diagonal second cumulant to zero: <c_x c_y (f*)> = rho u_x u_y
+    rng = np.random.default_rng(3)
+    u = np.array([0.02, 0.01, -0.015])
+    f = feq(1.0, u) * (1 + 0.05 * rng.standard_normal(27))
+    r = f.sum()
+    uu = CV.T @ f / r
+    out = O.collide_cell(f, r, uu, 1.0, capi.LBM_COLLISION_CUMULANT2015)
+    pxy = (CV[:, 0] * CV[:, 1]) @ out
+    assert abs(pxy - r * uu[0] * uu[1]) < 1e-14
+
+
+def test_wall_pass_matches_oracle_and_numpy(oracle_lib, built_lib):
+    rng = np.random.default_rng(0)
+    f = (rng.random((9, 11, 13)) > 0.3).astype(np.int32)
+    a = O.wall_pass(f.copy())
+    b = cases.wall_pass_numpy(f)
+    c = cases.wall_pass(f.copy())
+    assert np.array_equal(a, b) and np.array_equal(a, c)
+
+
+def _box_sim(n, flags, periodic, **kw):
+    cfg = capi.make_config(*n, periodic=periodic, **kw)
+    s = O.OracleSim(cfg, 64)
+    s.set_flags(flags)
+    return s
+
+
+def test_ghost_plane_periodic_equals_index_wrap(oracle_lib):
+    """Periodic.h ghost planes (planes 1 and L+1 mirror each other, perIdx pointing across) on a
+    box wrapped in y, z == native wrap in x over the L interior planes."""
+    L, ny, nz = 10, 6, 5
+    rng = np.random.default_rng(7)
+    N = L * ny * nz
+    rho = 1 + 0.01 * rng.standard_normal(N)
+    u = 0.03 * rng.standard_normal((3, N))
+    # native wrap: planes 0..L-1
+    a = _box_sim((L, ny, nz), np.ones((nz, ny, L), np.int32), (1, 1, 1), nu=0.02,
+                 collision=capi.LBM_COLLISION_CUMULANT2015, closure=capi.LBM_CLOSURE_SMAGORINSKY)
+    a.init_fields(rho, u)
+    # ghost form: X = L + 3 planes: solid 0, periodic 1 (copy of plane L+1... see below), interior, solid last
+    X = L + 3
+    fl = np.ones((nz, ny, X), np.int32)
+    fl[:, :, 0] = 0
+    fl[:, :, -1] = 0
+    fl[:, :, 1] = -3
+    fl[:, :, L + 1] = -3
+    # plane p in the ghost lattice holds native plane (p-1) mod L; plane L+1 duplicates plane 1 (native 0)
+    rho_g = np.ones((nz, ny, X))
+    u_g = np.zeros((3, nz, ny, X))
+    r3 = rho.reshape(nz, ny, L)
+    u3 = u.reshape(3, nz, ny, L)
+    for p in range(1, L + 2):
+        rho_g[:, :, p] = r3[:, :, (p - 1) % L]
+        u_g[:, :, :, p] = u3[:, :, :, (p - 1) % L]
+    b = _box_sim((X, ny, nz), fl, (0, 1, 1), nu=0.02, collision=capi.LBM_COLLISION_CUMULANT2015,
+                 closure=capi.LBM_CLOSURE_SMAGORINSKY)
+    recs = []
+    for k in range(nz):
+        for j in range(ny):
+            recs.append([1, j, k, -1, 0, 0, L + 1, 0])    # plane 1, normal -x, copies from plane L+1
+            recs.append([L + 1, j, k, 1, 0, 0, 1, 0])     # plane L+1, normal +x, copies from plane 1
+    b.set_periodic_list(recs)
+    b.init_fields(rho_g.reshape(-1), u_g.reshape(3, -1))
+    for _ in range(6):
+        a.step(1)
+        b.step(1)
+        ra, ua = a.moments()
+        rb, ub = b.moments()
+        ra = ra.reshape(nz, ny, L)
+        rb = rb.reshape(nz, ny, X)[:, :, 1:L + 1]
+        assert np.abs(ra - rb).max() < 1e-13
+        assert np.abs(ua.reshape(3, nz, ny, L) - ub.reshape(3, nz, ny, X)[:, :, :, 1:L + 1]).max() < 1e-13
+
+
+def test_cavity_mass_conserved_and_lid_drives_flow(oracle_lib):
+    c = cases.cavity(12, u_lid=0.05, re=100.0)
+    cfg = capi.make_config(12, 12, 12, collision=capi.LBM_COLLISION_CUMULANT2015, nu=c["nu"])
+    s = O.OracleSim(cfg, 64)
+    s.set_flags(c["flags"])
+    s.set_bc(c["inlets"], [])
+    s.init_equilibrium(1.0, (0, 0, 0))
+    m0 = s.diag().mass
+    s.step(50)
+    d = s.diag()
+    rho, u = s.moments()
+    ux = u[0].reshape(12, 12, 12)
+    assert d.nonfinite == 0
+    assert ux[6, 10, 6] > 0.005          # flow under the lid moves with it
+    assert abs(d.mass - m0) / m0 < 1e-3  # moving-wall nodes exchange little mass
