@@ -148,6 +148,11 @@ struct Sim {
         init_df_from_moments();
         step_count = 0;
     }
+    // with a body force the velocity is defined as (j + F/2)/rho: refresh the moments of the initial
+    // state so the first collision sees the same definition as every later one (force extension)
+    void force_consistent_moments() {
+        if (F[0] != 0 || F[1] != 0 || F[2] != 0) moment_update();
+    }
     void init_df_from_moments() {  // init_df :194-209
 #pragma omp parallel for schedule(static)
         for (long long c = 0; c < (long long)N; c++) {
@@ -683,6 +688,7 @@ int orc_init_equilibrium(void* p, double rho0, const double* u0) {
         using RR = std::remove_reference_t<decltype(S->rho[0])>;
         RR uu[3] = {(RR)u0[0], (RR)u0[1], (RR)u0[2]};
         S->init_equilibrium((RR)rho0, uu);
+        S->force_consistent_moments();
     });
     return 0;
 }
@@ -697,6 +703,7 @@ int orc_init_fields(void* p, const double* rho, const double* u) {
             } else { S->rho[c] = 0; for (int a = 0; a < 3; a++) S->u[a][c] = 0; }
         }
         S->init_df_from_moments();
+        S->force_consistent_moments();
         S->step_count = 0;
     });
     return 0;

@@ -68,20 +68,33 @@ def test_cavity_fp64_matches_oracle(built_lib, oracle_lib, coll, clos):
         compare(g, o, 0.05, 1e-12, 1e-12)
 
 
-@pytest.mark.parametrize("coll", ["cum", "srt"])
-def test_cavity_fp32_matches_oracle_fp32(built_lib, oracle_lib, coll):
+@pytest.mark.parametrize("coll,re", [("cum", 1000.0), ("srt", 400.0), ("srt", 1000.0)])
+def test_cavity_fp32_matches_oracle_fp32(built_lib, oracle_lib, coll, re):
+    """FP32 parity after 100 steps at tau = 0.5036 / 0.509.  The FP32 oracle itself drifts
+    0.9-1.4e-5 (of u_lid) from the FP64 oracle here (rounding noise that over-relaxation at
+    tau -> 1/2 amplifies), so the bar is: GPU FP32 within 3e-5 of the FP32 oracle, and no farther
+    from the FP64 oracle than 1.5x the FP32 oracle's own distance (+1e-6)."""
     n = 24
-    c = cases.cavity(n, u_lid=0.05, re=1000.0)
+    c = cases.cavity(n, u_lid=0.05, re=re)
     g, o = pair((n, n, n), c, coll, "smag", "f32", 32)
+    _, o64 = pair((n, n, n), c, coll, "smag", "f64", 64)
     init_both(g, o, c)
+    o64.init_equilibrium(1.0, (0, 0, 0))
     g.step(100)
     o.step(100)
-    compare(g, o, 0.05, 1e-5, 1e-5)
+    o64.step(100)
+    compare(g, o, 0.05, 3e-5, 3e-5)
+    _, ug = g.moments()
+    _, uo = o.moments()
+    _, ut = o64.moments()
+    e_gpu = np.abs(ug - ut).max() / 0.05
+    e_orc = np.abs(uo - ut).max() / 0.05
+    assert e_gpu <= 1.5 * e_orc + 1e-6, (e_gpu, e_orc)
 
 
 def test_channel_periodic_force_fp64(built_lib, oracle_lib):
     nx, ny, nz = 24, 14, 12
-    c = cases.channel(nx, ny, nz, re_tau=180.0, u_max=0.05, nu=0.01)
+    c = cases.channel(nx, ny, nz, re_tau=3.0, u_max=0.05, nu=0.01)  # u_tau = 0.005, F = 4e-6
     g, o = pair((nx, ny, nz), c, "cum", "smag", "f64", 64, force=c["force"])
     init_both(g, o, c)
     for _ in range(3):
@@ -92,7 +105,7 @@ def test_channel_periodic_force_fp64(built_lib, oracle_lib):
 
 def test_channel_srt_force_fp64(built_lib, oracle_lib):
     nx, ny, nz = 16, 12, 10
-    c = cases.channel(nx, ny, nz, re_tau=120.0, u_max=0.04, nu=0.02)
+    c = cases.channel(nx, ny, nz, re_tau=2.0, u_max=0.04, nu=0.02)  # u_tau = 0.008, F = 1.3e-5
     g, o = pair((nx, ny, nz), c, "srt", "none", "f64", 64, force=c["force"])
     init_both(g, o, c)
     g.step(60)
