@@ -163,13 +163,11 @@ template <class S>
 __global__ void __launch_bounds__(128) k_init(Params p, const double* rho_f, const double* u_f, double rho0,
                                               double u0x, double u0y, double u0z, const double* pops) {
     using R = typename S::R;
-    using T = typename S::T;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= p.nx) return;
     Cell c;
     make_cell(p, x, blockIdx.y, blockIdx.z, c);
     const int cl = p.cls[c.idx] & CLS_MASK;
-    T* A = (T*)p.f;
     const long long N = p.N;
     R r = (R)rho0, ux = (R)u0x, uy = (R)u0y, uz = (R)u0z;
     if (rho_f) { r = (R)rho_f[c.idx]; ux = (R)u_f[c.idx]; uy = (R)u_f[N + c.idx]; uz = (R)u_f[2 * N + c.idx]; }
@@ -188,7 +186,7 @@ __global__ void __launch_bounds__(128) k_init(Params p, const double* rho_f, con
     });
     sfor<0, 27>([&](auto vc) {
         constexpr int V = decltype(vc)::value;
-        Codec<S>::enc(A, V * N + c.idx, f[V], wr_of<S>(V, p), p);
+        store_at<S, V>(p, V * N + c.idx, f[V]);
     });
     if (cl == CLS_LID) {
         const int id = p.aux[c.idx];

@@ -90,9 +90,31 @@ static Params make_params(const lbm_ctx* c) {
     p.cles18 = 18.0 * c->cfg.cles;
     p.nu = c->cfg.nu;
     for (int a = 0; a < 3; a++) p.F[a] = c->cfg.force[a];
+    p.tauf = (float)p.tau; p.cles18f = (float)p.cles18; p.nuf = (float)p.nu;
+    p.omega0 = 1.0 / p.tau;
+    p.omega0f = (float)p.omega0;
+    for (int a = 0; a < 3; a++) p.Ff[a] = (float)p.F[a];
+    p.has_force = (p.F[0] != 0.0 || p.F[1] != 0.0 || p.F[2] != 0.0) ? 1 : 0;
     p.rho0 = (float)c->cfg.rho0;
     p.scale = std::ldexp(1.0f, c->cfg.f16_scale_log2);
     p.inv_scale = std::ldexp(1.0f, -c->cfg.f16_scale_log2);
+    p.scale2 = make_float2(p.scale, p.scale);
+    p.inv_scale2 = make_float2(p.inv_scale, p.inv_scale);
+    // per-direction addresses of the fast path (bulk cells off the periodic seams)
+    const unsigned long long base = (unsigned long long)c->d_f, es = (unsigned long long)c->esize;
+    const long long nx = c->cfg.nx, nxy = (long long)c->cfg.nx * c->cfg.ny;
+    for (int v = 0; v < 27; v++) {
+        const int o = opp(v);
+        const long long off = cx(v) + cy(v) * nx + cz(v) * nxy;  // element offset of x + c_v
+        p.wr[v] = (float)(wgt(v) * c->cfg.rho0);
+        p.nwrs[v] = -(float)(wgt(v) * c->cfg.rho0) * p.scale;
+        p.wr2[v] = make_float2(p.wr[v], p.wr[v]);
+        p.nwrs2[v] = make_float2(p.nwrs[v], p.nwrs[v]);
+        p.rd_even[v] = base + (unsigned long long)(v * c->N) * es;
+        p.rd_odd[v] = base + (unsigned long long)(o * c->N - off) * es;
+        p.wr_even[v] = base + (unsigned long long)(o * c->N) * es;
+        p.wr_odd[v] = base + (unsigned long long)(v * c->N + off) * es;
+    }
     p.lid_state = c->d_lid_state; p.lid_n = c->d_lid_n; p.lid_u = c->d_lid_u; p.n_lid = c->n_lid;
     p.in_probe = c->d_in_probe; p.in_u = c->d_in_u; p.in_dir = c->d_in_dir; p.n_in = c->n_in;
     p.out_save = c->d_out_save; p.out_rho = c->d_out_rho; p.out_dir = c->d_out_dir; p.n_out = c->n_out;

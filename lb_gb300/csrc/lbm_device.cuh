@@ -15,7 +15,9 @@
 //       stored two steps earlier (3-level table);
 //   density-interpolated outlets (OutletDensityInterpolated.h:170-252) read the upstream cell's and
 //       their own post-collision values of the previous step from a 2-parity side table.
-// Periodicity is by index wrap.  The same gather serves the read-only kernels (moments, diagnostics).
+// Periodicity is by index wrap.  Bulk cells away from a periodic seam (almost all cells) take a
+// fast path: every access is one precomputed per-direction base address plus the cell index.
+// The same general gather serves the read-only kernels (moments, diagnostics, probe).
 #pragma once
 
 #include <cuda_fp16.h>
@@ -24,10 +26,12 @@
 #include <cstdint>
 #include <type_traits>
 
-namespace lbm {
-
 #define LBM_HD __host__ __device__ __forceinline__
 #define LBM_D __device__ __forceinline__
+
+#include "lbm_math.cuh"
+
+namespace lbm {
 
 // ---- cell class byte ---------------------------------------------------------------------------
 enum : uint8_t { CLS_SOLID = 0, CLS_BULK = 1, CLS_EDGE = 2, CLS_LID = 3, CLS_INLET = 4, CLS_OUTLET = 5 };
@@ -39,43 +43,11 @@ enum : uint8_t {
 };
 constexpr uint8_t CLS_MASK = 7;
 
-// ---- D3Q27 in the reference's order (models/D3Q27/D3Q27.h:81-124) ------------------------------
-LBM_HD constexpr int cx(int v) {
-    constexpr int t[27] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, -1, 1, 0, 0, -1, 1, 0, 0, -1, 1, -1, 1, 1, -1, -1, 1};
-    return t[v];
-}
-LBM_HD constexpr int cy(int v) {
-    constexpr int t[27] = {0, 0, 0, 0, 0, -1, 1, 0, 0, 0, 0, -1, 1, 1, -1, 1, -1, 1, -1, 1, -1, -1, 1, -1, 1, -1, 1};
-    return t[v];
-}
-LBM_HD constexpr int cz(int v) {
-    constexpr int t[27] = {0, 0, 0, -1, 1, 0, 0, -1, 1, 1, -1, 0, 0, -1, 1, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1, -1, 1};
-    return t[v];
-}
-LBM_HD constexpr int opp(int v) { return v == 0 ? 0 : ((v & 1) ? v + 1 : v - 1); }
-LBM_HD constexpr double wgt(int v) {
-    return (cx(v) * cx(v) + cy(v) * cy(v) + cz(v) * cz(v)) == 0   ? 8.0 / 27.0
-           : (cx(v) * cx(v) + cy(v) * cy(v) + cz(v) * cz(v)) == 1 ? 2.0 / 27.0
-           : (cx(v) * cx(v) + cy(v) * cy(v) + cz(v) * cz(v)) == 2 ? 1.0 / 54.0
-                                                                   : 1.0 / 216.0;
-}
+// velocity set, lane types and collision math: lbm_math.cuh
 // the 9 directions with c_x = -s (s = +1: outlet facing +x) as used by the outlet side table
-LBM_HD constexpr int outlet_dir(int s, int k) {
-    constexpr int neg[9] = {2, 8, 10, 11, 15, 19, 21, 24, 25};  // c_x = -1
-    constexpr int pos[9] = {1, 7, 9, 12, 16, 20, 22, 23, 26};   // c_x = +1
-    return s > 0 ? neg[k] : pos[k];
-}
-LBM_HD constexpr int outlet_slot(int v) {  // k with outlet_dir(+-1, k) == v
+LBM_HD constexpr int outlet_slot(int v) {  // k of direction v among the 9 with the same c_x
     constexpr int t[27] = {-1, 0, 0, -1, -1, -1, -1, 1, 1, 2, 2, 3, 3, -1, -1, 4, 4, -1, -1, 5, 5, 6, 6, 7, 7, 8, 8};
     return t[v];
-}
-
-template <int I, int N, class F>
-LBM_D void sfor(F&& f) {
-    if constexpr (I < N) {
-        f(std::integral_constant<int, I>{});
-        sfor<I + 1, N>(f);
-    }
 }
 
 // ---- storage types -------------------------------------------------------------------------------
@@ -94,7 +66,21 @@ struct Params {
     int m;                   // index of the state being consumed (steps done so far)
     double tau, cles18, nu;  // relaxation time, 18*CLES, lattice viscosity (inlet rho_b)
     double F[3];             // body force
+    float tauf, cles18f, nuf, Ff[3];  // the same in FP32 (no FP64 instruction on the FP32 path)
+    double omega0;           // 1/tau
+    float omega0f;
+    int has_force;
     float rho0, scale, inv_scale;  // FP16-deviation encoding
+    float wr[27];            // w_v rho0            (decode f = h 2^-s + w_v rho0)
+    float nwrs[27];          // -w_v rho0 2^s       (encode h = f 2^s - w_v rho0 2^s)
+    float2 wr2[27], nwrs2[27];  // the same as (x, x) pairs for the packed two-cell path
+    float2 scale2, inv_scale2;
+    // byte addresses of the 27 slot arrays for bulk cells off the periodic seams:
+    // element = base + idx
+    unsigned long long rd_even[27];  // A[v]                  (even read of direction v)
+    unsigned long long rd_odd[27];   // A[opp v] - off(c_v)   (odd read: cell x - c_v)
+    unsigned long long wr_even[27];  // A[opp v]              (even write of f*_v)
+    unsigned long long wr_odd[27];   // A[v] + off(c_v)       (odd write: cell x + c_v)
     // moving-wall nodes
     void* lid_state;         // [3][27][n_lid] of S::R
     const float* lid_n;      // [3][n_lid] outward normals
@@ -114,37 +100,44 @@ struct Params {
     double* acc;             // time-average accumulators [10][N] (nullptr: off)
 };
 
+// scalar parameters in the compute type
+template <class R> LBM_D R p_tau(const Params& p) { if constexpr (std::is_same<R, float>::value) return p.tauf; else return p.tau; }
+template <class R> LBM_D R p_cles18(const Params& p) { if constexpr (std::is_same<R, float>::value) return p.cles18f; else return p.cles18; }
+template <class R> LBM_D R p_nu(const Params& p) { if constexpr (std::is_same<R, float>::value) return p.nuf; else return p.nu; }
+template <class R> LBM_D R p_F(const Params& p, int a) { if constexpr (std::is_same<R, float>::value) return p.Ff[a]; else return p.F[a]; }
+
+// ---- population codecs ------------------------------------------------------------------------------
 template <class S>
 struct Codec;
 template <>
 struct Codec<StF64> {
-    LBM_D static double dec(const double* A, long long i, double, const Params&) { return A[i]; }
-    LBM_D static void enc(double* A, long long i, double v, double, const Params&) { A[i] = v; }
+    template <int V> LBM_D static double dec(const double* a, const Params&) { return *a; }
+    template <int V> LBM_D static void enc(double* a, double v, const Params&) { *a = v; }
 };
 template <>
 struct Codec<StF32> {
-    LBM_D static float dec(const float* A, long long i, float, const Params&) { return __ldg(A + i); }
-    LBM_D static void enc(float* A, long long i, float v, float, const Params&) { A[i] = v; }
+    template <int V> LBM_D static float dec(const float* a, const Params&) { return __ldg(a); }
+    template <int V> LBM_D static void enc(float* a, float v, const Params&) { *a = v; }
 };
 template <>
 struct Codec<StF16> {
     // f = w_v rho0 + h 2^-s, stored h = (f - w_v rho0) 2^s  (the FP16-deviation encoding)
-    LBM_D static float dec(const __half* A, long long i, float wr, const Params& p) {
-        return fmaf(__half2float(A[i]), p.inv_scale, wr);
+    template <int V> LBM_D static float dec(const __half* a, const Params& p) {
+        return fmaf(__half2float(__ldg(a)), p.inv_scale, p.wr[V]);
     }
-    LBM_D static void enc(__half* A, long long i, float v, float wr, const Params& p) {
-        A[i] = __float2half_rn((v - wr) * p.scale);
+    template <int V> LBM_D static void enc(__half* a, float v, const Params& p) {
+        *a = __float2half_rn(fmaf(v, p.scale, p.nwrs[V]));
     }
 };
 
 // ---- equilibrium (second-order polynomial of the reference, e.g. OmegaLES.h:275-294) ----------
 template <int V, class R>
 LBM_D R feq(R r, R ux, R uy, R uz, R u2) {
-    const R cu = (R)cx(V) * ux + (R)cy(V) * uy + (R)cz(V) * uz;
+    const R cu = V == 0 ? (R)0 : cdotu<V>(ux, uy, uz);
     return (R)wgt(V) * r * ((R)1 + (R)3 * cu + (R)4.5 * cu * cu - (R)1.5 * u2);
 }
 
-// ---- cell geometry: wrapped neighbour coordinates -----------------------------------------------
+// ---- cell geometry: wrapped neighbour coordinates (general path) ----------------------------------
 struct Cell {
     int x, y, z;
     long long idx;
@@ -167,7 +160,6 @@ LBM_D void make_cell(const Params& p, int x, int y, int z, Cell& c) {
     if (!p.wrap[1]) c.oob |= (y == 0 ? 4u : 0u) | (y == p.ny - 1 ? 8u : 0u);
     if (!p.wrap[2]) c.oob |= (z == 0 ? 16u : 0u) | (z == p.nz - 1 ? 32u : 0u);
 }
-// index of the cell at offset (dx,dy,dz) in {-1,0,1}^3
 template <int DX, int DY, int DZ>
 LBM_D long long nbr(const Cell& c) { return c.X[DX + 1] + c.Y[DY + 1] + c.Z[DZ + 1]; }
 template <int DX, int DY, int DZ>
@@ -178,13 +170,43 @@ LBM_D bool nbr_oob(const Cell& c) {
     if (DZ < 0) m |= 16u; if (DZ > 0) m |= 32u;
     return (c.oob & m) != 0;
 }
+// true when a neighbour index of (x,y,z) wraps across a periodic seam
+LBM_D bool on_seam(const Params& p, int x, int y, int z) {
+    return (p.wrap[0] && (x == 0 || x == p.nx - 1)) || (p.wrap[1] && (y == 0 || y == p.ny - 1)) ||
+           (p.wrap[2] && (z == 0 || z == p.nz - 1));
+}
 
 // level of a 3-level side table for step index k (k may be -1 or -2)
 LBM_D int lvl3(int k) { return ((k % 3) + 3) % 3; }
 
-template <class S>
-LBM_D typename S::R wr_of(int v, const Params& p) {
-    if constexpr (S::kind == 2) return (float)wgt(v) * p.rho0; else return (typename S::R)0;
+template <class S, int V>
+LBM_D typename S::R load_at(const Params& p, long long e) {
+    return Codec<S>::template dec<V>((const typename S::T*)p.f + e, p);
+}
+template <class S, int V>
+LBM_D void store_at(const Params& p, long long e, typename S::R v) {
+    Codec<S>::template enc<V>((typename S::T*)p.f + e, v, p);
+}
+
+// ---- fast path: bulk cells off the seams ----------------------------------------------------------
+template <class S, bool ODD>
+LBM_D void load_fast(const Params& p, unsigned idx, typename S::R (&f)[27]) {
+    using T = typename S::T;
+    sfor<0, 27>([&](auto vc) {
+        constexpr int V = decltype(vc)::value;
+        // ODD reads slot opp(V) of cell x - c_V; even reads slot V of the cell itself
+        const T* a = (const T*)(ODD ? p.rd_odd[V] : p.rd_even[V]) + idx;
+        f[V] = Codec<S>::template dec<ODD ? opp(V) : V>(a, p);
+    });
+}
+template <class S, bool ODD>
+LBM_D void store_fast(const Params& p, unsigned idx, const typename S::R (&f)[27]) {
+    using T = typename S::T;
+    sfor<0, 27>([&](auto vc) {
+        constexpr int V = decltype(vc)::value;
+        T* a = (T*)(ODD ? p.wr_odd[V] : p.wr_even[V]) + idx;
+        Codec<S>::template enc<ODD ? V : opp(V)>(a, f[V], p);
+    });
 }
 
 // ---- gather: the pre-collision populations df_m(x, .) of a non-solid, non-inlet cell ----------
@@ -192,8 +214,6 @@ LBM_D typename S::R wr_of(int v, const Params& p) {
 template <class S, bool ODD, bool DRAG>
 LBM_D void gather(const Params& p, const Cell& c, int cl, typename S::R (&f)[27], typename S::R (&drag)[3]) {
     using R = typename S::R;
-    using T = typename S::T;
-    const T* A = (const T*)p.f;
     const long long N = p.N;
     if (cl == CLS_LID) {
         const R* st = (const R*)p.lid_state + (long long)lvl3(p.m) * 27 * p.n_lid;
@@ -205,9 +225,8 @@ LBM_D void gather(const Params& p, const Cell& c, int cl, typename S::R (&f)[27]
         // plain AA read; at m = 0 every cell reads its own (initial) slots
         sfor<0, 27>([&](auto vc) {
             constexpr int V = decltype(vc)::value;
-            const R wr = wr_of<S>(V, p);
-            if (ODD) f[V] = Codec<S>::dec(A, opp(V) * N + nbr<-cx(V), -cy(V), -cz(V)>(c), wr, p);
-            else     f[V] = Codec<S>::dec(A, V * N + c.idx, wr, p);
+            if (ODD) f[V] = load_at<S, opp(V)>(p, opp(V) * N + nbr<-cx(V), -cy(V), -cz(V)>(c));
+            else     f[V] = load_at<S, V>(p, V * N + c.idx);
         });
         return;
     }
@@ -215,19 +234,16 @@ LBM_D void gather(const Params& p, const Cell& c, int cl, typename S::R (&f)[27]
     const int osgn = (cl == CLS_OUTLET) ? p.out_dir[p.aux[c.idx]] : 0;
     sfor<0, 27>([&](auto vc) {
         constexpr int V = decltype(vc)::value;
-        const R wr = wr_of<S>(V, p);
         if (osgn != 0 && cx(V) == -osgn) { f[V] = (R)0; return; }  // interpolated below
-        if (V == 0 || nbr_oob<-cx(V), -cy(V), -cz(V)>(c)) {
-            // rest population, or a link leaving the box (rejected at set-up): own/plain read
-            if (ODD) f[V] = V == 0 ? Codec<S>::dec(A, c.idx, wr, p) : (R)0;
-            else     f[V] = Codec<S>::dec(A, V * N + c.idx, wr, p);
+        if (nbr_oob<-cx(V), -cy(V), -cz(V)>(c)) {  // a link from outside the box (rejected at set-up)
+            f[V] = (R)0;
             return;
         }
         const long long nb = nbr<-cx(V), -cy(V), -cz(V)>(c);
         const int ncl = p.cls[nb] & CLS_MASK;
         if (ncl == CLS_SOLID) {
             // half-way bounce-back: f_v(x) = f*_{opp v}(x) of the previous step
-            R b = ODD ? Codec<S>::dec(A, V * N + c.idx, wr, p) : Codec<S>::dec(A, opp(V) * N + nb, wr, p);
+            R b = ODD ? load_at<S, V>(p, V * N + c.idx) : load_at<S, opp(V)>(p, opp(V) * N + nb);
             f[V] = b;
             if (DRAG) {  // fluid momentum lost through the link: b*c_{opp v} - b*c_v = -2 b c_v
                 drag[0] -= (R)(2 * cx(V)) * b; drag[1] -= (R)(2 * cy(V)) * b; drag[2] -= (R)(2 * cz(V)) * b;
@@ -240,13 +256,14 @@ LBM_D void gather(const Params& p, const Cell& c, int cl, typename S::R (&f)[27]
             const R* pr = (const R*)p.in_probe + (long long)lvl3(p.m - 2) * 3 * p.n_in;
             const R r1 = pr[id], ux1 = pr[p.n_in + id], ux2 = pr[2 * p.n_in + id];
             const R ub0 = p.in_u[id], ub1 = p.in_u[p.n_in + id], ub2 = p.in_u[2 * p.n_in + id];
+            const R nu3 = p_nu<R>(p) / (R)3;
             R rb;
-            if (p.in_dir[id] > 0) rb = r1 + (R)p.nu / (R)3 * ((ux1 - ux2) - (ub0 - ux1));
-            else                  rb = r1 + (R)p.nu / (R)3 * ((ux1 - ub0) - (ux2 - ux1));
+            if (p.in_dir[id] > 0) rb = r1 + nu3 * ((ux1 - ux2) - (ub0 - ux1));
+            else                  rb = r1 + nu3 * ((ux1 - ub0) - (ux2 - ux1));
             f[V] = feq<V>(rb, ub0, ub1, ub2, ub0 * ub0 + ub1 * ub1 + ub2 * ub2);
         } else {
-            if (ODD) f[V] = Codec<S>::dec(A, opp(V) * N + nb, wr, p);
-            else     f[V] = Codec<S>::dec(A, V * N + c.idx, wr, p);
+            if (ODD) f[V] = load_at<S, opp(V)>(p, opp(V) * N + nb);
+            else     f[V] = load_at<S, V>(p, V * N + c.idx);
         }
     });
     if (osgn != 0) {
@@ -281,6 +298,20 @@ LBM_D void gather(const Params& p, const Cell& c, int cl, typename S::R (&f)[27]
     }
 }
 
+// general scatter of the post-collision populations (EDGE/OUTLET cells, seams)
+template <class S, bool ODD>
+LBM_D void scatter(const Params& p, const Cell& c, const typename S::R (&f)[27]) {
+    const long long N = p.N;
+    sfor<0, 27>([&](auto vc) {
+        constexpr int V = decltype(vc)::value;
+        if (ODD) {
+            if (!nbr_oob<cx(V), cy(V), cz(V)>(c)) store_at<S, V>(p, V * N + nbr<cx(V), cy(V), cz(V)>(c), f[V]);
+        } else {
+            store_at<S, opp(V)>(p, opp(V) * N + c.idx, f[V]);
+        }
+    });
+}
+
 // state df_m of an equilibrium-inlet node: f_eq(u_b, rho_b) with rho_b from the probe moments of
 // step m-1 (InletVelocityEquilibrium.h:148-160 run at the end of step m-1)
 template <class S>
@@ -290,284 +321,25 @@ LBM_D void inlet_state(const Params& p, const Cell& c, typename S::R (&f)[27]) {
     const R* pr = (const R*)p.in_probe + (long long)lvl3(p.m - 1) * 3 * p.n_in;
     const R r1 = pr[id], ux1 = pr[p.n_in + id], ux2 = pr[2 * p.n_in + id];
     const R ub0 = p.in_u[id], ub1 = p.in_u[p.n_in + id], ub2 = p.in_u[2 * p.n_in + id];
+    const R nu3 = p_nu<R>(p) / (R)3;
     R rb;
-    if (p.in_dir[id] > 0) rb = r1 + (R)p.nu / (R)3 * ((ux1 - ux2) - (ub0 - ux1));
-    else                  rb = r1 + (R)p.nu / (R)3 * ((ux1 - ub0) - (ux2 - ux1));
+    if (p.in_dir[id] > 0) rb = r1 + nu3 * ((ux1 - ux2) - (ub0 - ux1));
+    else                  rb = r1 + nu3 * ((ux1 - ub0) - (ux2 - ux1));
     const R u2 = ub0 * ub0 + ub1 * ub1 + ub2 * ub2;
     sfor<0, 27>([&](auto vc) { constexpr int V = decltype(vc)::value; f[V] = feq<V>(rb, ub0, ub1, ub2, u2); });
 }
 
-// ---- moments in the reference's summation order (MomentDensityVelocityN27.h:212-228) ----------
+// ---- moments of a gathered cell for the read-only kernels ------------------------------------------
+// rho and u as the reference's moment pass defines them (MomentDensityVelocityN27.h:212-228),
+// with the half-force velocity shift
 template <class R>
 LBM_D void moments(const R (&f)[27], const Params& p, R& rho, R& jx, R& jy, R& jz, R& ux, R& uy, R& uz) {
-    rho = 0; jx = 0; jy = 0; jz = 0;
-    sfor<0, 27>([&](auto vc) { constexpr int V = decltype(vc)::value; rho += f[V]; });
-    sfor<0, 27>([&](auto vc) {
-        constexpr int V = decltype(vc)::value;
-        if (cx(V)) jx += (R)cx(V) * f[V];
-        if (cy(V)) jy += (R)cy(V) * f[V];
-        if (cz(V)) jz += (R)cz(V) * f[V];
-    });
-    const R ri = (R)1 / rho;
-    ux = (jx + (R)0.5 * (R)p.F[0]) * ri;
-    uy = (jy + (R)0.5 * (R)p.F[1]) * ri;
-    uz = (jz + (R)0.5 * (R)p.F[2]) * ri;
-}
-
-// ---- raw second moments via z-, y-, x-pair sums ----------------------------------------------------
-template <class R>
-LBM_D void second_moments(const R (&f)[27], R& Mxx, R& Myy, R& Mzz, R& Mxy, R& Mxz, R& Myz) {
-    R xx = 0, yy = 0, zz = 0, xy = 0, xz = 0, yz = 0;
-    sfor<0, 27>([&](auto vc) {
-        constexpr int V = decltype(vc)::value;
-        if (cx(V)) xx += f[V];
-        if (cy(V)) yy += f[V];
-        if (cz(V)) zz += f[V];
-        if (cx(V) * cy(V)) xy += (R)(cx(V) * cy(V)) * f[V];
-        if (cx(V) * cz(V)) xz += (R)(cx(V) * cz(V)) * f[V];
-        if (cy(V) * cz(V)) yz += (R)(cy(V) * cz(V)) * f[V];
-    });
-    Mxx = xx; Myy = yy; Mzz = zz; Mxy = xy; Mxz = xz; Myz = yz;
-}
-
-// ---- relaxation rate ----------------------------------------------------------------------------
-// Smagorinsky (OmegaLES.h:312-357): Pi = sum c c (f - f_eq) = M - rho (u u + I/3),
-// tau_LES = tau/2 + sqrt(tau^2 + 18 CLES |Pi| / rho)/2
-template <class R, int CLOS>
-LBM_D R relax_rate(const Params& p, R rho, R ux, R uy, R uz, R Mxx, R Myy, R Mzz, R Mxy, R Mxz, R Myz) {
-    const R tau = (R)p.tau;
-    if constexpr (CLOS == 0) {
-        return (R)1 / tau;
-    } else {
-        const R third = rho * ((R)1 / (R)3);
-        const R pxx = Mxx - rho * ux * ux - third, pyy = Myy - rho * uy * uy - third, pzz = Mzz - rho * uz * uz - third;
-        const R pxy = Mxy - rho * ux * uy, pxz = Mxz - rho * ux * uz, pyz = Myz - rho * uy * uz;
-        const R PI2 = pxx * pxx + pyy * pyy + pzz * pzz + (R)2 * (pxy * pxy + pxz * pxz + pyz * pyz);
-        const R PI = sqrt(PI2);
-        const R tles = tau * (R)0.5 + (R)0.5 * sqrt(tau * tau + (R)p.cles18 / rho * PI);
-        return (R)1 / tles;
-    }
-}
-
-// ---- SRT (CollisionSRTTurbulent.h:386-391), Guo forcing when F != 0 --------------------------------
-template <class R>
-LBM_D void collide_srt(R (&f)[27], const Params& p, R rho, R ux, R uy, R uz, R om, bool force) {
-    const R u2 = ux * ux + uy * uy + uz * uz;
-    const R gf = (R)1 - (R)0.5 * om;
-    const R Fx = (R)p.F[0], Fy = (R)p.F[1], Fz = (R)p.F[2];
-    sfor<0, 27>([&](auto vc) {
-        constexpr int V = decltype(vc)::value;
-        R out = f[V] - (f[V] - feq<V>(rho, ux, uy, uz, u2)) * om;
-        if (force) {
-            const R cu = (R)cx(V) * ux + (R)cy(V) * uy + (R)cz(V) * uz;
-            const R s = ((R)3 * ((R)cx(V) - ux) + (R)9 * cu * (R)cx(V)) * Fx +
-                        ((R)3 * ((R)cy(V) - uy) + (R)9 * cu * (R)cy(V)) * Fy +
-                        ((R)3 * ((R)cz(V) - uz) + (R)9 * cu * (R)cz(V)) * Fz;
-            out += gf * (R)wgt(V) * s;
-        }
-        f[V] = out;
-    });
-}
-
-// ---- cumulant collision, Geier 2015 with omega_2..omega_10 = 1 -----------------------------------
-// Same operator as CollisionCumD3Q27Turbulent2015.h:80-485, written in closed form: with all higher
-// relaxation rates equal to one, every post-collision cumulant above second order is zero, so only
-// the second-order central moments are needed from the forward transform and the backward
-// (chimera, G2015 eq. 88-96) transform takes the products of eq. 81-84.
-template <class R>
-LBM_D void tri_bwd(R k0, R k1, R k2, R u, R A, R B, R onemu2, R& m, R& z, R& p) {
-    // (k0,k1,k2) central moments along one axis -> populations (m, 0, p) of that axis
-    m = k0 * A + k1 * B + (R)0.5 * k2;   // 0.5 (k0 (u^2-u) + k1 (2u-1) + k2)
-    p = m + k0 * u + k1;                  // 0.5 (k0 (u^2+u) + k1 (2u+1) + k2)
-    z = k0 * onemu2 - (R)2 * u * k1 - k2;
-}
-
-template <class R>
-LBM_D void collide_cum15(R (&f)[27], R rho, R jx, R jy, R jz, R ux, R uy, R uz, R om,
-                         R Mxx, R Myy, R Mzz, R Mxy, R Mxz, R Myz) {
-    const R ri = (R)1 / rho;
-    // central moments (k_100 = j_x - rho u_x carries the half-force shift, G2015 eq. 85-87)
-    const R k100 = jx - rho * ux, k010 = jy - rho * uy, k001 = jz - rho * uz;
-    const R C200 = Mxx + ux * (rho * ux - (R)2 * jx);
-    const R C020 = Myy + uy * (rho * uy - (R)2 * jy);
-    const R C002 = Mzz + uz * (rho * uz - (R)2 * jz);
-    const R C110 = Mxy - ux * jy - uy * jx + rho * ux * uy;
-    const R C101 = Mxz - ux * jz - uz * jx + rho * ux * uz;
-    const R C011 = Myz - uy * jz - uz * jy + rho * uy * uz;
-    // relaxation, G2015 eq. 55-63 with omega_2 = 1
-    const R h = (R)0.5 * ri;
-    const R Dxu = -om * h * ((R)2 * C200 - C020 - C002) - h * (C200 + C020 + C002 - rho);
-    const R Dyv = Dxu + (R)3 * om * h * (C200 - C020);
-    const R Dzw = Dxu + (R)3 * om * h * (C200 - C002);
-    const R o1 = (R)1 - om;
-    const R a = (R)3 * rho * ((R)1 - om * (R)0.5);
-    const R xD = ux * ux * Dxu, yD = uy * uy * Dyv, zD = uz * uz * Dzw;
-    const R E61 = o1 * (C200 - C020) - a * (xD - yD);
-    const R E64 = o1 * (C200 - C002) - a * (xD - zD);
-    const R E65 = rho - (R)1.5 * rho * (xD + yD + zD);
-    const R t3 = (R)1 / (R)3;
-    const R s200 = t3 * (E61 + E64 + E65);
-    const R s020 = t3 * (E64 - (R)2 * E61 + E65);
-    const R s002 = t3 * (E61 - (R)2 * E64 + E65);
-    const R s110 = o1 * C110, s101 = o1 * C101, s011 = o1 * C011;
-    // post-collision central moments from cumulants (G2015 eq. 81-84; third order and the
-    // relaxed higher cumulants are zero)
-    const R q211 = (s200 * s011 + (R)2 * s101 * s110) * ri;
-    const R q121 = (s020 * s101 + (R)2 * s110 * s011) * ri;
-    const R q112 = (s002 * s110 + (R)2 * s011 * s101) * ri;
-    const R q220 = (s020 * s200 + (R)2 * s110 * s110) * ri;
-    const R q022 = (s002 * s020 + (R)2 * s011 * s011) * ri;
-    const R q202 = (s200 * s002 + (R)2 * s101 * s101) * ri;
-    const R q222 = (s200 * q022 + s020 * q202 + s002 * q220 + (R)4 * (s011 * q211 + s101 * q121 + s110 * q112)) * ri -
-                   ((R)16 * s110 * s101 * s011 +
-                    (R)4 * (s101 * s101 * s020 + s011 * s011 * s200 + s110 * s110 * s002) +
-                    (R)2 * s200 * s020 * s002) * ri * ri;
-    const R q100 = -k100, q010 = -k010, q001 = -k001;
-    // backward chimera transform: x pass (9 triplets over (oy, oz)), then y, then z
-    const R Ax = (R)0.5 * (ux * ux - ux), Bx = ux - (R)0.5, Cx = (R)1 - ux * ux;
-    const R Ay = (R)0.5 * (uy * uy - uy), By = uy - (R)0.5, Cy = (R)1 - uy * uy;
-    const R Az = (R)0.5 * (uz * uz - uz), Bz = uz - (R)0.5, Cz = (R)1 - uz * uz;
-    R g[3][3][3];  // [sx][oy][oz]
-    const R zero = (R)0;
-    tri_bwd(rho,  q100, s200, ux, Ax, Bx, Cx, g[0][0][0], g[1][0][0], g[2][0][0]);
-    tri_bwd(q001, s101, zero, ux, Ax, Bx, Cx, g[0][0][1], g[1][0][1], g[2][0][1]);
-    tri_bwd(s002, zero, q202, ux, Ax, Bx, Cx, g[0][0][2], g[1][0][2], g[2][0][2]);
-    tri_bwd(q010, s110, zero, ux, Ax, Bx, Cx, g[0][1][0], g[1][1][0], g[2][1][0]);
-    tri_bwd(s011, zero, q211, ux, Ax, Bx, Cx, g[0][1][1], g[1][1][1], g[2][1][1]);
-    tri_bwd(zero, q112, zero, ux, Ax, Bx, Cx, g[0][1][2], g[1][1][2], g[2][1][2]);
-    tri_bwd(s020, zero, q220, ux, Ax, Bx, Cx, g[0][2][0], g[1][2][0], g[2][2][0]);
-    tri_bwd(zero, q121, zero, ux, Ax, Bx, Cx, g[0][2][1], g[1][2][1], g[2][2][1]);
-    tri_bwd(q022, zero, q222, ux, Ax, Bx, Cx, g[0][2][2], g[1][2][2], g[2][2][2]);
-    R hh[3][3][3];  // [sx][sy][oz]
-#pragma unroll
-    for (int sx = 0; sx < 3; sx++)
-#pragma unroll
-        for (int oz = 0; oz < 3; oz++)
-            tri_bwd(g[sx][0][oz], g[sx][1][oz], g[sx][2][oz], uy, Ay, By, Cy, hh[sx][0][oz], hh[sx][1][oz], hh[sx][2][oz]);
-    R o[3][3][3];  // [sx][sy][sz]
-#pragma unroll
-    for (int sx = 0; sx < 3; sx++)
-#pragma unroll
-        for (int sy = 0; sy < 3; sy++)
-            tri_bwd(hh[sx][sy][0], hh[sx][sy][1], hh[sx][sy][2], uz, Az, Bz, Cz, o[sx][sy][0], o[sx][sy][1], o[sx][sy][2]);
-    sfor<0, 27>([&](auto vc) {
-        constexpr int V = decltype(vc)::value;
-        f[V] = o[cx(V) + 1][cy(V) + 1][cz(V) + 1];
-    });
-}
-
-// ---- the fused step kernel ----------------------------------------------------------------------------
-// COLL: 0 SRT, 1 cumulant-2015.  CLOS: 0 none, 1 Smagorinsky.
-template <class S, int COLL, int CLOS, bool ODD>
-__global__ void __launch_bounds__(128) k_step(Params p) {
-    using R = typename S::R;
-    using T = typename S::T;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= p.nx) return;
-    Cell c;
-    make_cell(p, x, blockIdx.y, blockIdx.z, c);
-    const uint8_t fl = p.cls[c.idx];
-    const int cl = fl & CLS_MASK;
-    if (cl == CLS_SOLID) return;
-    R f[27];
-    if (cl == CLS_INLET) {
-        // node is not updated; only the time average (MomentTimeAvg runs over every cell) needs it
-        if (p.acc) {
-            inlet_state<S>(p, c, f);
-            R rho, jx, jy, jz, ux, uy, uz;
-            moments(f, p, rho, jx, jy, jz, ux, uy, uz);
-            double* a = p.acc;
-            const long long N = p.N;
-            a[c.idx] += rho; a[N + c.idx] += ux; a[2 * N + c.idx] += uy; a[3 * N + c.idx] += uz;
-            a[4 * N + c.idx] += (double)ux * ux; a[5 * N + c.idx] += (double)uy * uy; a[6 * N + c.idx] += (double)uz * uz;
-            a[7 * N + c.idx] += (double)ux * uy; a[8 * N + c.idx] += (double)ux * uz; a[9 * N + c.idx] += (double)uy * uz;
-        }
-        return;
-    }
-    R drag[3] = {0, 0, 0};
-    gather<S, ODD, false>(p, c, cl, f, drag);
-
-    R rho, jx, jy, jz, ux, uy, uz;
-    moments(f, p, rho, jx, jy, jz, ux, uy, uz);
-    if (fl & (BIT_PROBE1 | BIT_PROBE2)) {
-        R* pr = (R*)p.in_probe + (long long)lvl3(p.m) * 3 * p.n_in;
-        const int id = p.aux[c.idx];
-        if (fl & BIT_PROBE1) { pr[id] = rho; pr[p.n_in + id] = ux; }
-        else pr[2 * p.n_in + id] = ux;
-    }
-    if (p.acc) {
-        double* a = p.acc;
-        const long long N = p.N;
-        a[c.idx] += rho; a[N + c.idx] += ux; a[2 * N + c.idx] += uy; a[3 * N + c.idx] += uz;
-        a[4 * N + c.idx] += (double)ux * ux; a[5 * N + c.idx] += (double)uy * uy; a[6 * N + c.idx] += (double)uz * uz;
-        a[7 * N + c.idx] += (double)ux * uy; a[8 * N + c.idx] += (double)ux * uz; a[9 * N + c.idx] += (double)uy * uz;
-    }
-    R Mxx, Myy, Mzz, Mxy, Mxz, Myz;
-    second_moments(f, Mxx, Myy, Mzz, Mxy, Mxz, Myz);
-    const R om = relax_rate<R, CLOS>(p, rho, ux, uy, uz, Mxx, Myy, Mzz, Mxy, Mxz, Myz);
-    const bool force = p.F[0] != 0.0 || p.F[1] != 0.0 || p.F[2] != 0.0;
-    if constexpr (COLL == 0) collide_srt(f, p, rho, ux, uy, uz, om, force);
-    else collide_cum15(f, rho, jx, jy, jz, ux, uy, uz, om, Mxx, Myy, Mzz, Mxy, Mxz, Myz);
-
-    if (cl == CLS_LID) {
-        // InletVelocityMovingWall.h:40-53: for n.c_v > 0, df(x, opp v) = f*_v - 6 w_v rho (c_v . u_w);
-        // the other components keep their value.  Written to the next level.
-        const int id = p.aux[c.idx];
-        const int nl = p.n_lid;
-        const R* cur = (const R*)p.lid_state + (long long)lvl3(p.m) * 27 * nl;
-        R* nxt = (R*)p.lid_state + (long long)lvl3(p.m + 1) * 27 * nl;
-        const R n0 = p.lid_n[id], n1 = p.lid_n[nl + id], n2 = p.lid_n[2 * nl + id];
-        const R w0 = p.lid_u[id], w1 = p.lid_u[nl + id], w2 = p.lid_u[2 * nl + id];
-        sfor<0, 27>([&](auto vc) {
-            constexpr int V = decltype(vc)::value;
-            constexpr int O = opp(V);
-            // component O is set from f*_V when n.c_V > 0, else it keeps its value
-            if (n0 * (R)cx(V) + n1 * (R)cy(V) + n2 * (R)cz(V) > (R)0)
-                nxt[O * nl + id] = f[V] - (R)6 * (R)wgt(V) * rho * ((R)cx(V) * w0 + (R)cy(V) * w1 + (R)cz(V) * w2);
-            else
-                nxt[O * nl + id] = cur[O * nl + id];
-        });
-        return;
-    }
-    if (fl & BIT_OUTUP) {
-        const int id = p.aux[c.idx];
-        const int s = p.out_dir[id];
-        R* sv = (R*)p.out_save + (long long)(p.m & 1) * 18 * p.n_out;
-        sfor<0, 27>([&](auto vc) {
-            constexpr int V = decltype(vc)::value;
-            if constexpr (cx(V) != 0) if (cx(V) == -s) sv[outlet_slot(V) * p.n_out + id] = f[V];
-        });
-    }
-    if (cl == CLS_OUTLET) {
-        const int id = p.aux[c.idx];
-        const int s = p.out_dir[id];
-        R* sv = (R*)p.out_save + (long long)(p.m & 1) * 18 * p.n_out;
-        sfor<0, 27>([&](auto vc) {
-            constexpr int V = decltype(vc)::value;
-            if constexpr (cx(V) != 0) if (cx(V) == -s) sv[(9 + outlet_slot(V)) * p.n_out + id] = f[V];
-        });
-    }
-    // scatter (AA)
-    T* A = (T*)p.f;
-    const long long N = p.N;
-    if (cl == CLS_BULK) {
-        sfor<0, 27>([&](auto vc) {
-            constexpr int V = decltype(vc)::value;
-            const R wr = wr_of<S>(V, p);
-            if (ODD) Codec<S>::enc(A, V * N + nbr<cx(V), cy(V), cz(V)>(c), f[V], wr, p);
-            else     Codec<S>::enc(A, opp(V) * N + c.idx, f[V], wr, p);
-        });
-    } else {
-        sfor<0, 27>([&](auto vc) {
-            constexpr int V = decltype(vc)::value;
-            const R wr = wr_of<S>(V, p);
-            if (ODD) {
-                if (!nbr_oob<cx(V), cy(V), cz(V)>(c)) Codec<S>::enc(A, V * N + nbr<cx(V), cy(V), cz(V)>(c), f[V], wr, p);
-            } else {
-                Codec<S>::enc(A, opp(V) * N + c.idx, f[V], wr, p);
-            }
-        });
-    }
+    const Mom<R> m = raw_moments(f);
+    rho = m.rho; jx = m.jx; jy = m.jy; jz = m.jz;
+    const R ri = rcp(rho);
+    ux = (jx + (R)0.5 * p_F<R>(p, 0)) * ri;
+    uy = (jy + (R)0.5 * p_F<R>(p, 1)) * ri;
+    uz = (jz + (R)0.5 * p_F<R>(p, 2)) * ri;
 }
 
 }  // namespace lbm

@@ -3,14 +3,22 @@
 
 #include "lbm_aux.cuh"
 #include "lbm_launch.h"
+#include "lbm_step.cuh"
 
 namespace lbm {
 
 template <class S, int COLL, int CLOS>
 static cudaError_t step_parity(const Params& p, cudaStream_t st) {
-    dim3 g = cell_grid(p.nx, p.ny, p.nz), b = cell_block(p.nx);
-    if (p.m & 1) k_step<S, COLL, CLOS, true><<<g, b, 0, st>>>(p);
-    else         k_step<S, COLL, CLOS, false><<<g, b, 0, st>>>(p);
+    if constexpr (S::kind == 0) {
+        dim3 g = cell_grid(p.nx, p.ny, p.nz), b = cell_block(p.nx);
+        if (p.m & 1) k_step<S, COLL, CLOS, true><<<g, b, 0, st>>>(p);
+        else         k_step<S, COLL, CLOS, false><<<g, b, 0, st>>>(p);
+    } else {
+        const int half = (p.nx + 1) / 2;  // one thread per x-pair
+        dim3 g = cell_grid(half, p.ny, p.nz), b = cell_block(half);
+        if (p.m & 1) k_step2<S, COLL, CLOS, true><<<g, b, 0, st>>>(p);
+        else         k_step2<S, COLL, CLOS, false><<<g, b, 0, st>>>(p);
+    }
     return cudaGetLastError();
 }
 

@@ -1,0 +1,246 @@
+// lbm_step.cuh - the fused collide-and-stream step kernels.
+//
+// k_step  : one thread per cell (FP64 storage).
+// k_step2 : one thread per x-pair of cells (FP32 and FP16-deviation storage).  When both cells are
+//           plain bulk cells off the periodic seams, the pair is loaded with 64-bit (FP32) or 32-bit
+//           (FP16) accesses where the AA slot pair is aligned and collided in packed FP32 (F2 lanes:
+//           FADD2/FMUL2/FFMA2); otherwise each cell takes the scalar per-cell path.
+#pragma once
+
+#include "lbm_device.cuh"
+
+namespace lbm {
+
+template <class R> LBM_D R p_om0(const Params& p) { if constexpr (std::is_same<R, float>::value) return p.omega0f; else return p.omega0; }
+
+LBM_D void acc_add(const Params& p, long long i, double rho, double ux, double uy, double uz) {
+    double* a = p.acc;
+    const long long N = p.N;
+    a[i] += rho; a[N + i] += ux; a[2 * N + i] += uy; a[3 * N + i] += uz;
+    a[4 * N + i] += ux * ux; a[5 * N + i] += uy * uy; a[6 * N + i] += uz * uz;
+    a[7 * N + i] += ux * uy; a[8 * N + i] += ux * uz; a[9 * N + i] += uy * uz;
+}
+
+// relaxation rate and collision of one lane (a cell, or a pair of cells)
+template <int COLL, int CLOS, class L>
+LBM_D void collide_lane(L (&f)[27], const Mom<L>& mm, L ri, L ux, L uy, L uz, L tau, L cles18, L om0,
+                        bool force, L Fx, L Fy, L Fz) {
+    L om;
+    if constexpr (CLOS == 0) om = om0;
+    else om = omega_smagorinsky(tau, cles18, mm.rho, ri, ux, uy, uz, mm);
+    if constexpr (COLL == 0) {
+        collide_srt(f, mm.rho, ux, uy, uz, om);
+        if (force) srt_force(f, ux, uy, uz, om, Fx, Fy, Fz);
+    } else {
+        collide_cum15(f, mm.rho, ri, ux, uy, uz, om, mm);
+    }
+}
+
+// ---- one cell (scalar lane) --------------------------------------------------------------------------
+template <class S, int COLL, int CLOS, bool ODD>
+LBM_D void step_cell(const Params& p, int x, int y, int z) {
+    using R = typename S::R;
+    const unsigned idx = (unsigned)x + (unsigned)p.nx * ((unsigned)y + (unsigned)p.ny * (unsigned)z);
+    const uint8_t fl = p.cls[idx];
+    const int cl = fl & CLS_MASK;
+    if (cl == CLS_SOLID) return;
+    R f[27];
+    if (cl == CLS_INLET) {
+        // node is not updated; only the time average (MomentTimeAvg runs over every cell) needs it
+        if (p.acc) {
+            Cell c;
+            make_cell(p, x, y, z, c);
+            inlet_state<S>(p, c, f);
+            R rho, jx, jy, jz, ux, uy, uz;
+            moments(f, p, rho, jx, jy, jz, ux, uy, uz);
+            acc_add(p, idx, rho, ux, uy, uz);
+        }
+        return;
+    }
+    const bool fast = cl == CLS_BULK && !on_seam(p, x, y, z);
+    if (fast) {
+        load_fast<S, ODD>(p, idx, f);
+    } else {
+        Cell c;
+        make_cell(p, x, y, z, c);
+        R drag[3] = {0, 0, 0};
+        gather<S, ODD, false>(p, c, cl, f, drag);
+    }
+    const Mom<R> mm = raw_moments(f);
+    const R rho = mm.rho, ri = rcp(rho);
+    const R ux = (mm.jx + (R)0.5 * p_F<R>(p, 0)) * ri;
+    const R uy = (mm.jy + (R)0.5 * p_F<R>(p, 1)) * ri;
+    const R uz = (mm.jz + (R)0.5 * p_F<R>(p, 2)) * ri;
+    if (fl & (BIT_PROBE1 | BIT_PROBE2)) {
+        R* pr = (R*)p.in_probe + (long long)lvl3(p.m) * 3 * p.n_in;
+        const int id = p.aux[idx];
+        if (fl & BIT_PROBE1) { pr[id] = rho; pr[p.n_in + id] = ux; }
+        else pr[2 * p.n_in + id] = ux;
+    }
+    if (p.acc) acc_add(p, idx, rho, ux, uy, uz);
+    collide_lane<COLL, CLOS>(f, mm, ri, ux, uy, uz, p_tau<R>(p), p_cles18<R>(p), p_om0<R>(p), p.has_force != 0,
+                             p_F<R>(p, 0), p_F<R>(p, 1), p_F<R>(p, 2));
+    if (fl & BIT_OUTUP) {
+        const int id = p.aux[idx];
+        const int s = p.out_dir[id];
+        R* sv = (R*)p.out_save + (long long)(p.m & 1) * 18 * p.n_out;
+        sfor<0, 27>([&](auto vc) {
+            constexpr int V = decltype(vc)::value;
+            if constexpr (cx(V) != 0) if (cx(V) == -s) sv[outlet_slot(V) * p.n_out + id] = f[V];
+        });
+    }
+    if (fast) {
+        store_fast<S, ODD>(p, idx, f);
+        return;
+    }
+    if (cl == CLS_LID) {
+        // InletVelocityMovingWall.h:40-53: for n.c_v > 0, df(x, opp v) = f*_v - 6 w_v rho (c_v . u_w);
+        // the other components keep their value.  Written to the next level.
+        const int id = p.aux[idx];
+        const int nl = p.n_lid;
+        const R* cur = (const R*)p.lid_state + (long long)lvl3(p.m) * 27 * nl;
+        R* nxt = (R*)p.lid_state + (long long)lvl3(p.m + 1) * 27 * nl;
+        const R n0 = p.lid_n[id], n1 = p.lid_n[nl + id], n2 = p.lid_n[2 * nl + id];
+        const R w0 = p.lid_u[id], w1 = p.lid_u[nl + id], w2 = p.lid_u[2 * nl + id];
+        sfor<0, 27>([&](auto vc) {
+            constexpr int V = decltype(vc)::value;
+            constexpr int O = opp(V);
+            // component O is set from f*_V when n.c_V > 0, else it keeps its value
+            if (n0 * (R)cx(V) + n1 * (R)cy(V) + n2 * (R)cz(V) > (R)0)
+                nxt[O * nl + id] = f[V] - (R)6 * (R)wgt(V) * rho * ((R)cx(V) * w0 + (R)cy(V) * w1 + (R)cz(V) * w2);
+            else
+                nxt[O * nl + id] = cur[O * nl + id];
+        });
+        return;
+    }
+    if (cl == CLS_OUTLET) {
+        const int id = p.aux[idx];
+        const int s = p.out_dir[id];
+        R* sv = (R*)p.out_save + (long long)(p.m & 1) * 18 * p.n_out;
+        sfor<0, 27>([&](auto vc) {
+            constexpr int V = decltype(vc)::value;
+            if constexpr (cx(V) != 0) if (cx(V) == -s) sv[(9 + outlet_slot(V)) * p.n_out + id] = f[V];
+        });
+    }
+    Cell c;
+    make_cell(p, x, y, z, c);
+    scatter<S, ODD>(p, c, f);
+}
+
+// out-of-line copy for the pair kernel's fallback, so the packed hot path stays compact in the
+// instruction cache
+template <class S, int COLL, int CLOS, bool ODD>
+__device__ __noinline__ void step_cell_call(const Params& p, int x, int y, int z) {
+    step_cell<S, COLL, CLOS, ODD>(p, x, y, z);
+}
+
+// COLL: 0 SRT, 1 cumulant-2015.  CLOS: 0 none, 1 Smagorinsky.
+template <class S, int COLL, int CLOS, bool ODD>
+__global__ void __launch_bounds__(128) k_step(Params p) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= p.nx) return;
+    step_cell<S, COLL, CLOS, ODD>(p, x, blockIdx.y, blockIdx.z);
+}
+
+// ---- x-pairs in packed FP32 ----------------------------------------------------------------------------
+// Cells idx0 (even x0) and idx0+1 of a bulk pair.  Even steps touch only the pair's own slots and odd
+// steps with c_x = 0 a pair in a neighbouring row: one aligned 64-bit (FP32) / 32-bit (FP16) access.
+// Odd steps with c_x != 0 touch an x-shifted pair that straddles the alignment, fetched as two
+// scalars.  Relative to the per-direction pointers (which already carry the neighbour offset):
+//   read  c_x = +1: cells (x0-1, x0)   -> elements (eL, e1);  c_x = -1: (x0+1, x0+2) -> (e0, eR)
+//   write c_x = +1: cells (x0+1, x0+2) -> elements (e0, eR);  c_x = -1: (x0-1, x0)   -> (eL, e1)
+// with e0 = idx0, e1 = idx0+1, and eL / eR the same shifted by +-nx where x0-1 / x0+2 wraps across
+// a periodic x seam.
+struct PairIdx {
+    int e0, e1, eL, eR;  // signed: a wrapped index may sit below e0 by up to nx
+};
+// FP16 codec constants of the four weight classes (w rho0, -w rho0 2^s) as packed pairs
+struct PairCodec {
+    F2 inv_scale, scale, wr[4], nwrs[4];
+};
+
+template <class S, bool ODD>
+LBM_D void load_pair(const Params& p, const PairIdx& q, const PairCodec& k, F2 (&f)[27]) {
+    using T = typename S::T;
+    sfor<0, 27>([&](auto vc) {
+        constexpr int V = decltype(vc)::value;
+        const T* a = (const T*)(ODD ? p.rd_odd[V] : p.rd_even[V]);
+        constexpr bool split = ODD && cx(V) != 0;
+        const int i0 = cx(V) > 0 ? q.eL : q.e0, i1 = cx(V) > 0 ? q.e1 : q.eR;
+        if constexpr (S::kind == 1) {
+            if constexpr (split) f[V] = F2(__ldg(a + i0), __ldg(a + i1));
+            else f[V] = F2(__ldg((const float2*)(a + q.e0)));
+        } else {
+            float2 t;
+            if constexpr (split) t = make_float2(__half2float(__ldg(a + i0)), __half2float(__ldg(a + i1)));
+            else t = __half22float2(__ldg((const __half2*)(a + q.e0)));
+            f[V] = lfma(F2(t), k.inv_scale, k.wr[csq(V)]);
+        }
+    });
+}
+template <class S, bool ODD>
+LBM_D void store_pair(const Params& p, const PairIdx& q, const PairCodec& k, const F2 (&f)[27]) {
+    using T = typename S::T;
+    sfor<0, 27>([&](auto vc) {
+        constexpr int V = decltype(vc)::value;
+        T* a = (T*)(ODD ? p.wr_odd[V] : p.wr_even[V]);
+        constexpr bool split = ODD && cx(V) != 0;
+        const int i0 = cx(V) > 0 ? q.e0 : q.eL, i1 = cx(V) > 0 ? q.eR : q.e1;
+        if constexpr (S::kind == 1) {
+            if constexpr (split) { a[i0] = f[V].v.x; a[i1] = f[V].v.y; }
+            else *(float2*)(a + q.e0) = f[V].v;
+        } else {
+            const F2 e = lfma(f[V], k.scale, k.nwrs[csq(V)]);
+            const __half2 h = __float22half2_rn(e.v);
+            if constexpr (split) { a[i0] = __low2half(h); a[i1] = __high2half(h); }
+            else *(__half2*)(a + q.e0) = h;
+        }
+    });
+}
+
+template <class S, int COLL, int CLOS, bool ODD>
+__global__ void __launch_bounds__(128) k_step2(Params p) {
+    static_assert(S::kind != 0, "packed pairs are FP32 arithmetic");
+    const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (x0 >= p.nx) return;
+    const int y = blockIdx.y, z = blockIdx.z;
+    const bool two = x0 + 1 < p.nx;
+    const unsigned idx0 = (unsigned)x0 + (unsigned)p.nx * ((unsigned)y + (unsigned)p.ny * (unsigned)z);
+    const uint8_t f0 = p.cls[idx0] & (uint8_t)~BIT_REFBULK;
+    const uint8_t f1 = two ? (p.cls[idx0 + 1] & (uint8_t)~BIT_REFBULK) : (uint8_t)0;
+    // rows on a periodic y or z seam (whole blocks) take the per-cell path; x seams stay packed
+    const bool yz_seam = (p.wrap[1] && (y == 0 || y == p.ny - 1)) || (p.wrap[2] && (z == 0 || z == p.nz - 1));
+    const bool pair = two && f0 == CLS_BULK && f1 == CLS_BULK && (p.nx & 1) == 0 && p.acc == nullptr && !yz_seam;
+    if (!pair) {
+        step_cell_call<S, COLL, CLOS, ODD>(p, x0, y, z);
+        if (two) step_cell_call<S, COLL, CLOS, ODD>(p, x0 + 1, y, z);
+        return;
+    }
+    PairIdx q;
+    q.e0 = (int)idx0;
+    q.e1 = q.e0 + 1;
+    q.eL = (p.wrap[0] && x0 == 0) ? q.e0 + p.nx : q.e0;
+    q.eR = (p.wrap[0] && x0 + 2 == p.nx) ? q.e1 - p.nx : q.e1;
+    PairCodec k;
+    if constexpr (S::kind == 2) {
+        k.inv_scale = F2(p.inv_scale);
+        k.scale = F2(p.scale);
+        k.wr[0] = F2(p.wr[0]); k.wr[1] = F2(p.wr[1]); k.wr[2] = F2(p.wr[7]); k.wr[3] = F2(p.wr[19]);
+        k.nwrs[0] = F2(p.nwrs[0]); k.nwrs[1] = F2(p.nwrs[1]); k.nwrs[2] = F2(p.nwrs[7]); k.nwrs[3] = F2(p.nwrs[19]);
+    }
+    F2 f[27];
+    load_pair<S, ODD>(p, q, k, f);
+    const Mom<F2> mm = raw_moments(f);
+    const F2 ri = rcp(mm.rho);
+    F2 ux = mm.jx * ri, uy = mm.jy * ri, uz = mm.jz * ri;
+    if (p.has_force) {
+        ux = lfma(F2(p.Ff[0]), F2(0.5f), mm.jx) * ri;
+        uy = lfma(F2(p.Ff[1]), F2(0.5f), mm.jy) * ri;
+        uz = lfma(F2(p.Ff[2]), F2(0.5f), mm.jz) * ri;
+    }
+    collide_lane<COLL, CLOS>(f, mm, ri, ux, uy, uz, F2(p.tauf), F2(p.cles18f), F2(p.omega0f), p.has_force != 0,
+                             F2(p.Ff[0]), F2(p.Ff[1]), F2(p.Ff[2]));
+    store_pair<S, ODD>(p, q, k, f);
+}
+
+}  // namespace lbm
