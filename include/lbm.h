@@ -176,6 +176,26 @@ lbm_status lbm_voxelize_mesh(const double* verts, int32_t nv, const int32_t* tri
                              double res, double add, int32_t* flags_out, int32_t dims_out[3],
                              double bbox_out[6], int32_t device);
 
+/* ---- the same voxelizer for callers that cannot allocate device memory ---------------------
+ * No counterpart in the reference.  Some callers may not call cudaMalloc: an application whose
+ * memory manager has reserved the whole device heap for its own pool, or a real-time loop where an
+ * allocation's latency or failure is not acceptable.  This entry point gives the flags of
+ * lbm_voxelize_mesh without allocating anything: the caller passes the output as device memory
+ * (flags_out_device, dims[0]*dims[1]*dims[2] int32 on `device`; NULL queries dims and bbox only), and
+ * the library's own scratch is one fixed array compiled into the library (about 3.6 MB, held on every
+ * device that loads the library until the process exits).  Limits: at most
+ * LBM_VOXELIZE_NOALLOC_MAX_VERTICES vertices, LBM_VOXELIZE_NOALLOC_MAX_TRIANGLES triangles and
+ * LBM_VOXELIZE_NOALLOC_MAX_DIM cells per axis; larger inputs return LBM_ERR_UNSUPPORTED before any
+ * device work.  The first call on a device also looks up that array's device address, so make it
+ * before capturing any CUDA stream.  All calls in a process share the array: calls that overlapped on
+ * the GPU would race, so this function holds a lock and returns only after its kernels finished. */
+#define LBM_VOXELIZE_NOALLOC_MAX_VERTICES  32768
+#define LBM_VOXELIZE_NOALLOC_MAX_TRIANGLES 32768
+#define LBM_VOXELIZE_NOALLOC_MAX_DIM       4096
+lbm_status lbm_voxelize_mesh_noalloc(const double* verts, int32_t nv, const int32_t* tris, int32_t nt,
+                                     double res, double add, int32_t* flags_out_device,
+                                     int32_t dims_out[3], double bbox_out[6], int32_t device);
+
 #ifdef __cplusplus
 }
 #endif

@@ -147,6 +147,7 @@ def lib():
         "lbm_mesher_wall_pass": ([ip, i32, i32, i32], i32),
         "lbm_voxelize_off": ([C.c_char_p, f64, f64, dp, ip, ip, dp, i32], i32),
         "lbm_voxelize_mesh": ([dp, i32, ip, i32, f64, f64, ip, ip, dp, i32], i32),
+        "lbm_voxelize_mesh_noalloc": ([dp, i32, ip, i32, f64, f64, C.c_void_p, ip, dp, i32], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

@@ -20,6 +20,7 @@
 #include <cmath>
 #include <cstdint>
 #include <fstream>
+#include <mutex>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -210,6 +211,123 @@ lbm_status lbm_voxelize_mesh(const double* verts, int32_t nv, const int32_t* tri
     }
     cudaFree(dT); cudaFree(dx); cudaFree(dy); cudaFree(dz); cudaFree(dflags); cudaFree(dovf);
     return st;
+}
+
+}  // extern "C"
+
+// ---- allocation-free variant ------------------------------------------------------------------------
+// Everything the column kernel needs besides the caller's output lives in one file-scope device
+// array: the raw mesh copied from the host, the oriented triangle records, the sample coordinates
+// and two status words.  Each process holds it once per device that loads this library.
+namespace {
+
+struct VoxScratch {
+    double verts[3 * LBM_VOXELIZE_NOALLOC_MAX_VERTICES];
+    int32_t tris[3 * LBM_VOXELIZE_NOALLOC_MAX_TRIANGLES];
+    Tri prepared[LBM_VOXELIZE_NOALLOC_MAX_TRIANGLES];
+    float xs[LBM_VOXELIZE_NOALLOC_MAX_DIM], ys[LBM_VOXELIZE_NOALLOC_MAX_DIM], zs[LBM_VOXELIZE_NOALLOC_MAX_DIM];
+    int overflow;   // a column met more crossings than the kernel keeps
+    int bad_index;  // a triangle referenced a vertex outside [0, nv)
+};
+
+static __device__ __align__(256) unsigned char g_vox_scratch[sizeof(VoxScratch)];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_vox_mutex;                      // one call at a time per process
+VoxScratch* g_vox_addr[kMaxDevices] = {};    // device address of g_vox_scratch, per device
+
+// orient each triangle's (y, z) projection counter-clockwise, as the allocating path does on the
+// host; a triangle parallel to the rays gets NaN coordinates so that no column ever meets it
+__global__ void k_prepare(VoxScratch* s, int nv, int nt) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const int id[3] = {s->tris[3 * t], s->tris[3 * t + 1], s->tris[3 * t + 2]};
+    Tri r;
+    for (int a = 0; a < 3; a++) {
+        if (id[a] < 0 || id[a] >= nv) {
+            s->bad_index = 1;
+            for (int b = 0; b < 3; b++) r.x[b] = r.y[b] = r.z[b] = nan("");
+            s->prepared[t] = r;
+            return;
+        }
+        r.x[a] = s->verts[3 * id[a]];
+        r.y[a] = s->verts[3 * id[a] + 1];
+        r.z[a] = s->verts[3 * id[a] + 2];
+    }
+    // the same products as the host path, without FMA contraction
+    const double ar = __dsub_rn(__dmul_rn(__dsub_rn(r.y[1], r.y[0]), __dsub_rn(r.z[2], r.z[0])),
+                                __dmul_rn(__dsub_rn(r.z[1], r.z[0]), __dsub_rn(r.y[2], r.y[0])));
+    if (ar == 0) {
+        for (int b = 0; b < 3; b++) r.y[b] = r.z[b] = nan("");
+    } else if (ar < 0) {
+        double tx = r.x[1], ty = r.y[1], tz = r.z[1];
+        r.x[1] = r.x[2]; r.y[1] = r.y[2]; r.z[1] = r.z[2];
+        r.x[2] = tx; r.y[2] = ty; r.z[2] = tz;
+    }
+    s->prepared[t] = r;
+}
+
+// sample coordinates of geometryMesherOFF.h:94-96 (double arithmetic, stored as float)
+__global__ void k_samples(VoxScratch* s, int nx, int ny, int nz, float resf, float addf, float bx, float by, float bz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nx) s->xs[i] = (float)__dadd_rn(__ddiv_rn(__dsub_rn((double)i + 0.5, (double)addf), (double)resf), (double)bx);
+    if (i < ny) s->ys[i] = (float)__dadd_rn(__ddiv_rn(__dsub_rn((double)i + 0.5, (double)addf), (double)resf), (double)by);
+    if (i < nz) s->zs[i] = (float)__dadd_rn(__ddiv_rn(__dsub_rn((double)i + 0.5, (double)addf), (double)resf), (double)bz);
+}
+
+}  // namespace
+
+extern "C" {
+
+lbm_status lbm_voxelize_mesh_noalloc(const double* verts, int32_t nv, const int32_t* tris, int32_t nt, double res,
+                                     double add, int32_t* flags_out_device, int32_t dims_out[3], double bbox_out[6],
+                                     int32_t device) {
+    if (!verts || !tris || nv <= 0 || nt <= 0 || !dims_out || !(res > 0) || add < 0) return LBM_ERR_INVALID;
+    if (nv > LBM_VOXELIZE_NOALLOC_MAX_VERTICES || nt > LBM_VOXELIZE_NOALLOC_MAX_TRIANGLES) return LBM_ERR_UNSUPPORTED;
+    if (device < 0 || device >= kMaxDevices) return LBM_ERR_INVALID;
+    // grid exactly as lbm_voxelize_mesh (float BB, resolution and additional factor)
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int i = 0; i < nv; i++)
+        for (int a = 0; a < 3; a++) { lo[a] = std::min(lo[a], verts[3 * i + a]); hi[a] = std::max(hi[a], verts[3 * i + a]); }
+    const float resf = (float)res, addf = (float)add;
+    float blo[3], bhi[3];
+    for (int a = 0; a < 3; a++) { blo[a] = (float)lo[a]; bhi[a] = (float)hi[a]; }
+    for (int a = 0; a < 3; a++) dims_out[a] = (int32_t)std::ceil((bhi[a] - blo[a]) * resf + 2 * addf);
+    if (bbox_out) for (int a = 0; a < 3; a++) { bbox_out[a] = blo[a]; bbox_out[3 + a] = bhi[a]; }
+    if (!flags_out_device) return LBM_OK;
+    const int nx = dims_out[0], ny = dims_out[1], nz = dims_out[2];
+    if (nx <= 0 || ny <= 0 || nz <= 0) return LBM_ERR_INVALID;
+    if (nx > LBM_VOXELIZE_NOALLOC_MAX_DIM || ny > LBM_VOXELIZE_NOALLOC_MAX_DIM || nz > LBM_VOXELIZE_NOALLOC_MAX_DIM)
+        return LBM_ERR_UNSUPPORTED;
+
+    std::lock_guard<std::mutex> lock(g_vox_mutex);
+    if (cudaSetDevice(device) != cudaSuccess) return LBM_ERR_CUDA;
+    if (!g_vox_addr[device]) {
+        // first call on this device: find the device address of the scratch array
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_vox_scratch) != cudaSuccess || !p) return LBM_ERR_CUDA;
+        g_vox_addr[device] = (VoxScratch*)p;
+    }
+    VoxScratch* s = g_vox_addr[device];
+    // the status words start at zero; verts, tris, prepared and samples are overwritten for the
+    // ranges this call reads
+    if (cudaMemset(&s->overflow, 0, 2 * sizeof(int)) != cudaSuccess ||
+        cudaMemcpy(s->verts, verts, 3 * sizeof(double) * (size_t)nv, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(s->tris, tris, 3 * sizeof(int32_t) * (size_t)nt, cudaMemcpyHostToDevice) != cudaSuccess)
+        return LBM_ERR_CUDA;
+    const int bs = 128;
+    k_prepare<<<(nt + bs - 1) / bs, bs>>>(s, nv, nt);
+    const int nmax = std::max(nx, std::max(ny, nz));
+    k_samples<<<(nmax + bs - 1) / bs, bs>>>(s, nx, ny, nz, resf, addf, blo[0], blo[1], blo[2]);
+    const int cols = ny * nz;
+    k_columns<<<(cols + bs - 1) / bs, bs>>>(s->prepared, nt, s->ys, s->zs, s->xs, nx, ny, nz, flags_out_device,
+                                            &s->overflow);
+    int status[2] = {0, 0};
+    if (cudaGetLastError() != cudaSuccess || cudaMemcpy(status, &s->overflow, sizeof(status), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return LBM_ERR_CUDA;
+    if (status[1]) return LBM_ERR_INVALID;      // a triangle index outside [0, nv)
+    if (status[0]) return LBM_ERR_UNSUPPORTED;  // more than kMaxCross crossings on one column
+    return LBM_OK;
 }
 
 lbm_status lbm_voxelize_off(const char* path, double res, double add, const double outside[3], int32_t* flags_out,
