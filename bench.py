@@ -147,18 +147,19 @@ def channel_case(shape):
     return cases.channel(*shape, re_tau=180.0, u_max=0.05, amp=0.05)
 
 
-def make_solver(shape, case, storage, device):
+def make_solver(shape, case, storage, device, options=0):
     from lb_gb300.solver import CollisionCumD3Q27Turbulent2015, OmegaLES, Solver
     s = Solver(shape, collision=CollisionCumD3Q27Turbulent2015, turbulence=OmegaLES, storage=storage,
-               nu=case["nu"], cles=0.17, periodic=case["periodic"], force=case["force"], device=device)
+               nu=case["nu"], cles=0.17, periodic=case["periodic"], force=case["force"], device=device,
+               options=options)
     s.set_flags(case["flags"])
     s.set_bc()
     s.init_fields(case["rho"], case["u"])
     return s
 
 
-def time_storage(shape, case, storage, steps, warmup, device, dist, with_clocks):
-    s = make_solver(shape, case, storage, device)
+def time_storage(shape, case, storage, steps, warmup, device, dist, with_clocks, options=0):
+    s = make_solver(shape, case, storage, device, options)
     s.step(warmup)
     s.synchronize()
     barrier(dist)
@@ -174,12 +175,13 @@ def time_storage(shape, case, storage, steps, warmup, device, dist, with_clocks)
     return ms, d, (sampler.summary() if sampler else None)
 
 
-def e2e_run(shape, case, storage, steps, device):
+def e2e_run(shape, case, storage, steps, device, options=0):
     """End to end through the public API with host buffers: upload flags + initial fields, then
     every step lbm_step + the reference's per-step probe read-back (u, rho of one cell)."""
     from lb_gb300.solver import CollisionCumD3Q27Turbulent2015, OmegaLES, Solver
     s = Solver(shape, collision=CollisionCumD3Q27Turbulent2015, turbulence=OmegaLES, storage=storage,
-               nu=case["nu"], cles=0.17, periodic=case["periodic"], force=case["force"], device=device)
+               nu=case["nu"], cles=0.17, periodic=case["periodic"], force=case["force"], device=device,
+               options=options)
     flags = np.ascontiguousarray(case["flags"], dtype=np.int32)
     rho = np.ascontiguousarray(case["rho"], dtype=np.float64)
     u = np.ascontiguousarray(case["u"], dtype=np.float64)
@@ -236,6 +238,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for the CPU arms")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--options", type=int, default=0, help="LBM_OPT_* bits passed to lbm_create")
     args = ap.parse_args()
     shape = tuple(int(v) for v in args.shape.split(","))
     N = shape[0] * shape[1] * shape[2]
@@ -271,8 +274,9 @@ def main():
     hbm, peak_kind = peaks()
     traffic = ncu_traffic()
 
-    ms16, d16, clk = time_storage(shape, case, "f16dev", args.steps, args.warmup, device, dist, rank == 0)
-    ms32, d32, _ = time_storage(shape, case, "f32", args.steps, args.warmup, device, dist, False)
+    ms16, d16, clk = time_storage(shape, case, "f16dev", args.steps, args.warmup, device, dist, rank == 0,
+                                 args.options)
+    ms32, d32, _ = time_storage(shape, case, "f32", args.steps, args.warmup, device, dist, False, args.options)
     ms16 = dist_max(dist, ms16)
     ms32 = dist_max(dist, ms32)
     cells = dist_sum(dist, float(N) * args.steps)
@@ -290,7 +294,7 @@ def main():
     e2e = None
     if not args.no_e2e:
         k = min(args.steps, 200)
-        dt, h2d, d2h = e2e_run(shape, case, "f16dev", k, device)
+        dt, h2d, d2h = e2e_run(shape, case, "f16dev", k, device, args.options)
         dt = dist_max(dist, dt)
         e2e = {"value": dist_sum(dist, float(N) * k) / dt / 1e9, "unit": "GLUPS",
                "h2d_bytes_per_step": h2d / k, "d2h_bytes_per_step": d2h, "steps": k,
@@ -314,11 +318,12 @@ def main():
                        "storage": "f16dev (f - w rho0) * 2^10, FP32 collision", "closure": "smagorinsky",
                        "learned_closure": "not in this measurement",
                        "l2": "state 1.8 GB (f16) / 3.6 GB (f32) >> 129 MB L2; no flush needed",
-                       "parallelism": f"{ws} independent replica(s)"},
+                       "parallelism": f"{ws} independent replica(s)", "options": args.options},
             "roofline": roof("f16dev", ms16),
             "fp32_plain": {"value": glups32, "ms_per_step": ms32 / args.steps, "roofline": roof("f32", ms32),
                            "speedup_f16_over_f32": glups16 / glups32},
-            "gpu_launches": args.steps, "clocks": clk, "cpu_baseline": cpu, "e2e": e2e,
+            # one fused step kernel per step; the row-staged step adds the launch over the wall rows
+            "gpu_launches": args.steps * (2 if args.options & 1 else 1), "clocks": clk, "cpu_baseline": cpu, "e2e": e2e,
             "check": {"f16_mass": d16.mass, "f32_mass": d32.mass, "nonfinite": d16.nonfinite + d32.nonfinite}}
     print(json.dumps(line))
 

@@ -75,7 +75,11 @@ typedef struct lbm_config {
     double  rho0;             /* reference density of the FP16-deviation encoding */
     int32_t f16_scale_log2;   /* s of the FP16-deviation encoding (10 => 2^10) */
     int32_t device;           /* CUDA device ordinal */
+    int32_t options;          /* LBM_OPT_* bits (0: defaults) */
 } lbm_config;
+
+/* implementation options (results are identical either way) */
+#define LBM_OPT_ROW_STAGING  1  /* FP16 storage: rows of bulk cells through the shared-memory row-staged step */
 
 /* boundary-condition records, mirroring LBMTraits.h:17-43 */
 typedef struct lbm_vertex { int32_t x, y, z; } lbm_vertex;

@@ -51,6 +51,11 @@ struct lbm_ctx {
     double* d_red = nullptr;
     double *d_rho_out = nullptr, *d_u_out = nullptr, *d_f_out = nullptr;
     double* d_probe = nullptr;
+    int32_t* d_bulk_rows = nullptr;   // (y,z) rows whose cells are all bulk fluid
+    int32_t* d_other_rows = nullptr;  // the remaining rows
+    int n_bulk_rows = 0, n_other_rows = 0;
+    int* d_err = nullptr;             // device error word
+    bool rows_ok = false;             // the row-staged step applies to this lattice
     std::string err;
 };
 
@@ -119,10 +124,15 @@ static Params make_params(const lbm_ctx* c) {
     p.in_probe = c->d_in_probe; p.in_u = c->d_in_u; p.in_dir = c->d_in_dir; p.n_in = c->n_in;
     p.out_save = c->d_out_save; p.out_rho = c->d_out_rho; p.out_dir = c->d_out_dir; p.n_out = c->n_out;
     p.acc = nullptr;
+    p.err = c->d_err;
     return p;
 }
 
 static cudaError_t do_step(lbm_ctx* c, const Params& p) {
+    if (c->rows_ok && p.acc == nullptr && c->cfg.collision == LBM_COLLISION_CUMULANT2015 &&
+        c->cfg.storage == LBM_STORAGE_F16DEV)
+        return launch_step_rows<StF16>(p, c->cfg.closure, c->d_bulk_rows, c->n_bulk_rows, c->d_other_rows,
+                                       c->n_other_rows, c->st);
     switch (c->cfg.storage) {
         case LBM_STORAGE_F64: return launch_step<StF64>(p, c->cfg.collision, c->cfg.closure, c->st);
         case LBM_STORAGE_F32: return launch_step<StF32>(p, c->cfg.collision, c->cfg.closure, c->st);
@@ -199,7 +209,9 @@ lbm_status lbm_create(const lbm_config* cfg, lbm_ctx** out) {
         (e = cudaMalloc(&c->d_f, 27 * (size_t)N * c->esize)) != cudaSuccess ||
         (e = cudaMalloc(&c->d_cls, (size_t)N)) != cudaSuccess ||
         (e = cudaMalloc(&c->d_aux, (size_t)N * 4)) != cudaSuccess ||
-        (e = cudaMalloc(&c->d_red, RED_COUNT * sizeof(double))) != cudaSuccess) {
+        (e = cudaMalloc(&c->d_red, RED_COUNT * sizeof(double))) != cudaSuccess ||
+        (e = cudaMalloc(&c->d_err, sizeof(int))) != cudaSuccess ||
+        (e = cudaMemset(c->d_err, 0, sizeof(int))) != cudaSuccess) {
         s = fail(nullptr, e == cudaErrorMemoryAllocation ? LBM_ERR_OOM : LBM_ERR_CUDA, "lbm_create: %s", cudaGetErrorString(e));
         lbm_destroy(c);
         return s;
@@ -228,6 +240,7 @@ lbm_status lbm_destroy(lbm_ctx* c) {
     free_side(c);
     dfree(c->d_acc); dfree(c->d_uerr); dfree(c->d_red);
     dfree(c->d_rho_out); dfree(c->d_u_out); dfree(c->d_f_out); dfree(c->d_probe);
+    dfree(c->d_bulk_rows); dfree(c->d_other_rows); dfree(c->d_err);
     if (c->st) cudaStreamDestroy(c->st);
     delete c;
     return LBM_OK;
@@ -446,6 +459,33 @@ static lbm_status build_geometry(lbm_ctx* c) {
         CU(c, cudaMemcpy(c->d_out_dir, out_dir.data(), (size_t)n_out * 4, cudaMemcpyHostToDevice));
     }
     CU(c, cudaStreamSynchronize(c->st));
+    // rows the row-staged step may take (FP16-deviation storage): every cell bulk fluid, x periodic,
+    // segments a multiple of 16 bytes, one thread per x-pair
+    {
+        const long long nrow = (long long)ny * nz;
+        std::vector<int32_t> bulk, other;
+        c->rows_ok = (c->cfg.options & LBM_OPT_ROW_STAGING) && c->cfg.storage == LBM_STORAGE_F16DEV && wrap[0] &&
+                     nx % 2 == 0 && nx >= 64 && nx <= 1024 &&
+                     ((size_t)nx * c->esize) % 16 == 0 && nrow < (1LL << 31);
+        for (long long r = 0; r < nrow && c->rows_ok; r++) {
+            bool all = true;
+            for (int i = 0; i < nx && all; i++) all = (cls[(size_t)(r * nx + i)] & (uint8_t)~BIT_REFBULK) == CLS_BULK;
+            (all ? bulk : other).push_back((int32_t)r);
+        }
+        if (bulk.empty()) c->rows_ok = false;
+        dfree(c->d_bulk_rows); dfree(c->d_other_rows);
+        c->d_bulk_rows = c->d_other_rows = nullptr;
+        c->n_bulk_rows = (int)bulk.size();
+        c->n_other_rows = (int)other.size();
+        if (c->rows_ok) {
+            CU(c, cudaMalloc(&c->d_bulk_rows, bulk.size() * 4));
+            CU(c, cudaMemcpy(c->d_bulk_rows, bulk.data(), bulk.size() * 4, cudaMemcpyHostToDevice));
+            if (!other.empty()) {
+                CU(c, cudaMalloc(&c->d_other_rows, other.size() * 4));
+                CU(c, cudaMemcpy(c->d_other_rows, other.data(), other.size() * 4, cudaMemcpyHostToDevice));
+            }
+        }
+    }
     c->have_geom = true;
     return LBM_OK;
 }
@@ -561,11 +601,23 @@ lbm_status lbm_probe(lbm_ctx* c, int32_t x, int32_t y, int32_t z, double out[4])
     return LBM_OK;
 }
 
+// a bounded device wait that gave up leaves a code in the error word
+static lbm_status check_device_error(lbm_ctx* c) {
+    int h = 0;
+    CU(c, cudaMemcpyAsync(&h, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    if (h != 0) {
+        CU(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
+        return fail(c, LBM_ERR_TIMEOUT, "a row-staged step gave up waiting for its bulk copies (code %d)", h);
+    }
+    return LBM_OK;
+}
+
 lbm_status lbm_synchronize(lbm_ctx* c) {
     if (!c) return fail(c, LBM_ERR_INVALID, "null ctx");
     cudaSetDevice(c->cfg.device);
     CU(c, cudaStreamSynchronize(c->st));
-    return LBM_OK;
+    return check_device_error(c);
 }
 
 static lbm_status run_read(lbm_ctx* c, ReadOut& o) {
@@ -631,6 +683,8 @@ lbm_status lbm_reduce(lbm_ctx* c, lbm_diag* out) {
     out->nonfinite = (int64_t)h[RED_BAD];
     out->fluid_cells = (int64_t)h[RED_FLUID];
     out->step = c->m;
+    lbm_status ds = check_device_error(c);
+    if (ds) return ds;
     if (out->nonfinite > 0) return fail(c, LBM_ERR_NONFINITE, "%lld cells hold non-finite populations at step %lld",
                                         (long long)out->nonfinite, (long long)c->m);
     return LBM_OK;

@@ -98,6 +98,7 @@ struct Params {
     int n_out;
     // per-step options
     double* acc;             // time-average accumulators [10][N] (nullptr: off)
+    int* err;                // device error word (bounded waits that gave up)
 };
 
 // scalar parameters in the compute type

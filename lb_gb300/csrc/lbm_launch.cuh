@@ -4,6 +4,7 @@
 #include "lbm_aux.cuh"
 #include "lbm_launch.h"
 #include "lbm_step.cuh"
+#include "lbm_tma.cuh"
 
 namespace lbm {
 
@@ -26,6 +27,65 @@ template <class S>
 cudaError_t launch_step(const Params& p, int collision, int closure, cudaStream_t st) {
     if (collision == 0) return closure == 0 ? step_parity<S, 0, 0>(p, st) : step_parity<S, 0, 1>(p, st);
     return closure == 0 ? step_parity<S, 1, 0>(p, st) : step_parity<S, 1, 1>(p, st);
+}
+
+// row-staged step (cumulant collision, FP16-deviation storage); SW = shared elements per segment
+template <class S, int CLOS, int SW, bool ODD>
+static cudaError_t rows_launch(const Params& p, const int32_t* bulk, int nbulk, cudaStream_t st) {
+    const size_t smem = (size_t)kStages * 27 * SW * sizeof(typename S::T) + 64;
+    static int grid_of[64] = {};  // persistent grid per device (0: not computed yet)
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 64) return cudaErrorInvalidDevice;
+    const int threads = p.nx / 2;
+    if (grid_of[dev] == 0) {
+        cudaError_t e = cudaFuncSetAttribute(k_step_rows<S, 1, CLOS, ODD, SW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        int per_sm = 0, sms = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_rows<S, 1, CLOS, ODD, SW>, threads, smem);
+        if (e != cudaSuccess) return e;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+        grid_of[dev] = per_sm > 0 ? per_sm * sms : -1;
+    }
+    if (grid_of[dev] < 0) return cudaErrorInvalidConfiguration;
+    const int g = grid_of[dev] < nbulk ? grid_of[dev] : nbulk;
+    k_step_rows<S, 1, CLOS, ODD, SW><<<g, threads, smem, st>>>(p, bulk, nbulk);
+    return cudaGetLastError();
+}
+
+template <class S, int CLOS, int SW>
+static cudaError_t rows_parity(const Params& p, const int32_t* bulk, int nbulk, const int32_t* other, int nother,
+                               cudaStream_t st) {
+    const bool odd = (p.m & 1) != 0;
+    if (nother > 0) {
+        dim3 b = cell_block((p.nx + 1) / 2), g(((p.nx + 1) / 2 + b.x - 1) / b.x, nother);
+        if (odd) k_step_rowlist<S, 1, CLOS, true><<<g, b, 0, st>>>(p, other);
+        else     k_step_rowlist<S, 1, CLOS, false><<<g, b, 0, st>>>(p, other);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (nbulk > 0) return odd ? rows_launch<S, CLOS, SW, true>(p, bulk, nbulk, st) : rows_launch<S, CLOS, SW, false>(p, bulk, nbulk, st);
+    return cudaSuccess;
+}
+
+template <class S>
+cudaError_t launch_step_rows(const Params& p, int closure, const int32_t* bulk, int nbulk, const int32_t* other,
+                             int nother, cudaStream_t st) {
+    if constexpr (S::kind != 2) {
+        return cudaErrorInvalidValue;
+    } else {
+        constexpr int H = RowGeom<S>::H;
+        if (p.nx <= 256)
+            return closure == 0 ? rows_parity<S, 0, 256 + 2 * H>(p, bulk, nbulk, other, nother, st)
+                                : rows_parity<S, 1, 256 + 2 * H>(p, bulk, nbulk, other, nother, st);
+        if (p.nx <= 512)
+            return closure == 0 ? rows_parity<S, 0, 512 + 2 * H>(p, bulk, nbulk, other, nother, st)
+                                : rows_parity<S, 1, 512 + 2 * H>(p, bulk, nbulk, other, nother, st);
+        return closure == 0 ? rows_parity<S, 0, 1024 + 2 * H>(p, bulk, nbulk, other, nother, st)
+                            : rows_parity<S, 1, 1024 + 2 * H>(p, bulk, nbulk, other, nother, st);
+    }
 }
 
 template <class S>
@@ -56,6 +116,7 @@ cudaError_t launch_probe(const Params& p, int x, int y, int z, double* out, cuda
     template cudaError_t launch_read<S>(const Params&, const ReadOut&, cudaStream_t);                   \
     template cudaError_t launch_init<S>(const Params&, const double*, const double*, double, const double*, \
                                         const double*, cudaStream_t);                            \
-    template cudaError_t launch_probe<S>(const Params&, int, int, int, double*, cudaStream_t);
+    template cudaError_t launch_probe<S>(const Params&, int, int, int, double*, cudaStream_t);                  \
+    template cudaError_t launch_step_rows<S>(const Params&, int, const int32_t*, int, const int32_t*, int, cudaStream_t);
 
 }  // namespace lbm

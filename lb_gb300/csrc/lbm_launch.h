@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdint>
+
 namespace lbm {
 
 struct Params;
@@ -17,6 +19,11 @@ template <class S>
 cudaError_t launch_init(const Params& p, const double* rho, const double* u, double rho0, const double u0[3],
                         const double* pops, cudaStream_t st);
 
+// row-staged step for rows of bulk cells (cumulant, FP16-deviation storage, periodic x, nx <= 1024):
+// `bulk` lists the (y,z) rows whose cells are all bulk fluid, `other` the remaining rows
+template <class S>
+cudaError_t launch_step_rows(const Params& p, int closure, const int32_t* bulk, int nbulk, const int32_t* other,
+                             int nother, cudaStream_t st);
 template <class S>
 cudaError_t launch_probe(const Params& p, int x, int y, int z, double* out, cudaStream_t st);
 

@@ -142,6 +142,26 @@ __global__ void __launch_bounds__(128) k_step(Params p) {
     step_cell<S, COLL, CLOS, ODD>(p, x, blockIdx.y, blockIdx.z);
 }
 
+// moments, relaxation rate and collision of a packed pair of bulk cells
+// (time-average accumulation of the two cells idx0, idx0+1 when p.acc is set)
+template <int COLL, int CLOS>
+LBM_D void collide_pair(const Params& p, F2 (&f)[27], long long idx0) {
+    const Mom<F2> mm = raw_moments(f);
+    const F2 ri = rcp(mm.rho);
+    F2 ux = mm.jx * ri, uy = mm.jy * ri, uz = mm.jz * ri;
+    if (p.has_force) {
+        ux = lfma(F2(p.Ff[0]), F2(0.5f), mm.jx) * ri;
+        uy = lfma(F2(p.Ff[1]), F2(0.5f), mm.jy) * ri;
+        uz = lfma(F2(p.Ff[2]), F2(0.5f), mm.jz) * ri;
+    }
+    if (p.acc) {
+        acc_add(p, idx0, mm.rho.v.x, ux.v.x, uy.v.x, uz.v.x);
+        acc_add(p, idx0 + 1, mm.rho.v.y, ux.v.y, uy.v.y, uz.v.y);
+    }
+    collide_lane<COLL, CLOS>(f, mm, ri, ux, uy, uz, F2(p.tauf), F2(p.cles18f), F2(p.omega0f), p.has_force != 0,
+                             F2(p.Ff[0]), F2(p.Ff[1]), F2(p.Ff[2]));
+}
+
 // ---- x-pairs in packed FP32 ----------------------------------------------------------------------------
 // Cells idx0 (even x0) and idx0+1 of a bulk pair.  Even steps touch only the pair's own slots and odd
 // steps with c_x = 0 a pair in a neighbouring row: one aligned 64-bit (FP32) / 32-bit (FP16) access.
@@ -198,29 +218,83 @@ LBM_D void store_pair(const Params& p, const PairIdx& q, const PairCodec& k, con
     });
 }
 
+// bulk pairs on a periodic y or z seam: the neighbour rows wrap, so every access is formed from the
+// wrapped row bases R[dy+1][dz+1] and the wrapped x positions xm = x0-1, x2 = x0+2
+struct PairRows {
+    long long R[3][3];
+    int x0, xm, x2;
+};
+LBM_D void make_pair_rows(const Params& p, int x0, int y, int z, PairRows& w) {
+    for (int dz = -1; dz <= 1; dz++)
+        for (int dy = -1; dy <= 1; dy++) {
+            int yy = y + dy, zz = z + dz;
+            if (yy < 0) yy += p.ny; else if (yy >= p.ny) yy -= p.ny;
+            if (zz < 0) zz += p.nz; else if (zz >= p.nz) zz -= p.nz;
+            w.R[dy + 1][dz + 1] = ((long long)zz * p.ny + yy) * p.nx;
+        }
+    w.x0 = x0;
+    w.xm = x0 == 0 ? p.nx - 1 : x0 - 1;
+    w.x2 = x0 + 2 == p.nx ? 0 : x0 + 2;
+}
+template <class S, bool ODD>
+LBM_D void load_pair_rows(const Params& p, const PairRows& w, const PairCodec& k, F2 (&f)[27]) {
+    using T = typename S::T;
+    const T* A = (const T*)p.f;
+    sfor<0, 27>([&](auto vc) {
+        constexpr int V = decltype(vc)::value;
+        constexpr int slot = ODD ? opp(V) : V;
+        const T* a = A + (long long)slot * p.N + (ODD ? w.R[1 - cy(V)][1 - cz(V)] : w.R[1][1]);
+        constexpr bool split = ODD && cx(V) != 0;
+        // reads of cell x - c_v: c_x = +1 -> (x0-1, x0), c_x = -1 -> (x0+1, x0+2)
+        const int i0 = cx(V) > 0 ? w.xm : w.x0 + 1, i1 = cx(V) > 0 ? w.x0 : w.x2;
+        if constexpr (S::kind == 1) {
+            if constexpr (split) f[V] = F2(__ldg(a + i0), __ldg(a + i1));
+            else f[V] = F2(__ldg((const float2*)(a + w.x0)));
+        } else {
+            float2 t;
+            if constexpr (split) t = make_float2(__half2float(__ldg(a + i0)), __half2float(__ldg(a + i1)));
+            else t = __half22float2(__ldg((const __half2*)(a + w.x0)));
+            f[V] = lfma(F2(t), k.inv_scale, k.wr[csq(V)]);
+        }
+    });
+}
+template <class S, bool ODD>
+LBM_D void store_pair_rows(const Params& p, const PairRows& w, const PairCodec& k, const F2 (&f)[27]) {
+    using T = typename S::T;
+    T* A = (T*)p.f;
+    sfor<0, 27>([&](auto vc) {
+        constexpr int V = decltype(vc)::value;
+        constexpr int slot = ODD ? V : opp(V);
+        T* a = A + (long long)slot * p.N + (ODD ? w.R[1 + cy(V)][1 + cz(V)] : w.R[1][1]);
+        constexpr bool split = ODD && cx(V) != 0;
+        // writes to cell x + c_v: c_x = +1 -> (x0+1, x0+2), c_x = -1 -> (x0-1, x0)
+        const int i0 = cx(V) > 0 ? w.x0 + 1 : w.xm, i1 = cx(V) > 0 ? w.x2 : w.x0;
+        if constexpr (S::kind == 1) {
+            if constexpr (split) { a[i0] = f[V].v.x; a[i1] = f[V].v.y; }
+            else *(float2*)(a + w.x0) = f[V].v;
+        } else {
+            const F2 e = lfma(f[V], k.scale, k.nwrs[csq(V)]);
+            const __half2 h = __float22half2_rn(e.v);
+            if constexpr (split) { a[i0] = __low2half(h); a[i1] = __high2half(h); }
+            else *(__half2*)(a + w.x0) = h;
+        }
+    });
+}
+
+// one x-pair (x0 even): packed path for two bulk cells, else the per-cell path for each
 template <class S, int COLL, int CLOS, bool ODD>
-__global__ void __launch_bounds__(128) k_step2(Params p) {
+LBM_D void step_pair(const Params& p, int x0, int y, int z) {
     static_assert(S::kind != 0, "packed pairs are FP32 arithmetic");
-    const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
-    if (x0 >= p.nx) return;
-    const int y = blockIdx.y, z = blockIdx.z;
     const bool two = x0 + 1 < p.nx;
     const unsigned idx0 = (unsigned)x0 + (unsigned)p.nx * ((unsigned)y + (unsigned)p.ny * (unsigned)z);
     const uint8_t f0 = p.cls[idx0] & (uint8_t)~BIT_REFBULK;
     const uint8_t f1 = two ? (p.cls[idx0 + 1] & (uint8_t)~BIT_REFBULK) : (uint8_t)0;
-    // rows on a periodic y or z seam (whole blocks) take the per-cell path; x seams stay packed
-    const bool yz_seam = (p.wrap[1] && (y == 0 || y == p.ny - 1)) || (p.wrap[2] && (z == 0 || z == p.nz - 1));
-    const bool pair = two && f0 == CLS_BULK && f1 == CLS_BULK && (p.nx & 1) == 0 && p.acc == nullptr && !yz_seam;
+    const bool pair = two && f0 == CLS_BULK && f1 == CLS_BULK && (p.nx & 1) == 0;
     if (!pair) {
         step_cell_call<S, COLL, CLOS, ODD>(p, x0, y, z);
         if (two) step_cell_call<S, COLL, CLOS, ODD>(p, x0 + 1, y, z);
         return;
     }
-    PairIdx q;
-    q.e0 = (int)idx0;
-    q.e1 = q.e0 + 1;
-    q.eL = (p.wrap[0] && x0 == 0) ? q.e0 + p.nx : q.e0;
-    q.eR = (p.wrap[0] && x0 + 2 == p.nx) ? q.e1 - p.nx : q.e1;
     PairCodec k;
     if constexpr (S::kind == 2) {
         k.inv_scale = F2(p.inv_scale);
@@ -228,19 +302,33 @@ __global__ void __launch_bounds__(128) k_step2(Params p) {
         k.wr[0] = F2(p.wr[0]); k.wr[1] = F2(p.wr[1]); k.wr[2] = F2(p.wr[7]); k.wr[3] = F2(p.wr[19]);
         k.nwrs[0] = F2(p.nwrs[0]); k.nwrs[1] = F2(p.nwrs[1]); k.nwrs[2] = F2(p.nwrs[7]); k.nwrs[3] = F2(p.nwrs[19]);
     }
+    // rows on a periodic y or z seam (uniform per block) form their addresses from wrapped rows;
+    // all other rows use the per-direction base addresses (x seams wrap through eL / eR)
+    const bool yz_seam = (p.wrap[1] && (y == 0 || y == p.ny - 1)) || (p.wrap[2] && (z == 0 || z == p.nz - 1));
     F2 f[27];
-    load_pair<S, ODD>(p, q, k, f);
-    const Mom<F2> mm = raw_moments(f);
-    const F2 ri = rcp(mm.rho);
-    F2 ux = mm.jx * ri, uy = mm.jy * ri, uz = mm.jz * ri;
-    if (p.has_force) {
-        ux = lfma(F2(p.Ff[0]), F2(0.5f), mm.jx) * ri;
-        uy = lfma(F2(p.Ff[1]), F2(0.5f), mm.jy) * ri;
-        uz = lfma(F2(p.Ff[2]), F2(0.5f), mm.jz) * ri;
+    if (!yz_seam) {
+        PairIdx q;
+        q.e0 = (int)idx0;
+        q.e1 = q.e0 + 1;
+        q.eL = (p.wrap[0] && x0 == 0) ? q.e0 + p.nx : q.e0;
+        q.eR = (p.wrap[0] && x0 + 2 == p.nx) ? q.e1 - p.nx : q.e1;
+        load_pair<S, ODD>(p, q, k, f);
+        collide_pair<COLL, CLOS>(p, f, idx0);
+        store_pair<S, ODD>(p, q, k, f);
+    } else {
+        PairRows w;
+        make_pair_rows(p, x0, y, z, w);
+        load_pair_rows<S, ODD>(p, w, k, f);
+        collide_pair<COLL, CLOS>(p, f, idx0);
+        store_pair_rows<S, ODD>(p, w, k, f);
     }
-    collide_lane<COLL, CLOS>(f, mm, ri, ux, uy, uz, F2(p.tauf), F2(p.cles18f), F2(p.omega0f), p.has_force != 0,
-                             F2(p.Ff[0]), F2(p.Ff[1]), F2(p.Ff[2]));
-    store_pair<S, ODD>(p, q, k, f);
+}
+
+template <class S, int COLL, int CLOS, bool ODD>
+__global__ void __launch_bounds__(128) k_step2(Params p) {
+    const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (x0 >= p.nx) return;
+    step_pair<S, COLL, CLOS, ODD>(p, x0, blockIdx.y, blockIdx.z);
 }
 
 }  // namespace lbm
