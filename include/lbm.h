@@ -200,6 +200,66 @@ lbm_status lbm_voxelize_mesh_noalloc(const double* verts, int32_t nv, const int3
                                      double res, double add, int32_t* flags_out_device,
                                      int32_t dims_out[3], double bbox_out[6], int32_t device);
 
+/* ---- learned LES closure (no reference counterpart; the reference has OmegaLES only) -----------
+ * A per-cell MLP  x(7) -> 32 -> 32 -> 1  maps strain-rate invariants and density to the eddy
+ * viscosity:  nu_t = out_scale * softplus(z).  Hidden activation: GELU in its sigmoid form
+ * x * sigmoid(1.702 x).  Inputs, from the strain-rate tensor S (lattice units) and rho:
+ *   0 tr S, 1 I2 = (tr^2 S - S:S)/2, 2 I3 = det S, 3 Lode parameter 3 sqrt(6) det(S_d)/|S_d|^3,
+ *   4 S_d:S_d / S:S, 5 rho, 6 |S| = sqrt(2 S:S)        (S_d: deviatoric part)
+ * normalised as (x - in_mean) / in_std before the first layer.  Training keeps FP32 parameters;
+ * the step kernel evaluates FP16 copies on the tensor cores with FP32 accumulation and relaxes with
+ * tau = tau_0 + 3 nu_t.  In the step kernel S is estimated locally from the non-equilibrium stress,
+ * S = -3 Pi / (2 rho tau_S), tau_S being the Smagorinsky relaxation time; a cell whose raw input lies
+ * outside [in_lo, in_hi] (the training range), or that is not a bulk cell, relaxes with tau_S.
+ * params layout: w1[32][7], b1[32], w2[32][32], b2[32], w3[32], b3 (out x in, row-major). */
+#define LBM_MLP_INPUTS  7
+#define LBM_MLP_HIDDEN  32
+#define LBM_MLP_PARAMS  1345
+#define LBM_MLP_SAMPLE  10   /* floats per training sample: x[7], a, b, c */
+typedef struct lbm_mlp_model {
+    float params[LBM_MLP_PARAMS];
+    float in_mean[LBM_MLP_INPUTS], in_std[LBM_MLP_INPUTS];
+    float in_lo[LBM_MLP_INPUTS], in_hi[LBM_MLP_INPUTS];
+    float out_scale;
+} lbm_mlp_model;
+
+/* model of a context created with closure LBM_CLOSURE_MLP (FP32 or FP16DEV storage); required before
+ * the first lbm_step of such a context; may be replaced between steps */
+lbm_status lbm_mlp_load(lbm_ctx* ctx, const lbm_mlp_model* model);
+
+/* training samples from the current state of a run on a 4x-finer (generally width-x-finer) lattice:
+ * box filter of `width` fine cells per coarse cell, strain rate of the filtered velocity by central
+ * differences in coarse lattice units, filtered stress tau = <u u> - <u><u>.  A sample is
+ *   x[7] (the inputs above, of the filtered S and rho), a = tau_d:S_d, b = S_d:S_d, c = tau_d:tau_d,
+ * so that |tau_d + 2 nu_t S_d|^2 = c + 4 nu_t a + 4 nu_t^2 b is the subgrid-stress error of nu_t.
+ * Coarse cells whose 3x3x3 stencil touches a solid fine cell are left out.  Samples are written in
+ * coarse-cell order (x fastest) to out (LBM_MLP_SAMPLE floats each, nullable), at most `capacity`;
+ * *count receives the number of samples of the state (which may exceed capacity). */
+lbm_status lbm_les_samples(lbm_ctx* fine, int32_t width, float* out, int64_t capacity, int64_t* count);
+
+/* nu_t of n raw input vectors (x: n*7 floats) through the step kernel's FP16 tensor-core path;
+ * in_range (nullable) receives 1 where every input lies in [in_lo, in_hi] */
+lbm_status lbm_mlp_eval(const lbm_mlp_model* model, const float* x, int64_t n, float* nu,
+                        int32_t* in_range, int32_t device);
+
+/* GPU trainer: the samples (n * LBM_MLP_SAMPLE floats) are copied to the device once.  Loss of a set
+ * of samples: the mean of (c + 4 nu_t a + 4 nu_t^2 b) / K with K the mean of c over all the trainer's
+ * samples (loss 1 = the error of nu_t = 0). */
+typedef struct lbm_mlp_trainer lbm_mlp_trainer;
+lbm_status lbm_mlp_trainer_create(const float* samples, int64_t n, int32_t device, lbm_mlp_trainer** out);
+lbm_status lbm_mlp_trainer_destroy(lbm_mlp_trainer* trainer);
+double     lbm_mlp_trainer_norm(const lbm_mlp_trainer* trainer);   /* K */
+/* loss and its gradient (LBM_MLP_PARAMS floats, params layout) over samples [first, first+count),
+ * FP32 forward and backward kernels */
+lbm_status lbm_mlp_gradient(lbm_mlp_trainer* trainer, const lbm_mlp_model* model, int64_t first,
+                            int64_t count, float* grad, double* loss);
+/* `epochs` passes of Adam (beta 0.9, 0.999) over minibatches of `batch` samples (a multiple of 128)
+ * in a seeded random order; model->params is updated in place; loss_per_epoch (nullable, epochs
+ * floats) receives the mean minibatch loss of each epoch */
+lbm_status lbm_mlp_train(lbm_mlp_trainer* trainer, lbm_mlp_model* model, int32_t epochs, int32_t batch,
+                         float lr, uint64_t seed, float* loss_per_epoch);
+const char* lbm_mlp_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -49,6 +49,19 @@ class LbmConfig(C.Structure):
 LBM_OPT_ROW_STAGING = 1
 
 
+LBM_MLP_INPUTS = 7
+LBM_MLP_HIDDEN = 32
+LBM_MLP_PARAMS = 1345
+LBM_MLP_SAMPLE = 10
+
+
+class LbmMlpModel(C.Structure):
+    _fields_ = [("params", C.c_float * LBM_MLP_PARAMS),
+                ("in_mean", C.c_float * LBM_MLP_INPUTS), ("in_std", C.c_float * LBM_MLP_INPUTS),
+                ("in_lo", C.c_float * LBM_MLP_INPUTS), ("in_hi", C.c_float * LBM_MLP_INPUTS),
+                ("out_scale", C.c_float)]
+
+
 class LbmVertex(C.Structure):
     _fields_ = [("x", C.c_int32), ("y", C.c_int32), ("z", C.c_int32)]
 
@@ -124,6 +137,7 @@ def lib():
     L = C.CDLL(LIB_PATH)
     vp, i32, f64 = C.c_void_p, C.c_int32, C.c_double
     dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int32)
+    fp, i64 = C.POINTER(C.c_float), C.c_int64
     sig = {
         "lbm_create": ([C.POINTER(LbmConfig), C.POINTER(vp)], i32),
         "lbm_destroy": ([vp], i32),
@@ -152,6 +166,15 @@ def lib():
         "lbm_voxelize_off": ([C.c_char_p, f64, f64, dp, ip, ip, dp, i32], i32),
         "lbm_voxelize_mesh": ([dp, i32, ip, i32, f64, f64, ip, ip, dp, i32], i32),
         "lbm_voxelize_mesh_noalloc": ([dp, i32, ip, i32, f64, f64, C.c_void_p, ip, dp, i32], i32),
+        "lbm_mlp_load": ([vp, C.POINTER(LbmMlpModel)], i32),
+        "lbm_les_samples": ([vp, i32, fp, i64, C.POINTER(i64)], i32),
+        "lbm_mlp_eval": ([C.POINTER(LbmMlpModel), fp, i64, fp, ip, i32], i32),
+        "lbm_mlp_trainer_create": ([fp, i64, i32, C.POINTER(vp)], i32),
+        "lbm_mlp_trainer_destroy": ([vp], i32),
+        "lbm_mlp_trainer_norm": ([vp], f64),
+        "lbm_mlp_gradient": ([vp, C.POINTER(LbmMlpModel), i64, i64, fp, dp], i32),
+        "lbm_mlp_train": ([vp, C.POINTER(LbmMlpModel), i32, i32, C.c_float, C.c_uint64, fp], i32),
+        "lbm_mlp_last_error": ([], C.c_char_p),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -161,9 +184,9 @@ def lib():
     return L
 
 
-def check(status, ctx=None):
+def check(status, ctx=None, mlp=False):
     if status != LBM_OK:
         L = lib()
-        msg = L.lbm_last_error(ctx)
+        msg = L.lbm_mlp_last_error() if mlp else L.lbm_last_error(ctx)
         raise LbmError(status, (msg or b"").decode() or L.lbm_status_string(status).decode())
     return status

@@ -10,6 +10,7 @@
 #include "lbm_device.cuh"
 #include "lbm_aux.cuh"
 #include "lbm_launch.h"
+#include "lbm_mlp_host.h"
 
 #include <cmath>
 #include <cstdarg>
@@ -56,6 +57,9 @@ struct lbm_ctx {
     int n_bulk_rows = 0, n_other_rows = 0;
     int* d_err = nullptr;             // device error word
     bool rows_ok = false;             // the row-staged step applies to this lattice
+    uint4* d_mlp_frag = nullptr;      // learned closure: fragment table
+    MlpNorm mlp_norm{};
+    bool have_mlp = false;
     std::string err;
 };
 
@@ -123,6 +127,8 @@ static Params make_params(const lbm_ctx* c) {
     p.lid_state = c->d_lid_state; p.lid_n = c->d_lid_n; p.lid_u = c->d_lid_u; p.n_lid = c->n_lid;
     p.in_probe = c->d_in_probe; p.in_u = c->d_in_u; p.in_dir = c->d_in_dir; p.n_in = c->n_in;
     p.out_save = c->d_out_save; p.out_rho = c->d_out_rho; p.out_dir = c->d_out_dir; p.n_out = c->n_out;
+    p.mlp_frag = c->d_mlp_frag;
+    p.mlp = c->mlp_norm;
     p.acc = nullptr;
     p.err = c->d_err;
     return p;
@@ -186,8 +192,10 @@ lbm_status lbm_create(const lbm_config* cfg, lbm_ctx** out) {
         return fail(nullptr, LBM_ERR_UNSUPPORTED, "lattice of %lld cells is too large", N);
     if (cfg->collision != LBM_COLLISION_SRT && cfg->collision != LBM_COLLISION_CUMULANT2015)
         return fail(nullptr, LBM_ERR_UNSUPPORTED, "collision %d not implemented", cfg->collision);
-    if (cfg->closure != LBM_CLOSURE_NONE && cfg->closure != LBM_CLOSURE_SMAGORINSKY)
+    if (cfg->closure != LBM_CLOSURE_NONE && cfg->closure != LBM_CLOSURE_SMAGORINSKY && cfg->closure != LBM_CLOSURE_MLP)
         return fail(nullptr, LBM_ERR_UNSUPPORTED, "closure %d not implemented", cfg->closure);
+    if (cfg->closure == LBM_CLOSURE_MLP && cfg->storage == LBM_STORAGE_F64)
+        return fail(nullptr, LBM_ERR_UNSUPPORTED, "the learned closure runs with FP32 or FP16-deviation storage");
     if (cfg->storage < LBM_STORAGE_F64 || cfg->storage > LBM_STORAGE_F16DEV)
         return fail(nullptr, LBM_ERR_INVALID, "storage %d", cfg->storage);
     double tau = cfg->tau > 0 ? cfg->tau : 3.0 * cfg->nu + 0.5;
@@ -240,7 +248,7 @@ lbm_status lbm_destroy(lbm_ctx* c) {
     free_side(c);
     dfree(c->d_acc); dfree(c->d_uerr); dfree(c->d_red);
     dfree(c->d_rho_out); dfree(c->d_u_out); dfree(c->d_f_out); dfree(c->d_probe);
-    dfree(c->d_bulk_rows); dfree(c->d_other_rows); dfree(c->d_err);
+    dfree(c->d_bulk_rows); dfree(c->d_other_rows); dfree(c->d_err); dfree(c->d_mlp_frag);
     if (c->st) cudaStreamDestroy(c->st);
     delete c;
     return LBM_OK;
@@ -464,7 +472,7 @@ static lbm_status build_geometry(lbm_ctx* c) {
     {
         const long long nrow = (long long)ny * nz;
         std::vector<int32_t> bulk, other;
-        c->rows_ok = (c->cfg.options & LBM_OPT_ROW_STAGING) && c->cfg.storage == LBM_STORAGE_F16DEV && wrap[0] &&
+        c->rows_ok = (c->cfg.options & LBM_OPT_ROW_STAGING) && c->cfg.closure != LBM_CLOSURE_MLP && c->cfg.storage == LBM_STORAGE_F16DEV && wrap[0] &&
                      nx % 2 == 0 && nx >= 64 && nx <= 1024 &&
                      ((size_t)nx * c->esize) % 16 == 0 && nrow < (1LL << 31);
         for (long long r = 0; r < nrow && c->rows_ok; r++) {
@@ -545,6 +553,8 @@ lbm_status lbm_set_populations(lbm_ctx* c, const double* f) {
 lbm_status lbm_step(lbm_ctx* c, int32_t n) {
     if (!c || n < 0) return fail(c, LBM_ERR_INVALID, "lbm_step: bad argument");
     if (!c->initialized) return fail(c, LBM_ERR_STATE, "lbm_step before initialisation");
+    if (c->cfg.closure == LBM_CLOSURE_MLP && !c->have_mlp)
+        return fail(c, LBM_ERR_STATE, "closure LBM_CLOSURE_MLP needs lbm_mlp_load before lbm_step");
     cudaSetDevice(c->cfg.device);
     for (int s = 0; s < n; s++) {
         Params p = make_params(c);
@@ -868,6 +878,78 @@ lbm_status lbm_mesher_wall_pass(int32_t* fl, int32_t nx, int32_t ny, int32_t nz)
                         }
                 at(i, j, k) += add;
             }
+    return LBM_OK;
+}
+
+}  // extern "C"
+
+// ---- learned closure ----------------------------------------------------------------------------------
+extern "C" {
+
+lbm_status lbm_mlp_load(lbm_ctx* c, const lbm_mlp_model* m) {
+    if (!c || !m) return fail(c, LBM_ERR_INVALID, "lbm_mlp_load: null argument");
+    if (c->cfg.closure != LBM_CLOSURE_MLP)
+        return fail(c, LBM_ERR_STATE, "lbm_mlp_load: the context was not created with LBM_CLOSURE_MLP");
+    if (!mlp_model_valid(m)) return fail(c, LBM_ERR_INVALID, "lbm_mlp_load: non-finite parameters or bad scales");
+    cudaSetDevice(c->cfg.device);
+    std::vector<uint4> frag(kMlpFragRows * 32);
+    MlpNorm nm;
+    mlp_pack(*m, frag.data(), nm);
+    if (!c->d_mlp_frag) CU(c, cudaMalloc(&c->d_mlp_frag, frag.size() * sizeof(uint4)));
+    // ordered after the steps already queued on the context's stream
+    CU(c, cudaMemcpyAsync(c->d_mlp_frag, frag.data(), frag.size() * sizeof(uint4), cudaMemcpyHostToDevice, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    c->mlp_norm = nm;
+    c->have_mlp = true;
+    return LBM_OK;
+}
+
+lbm_status lbm_les_samples(lbm_ctx* c, int32_t w, float* out, int64_t capacity, int64_t* count) {
+    if (!c || !count || w < 1 || capacity < 0 || (capacity > 0 && !out))
+        return fail(c, LBM_ERR_INVALID, "lbm_les_samples: bad argument");
+    if (!c->initialized) return fail(c, LBM_ERR_STATE, "lbm_les_samples before initialisation");
+    const int nx = c->cfg.nx, ny = c->cfg.ny, nz = c->cfg.nz;
+    if (nx / w < 3 || ny / w < 3 || nz / w < 3)
+        return fail(c, LBM_ERR_INVALID, "lbm_les_samples: fewer than 3 coarse cells per axis");
+    cudaSetDevice(c->cfg.device);
+    const long long Nc = (long long)(nx / w) * (ny / w) * (nz / w);
+    double *d_rho = nullptr, *d_u = nullptr;
+    float *d_cf = nullptr, *d_out = nullptr;
+    auto cleanup = [&]() { dfree(d_rho); dfree(d_u); dfree(d_cf); dfree(d_out); };
+    cudaError_t e = cudaMalloc(&d_rho, (size_t)c->N * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&d_u, 3 * (size_t)c->N * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&d_cf, 11 * (size_t)Nc * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&d_out, 11 * (size_t)Nc * sizeof(float));
+    if (e != cudaSuccess) {
+        cleanup();
+        return fail(c, e == cudaErrorMemoryAllocation ? LBM_ERR_OOM : LBM_ERR_CUDA, "lbm_les_samples: %s",
+                    cudaGetErrorString(e));
+    }
+    Params p = make_params(c);
+    ReadOut o{};
+    o.rho = d_rho;
+    o.u = d_u;
+    o.mode = READ_MOMENTS;
+    switch (c->cfg.storage) {
+        case LBM_STORAGE_F64: e = launch_read<StF64>(p, o, c->st); break;
+        case LBM_STORAGE_F32: e = launch_read<StF32>(p, o, c->st); break;
+        default: e = launch_read<StF16>(p, o, c->st); break;
+    }
+    const int wrap[3] = {p.wrap[0], p.wrap[1], p.wrap[2]};
+    if (e == cudaSuccess) e = launch_les_samples(d_rho, d_u, c->d_cls, nx, ny, nz, w, wrap, d_cf, d_out, c->st);
+    std::vector<float> h(11 * (size_t)Nc);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), d_out, h.size() * sizeof(float), cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    cleanup();
+    if (e != cudaSuccess) return fail(c, LBM_ERR_CUDA, "lbm_les_samples: %s", cudaGetErrorString(e));
+    long long n = 0;
+    for (long long i = 0; i < Nc; i++) {
+        const float* r = &h[(size_t)i * 11];
+        if (r[10] < 0.5f) continue;
+        if (n < capacity) std::memcpy(out + (size_t)n * LBM_MLP_SAMPLE, r, LBM_MLP_SAMPLE * sizeof(float));
+        n++;
+    }
+    *count = n;
     return LBM_OK;
 }
 

@@ -30,6 +30,7 @@
 #define LBM_D __device__ __forceinline__
 
 #include "lbm_math.cuh"
+#include "lbm_mlp.cuh"
 
 namespace lbm {
 
@@ -96,6 +97,9 @@ struct Params {
     const float* out_rho;    // prescribed density
     const int32_t* out_dir;  // +1: normal +x, -1: normal -x
     int n_out;
+    // learned closure (LBM_CLOSURE_MLP): fragment table [kMlpFragRows][32] and input normalisation
+    const uint4* mlp_frag;
+    MlpNorm mlp;
     // per-step options
     double* acc;             // time-average accumulators [10][N] (nullptr: off)
     int* err;                // device error word (bounded waits that gave up)

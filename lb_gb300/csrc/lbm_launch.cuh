@@ -4,6 +4,7 @@
 #include "lbm_aux.cuh"
 #include "lbm_launch.h"
 #include "lbm_step.cuh"
+#include "lbm_step_mlp.cuh"
 #include "lbm_tma.cuh"
 
 namespace lbm {
@@ -17,14 +18,24 @@ static cudaError_t step_parity(const Params& p, cudaStream_t st) {
     } else {
         const int half = (p.nx + 1) / 2;  // one thread per x-pair
         dim3 g = cell_grid(half, p.ny, p.nz), b = cell_block(half);
-        if (p.m & 1) k_step2<S, COLL, CLOS, true><<<g, b, 0, st>>>(p);
-        else         k_step2<S, COLL, CLOS, false><<<g, b, 0, st>>>(p);
+        if constexpr (CLOS == 2) {
+            if (p.m & 1) k_step2_mlp<S, COLL, true><<<g, b, 0, st>>>(p);
+            else         k_step2_mlp<S, COLL, false><<<g, b, 0, st>>>(p);
+        } else {
+            if (p.m & 1) k_step2<S, COLL, CLOS, true><<<g, b, 0, st>>>(p);
+            else         k_step2<S, COLL, CLOS, false><<<g, b, 0, st>>>(p);
+        }
     }
     return cudaGetLastError();
 }
 
+// closure 2 (learned) runs on the packed path only: FP32 and FP16-deviation storage
 template <class S>
 cudaError_t launch_step(const Params& p, int collision, int closure, cudaStream_t st) {
+    if (closure == 2) {
+        if constexpr (S::kind == 0) return cudaErrorInvalidValue;
+        else return collision == 0 ? step_parity<S, 0, 2>(p, st) : step_parity<S, 1, 2>(p, st);
+    }
     if (collision == 0) return closure == 0 ? step_parity<S, 0, 0>(p, st) : step_parity<S, 0, 1>(p, st);
     return closure == 0 ? step_parity<S, 1, 0>(p, st) : step_parity<S, 1, 1>(p, st);
 }

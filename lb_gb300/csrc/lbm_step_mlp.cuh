@@ -1,0 +1,128 @@
+// lbm_step_mlp.cuh - the pair step kernel with the learned closure (LBM_CLOSURE_MLP, FP32 and
+// FP16-deviation storage).
+//
+// Same loads, collision and stores as k_step2; only the relaxation rate differs.  Per packed pair:
+//   1. moments and the non-equilibrium stress Pi = M - rho (u u + I/3), as the Smagorinsky closure;
+//   2. the Smagorinsky relaxation time tau_S (OmegaLES.h:117-124) and from it the strain-rate estimate
+//      S = -3 Pi / (2 rho tau_S), which is exact when the cell relaxed with tau_S (Pi = -2/3 rho tau S);
+//   3. the seven inputs of S and rho, normalised, as FP16 rows; the warp's 64 cells go through the
+//      tensor-core MLP together (mlp_warp), so every lane reaches it, including lanes without a pair;
+//   4. tau = tau_0 + 3 nu_t for cells whose inputs lie in the training range, tau_S otherwise.
+// Cells that are not packed bulk pairs take the per-cell path with the Smagorinsky closure.
+#pragma once
+
+#include "lbm_mlp.cuh"
+#include "lbm_step.cuh"
+
+namespace lbm {
+
+template <int COLL, class L>
+LBM_D void collide_with_rate(L (&f)[27], const Mom<L>& mm, L ri, L ux, L uy, L uz, L om, bool force, L Fx, L Fy,
+                             L Fz) {
+    if constexpr (COLL == 0) {
+        collide_srt(f, mm.rho, ux, uy, uz, om);
+        if (force) srt_force(f, ux, uy, uz, om, Fx, Fy, Fz);
+    } else {
+        collide_cum15(f, mm.rho, ri, ux, uy, uz, om, mm);
+    }
+}
+
+template <class S, int COLL, bool ODD>
+__global__ void __launch_bounds__(128) k_step2_mlp(Params p) {
+    static_assert(S::kind != 0, "the learned closure runs on the packed FP32 path");
+    __shared__ uint4 wf[kMlpFragRows][32];
+    __shared__ uint4 stage[4][64];
+    for (int i = threadIdx.x; i < kMlpFragRows * 32; i += blockDim.x) (&wf[0][0])[i] = p.mlp_frag[i];
+    __syncthreads();
+
+    const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = blockIdx.y, z = blockIdx.z;
+    const bool live = x0 < p.nx;
+    const bool two = x0 + 1 < p.nx;
+    const unsigned idx0 = (unsigned)(live ? x0 : 0) + (unsigned)p.nx * ((unsigned)y + (unsigned)p.ny * (unsigned)z);
+    const uint8_t f0 = live ? (p.cls[idx0] & (uint8_t)~BIT_REFBULK) : (uint8_t)0;
+    const uint8_t f1 = two ? (p.cls[idx0 + 1] & (uint8_t)~BIT_REFBULK) : (uint8_t)0;
+    const bool pair = two && f0 == CLS_BULK && f1 == CLS_BULK && (p.nx & 1) == 0;
+
+    PairCodec k;
+    if constexpr (S::kind == 2) {
+        k.inv_scale = F2(p.inv_scale);
+        k.scale = F2(p.scale);
+        k.wr[0] = F2(p.wr[0]); k.wr[1] = F2(p.wr[1]); k.wr[2] = F2(p.wr[7]); k.wr[3] = F2(p.wr[19]);
+        k.nwrs[0] = F2(p.nwrs[0]); k.nwrs[1] = F2(p.nwrs[1]); k.nwrs[2] = F2(p.nwrs[7]); k.nwrs[3] = F2(p.nwrs[19]);
+    }
+    const bool yz_seam = (p.wrap[1] && (y == 0 || y == p.ny - 1)) || (p.wrap[2] && (z == 0 || z == p.nz - 1));
+    PairIdx q;
+    q.e0 = (int)idx0;
+    q.e1 = q.e0 + 1;
+    q.eL = (p.wrap[0] && x0 == 0) ? q.e0 + p.nx : q.e0;
+    q.eR = (p.wrap[0] && x0 + 2 == p.nx) ? q.e1 - p.nx : q.e1;
+
+    F2 f[27];
+    Mom<F2> mm;
+    F2 ri, ux, uy, uz, om_s;
+    uint4 rowA = make_uint4(0, 0, 0, 0), rowB = rowA;
+    bool inA = false, inB = false;
+    if (pair) {
+        if (!yz_seam) {
+            load_pair<S, ODD>(p, q, k, f);
+        } else {
+            PairRows w;
+            make_pair_rows(p, x0, y, z, w);
+            load_pair_rows<S, ODD>(p, w, k, f);
+        }
+        mm = raw_moments(f);
+        ri = rcp(mm.rho);
+        ux = mm.jx * ri; uy = mm.jy * ri; uz = mm.jz * ri;
+        if (p.has_force) {
+            ux = lfma(F2(p.Ff[0]), F2(0.5f), mm.jx) * ri;
+            uy = lfma(F2(p.Ff[1]), F2(0.5f), mm.jy) * ri;
+            uz = lfma(F2(p.Ff[2]), F2(0.5f), mm.jz) * ri;
+        }
+        if (p.acc) {
+            acc_add(p, idx0, mm.rho.v.x, ux.v.x, uy.v.x, uz.v.x);
+            acc_add(p, idx0 + 1, mm.rho.v.y, ux.v.y, uy.v.y, uz.v.y);
+        }
+        // Pi and tau_S exactly as omega_smagorinsky
+        const F2 third = mm.rho * F2(1.0f / 3.0f);
+        const F2 rux = mm.rho * ux, ruy = mm.rho * uy, ruz = mm.rho * uz;
+        const F2 pxx = lfma(-rux, ux, mm.Mxx - third), pyy = lfma(-ruy, uy, mm.Myy - third),
+                 pzz = lfma(-ruz, uz, mm.Mzz - third);
+        const F2 pxy = lfma(-rux, uy, mm.Mxy), pxz = lfma(-rux, uz, mm.Mxz), pyz = lfma(-ruy, uz, mm.Myz);
+        const F2 off = lfma(pxy, pxy, lfma(pxz, pxz, pyz * pyz));
+        const F2 PI2 = lfma(pxx, pxx, lfma(pyy, pyy, lfma(pzz, pzz, off + off)));
+        const F2 PI = sqrt_pos(PI2);
+        const F2 tau = F2(p.tauf);
+        const F2 tles = lfma(tau, F2(0.5f), F2(0.5f) * sqrt_pos(lfma(tau, tau, F2(p.cles18f) * ri * PI)));
+        om_s = rcp(tles);
+        // strain rate S = -3 Pi / (2 rho tau_S)
+        const F2 sc = F2(-1.5f) * ri * om_s;
+        const F2 s[6] = {pxx * sc, pyy * sc, pzz * sc, pxy * sc, pxz * sc, pyz * sc};
+        F2 xf[7];
+        mlp_features(s, mm.rho, xf);
+        float xa[7], xb[7];
+#pragma unroll
+        for (int i = 0; i < 7; i++) { xa[i] = xf[i].v.x; xb[i] = xf[i].v.y; }
+        rowA = mlp_row(xa, p.mlp, inA);
+        rowB = mlp_row(xb, p.mlp, inB);
+    }
+    const float2 zo = mlp_warp(rowA, rowB, stage[threadIdx.x >> 5], wf);
+    if (pair) {
+        const float ta = p.tauf + 3.0f * mlp_nu(zo.x, p.mlp), tb = p.tauf + 3.0f * mlp_nu(zo.y, p.mlp);
+        const F2 om(inA ? __fdividef(1.0f, ta) : om_s.v.x, inB ? __fdividef(1.0f, tb) : om_s.v.y);
+        collide_with_rate<COLL>(f, mm, ri, ux, uy, uz, om, p.has_force != 0, F2(p.Ff[0]), F2(p.Ff[1]),
+                                F2(p.Ff[2]));
+        if (!yz_seam) {
+            store_pair<S, ODD>(p, q, k, f);
+        } else {
+            PairRows w;
+            make_pair_rows(p, x0, y, z, w);
+            store_pair_rows<S, ODD>(p, w, k, f);
+        }
+    } else if (live) {
+        step_cell_call<S, COLL, 1, ODD>(p, x0, y, z);
+        if (two) step_cell_call<S, COLL, 1, ODD>(p, x0 + 1, y, z);
+    }
+}
+
+}  // namespace lbm

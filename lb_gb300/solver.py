@@ -48,6 +48,10 @@ class OmegaNo:                                  # turbulence/OmegaNo.h
     code = capi.LBM_CLOSURE_NONE
 
 
+class OmegaMLP:                                 # learned closure (lb_gb300.les); no reference policy
+    code = capi.LBM_CLOSURE_MLP
+
+
 class StreamingAB:                              # streamings/StreamingAB.h (AA in place here)
     pass
 
@@ -252,6 +256,21 @@ class Solver:
         cnt = C.c_int64(0)
         self._check(lib().lbm_timeavg_get(self._ctx, _dp(r), _dp(u), _dp(uu), C.byref(cnt)))
         return r, u.reshape(3, self.N), uu.reshape(6, self.N), cnt.value
+
+    # -- learned closure
+    def load_mlp(self, model):
+        """Attach an lb_gb300.les.MlpModel (closure OmegaMLP)."""
+        self._check(lib().lbm_mlp_load(self._ctx, C.byref(model.struct())))
+
+    def les_samples(self, width=4):
+        """Filtered training samples of the current state (n x 10 float32, see lbm_les_samples)."""
+        n = C.c_int64(0)
+        self._check(lib().lbm_les_samples(self._ctx, int(width), None, 0, C.byref(n)))
+        out = np.zeros((n.value, capi.LBM_MLP_SAMPLE), np.float32)
+        if n.value:
+            self._check(lib().lbm_les_samples(self._ctx, int(width), out.ctypes.data_as(C.POINTER(C.c_float)),
+                                              n.value, C.byref(n)))
+        return out
 
     def checkpoint_save(self, path):
         self._check(lib().lbm_checkpoint_save(self._ctx, str(path).encode()))

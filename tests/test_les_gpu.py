@@ -1,0 +1,162 @@
+"""GPU checks of the learned LES closure: filtered samples, training gradients and FP16 evaluation
+against the CPU oracle (oracle/les_oracle.py); the fused step kernel's fallback; and what a network
+trained on the GPU gains over the Smagorinsky closure on held-out filtered data."""
+import numpy as np
+import pytest
+
+from lb_gb300 import cases, les
+from lb_gb300.solver import OmegaLES, OmegaMLP, Solver
+from oracle import les_oracle as lo
+
+pytestmark = pytest.mark.gpu
+
+
+def fine_channel(shape, steps, snapshots=(), storage="f32", seed=cases.SEED):
+    """FP32 cumulant + Smagorinsky channel; returns {step: samples} at the requested steps and the solver."""
+    c = cases.channel(*shape, re_tau=180.0, u_max=0.05, amp=0.3, seed=seed)
+    s = Solver(shape, turbulence=OmegaLES, storage=storage, nu=c["nu"], cles=0.17, periodic=c["periodic"],
+               force=c["force"])
+    s.set_flags(c["flags"])
+    s.set_bc()
+    s.init_fields(c["rho"], c["u"])
+    out = {}
+    done = 0
+    for k in sorted(set(snapshots) | {steps}):
+        s.step(k - done)
+        done = k
+        if k in snapshots:
+            out[k] = s.les_samples(4)
+    return out, s, c
+
+
+def test_samples_match_oracle(built_lib):
+    shape = (64, 34, 32)  # y: 32 fluid rows between the solid rows -> ny % 4 != 0 is left out
+    snaps, s, c = fine_channel(shape, 120, snapshots=(120,))
+    g = snaps[120]
+    rho, u = s.moments()
+    nx, ny, nz = shape
+    solid = c["flags"].reshape(nz, ny, nx) == 0
+    ref, idx = lo.samples_from_fields(rho.reshape(nz, ny, nx), u.reshape(3, nz, ny, nx), solid, 4, (1, 0, 1))
+    s.close()
+    assert g.shape == ref.shape and g.shape[0] > 100
+    for k in range(10):
+        col = ref[:, k]
+        rms = np.sqrt(np.mean(col * col)) + 1e-30
+        err = np.abs(g[:, k] - col) / rms
+        assert np.quantile(err, 0.999) < 2e-3, (k, np.quantile(err, 0.999))
+        assert err.max() < 5e-2, (k, err.max())
+
+
+def _model_and_samples(seed=7, n=4096):
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal((n, 7)) * np.array([1e-4, 1e-7, 1e-11, 0.5, 0.2, 1e-3, 1e-3]) + \
+        np.array([0, -1e-7, 0, 0, 0.9, 1.0, 2e-3])
+    b = np.abs(rng.standard_normal(n)) * 1e-6 + 1e-8
+    a = -np.abs(rng.standard_normal(n)) * 1e-9
+    c = a * a / b + np.abs(rng.standard_normal(n)) * 1e-12
+    s = np.concatenate([x, a[:, None], b[:, None], c[:, None]], axis=1).astype(np.float32)
+    m = les.MlpModel.init_from_samples(s, seed=seed)
+    return m, s
+
+
+def test_gradient_matches_oracle(built_lib):
+    m, s = _model_and_samples()
+    t = les.Trainer(s)
+    K = float(np.mean(s[:, 9].astype(np.float64)))
+    assert abs(t.norm - K) <= 1e-6 * K
+    for first, count in ((0, 4096), (128, 1000)):
+        loss, g = t.gradient(m, first, count)
+        ref_loss, ref_g = lo.loss_and_grad(m.params, s[first:first + count], m.in_mean, m.in_std, m.out_scale, t.norm)
+        assert abs(loss - ref_loss) <= 1e-5 * abs(ref_loss)
+        assert np.linalg.norm(g - ref_g) <= 1e-4 * np.linalg.norm(ref_g), np.linalg.norm(g - ref_g) / np.linalg.norm(ref_g)
+    t.close()
+
+
+def test_eval_matches_fp16_oracle(built_lib):
+    m, s = _model_and_samples(seed=11)
+    m.params[:] = np.random.default_rng(5).standard_normal(les.NPAR).astype(np.float32) * 0.3
+    x = s[:1000, :7]
+    nu, ok = les.evaluate(m, x)
+    ref, ref_ok = lo.infer_fp16(m.params, x, m.in_mean, m.in_std, m.in_lo, m.in_hi, m.out_scale)
+    assert np.array_equal(ok, ref_ok)
+    # tanh.approx.f16x2 against the exact tanh of the emulation, FP16 activations: 2 % of nu
+    rel = np.abs(nu - ref) / np.abs(ref)
+    assert np.quantile(rel, 0.99) < 2e-2 and rel.max() < 5e-2, (np.quantile(rel, 0.99), rel.max())
+    # inputs outside the range are flagged
+    xo = x.copy()
+    xo[::2, 6] = m.in_hi[6] * 2 + 1
+    _, ok2 = les.evaluate(m, xo)
+    assert not ok2[::2].any()
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16dev"])
+def test_fused_mlp_out_of_range_is_smagorinsky(built_lib, storage):
+    """A model whose training range excludes every input relaxes every cell with the Smagorinsky rate:
+    the populations equal those of the Smagorinsky kernel bit for bit."""
+    shape = (64, 18, 12)
+    c = cases.channel(*shape, re_tau=3.0, u_max=0.05, nu=0.01)
+    m, _ = _model_and_samples()
+    m.in_lo[:] = 1e30
+    m.in_hi[:] = 2e30
+    out = []
+    for clos in (OmegaLES, OmegaMLP):
+        s = Solver(shape, turbulence=clos, storage=storage, nu=c["nu"], cles=0.17, periodic=c["periodic"],
+                   force=c["force"])
+        s.set_flags(c["flags"])
+        s.set_bc()
+        s.init_fields(c["rho"], c["u"])
+        if clos is OmegaMLP:
+            s.load_mlp(m)
+        s.step(7)
+        out.append(s.populations())
+        s.close()
+    assert np.array_equal(out[0], out[1])
+
+
+def test_trained_closure_beats_smagorinsky(built_lib):
+    """Filtered samples of a 4x-finer channel at two times train the network on the GPU; on a third,
+    later time it must explain more of the filtered subgrid stress than the Smagorinsky closure (both as
+    the solver runs it, CLES = 0.17, and with the constant fitted to the training samples)."""
+    snaps, s, _ = fine_channel((128, 66, 64), 900, snapshots=(300, 600, 900))
+    s.close()
+    train = np.concatenate([snaps[300], snaps[600]])
+    test = snaps[900]
+    assert train.shape[0] > 4000 and test.shape[0] > 2000
+    m = les.MlpModel.init_from_samples(train)
+    t = les.Trainer(train)
+    hist = t.train(m, epochs=150, batch=512, lr=3e-3)
+    t.close()
+    assert hist[-1] < hist[0]
+    nu, ok = les.evaluate(m, test[:, :7])
+    nu = np.where(ok, nu, les.smagorinsky_nu(test, 0.17))
+    e_mlp = les.sgs_error(nu, test)
+    e_smag = les.sgs_error(les.smagorinsky_nu(test, 0.17), test)
+    cbest = les.best_constant(train)
+    e_best = les.sgs_error(les.smagorinsky_nu(test, cbest), test)
+    print(f"held-out relative SGS error: MLP {e_mlp:.4f}, Smagorinsky(0.17) {e_smag:.4f}, "
+          f"Smagorinsky(C*={cbest:.4f}) {e_best:.4f}, in range {ok.mean():.3f}")
+    assert e_mlp < e_best
+    assert e_mlp < e_smag
+
+
+def test_fused_mlp_channel_is_stable_and_conserves_mass(built_lib):
+    shape = (64, 34, 32)
+    snaps, s, c = fine_channel(shape, 200, snapshots=(200,))
+    s.close()
+    m = les.MlpModel.init_from_samples(snaps[200])
+    t = les.Trainer(snaps[200])
+    t.train(m, epochs=20, batch=256, lr=3e-3)
+    t.close()
+    for storage in ("f32", "f16dev"):
+        g = Solver(shape, turbulence=OmegaMLP, storage=storage, nu=c["nu"], cles=0.17, periodic=c["periodic"],
+                   force=c["force"])
+        g.set_flags(c["flags"])
+        g.set_bc()
+        g.init_fields(c["rho"], c["u"])
+        g.load_mlp(m)
+        d0 = g.reduce()
+        g.step(300)
+        d1 = g.reduce()
+        g.close()
+        assert d1.nonfinite == 0
+        assert abs(d1.mass - d0.mass) <= 2e-6 * d0.mass
