@@ -147,19 +147,22 @@ def channel_case(shape):
     return cases.channel(*shape, re_tau=180.0, u_max=0.05, amp=0.05)
 
 
-def make_solver(shape, case, storage, device, options=0):
-    from lb_gb300.solver import CollisionCumD3Q27Turbulent2015, OmegaLES, Solver
-    s = Solver(shape, collision=CollisionCumD3Q27Turbulent2015, turbulence=OmegaLES, storage=storage,
-               nu=case["nu"], cles=0.17, periodic=case["periodic"], force=case["force"], device=device,
-               options=options)
+def make_solver(shape, case, storage, device, options=0, model=None, interval=1):
+    """Cumulant collision with the Smagorinsky closure, or with the learned closure when a model is given."""
+    from lb_gb300.solver import CollisionCumD3Q27Turbulent2015, OmegaLES, OmegaMLP, Solver
+    s = Solver(shape, collision=CollisionCumD3Q27Turbulent2015, turbulence=OmegaMLP if model else OmegaLES,
+               storage=storage, nu=case["nu"], cles=0.17, periodic=case["periodic"], force=case["force"],
+               device=device, options=options, mlp_interval=interval)
     s.set_flags(case["flags"])
     s.set_bc()
     s.init_fields(case["rho"], case["u"])
+    if model:
+        s.load_mlp(model)
     return s
 
 
-def time_storage(shape, case, storage, steps, warmup, device, dist, with_clocks, options=0):
-    s = make_solver(shape, case, storage, device, options)
+def time_storage(shape, case, storage, steps, warmup, device, dist, with_clocks, options=0, model=None, interval=1):
+    s = make_solver(shape, case, storage, device, options, model, interval)
     s.step(warmup)
     s.synchronize()
     barrier(dist)
@@ -175,13 +178,14 @@ def time_storage(shape, case, storage, steps, warmup, device, dist, with_clocks,
     return ms, d, (sampler.summary() if sampler else None)
 
 
-def e2e_run(shape, case, storage, steps, device, options=0):
-    """End to end through the public API with host buffers: upload flags + initial fields, then
-    every step lbm_step + the reference's per-step probe read-back (u, rho of one cell)."""
-    from lb_gb300.solver import CollisionCumD3Q27Turbulent2015, OmegaLES, Solver
-    s = Solver(shape, collision=CollisionCumD3Q27Turbulent2015, turbulence=OmegaLES, storage=storage,
-               nu=case["nu"], cles=0.17, periodic=case["periodic"], force=case["force"], device=device,
-               options=options)
+def e2e_run(shape, case, storage, steps, device, options=0, model=None):
+    """End to end through the public API with host buffers: upload flags + initial fields (and the
+    learned closure's weights), then every step lbm_step + the reference's per-step probe read-back
+    (u, rho of one cell)."""
+    from lb_gb300.solver import CollisionCumD3Q27Turbulent2015, OmegaLES, OmegaMLP, Solver
+    s = Solver(shape, collision=CollisionCumD3Q27Turbulent2015, turbulence=OmegaMLP if model else OmegaLES,
+               storage=storage, nu=case["nu"], cles=0.17, periodic=case["periodic"], force=case["force"],
+               device=device, options=options)
     flags = np.ascontiguousarray(case["flags"], dtype=np.int32)
     rho = np.ascontiguousarray(case["rho"], dtype=np.float64)
     u = np.ascontiguousarray(case["u"], dtype=np.float64)
@@ -191,6 +195,8 @@ def e2e_run(shape, case, storage, steps, device, options=0):
     s.set_flags(flags)
     s.set_bc()
     s.init_fields(rho, u)
+    if model:
+        s.load_mlp(model)
     for _ in range(steps):
         s.step(1)
         s.probe(px, py, pz)
@@ -228,6 +234,24 @@ def cpu_reference(shape, case, steps, warmup, budget_s, threads=None):
     return dt / n, n, nth
 
 
+def learned_block(path, model, glups_mlp, glups_smag, interval=None):
+    if model is None:
+        return {"model": None, "note": "no model file: headline ran the Smagorinsky closure"}
+    rep = None
+    jp = path.replace(".npz", ".json")
+    if os.path.exists(jp):
+        with open(jp) as fh:
+            r = json.load(fh)
+        rep = {k: r.get(k) for k in ("fine_lattice", "train_samples", "held_out_sgs_error", "in_range_fraction")}
+    out = {"model": os.path.relpath(path, ROOT), "glups_f16_mlp": glups_mlp, "glups_f16_smagorinsky": glups_smag,
+           "throughput_cost": 1.0 - glups_mlp / glups_smag, "training": rep}
+    if interval:
+        k, g = interval
+        out["refresh_interval"] = {"k": k, "glups_f16_mlp": g, "throughput_cost": 1.0 - g / glups_smag,
+                                   "note": "network every k-th step, nu_t kept per cell in FP16 in between"}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -239,6 +263,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--options", type=int, default=0, help="LBM_OPT_* bits passed to lbm_create")
+    ap.add_argument("--mlp-interval", type=int, default=4,
+                    help="also time the learned closure with nu_t refreshed every k-th step")
+    ap.add_argument("--mlp", default=os.path.join(ROOT, "lb_gb300", "data", "les_mlp_channel.npz"),
+                    help="learned-closure model (lb_gb300.les_train); the headline runs FP16 storage with it")
     args = ap.parse_args()
     shape = tuple(int(v) for v in args.shape.split(","))
     N = shape[0] * shape[1] * shape[2]
@@ -274,13 +302,27 @@ def main():
     hbm, peak_kind = peaks()
     traffic = ncu_traffic()
 
+    model = None
+    if args.mlp and os.path.exists(args.mlp):
+        from lb_gb300 import les
+        model = les.MlpModel.load(args.mlp)
+    # headline: FP16-deviation storage with the learned closure (Smagorinsky when no model is present)
     ms16, d16, clk = time_storage(shape, case, "f16dev", args.steps, args.warmup, device, dist, rank == 0,
-                                 args.options)
+                                 args.options, model)
+    ms16s, d16s, _ = time_storage(shape, case, "f16dev", args.steps, args.warmup, device, dist, False, args.options) \
+        if model else (ms16, d16, None)
     ms32, d32, _ = time_storage(shape, case, "f32", args.steps, args.warmup, device, dist, False, args.options)
+    ms16k = None
+    if model and args.mlp_interval > 1:
+        ms16k, _, _ = time_storage(shape, case, "f16dev", args.steps, args.warmup, device, dist, False, args.options,
+                                   model, args.mlp_interval)
+        ms16k = dist_max(dist, ms16k)
     ms16 = dist_max(dist, ms16)
+    ms16s = dist_max(dist, ms16s)
     ms32 = dist_max(dist, ms32)
     cells = dist_sum(dist, float(N) * args.steps)
     glups16 = cells / (ms16 * 1e-3) / 1e9
+    glups16s = cells / (ms16s * 1e-3) / 1e9
     glups32 = cells / (ms32 * 1e-3) / 1e9
 
     def roof(kind, ms):
@@ -294,12 +336,12 @@ def main():
     e2e = None
     if not args.no_e2e:
         k = min(args.steps, 200)
-        dt, h2d, d2h = e2e_run(shape, case, "f16dev", k, device, args.options)
+        dt, h2d, d2h = e2e_run(shape, case, "f16dev", k, device, args.options, model)
         dt = dist_max(dist, dt)
         e2e = {"value": dist_sum(dist, float(N) * k) / dt / 1e9, "unit": "GLUPS",
                "h2d_bytes_per_step": h2d / k, "d2h_bytes_per_step": d2h, "steps": k,
-               "includes": "lbm_set_flags + lbm_set_bc + lbm_init_fields from host buffers, then per step "
-                           "lbm_step + lbm_probe (device->host read of u, rho)"}
+               "includes": "lbm_set_flags + lbm_set_bc + lbm_init_fields (+ lbm_mlp_load) from host buffers, "
+                           "then per step lbm_step + lbm_probe (device->host read of u, rho)"}
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         from oracle import build as obuild
@@ -315,16 +357,21 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms16 / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": workload, "nx": shape[0], "ny": shape[1], "nz": shape[2],
-                       "storage": "f16dev (f - w rho0) * 2^10, FP32 collision", "closure": "smagorinsky",
-                       "learned_closure": "not in this measurement",
+                       "storage": "f16dev (f - w rho0) * 2^10, FP32 collision",
+                       "closure": "learned MLP (tensor cores, fused), Smagorinsky fallback" if model else "smagorinsky",
                        "l2": "state 1.8 GB (f16) / 3.6 GB (f32) >> 129 MB L2; no flush needed",
                        "parallelism": f"{ws} independent replica(s)", "options": args.options},
             "roofline": roof("f16dev", ms16),
             "fp32_plain": {"value": glups32, "ms_per_step": ms32 / args.steps, "roofline": roof("f32", ms32),
-                           "speedup_f16_over_f32": glups16 / glups32},
+                           "closure": "smagorinsky", "speedup_f16_over_f32": glups16 / glups32},
+            "f16_smagorinsky": {"value": glups16s, "ms_per_step": ms16s / args.steps, "roofline": roof("f16dev", ms16s),
+                                "speedup_over_f32": glups16s / glups32},
+            "learned_closure": learned_block(args.mlp, model, glups16, glups16s,
+                                             (args.mlp_interval, cells / (ms16k * 1e-3) / 1e9) if ms16k else None),
             # one fused step kernel per step; the row-staged step adds the launch over the wall rows
             "gpu_launches": args.steps * (2 if args.options & 1 else 1), "clocks": clk, "cpu_baseline": cpu, "e2e": e2e,
-            "check": {"f16_mass": d16.mass, "f32_mass": d32.mass, "nonfinite": d16.nonfinite + d32.nonfinite}}
+            "check": {"f16_mass": d16.mass, "f32_mass": d32.mass,
+                      "nonfinite": d16.nonfinite + d32.nonfinite + d16s.nonfinite}}
     print(json.dumps(line))
 
 

@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define LBM_ABI_VERSION 1
+#define LBM_ABI_VERSION 2
 
 typedef int32_t lbm_status;
 #define LBM_OK                 0
@@ -76,6 +76,8 @@ typedef struct lbm_config {
     int32_t f16_scale_log2;   /* s of the FP16-deviation encoding (10 => 2^10) */
     int32_t device;           /* CUDA device ordinal */
     int32_t options;          /* LBM_OPT_* bits (0: defaults) */
+    int32_t mlp_interval;     /* learned closure: the network runs every k-th step (0, 1: every step);
+                                 in between each cell relaxes with its last nu_t (kept in FP16) */
 } lbm_config;
 
 /* implementation options (results are identical either way) */

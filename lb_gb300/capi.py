@@ -43,6 +43,7 @@ class LbmConfig(C.Structure):
         ("f16_scale_log2", C.c_int32),
         ("device", C.c_int32),
         ("options", C.c_int32),
+        ("mlp_interval", C.c_int32),
     ]
 
 
@@ -85,7 +86,7 @@ class LbmDiag(C.Structure):
 def make_config(nx, ny, nz, periodic=(0, 0, 0), collision=LBM_COLLISION_CUMULANT2015,
                 closure=LBM_CLOSURE_NONE, storage=LBM_STORAGE_F32, inlet_kind=LBM_INLET_MOVING_WALL,
                 nu=1.0 / 6.0, tau=0.0, cles=0.173, force=(0.0, 0.0, 0.0), rho0=1.0,
-                f16_scale_log2=10, device=0, options=0):
+                f16_scale_log2=10, device=0, options=0, mlp_interval=1):
     c = LbmConfig()
     c.nx, c.ny, c.nz = int(nx), int(ny), int(nz)
     for a in range(3):
@@ -94,6 +95,7 @@ def make_config(nx, ny, nz, periodic=(0, 0, 0), collision=LBM_COLLISION_CUMULANT
     c.collision, c.closure, c.storage, c.inlet_kind = int(collision), int(closure), int(storage), int(inlet_kind)
     c.nu, c.tau, c.cles, c.rho0 = float(nu), float(tau), float(cles), float(rho0)
     c.f16_scale_log2, c.device, c.options = int(f16_scale_log2), int(device), int(options)
+    c.mlp_interval = int(mlp_interval)
     return c
 
 

@@ -73,11 +73,49 @@ def cavity(n=64, u_lid=0.05, re=1000.0, wall=wall_pass_numpy):
 
 
 # ---- configs 2/3: turbulent channel -------------------------------------------------------------------
-def channel(nx, ny, nz, re_tau=180.0, u_max=0.05, amp=0.05, seed=SEED, nu=None, wall=wall_pass_numpy):
+def channel_modes(nx, ny, nz, h, rms, seed, n_modes=12):
+    """Divergence-free large-scale perturbation that vanishes at the walls: u = curl(chi, 0, psi) with
+    psi, chi = sum of g(eta) sin(k_x x + k_z z + phase), g = sin^2(pi eta), eta = (y - 0.5) / (2h), over
+    seeded modes k_x = 2 pi m_x / nx, k_z = 2 pi m_z / nz (m = 1..4).  Each component is a y-profile
+    times an (x, z) plane, so the field costs O(N).  Returns (3, nz, ny, nx) scaled to the given rms."""
+    rng = np.random.default_rng(seed)
+    y = np.arange(ny, dtype=np.float64)
+    eta = np.clip((y - 0.5) / (2.0 * h), 0.0, 1.0)
+    g = np.sin(np.pi * eta) ** 2
+    dg = np.pi * np.sin(2.0 * np.pi * eta) / (2.0 * h)  # d g / d y
+    dg[(eta <= 0.0) | (eta >= 1.0)] = 0.0
+    x = np.arange(nx, dtype=np.float64)[None, :]
+    z = np.arange(nz, dtype=np.float64)[:, None]
+    pu = np.zeros((nz, nx))
+    pv = np.zeros((nz, nx))
+    pw = np.zeros((nz, nx))
+    for _ in range(n_modes):
+        kx = 2.0 * np.pi * rng.integers(1, 5) / nx
+        kz = 2.0 * np.pi * rng.integers(1, 5) / nz
+        a, b = rng.standard_normal(2)
+        ph1, ph2 = rng.uniform(0.0, 2.0 * np.pi, 2)
+        t1 = kx * x + kz * z + ph1
+        t2 = kx * x + kz * z + ph2
+        pu += a * np.sin(t1)                              # u = d psi / d y
+        pv += -a * kx * np.cos(t1) + b * kz * np.cos(t2)  # v = -d psi / d x + d chi / d z
+        pw += -b * np.sin(t2)                             # w = -d chi / d y
+    u = np.empty((3, nz, ny, nx))
+    u[0] = dg[None, :, None] * pu[:, None, :]
+    u[1] = g[None, :, None] * pv[:, None, :]
+    u[2] = dg[None, :, None] * pw[:, None, :]
+    cur = np.sqrt(np.mean(u * u))
+    if cur > 0:
+        u *= rms / cur
+    return u
+
+
+def channel(nx, ny, nz, re_tau=180.0, u_max=0.05, amp=0.05, seed=SEED, nu=None, wall=wall_pass_numpy, modes=0.0):
     """Periodic in x and z, bounce-back solid rows y=0 and y=ny-1 (walls at y=0.5 and ny-1.5, half
     height h=(ny-2)/2).  Body force F_x = u_tau^2/h for Re_tau = u_tau h / nu.  nu (builder's
     choice when not given): the turbulent centre-line velocity of a Re_tau = 180 channel is about
-    18.3 u_tau, so u_tau = u_max / 18.3 and nu = u_tau h / Re_tau (tau = 0.5058 at h = 127)."""
+    18.3 u_tau, so u_tau = u_max / 18.3 and nu = u_tau h / Re_tau (tau = 0.5058 at h = 127).
+    Initial velocity: laminar profile, uniform seeded noise of amplitude amp * u_max per cell and
+    component, and (modes > 0) the divergence-free large-scale perturbation of rms modes * u_max."""
     f = np.ones((nz, ny, nx), dtype=np.int32)
     f[:, 0, :] = 0
     f[:, -1, :] = 0
@@ -97,6 +135,8 @@ def channel(nx, ny, nz, re_tau=180.0, u_max=0.05, amp=0.05, seed=SEED, nu=None, 
     for a in range(3):
         u[a] = (uniform(seed, idx, a) * 2.0 - 1.0) * amp * u_max
     u[0] += np.broadcast_to(prof[None, :, None], (nz, ny, nx)).reshape(-1)
+    if modes > 0.0:
+        u += channel_modes(nx, ny, nz, h, modes * u_max, seed).reshape(3, -1)
     solid = f.reshape(-1) == 0
     u[:, solid] = 0.0
     rho = np.ones(N)

@@ -60,6 +60,8 @@ struct lbm_ctx {
     uint4* d_mlp_frag = nullptr;      // learned closure: fragment table
     MlpNorm mlp_norm{};
     bool have_mlp = false;
+    __half* d_nut = nullptr;          // kept nu_t per cell (refresh interval > 1)
+    long long mlp_due = 0;            // next step in which the network runs
     std::string err;
 };
 
@@ -129,6 +131,8 @@ static Params make_params(const lbm_ctx* c) {
     p.out_save = c->d_out_save; p.out_rho = c->d_out_rho; p.out_dir = c->d_out_dir; p.n_out = c->n_out;
     p.mlp_frag = c->d_mlp_frag;
     p.mlp = c->mlp_norm;
+    p.nut = c->d_nut;
+    p.mlp_run = 0;
     p.acc = nullptr;
     p.err = c->d_err;
     return p;
@@ -194,6 +198,7 @@ lbm_status lbm_create(const lbm_config* cfg, lbm_ctx** out) {
         return fail(nullptr, LBM_ERR_UNSUPPORTED, "collision %d not implemented", cfg->collision);
     if (cfg->closure != LBM_CLOSURE_NONE && cfg->closure != LBM_CLOSURE_SMAGORINSKY && cfg->closure != LBM_CLOSURE_MLP)
         return fail(nullptr, LBM_ERR_UNSUPPORTED, "closure %d not implemented", cfg->closure);
+    if (cfg->mlp_interval < 0) return fail(nullptr, LBM_ERR_INVALID, "mlp_interval %d < 0", cfg->mlp_interval);
     if (cfg->closure == LBM_CLOSURE_MLP && cfg->storage == LBM_STORAGE_F64)
         return fail(nullptr, LBM_ERR_UNSUPPORTED, "the learned closure runs with FP32 or FP16-deviation storage");
     if (cfg->storage < LBM_STORAGE_F64 || cfg->storage > LBM_STORAGE_F16DEV)
@@ -248,7 +253,7 @@ lbm_status lbm_destroy(lbm_ctx* c) {
     free_side(c);
     dfree(c->d_acc); dfree(c->d_uerr); dfree(c->d_red);
     dfree(c->d_rho_out); dfree(c->d_u_out); dfree(c->d_f_out); dfree(c->d_probe);
-    dfree(c->d_bulk_rows); dfree(c->d_other_rows); dfree(c->d_err); dfree(c->d_mlp_frag);
+    dfree(c->d_bulk_rows); dfree(c->d_other_rows); dfree(c->d_err); dfree(c->d_mlp_frag); dfree(c->d_nut);
     if (c->st) cudaStreamDestroy(c->st);
     delete c;
     return LBM_OK;
@@ -563,6 +568,10 @@ lbm_status lbm_step(lbm_ctx* c, int32_t n) {
             c->avg_last = c->m;
             c->avg_count++;
         }
+        if (c->d_nut && c->m >= c->mlp_due) {
+            p.mlp_run = 1;
+            c->mlp_due = c->m + c->cfg.mlp_interval;
+        }
         cudaError_t e = do_step(c, p);
         if (e != cudaSuccess) return fail(c, LBM_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));
         c->m++;
@@ -856,6 +865,7 @@ lbm_status lbm_checkpoint_load(lbm_ctx* c, const char* path) {
     std::fclose(fp);
     if (!ok) return fail(c, LBM_ERR_IO, "reading %s failed", path);
     c->m = m;
+    c->mlp_due = m;  // kept nu_t are not in the file: the network runs in the next step
     c->initialized = true;
     c->avg_on = false;
     return LBM_OK;
@@ -898,9 +908,14 @@ lbm_status lbm_mlp_load(lbm_ctx* c, const lbm_mlp_model* m) {
     if (!c->d_mlp_frag) CU(c, cudaMalloc(&c->d_mlp_frag, frag.size() * sizeof(uint4)));
     // ordered after the steps already queued on the context's stream
     CU(c, cudaMemcpyAsync(c->d_mlp_frag, frag.data(), frag.size() * sizeof(uint4), cudaMemcpyHostToDevice, c->st));
+    if (c->cfg.mlp_interval > 1 && !c->d_nut) {
+        CU(c, cudaMalloc(&c->d_nut, (size_t)c->N * sizeof(__half)));
+        CU(c, cudaMemsetAsync(c->d_nut, 0xFF, (size_t)c->N * sizeof(__half), c->st));  // not a number: fallback
+    }
     CU(c, cudaStreamSynchronize(c->st));
     c->mlp_norm = nm;
     c->have_mlp = true;
+    c->mlp_due = c->m;  // the network runs in the next step
     return LBM_OK;
 }
 

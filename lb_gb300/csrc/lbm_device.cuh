@@ -100,6 +100,8 @@ struct Params {
     // learned closure (LBM_CLOSURE_MLP): fragment table [kMlpFragRows][32] and input normalisation
     const uint4* mlp_frag;
     MlpNorm mlp;
+    __half* nut;             // per-cell nu_t of the last network evaluation (refresh interval > 1)
+    int mlp_run;             // with nut: the network runs in this step
     // per-step options
     double* acc;             // time-average accumulators [10][N] (nullptr: off)
     int* err;                // device error word (bounded waits that gave up)

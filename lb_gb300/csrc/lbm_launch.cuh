@@ -19,8 +19,17 @@ static cudaError_t step_parity(const Params& p, cudaStream_t st) {
         const int half = (p.nx + 1) / 2;  // one thread per x-pair
         dim3 g = cell_grid(half, p.ny, p.nz), b = cell_block(half);
         if constexpr (CLOS == 2) {
-            if (p.m & 1) k_step2_mlp<S, COLL, true><<<g, b, 0, st>>>(p);
-            else         k_step2_mlp<S, COLL, false><<<g, b, 0, st>>>(p);
+            // p.nut == nullptr: network every step; else mlp_run says whether it runs in this step
+            if (!p.nut) {
+                if (p.m & 1) k_step2_mlp<S, COLL, true, 0><<<g, b, 0, st>>>(p);
+                else         k_step2_mlp<S, COLL, false, 0><<<g, b, 0, st>>>(p);
+            } else if (p.mlp_run) {
+                if (p.m & 1) k_step2_mlp<S, COLL, true, 1><<<g, b, 0, st>>>(p);
+                else         k_step2_mlp<S, COLL, false, 1><<<g, b, 0, st>>>(p);
+            } else {
+                if (p.m & 1) k_step2_mlp<S, COLL, true, 2><<<g, b, 0, st>>>(p);
+                else         k_step2_mlp<S, COLL, false, 2><<<g, b, 0, st>>>(p);
+            }
         } else {
             if (p.m & 1) k_step2<S, COLL, CLOS, true><<<g, b, 0, st>>>(p);
             else         k_step2<S, COLL, CLOS, false><<<g, b, 0, st>>>(p);

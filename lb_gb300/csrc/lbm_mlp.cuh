@@ -110,9 +110,10 @@ LBM_D void ldmatrix_x4(uint32_t (&r)[4], const void* smem_row) {
                  : "r"(a));
 }
 
-// normalisation and training range of the inputs (uniform over the launch)
+// normalisation and training range of the inputs (uniform over the launch):
+// normalised input = fma(x, isd, nmi) with isd = 1/std, nmi = -mean/std (rounded to FP32)
 struct MlpNorm {
-    float mu[7], isd[7], lo[7], hi[7];
+    float isd[7], nmi[7], lo[7], hi[7];
     float b3, scale;
 };
 
@@ -122,7 +123,7 @@ LBM_D uint4 mlp_row(const float (&x)[7], const MlpNorm& nm, bool& in_range) {
     bool ok = true;
 #pragma unroll
     for (int i = 0; i < 7; i++) {
-        h[i] = (x[i] - nm.mu[i]) * nm.isd[i];
+        h[i] = fmaf(x[i], nm.isd[i], nm.nmi[i]);
         ok = ok && h[i] >= nm.lo[i] && h[i] <= nm.hi[i];
     }
     h[7] = 1.0f;
@@ -133,6 +134,27 @@ LBM_D uint4 mlp_row(const float (&x)[7], const MlpNorm& nm, bool& in_range) {
     r.z = h2_bits(__floats2half2_rn(h[4], h[5]));
     r.w = h2_bits(__floats2half2_rn(h[6], h[7]));
     return r;
+}
+// the same for the two cells of a packed pair (one FFMA2 per input)
+LBM_D void mlp_rows2(const F2 (&x)[7], const MlpNorm& nm, uint4& ra, uint4& rb, bool& ia, bool& ib) {
+    F2 h[7];
+    bool oa = true, ob = true;
+#pragma unroll
+    for (int i = 0; i < 7; i++) {
+        h[i] = lfma(x[i], F2(nm.isd[i]), F2(nm.nmi[i]));
+        oa = oa && h[i].v.x >= nm.lo[i] && h[i].v.x <= nm.hi[i];
+        ob = ob && h[i].v.y >= nm.lo[i] && h[i].v.y <= nm.hi[i];
+    }
+    ia = oa;
+    ib = ob;
+    ra.x = h2_bits(__floats2half2_rn(h[0].v.x, h[1].v.x));
+    ra.y = h2_bits(__floats2half2_rn(h[2].v.x, h[3].v.x));
+    ra.z = h2_bits(__floats2half2_rn(h[4].v.x, h[5].v.x));
+    ra.w = h2_bits(__floats2half2_rn(h[6].v.x, 1.0f));
+    rb.x = h2_bits(__floats2half2_rn(h[0].v.y, h[1].v.y));
+    rb.y = h2_bits(__floats2half2_rn(h[2].v.y, h[3].v.y));
+    rb.z = h2_bits(__floats2half2_rn(h[4].v.y, h[5].v.y));
+    rb.w = h2_bits(__floats2half2_rn(h[6].v.y, 1.0f));
 }
 
 // Output pre-activation z (without b3) of the two cells of every lane.  Rows: lane l's first cell is
@@ -147,20 +169,14 @@ LBM_D float2 mlp_warp(uint4 rowA, uint4 rowB, uint4* stage, const uint4 (*wf)[32
     ldmatrix_x4(a01, stage + lane);       // m-tiles 0, 1 (rows 0..31)
     ldmatrix_x4(a23, stage + 32 + lane);  // m-tiles 2, 3 (rows 32..63)
     __syncwarp();                          // the stage takes the outputs below
-    const uint4 w1 = wf[0][lane];
-    uint4 w2[4];
-#pragma unroll
-    for (int j = 0; j < 4; j++) w2[j] = wf[1 + j][lane];
-    const uint4 w3 = wf[5][lane];
-    const float4 bA = *reinterpret_cast<const float4*>(&wf[6][lane]);
-    const float4 bB = *reinterpret_cast<const float4*>(&wf[7][lane]);
-    const float b2[4][2] = {{bA.x, bA.y}, {bA.z, bA.w}, {bB.x, bB.y}, {bB.z, bB.w}};
-    const uint32_t w1j[4] = {w1.x, w1.y, w1.z, w1.w};
     float* out = reinterpret_cast<float*>(stage);
-#pragma unroll
+    // one m-tile at a time, weight fragments re-read from shared memory per tile (few live registers)
+#pragma unroll 1
     for (int t = 0; t < 4; t++) {
-        const uint32_t a0 = t < 2 ? a01[2 * t] : a23[2 * (t - 2)];
-        const uint32_t a1 = t < 2 ? a01[2 * t + 1] : a23[2 * (t - 2) + 1];
+        const uint32_t a0 = t == 0 ? a01[0] : t == 1 ? a01[2] : t == 2 ? a23[0] : a23[2];
+        const uint32_t a1 = t == 0 ? a01[1] : t == 1 ? a01[3] : t == 2 ? a23[1] : a23[3];
+        const uint4 w1 = wf[0][lane];
+        const uint32_t w1j[4] = {w1.x, w1.y, w1.z, w1.w};
         uint32_t h[4][2];
 #pragma unroll
         for (int j = 0; j < 4; j++) {
@@ -169,15 +185,20 @@ LBM_D float2 mlp_warp(uint4 rowA, uint4 rowB, uint4* stage, const uint4 (*wf)[32
             h[j][0] = mlp_act(d[0], d[1]);
             h[j][1] = mlp_act(d[2], d[3]);
         }
+        const float4 bA = *reinterpret_cast<const float4*>(&wf[6][lane]);
+        const float4 bB = *reinterpret_cast<const float4*>(&wf[7][lane]);
+        const float b2[4][2] = {{bA.x, bA.y}, {bA.z, bA.w}, {bB.x, bB.y}, {bB.z, bB.w}};
         uint32_t h2[4][2];
 #pragma unroll
         for (int j = 0; j < 4; j++) {
+            const uint4 w2 = wf[1 + j][lane];
             float d[4] = {b2[j][0], b2[j][1], b2[j][0], b2[j][1]};
-            mma_k16(d, h[0][0], h[0][1], h[1][0], h[1][1], w2[j].x, w2[j].y);
-            mma_k16(d, h[2][0], h[2][1], h[3][0], h[3][1], w2[j].z, w2[j].w);
+            mma_k16(d, h[0][0], h[0][1], h[1][0], h[1][1], w2.x, w2.y);
+            mma_k16(d, h[2][0], h[2][1], h[3][0], h[3][1], w2.z, w2.w);
             h2[j][0] = mlp_act(d[0], d[1]);
             h2[j][1] = mlp_act(d[2], d[3]);
         }
+        const uint4 w3 = wf[5][lane];
         float d[4] = {0.f, 0.f, 0.f, 0.f};
         mma_k16(d, h2[0][0], h2[0][1], h2[1][0], h2[1][1], w3.x, w3.y);
         mma_k16(d, h2[2][0], h2[2][1], h2[3][0], h2[3][1], w3.z, w3.w);

@@ -9,6 +9,9 @@
 //      tensor-core MLP together (mlp_warp), so every lane reaches it, including lanes without a pair;
 //   4. tau = tau_0 + 3 nu_t for cells whose inputs lie in the training range, tau_S otherwise.
 // Cells that are not packed bulk pairs take the per-cell path with the Smagorinsky closure.
+// MODE 0: the network runs in this step.  MODE 1: it runs and its nu_t (or -1 for the fallback) is kept
+// per cell in FP16 (Params::nut).  MODE 2: it does not run; each pair relaxes with the kept nu_t (the
+// Smagorinsky rate where the kept value is negative or not a number).
 #pragma once
 
 #include "lbm_mlp.cuh"
@@ -27,13 +30,15 @@ LBM_D void collide_with_rate(L (&f)[27], const Mom<L>& mm, L ri, L ux, L uy, L u
     }
 }
 
-template <class S, int COLL, bool ODD>
+template <class S, int COLL, bool ODD, int MODE>
 __global__ void __launch_bounds__(128) k_step2_mlp(Params p) {
     static_assert(S::kind != 0, "the learned closure runs on the packed FP32 path");
-    __shared__ uint4 wf[kMlpFragRows][32];
-    __shared__ uint4 stage[4][64];
-    for (int i = threadIdx.x; i < kMlpFragRows * 32; i += blockDim.x) (&wf[0][0])[i] = p.mlp_frag[i];
-    __syncthreads();
+    __shared__ uint4 wf[MODE == 2 ? 1 : kMlpFragRows][32];
+    __shared__ uint4 stage[MODE == 2 ? 1 : 4][64];
+    if constexpr (MODE != 2) {
+        for (int i = threadIdx.x; i < kMlpFragRows * 32; i += blockDim.x) (&wf[0][0])[i] = p.mlp_frag[i];
+        __syncthreads();
+    }
 
     const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int y = blockIdx.y, z = blockIdx.z;
@@ -63,6 +68,7 @@ __global__ void __launch_bounds__(128) k_step2_mlp(Params p) {
     F2 ri, ux, uy, uz, om_s;
     uint4 rowA = make_uint4(0, 0, 0, 0), rowB = rowA;
     bool inA = false, inB = false;
+    (void)rowA; (void)rowB; (void)inA; (void)inB;
     if (pair) {
         if (!yz_seam) {
             load_pair<S, ODD>(p, q, k, f);
@@ -95,21 +101,30 @@ __global__ void __launch_bounds__(128) k_step2_mlp(Params p) {
         const F2 tau = F2(p.tauf);
         const F2 tles = lfma(tau, F2(0.5f), F2(0.5f) * sqrt_pos(lfma(tau, tau, F2(p.cles18f) * ri * PI)));
         om_s = rcp(tles);
-        // strain rate S = -3 Pi / (2 rho tau_S)
-        const F2 sc = F2(-1.5f) * ri * om_s;
-        const F2 s[6] = {pxx * sc, pyy * sc, pzz * sc, pxy * sc, pxz * sc, pyz * sc};
-        F2 xf[7];
-        mlp_features(s, mm.rho, xf);
-        float xa[7], xb[7];
-#pragma unroll
-        for (int i = 0; i < 7; i++) { xa[i] = xf[i].v.x; xb[i] = xf[i].v.y; }
-        rowA = mlp_row(xa, p.mlp, inA);
-        rowB = mlp_row(xb, p.mlp, inB);
+        if constexpr (MODE != 2) {
+            // strain rate S = -3 Pi / (2 rho tau_S)
+            const F2 sc = F2(-1.5f) * ri * om_s;
+            const F2 s[6] = {pxx * sc, pyy * sc, pzz * sc, pxy * sc, pxz * sc, pyz * sc};
+            F2 xf[7];
+            mlp_features(s, mm.rho, xf);
+            mlp_rows2(xf, p.mlp, rowA, rowB, inA, inB);
+        }
     }
-    const float2 zo = mlp_warp(rowA, rowB, stage[threadIdx.x >> 5], wf);
+    float nuA = -1.0f, nuB = -1.0f;
+    if constexpr (MODE != 2) {
+        const float2 zo = mlp_warp(rowA, rowB, stage[threadIdx.x >> 5], wf);
+        if (inA) nuA = mlp_nu(zo.x, p.mlp);
+        if (inB) nuB = mlp_nu(zo.y, p.mlp);
+        if (MODE == 1 && pair) *(__half2*)(p.nut + idx0) = __floats2half2_rn(nuA, nuB);
+    } else if (pair) {
+        const float2 kept = __half22float2(*(const __half2*)(p.nut + idx0));
+        nuA = kept.x;
+        nuB = kept.y;
+    }
     if (pair) {
-        const float ta = p.tauf + 3.0f * mlp_nu(zo.x, p.mlp), tb = p.tauf + 3.0f * mlp_nu(zo.y, p.mlp);
-        const F2 om(inA ? __fdividef(1.0f, ta) : om_s.v.x, inB ? __fdividef(1.0f, tb) : om_s.v.y);
+        // nu >= 0 is false for the fallback mark (-1) and for a kept value that is not a number
+        const F2 om(nuA >= 0.0f ? __fdividef(1.0f, lfma(3.0f, nuA, p.tauf)) : om_s.v.x,
+                    nuB >= 0.0f ? __fdividef(1.0f, lfma(3.0f, nuB, p.tauf)) : om_s.v.y);
         collide_with_rate<COLL>(f, mm, ri, ux, uy, uz, om, p.has_force != 0, F2(p.Ff[0]), F2(p.Ff[1]),
                                 F2(p.Ff[2]));
         if (!yz_seam) {

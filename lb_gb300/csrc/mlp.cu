@@ -346,10 +346,10 @@ void mlp_pack(const lbm_mlp_model& m, uint4* frag, MlpNorm& nm) {
         frag[7 * 32 + lane] = make_uint4(B2(16 + 2 * c), B2(17 + 2 * c), B2(24 + 2 * c), B2(25 + 2 * c));
     }
     for (int i = 0; i < 7; i++) {
-        nm.mu[i] = m.in_mean[i];
         nm.isd[i] = 1.0f / m.in_std[i];
-        nm.lo[i] = (m.in_lo[i] - m.in_mean[i]) * nm.isd[i];
-        nm.hi[i] = (m.in_hi[i] - m.in_mean[i]) * nm.isd[i];
+        nm.nmi[i] = -(m.in_mean[i] * nm.isd[i]);
+        nm.lo[i] = std::fma(m.in_lo[i], nm.isd[i], nm.nmi[i]);
+        nm.hi[i] = std::fma(m.in_hi[i], nm.isd[i], nm.nmi[i]);
     }
     nm.b3 = m.params[kMlpB3];
     nm.scale = m.out_scale;

@@ -143,6 +143,15 @@ def sgs_error(nu, samples):
     return float(np.sum(c + 4.0 * nu * a + 4.0 * nu * nu * b) / np.sum(c))
 
 
+def sgs_dissipation_error(nu, samples):
+    """Relative error of the subgrid dissipation: the model transfers 2 nu S_d:S_d = 2 nu b, the filtered
+    field -tau_d:S_d = -a; returns sum (2 nu b + a)^2 / sum a^2."""
+    s = np.asarray(samples, np.float64)
+    nu = np.asarray(nu, np.float64)
+    a, b = s[:, 7], s[:, 8]
+    return float(np.sum((2.0 * nu * b + a) ** 2) / np.sum(a * a))
+
+
 def smagorinsky_nu(samples, cles):
     """The eddy viscosity of the Smagorinsky closure as the solver runs it (OmegaLES.h:117-124):
     tau_S = tau/2 + sqrt(tau^2 + 18 CLES |Pi|/rho)/2 with |Pi| = 2/3 rho tau_S |S|_F gives

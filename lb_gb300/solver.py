@@ -141,14 +141,16 @@ class Solver:
 
     def __init__(self, shape, collision=CollisionCumD3Q27Turbulent2015, turbulence=OmegaNo,
                  inlet=InletVelocityMovingWall, storage="f32", nu=1.0 / 6.0, tau=0.0, cles=0.173,
-                 periodic=(0, 0, 0), force=(0.0, 0.0, 0.0), rho0=1.0, f16_scale_log2=10, device=0, options=0):
+                 periodic=(0, 0, 0), force=(0.0, 0.0, 0.0), rho0=1.0, f16_scale_log2=10, device=0, options=0,
+                 mlp_interval=1):
         nx, ny, nz = shape
         self.shape = (int(nx), int(ny), int(nz))
         self.N = nx * ny * nz
         self.cfg = capi.make_config(nx, ny, nz, periodic=periodic, collision=collision.code,
                                     closure=turbulence.code, storage=STORAGE[storage],
                                     inlet_kind=inlet.code, nu=nu, tau=tau, cles=cles, force=force,
-                                    rho0=rho0, f16_scale_log2=f16_scale_log2, device=device, options=options)
+                                    rho0=rho0, f16_scale_log2=f16_scale_log2, device=device, options=options,
+                                    mlp_interval=mlp_interval)
         self._ctx = C.c_void_p()
         check(lib().lbm_create(C.byref(self.cfg), C.byref(self._ctx)))
 

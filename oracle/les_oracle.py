@@ -162,9 +162,15 @@ def infer_fp16(p, x, mean, std, lo, hi, scale):
     w1, b1, w2, b2, w3, b3 = unpack(p)
     hA = 0.5 * GELU_A
     x = np.asarray(x, np.float64)
-    xn = ((x.astype(np.float32) - np.float32(mean)) * (np.float32(1.0) / np.float32(std))).astype(np.float64)
-    lo_n = (np.float32(lo) - np.float32(mean)) * (np.float32(1.0) / np.float32(std))
-    hi_n = (np.float32(hi) - np.float32(mean)) * (np.float32(1.0) / np.float32(std))
+    # normalised input = fma(x, isd, nmi) in FP32: the product of two floats is exact in float64
+    isd = (np.float32(1.0) / np.asarray(std, np.float32)).astype(np.float64)
+    nmi = (-(np.asarray(mean, np.float32) * isd.astype(np.float32))).astype(np.float64)
+
+    def fma32(a):
+        return (np.asarray(a, np.float32).astype(np.float64) * isd + nmi).astype(np.float32).astype(np.float64)
+
+    xn = fma32(x)
+    lo_n, hi_n = fma32(lo), fma32(hi)
     ok = np.all((xn >= lo_n) & (xn <= hi_n), axis=1)
     xin = np.concatenate([_h(xn), np.ones((x.shape[0], 1))], axis=1)
     W1e = _h(np.concatenate([(hA * w1).astype(np.float32), (hA * b1).astype(np.float32)[:, None]], axis=1))

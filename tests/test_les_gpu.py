@@ -113,6 +113,54 @@ def test_fused_mlp_out_of_range_is_smagorinsky(built_lib, storage):
     assert np.array_equal(out[0], out[1])
 
 
+@pytest.mark.parametrize("storage", ["f32", "f16dev"])
+def test_interval_out_of_range_is_smagorinsky(built_lib, storage):
+    """With a refresh interval the kept nu_t carry the fallback mark: an all-out-of-range model still
+    reproduces the Smagorinsky kernel bit for bit (steps that run the network and steps that reuse)."""
+    shape = (64, 18, 12)
+    c = cases.channel(*shape, re_tau=3.0, u_max=0.05, nu=0.01)
+    m, _ = _model_and_samples()
+    m.in_lo[:] = 1e30
+    m.in_hi[:] = 2e30
+    out = []
+    for clos in (OmegaLES, OmegaMLP):
+        s = Solver(shape, turbulence=clos, storage=storage, nu=c["nu"], cles=0.17, periodic=c["periodic"],
+                   force=c["force"], mlp_interval=3)
+        s.set_flags(c["flags"])
+        s.set_bc()
+        s.init_fields(c["rho"], c["u"])
+        if clos is OmegaMLP:
+            s.load_mlp(m)
+        s.step(8)
+        out.append(s.populations())
+        s.close()
+    assert np.array_equal(out[0], out[1])
+
+
+def test_interval_tracks_every_step_evaluation(built_lib):
+    """nu_t refreshed every 4th step stays close to the every-step evaluation (and is not identical)."""
+    shape = (64, 34, 32)
+    snaps, s, c = fine_channel(shape, 200, snapshots=(200,))
+    s.close()
+    m = les.MlpModel.init_from_samples(snaps[200])
+    t = les.Trainer(snaps[200])
+    t.train(m, epochs=20, batch=256, lr=3e-3)
+    t.close()
+    us = []
+    for k in (1, 4):
+        g = Solver(shape, turbulence=OmegaMLP, storage="f32", nu=c["nu"], cles=0.17, periodic=c["periodic"],
+                   force=c["force"], mlp_interval=k)
+        g.set_flags(c["flags"])
+        g.set_bc()
+        g.init_fields(c["rho"], c["u"])
+        g.load_mlp(m)
+        g.step(40)
+        us.append(g.moments()[1])
+        g.close()
+    d = np.linalg.norm(us[0] - us[1]) / np.linalg.norm(us[0])
+    assert 0.0 < d < 1e-3, d
+
+
 def test_trained_closure_beats_smagorinsky(built_lib):
     """Filtered samples of a 4x-finer channel at two times train the network on the GPU; on a third,
     later time it must explain more of the filtered subgrid stress than the Smagorinsky closure (both as
