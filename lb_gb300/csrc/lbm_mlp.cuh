@@ -160,45 +160,57 @@ LBM_D void mlp_rows2(const F2 (&x)[7], const MlpNorm& nm, uint4& ra, uint4& rb, 
 // Output pre-activation z (without b3) of the two cells of every lane.  Rows: lane l's first cell is
 // row l, its second row 32 + l.  stage: this warp's 64 x 16 B of shared memory; wf: the fragment table
 // [kMlpFragRows][32] in shared memory.  Every lane of the warp must call it.
+// 128-bit shared-memory load that the compiler keeps where it is written (re-read per m-tile instead
+// of holding the 16 W2 registers across the whole evaluation)
+LBM_D uint4 lds128(const uint4* p) {
+    uint4 r;
+    asm volatile("ld.shared.v4.u32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+                 : "r"((unsigned)__cvta_generic_to_shared(p)));
+    return r;
+}
+
 LBM_D float2 mlp_warp(uint4 rowA, uint4 rowB, uint4* stage, const uint4 (*wf)[32]) {
     const int lane = threadIdx.x & 31;
     stage[lane] = rowA;
     stage[32 + lane] = rowB;
     __syncwarp();
-    uint32_t a01[4], a23[4];
-    ldmatrix_x4(a01, stage + lane);       // m-tiles 0, 1 (rows 0..31)
-    ldmatrix_x4(a23, stage + 32 + lane);  // m-tiles 2, 3 (rows 32..63)
-    __syncwarp();                          // the stage takes the outputs below
+    uint32_t a[8];
+    {
+        uint32_t r[4];
+        ldmatrix_x4(r, stage + lane);       // m-tiles 0, 1 (rows 0..31)
+        a[0] = r[0]; a[1] = r[1]; a[2] = r[2]; a[3] = r[3];
+        ldmatrix_x4(r, stage + 32 + lane);  // m-tiles 2, 3 (rows 32..63)
+        a[4] = r[0]; a[5] = r[1]; a[6] = r[2]; a[7] = r[3];
+    }
+    __syncwarp();                            // the stage takes the outputs below
     float* out = reinterpret_cast<float*>(stage);
-    // one m-tile at a time, weight fragments re-read from shared memory per tile (few live registers)
-#pragma unroll 1
+    const uint4 w1 = lds128(&wf[0][lane]);
+    const uint4 w3 = lds128(&wf[5][lane]);
+    const uint4 bA = lds128(&wf[6][lane]), bB = lds128(&wf[7][lane]);
+    const uint32_t w1j[4] = {w1.x, w1.y, w1.z, w1.w};
+    const uint32_t b2[4][2] = {{bA.x, bA.y}, {bA.z, bA.w}, {bB.x, bB.y}, {bB.z, bB.w}};
+#pragma unroll
     for (int t = 0; t < 4; t++) {
-        const uint32_t a0 = t == 0 ? a01[0] : t == 1 ? a01[2] : t == 2 ? a23[0] : a23[2];
-        const uint32_t a1 = t == 0 ? a01[1] : t == 1 ? a01[3] : t == 2 ? a23[1] : a23[3];
-        const uint4 w1 = wf[0][lane];
-        const uint32_t w1j[4] = {w1.x, w1.y, w1.z, w1.w};
         uint32_t h[4][2];
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             float d[4] = {0.f, 0.f, 0.f, 0.f};
-            mma_k8(d, a0, a1, w1j[j]);
+            mma_k8(d, a[2 * t], a[2 * t + 1], w1j[j]);
             h[j][0] = mlp_act(d[0], d[1]);
             h[j][1] = mlp_act(d[2], d[3]);
         }
-        const float4 bA = *reinterpret_cast<const float4*>(&wf[6][lane]);
-        const float4 bB = *reinterpret_cast<const float4*>(&wf[7][lane]);
-        const float b2[4][2] = {{bA.x, bA.y}, {bA.z, bA.w}, {bB.x, bB.y}, {bB.z, bB.w}};
         uint32_t h2[4][2];
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            const uint4 w2 = wf[1 + j][lane];
-            float d[4] = {b2[j][0], b2[j][1], b2[j][0], b2[j][1]};
+            const uint4 w2 = lds128(&wf[1 + j][lane]);
+            const float c0 = __uint_as_float(b2[j][0]), c1 = __uint_as_float(b2[j][1]);
+            float d[4] = {c0, c1, c0, c1};
             mma_k16(d, h[0][0], h[0][1], h[1][0], h[1][1], w2.x, w2.y);
             mma_k16(d, h[2][0], h[2][1], h[3][0], h[3][1], w2.z, w2.w);
             h2[j][0] = mlp_act(d[0], d[1]);
             h2[j][1] = mlp_act(d[2], d[3]);
         }
-        const uint4 w3 = wf[5][lane];
         float d[4] = {0.f, 0.f, 0.f, 0.f};
         mma_k16(d, h2[0][0], h2[0][1], h2[1][0], h2[1][1], w3.x, w3.y);
         mma_k16(d, h2[2][0], h2[2][1], h2[3][0], h2[3][1], w3.z, w3.w);

@@ -142,6 +142,21 @@ __global__ void __launch_bounds__(128) k_step(Params p) {
     step_cell<S, COLL, CLOS, ODD>(p, x, blockIdx.y, blockIdx.z);
 }
 
+template <int COLL, class L>
+LBM_D void collide_with_rate(L (&f)[27], const Mom<L>& mm, L ri, L ux, L uy, L uz, L om, bool force, L Fx, L Fy,
+                             L Fz) {
+    if constexpr (COLL == 0) {
+        collide_srt(f, mm.rho, ux, uy, uz, om);
+        if (force) srt_force(f, ux, uy, uz, om, Fx, Fy, Fz);
+    } else {
+        collide_cum15(f, mm.rho, ri, ux, uy, uz, om, mm);
+    }
+}
+
+// relaxation rate of a cell with a kept learned eddy viscosity: 1/(tau + 3 nu_t), or the Smagorinsky
+// rate where the kept value is negative (fallback mark) or not a number
+LBM_D float rate_kept(float nu, float tau, float om_s) { return nu >= 0.0f ? __fdividef(1.0f, lfma(3.0f, nu, tau)) : om_s; }
+
 // moments, relaxation rate and collision of a packed pair of bulk cells
 // (time-average accumulation of the two cells idx0, idx0+1 when p.acc is set)
 template <int COLL, int CLOS>

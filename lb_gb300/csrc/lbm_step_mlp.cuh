@@ -11,24 +11,13 @@
 // Cells that are not packed bulk pairs take the per-cell path with the Smagorinsky closure.
 // MODE 0: the network runs in this step.  MODE 1: it runs and its nu_t (or -1 for the fallback) is kept
 // per cell in FP16 (Params::nut).  MODE 2: it does not run; each pair relaxes with the kept nu_t (the
-// Smagorinsky rate where the kept value is negative or not a number).
+// Smagorinsky rate where the kept value is negative or not a number), fetched before the populations.
 #pragma once
 
 #include "lbm_mlp.cuh"
 #include "lbm_step.cuh"
 
 namespace lbm {
-
-template <int COLL, class L>
-LBM_D void collide_with_rate(L (&f)[27], const Mom<L>& mm, L ri, L ux, L uy, L uz, L om, bool force, L Fx, L Fy,
-                             L Fz) {
-    if constexpr (COLL == 0) {
-        collide_srt(f, mm.rho, ux, uy, uz, om);
-        if (force) srt_force(f, ux, uy, uz, om, Fx, Fy, Fz);
-    } else {
-        collide_cum15(f, mm.rho, ri, ux, uy, uz, om, mm);
-    }
-}
 
 template <class S, int COLL, bool ODD, int MODE>
 __global__ void __launch_bounds__(128) k_step2_mlp(Params p) {
@@ -63,12 +52,13 @@ __global__ void __launch_bounds__(128) k_step2_mlp(Params p) {
     q.eL = (p.wrap[0] && x0 == 0) ? q.e0 + p.nx : q.e0;
     q.eR = (p.wrap[0] && x0 + 2 == p.nx) ? q.e1 - p.nx : q.e1;
 
+    float2 kept = make_float2(-1.f, -1.f);
+    if (MODE == 2 && pair) kept = __half22float2(__ldg((const __half2*)(p.nut + idx0)));
     F2 f[27];
     Mom<F2> mm;
     F2 ri, ux, uy, uz, om_s;
     uint4 rowA = make_uint4(0, 0, 0, 0), rowB = rowA;
     bool inA = false, inB = false;
-    (void)rowA; (void)rowB; (void)inA; (void)inB;
     if (pair) {
         if (!yz_seam) {
             load_pair<S, ODD>(p, q, k, f);
@@ -110,21 +100,17 @@ __global__ void __launch_bounds__(128) k_step2_mlp(Params p) {
             mlp_rows2(xf, p.mlp, rowA, rowB, inA, inB);
         }
     }
-    float nuA = -1.0f, nuB = -1.0f;
+    float nuA = kept.x, nuB = kept.y;
     if constexpr (MODE != 2) {
         const float2 zo = mlp_warp(rowA, rowB, stage[threadIdx.x >> 5], wf);
-        if (inA) nuA = mlp_nu(zo.x, p.mlp);
-        if (inB) nuB = mlp_nu(zo.y, p.mlp);
+        nuA = inA ? mlp_nu(zo.x, p.mlp) : -1.0f;
+        nuB = inB ? mlp_nu(zo.y, p.mlp) : -1.0f;
         if (MODE == 1 && pair) *(__half2*)(p.nut + idx0) = __floats2half2_rn(nuA, nuB);
-    } else if (pair) {
-        const float2 kept = __half22float2(*(const __half2*)(p.nut + idx0));
-        nuA = kept.x;
-        nuB = kept.y;
     }
+    (void)rowA; (void)rowB; (void)inA; (void)inB;
     if (pair) {
         // nu >= 0 is false for the fallback mark (-1) and for a kept value that is not a number
-        const F2 om(nuA >= 0.0f ? __fdividef(1.0f, lfma(3.0f, nuA, p.tauf)) : om_s.v.x,
-                    nuB >= 0.0f ? __fdividef(1.0f, lfma(3.0f, nuB, p.tauf)) : om_s.v.y);
+        const F2 om(rate_kept(nuA, p.tauf, om_s.v.x), rate_kept(nuB, p.tauf, om_s.v.y));
         collide_with_rate<COLL>(f, mm, ri, ux, uy, uz, om, p.has_force != 0, F2(p.Ff[0]), F2(p.Ff[1]),
                                 F2(p.Ff[2]));
         if (!yz_seam) {
