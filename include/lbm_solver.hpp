@@ -1,0 +1,230 @@
+// lbm_solver.hpp - C++ host side of the solver: the reference's compile-time policy interface over the
+// C ABI of lbm.h (header-only, C++17).
+//
+// The reference composes its solver from policy types (3D/simulation/src/solvers/SolverTurbulentLES.h:67-82)
+// and owns its state in LBMConstants / LBMData (3D/simulation/src/data/LBMConstants.h:4-113,
+// LBMData.h:3-77).  This header keeps those names: the same fourteen template parameters, tag types named
+// after the reference's policies, and SolverTurbulentLES with initializeSimulation / runSimulation /
+// probeWrite / convertToLattice.  A policy is a tag here, not a kernel: the whole step (omega, collision,
+// streaming, boundaries, moments) is one fused kernel behind lbm_step, and the tags only select what it does.
+// Policies the fused kernel does not implement fail to compile (static_assert) instead of running
+// something else.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "lbm.h"
+
+namespace lbm_gb300 {
+
+// ---- policy tags (reference file of each in the comment) ----------------------------------------------
+struct D3Q27 { static constexpr int numberOfDiscreteVelocities = 27; };           // models/D3Q27/D3Q27.h
+struct CollisionCumD3Q27Turbulent2015 { static constexpr int32_t code = LBM_COLLISION_CUMULANT2015; };
+struct CollisionSRTTurbulent { static constexpr int32_t code = LBM_COLLISION_SRT; };  // collisions/CollisionSRTTurbulent.h
+struct OmegaLES { static constexpr int32_t code = LBM_CLOSURE_SMAGORINSKY; };      // turbulence/OmegaLES.h
+struct OmegaNo { static constexpr int32_t code = LBM_CLOSURE_NONE; };             // turbulence/OmegaNo.h
+struct OmegaMLP { static constexpr int32_t code = LBM_CLOSURE_MLP; };             // learned closure (no reference policy)
+struct StreamingAB {};                     // streamings/StreamingAB.h (AA pattern in place here)
+struct BounceBackWallHalf {};              // boundaryConditions/Wall/BounceBackWallHalf.h
+struct NoSymmetry {};                      // boundaryConditions/Symmetry/NoSymmetry.h
+struct Periodic { static constexpr bool on = true; };    // boundaryConditions/Periodic/Periodic.h (index wrap)
+struct NoPeriodic { static constexpr bool on = false; };
+struct InletVelocityMovingWall { static constexpr int32_t code = LBM_INLET_MOVING_WALL; };
+struct InletVelocityEquilibrium { static constexpr int32_t code = LBM_INLET_EQUILIBRIUM; };
+struct OutletDensityInterpolated {};       // boundaryConditions/Outlet/OutletDensityInterpolated.h
+struct MomentDensityVelocityN27 {};        // moments/MomentDensityVelocityN27.h
+struct MomentTimeAvg {};                   // moments/MomentTimeAvg.h
+struct ErrorQuadratic {};                  // errorEvaluations/ErrorQuadratic.h
+struct InitializationEquilibriumConstVector {};  // initializations/InitializationEquilibriumConstVector.h
+struct NonDimensiolnaliseFactorsVelocity {};     // nonDimensionalisions/NonDimensiolnaliseFactorsVelocity.h
+
+// ---- state carriers (the fields of LBMConstants / LBMData this path uses) ------------------------------
+struct LBMConstants {
+    int dimX_int = 0, dimY_int = 0, dimZ_int = 0;
+    double ny = 1.0 / 6.0;            // lattice kinematic viscosity
+    double tau = 0.0;                 // > 0 overrides 3 ny + 1/2
+    double CLES = 0.173;              // LBMConstants.h:70
+    double Fx = 0.0, Fy = 0.0, Fz = 0.0;
+    double rho0 = 1.0;
+    double VelocityInit[3] = {0.0, 0.0, 0.0};
+    int periodic[3] = {0, 0, 0};      // per axis, used when the Periodic policy is selected
+    int iterations = 0;
+    int iterationsMomentAvg = 0;      // average over the last iterationsMomentAvg steps
+    int err_every_it = -1;
+    int probe_every_it = -1;
+    int probe_iterations = -1;
+    int ProbeLocationLat[3] = {0, 0, 0};
+    double err = 0.0;
+    // storage of the populations on the GPU (lbm.h LBM_STORAGE_*), device, learned-closure model
+    int32_t storage = LBM_STORAGE_F32;
+    int32_t device = 0;
+    int32_t mlp_interval = 1;
+    const lbm_mlp_model* mlp = nullptr;
+};
+
+struct LBMData {
+    std::vector<int32_t> meshFluid;            // reference flag encoding, x fastest
+    std::vector<lbm_bc_inlet> meshBoundaryInlet;
+    std::vector<lbm_bc_outlet> meshBoundaryOutlet;
+    std::vector<double> rhoInit, uInit;        // optional initial fields (else VelocityInit everywhere)
+    std::vector<double> rho, u;                // host copies after the run (u: ux[N], uy[N], uz[N])
+    std::vector<double> rhoTimeAvg, uTimeAvg, uuTimeAvg;
+    std::vector<double> probe;                 // u_x, u_y, u_z, rho per probe sample
+    std::vector<double> errors;                // ErrorQuadratic values, one per evaluation
+};
+
+class Error : public std::runtime_error {
+public:
+    Error(lbm_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+    lbm_status status;
+};
+
+inline void check(lbm_status s, const lbm_ctx* ctx, const char* what) {
+    if (s != LBM_OK) throw Error(s, std::string(what) + ": " + lbm_last_error(ctx));
+}
+
+template <typename MODELTYPE, typename INITIALIZATIONTYPE, typename COLLISIONTYPE, typename STREAMINGTYPE,
+          typename BOUNCEBACKWALLTYPE, typename SYMMETRYTYPE, typename PERIODICTYPE, typename INLETTYPE,
+          typename OUTLETTYPE, typename MOMENTTYPE, typename TURBULENCETYPE, typename ERRORTYPE, typename NONDYM,
+          typename MOMENTTIMEAVGTYPE>
+class SolverTurbulentLES {
+    static_assert(MODELTYPE::numberOfDiscreteVelocities == 27, "the kernels are D3Q27");
+    static_assert(std::is_same<STREAMINGTYPE, StreamingAB>::value, "streaming: StreamingAB (AA pattern in place)");
+    static_assert(std::is_same<BOUNCEBACKWALLTYPE, BounceBackWallHalf>::value, "wall: BounceBackWallHalf");
+    static_assert(std::is_same<SYMMETRYTYPE, NoSymmetry>::value, "symmetry planes are not implemented");
+    static_assert(std::is_same<OUTLETTYPE, OutletDensityInterpolated>::value, "outlet: OutletDensityInterpolated");
+    static_assert(std::is_same<MOMENTTYPE, MomentDensityVelocityN27>::value, "moments: MomentDensityVelocityN27");
+    static_assert(std::is_same<ERRORTYPE, ErrorQuadratic>::value, "error: ErrorQuadratic");
+    static_assert(std::is_same<INITIALIZATIONTYPE, InitializationEquilibriumConstVector>::value,
+                  "initialisation: InitializationEquilibriumConstVector");
+    static_assert(std::is_same<MOMENTTIMEAVGTYPE, MomentTimeAvg>::value, "time average: MomentTimeAvg");
+
+public:
+    SolverTurbulentLES() = delete;
+    SolverTurbulentLES(LBMConstants& constants, LBMData& data) : Constants(constants), Data(data) {}
+    SolverTurbulentLES(const SolverTurbulentLES&) = delete;
+    SolverTurbulentLES& operator=(const SolverTurbulentLES&) = delete;
+    ~SolverTurbulentLES() {
+        if (ctx) lbm_destroy(ctx);
+    }
+
+    // NonDimensiolnaliseFactorsVelocity converts physical inputs to lattice units; the constants here
+    // are lattice units already (as after the reference's convertToLattice)
+    void convertToLattice(bool /*verbose*/) {}
+
+    // the context, geometry, boundary records and the equilibrium initial state
+    // (SolverTurbulentLES.h:103-146; InitializationEquilibriumConstVector.h:103-224)
+    void initializeSimulation(bool verbose) {
+        lbm_config c{};
+        c.nx = Constants.dimX_int; c.ny = Constants.dimY_int; c.nz = Constants.dimZ_int;
+        for (int a = 0; a < 3; a++) c.periodic[a] = PERIODICTYPE::on ? Constants.periodic[a] : 0;
+        c.collision = COLLISIONTYPE::code;
+        c.closure = TURBULENCETYPE::code;
+        c.storage = Constants.storage;
+        c.inlet_kind = INLETTYPE::code;
+        c.nu = Constants.ny;
+        c.tau = Constants.tau;
+        c.cles = Constants.CLES;
+        c.force[0] = Constants.Fx; c.force[1] = Constants.Fy; c.force[2] = Constants.Fz;
+        c.rho0 = Constants.rho0;
+        c.f16_scale_log2 = 10;
+        c.device = Constants.device;
+        c.mlp_interval = Constants.mlp_interval;
+        if (ctx) lbm_destroy(ctx);
+        ctx = nullptr;
+        check(lbm_create(&c, &ctx), nullptr, "lbm_create");
+        const size_t N = (size_t)c.nx * c.ny * c.nz;
+        if (Data.meshFluid.size() != N) throw Error(LBM_ERR_INVALID, "meshFluid has the wrong size");
+        check(lbm_set_flags(ctx, Data.meshFluid.data()), ctx, "lbm_set_flags");
+        check(lbm_set_bc(ctx, Data.meshBoundaryInlet.data(), (int32_t)Data.meshBoundaryInlet.size(),
+                         Data.meshBoundaryOutlet.data(), (int32_t)Data.meshBoundaryOutlet.size()),
+              ctx, "lbm_set_bc");
+        if (!Data.rhoInit.empty()) {
+            if (Data.rhoInit.size() != N || Data.uInit.size() != 3 * N)
+                throw Error(LBM_ERR_INVALID, "rhoInit / uInit have the wrong size");
+            check(lbm_init_fields(ctx, Data.rhoInit.data(), Data.uInit.data()), ctx, "lbm_init_fields");
+        } else {
+            check(lbm_init_equilibrium(ctx, Constants.rho0, Constants.VelocityInit), ctx, "lbm_init_equilibrium");
+        }
+        if (std::is_same<TURBULENCETYPE, OmegaMLP>::value) {
+            if (!Constants.mlp) throw Error(LBM_ERR_STATE, "OmegaMLP needs LBMConstants::mlp");
+            check(lbm_mlp_load(ctx, Constants.mlp), ctx, "lbm_mlp_load");
+        }
+        if (verbose) std::printf("Initialization of simulation done (%d x %d x %d).\n", c.nx, c.ny, c.nz);
+    }
+
+    // u_x, u_y, u_z, rho of the probe cell appended to Data.probe (SolverTurbulentLES.h:150-177)
+    void probeWrite() {
+        double out[4];
+        check(lbm_probe(ctx, Constants.ProbeLocationLat[0], Constants.ProbeLocationLat[1],
+                        Constants.ProbeLocationLat[2], out),
+              ctx, "lbm_probe");
+        Data.probe.insert(Data.probe.end(), out, out + 4);
+    }
+
+    // the reference's step loop (SolverTurbulentLES.h:179-268).  After step k: the state is added to the
+    // time average when k > iterations - iterationsMomentAvg, the probe is sampled when
+    // k % probe_every_it == 0 within the last probe_iterations steps, the error is evaluated when
+    // k % err_every_it == 0 (k > 0) and a NaN error ends the loop.  The steps between two such events
+    // go to the GPU as one lbm_step call.
+    void runSimulation() {
+        if (!ctx) throw Error(LBM_ERR_STATE, "runSimulation before initializeSimulation");
+        const int it = Constants.iterations;
+        const int avg = Constants.iterationsMomentAvg;
+        const int avg_begin = it - avg + 1;  // lbm_timeavg counts the states produced after the call
+        auto probe_after = [&](int k) {
+            return Constants.probe_every_it > 0 && k % Constants.probe_every_it == 0 &&
+                   k >= it - Constants.probe_iterations;
+        };
+        auto err_after = [&](int k) { return Constants.err_every_it > 0 && k % Constants.err_every_it == 0 && k != 0; };
+        bool averaging = false;
+        int k = 0;  // steps done
+        while (k < it) {
+            if (avg > 0 && !averaging && k >= avg_begin) {
+                check(lbm_timeavg_begin(ctx), ctx, "lbm_timeavg_begin");
+                averaging = true;
+            }
+            int j = k;  // the last step of this batch: the first with an event after it
+            while (j < it - 1 && !probe_after(j) && !err_after(j) && !(avg > 0 && !averaging && j + 1 >= avg_begin)) j++;
+            check(lbm_step(ctx, j - k + 1), ctx, "lbm_step");
+            k = j + 1;
+            if (probe_after(j)) probeWrite();
+            if (err_after(j)) {
+                double e = 0.0;
+                check(lbm_error_evaluation(ctx, &e), ctx, "lbm_error_evaluation");
+                Constants.err = e;
+                Data.errors.push_back(e);
+                if (std::isnan(e)) break;
+            }
+        }
+        if (averaging) check(lbm_timeavg_end(ctx), ctx, "lbm_timeavg_end");
+        check(lbm_synchronize(ctx), ctx, "lbm_synchronize");
+        const size_t N = (size_t)Constants.dimX_int * Constants.dimY_int * Constants.dimZ_int;
+        Data.rho.resize(N);
+        Data.u.resize(3 * N);
+        check(lbm_get_moments(ctx, Data.rho.data(), Data.u.data()), ctx, "lbm_get_moments");
+        if (averaging) {
+            Data.rhoTimeAvg.resize(N);
+            Data.uTimeAvg.resize(3 * N);
+            Data.uuTimeAvg.resize(6 * N);
+            check(lbm_timeavg_get(ctx, Data.rhoTimeAvg.data(), Data.uTimeAvg.data(), Data.uuTimeAvg.data(), nullptr),
+                  ctx, "lbm_timeavg_get");
+        }
+    }
+
+    lbm_ctx* context() { return ctx; }
+
+    LBMConstants& Constants;
+    LBMData& Data;
+
+private:
+    lbm_ctx* ctx = nullptr;
+};
+
+}  // namespace lbm_gb300

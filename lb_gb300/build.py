@@ -11,6 +11,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblbm_gb300.so")
+DRIVER = os.path.join(HERE, "lbm_run")          # C++ host driver (lb_gb300/host/lbm_run.cpp)
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -30,9 +31,26 @@ def _deps_mtime():
     return max(os.path.getmtime(f) for f in files)
 
 
+def build_driver(force=False):
+    """g++ the C++ host driver against the library (rpath next to it)."""
+    src = os.path.join(HERE, "host", "lbm_run.cpp")
+    deps = [src, os.path.join(INCLUDE, "lbm.h"), os.path.join(INCLUDE, "lbm_solver.hpp"), LIB]
+    if not force and os.path.exists(DRIVER) and os.path.getmtime(DRIVER) >= max(os.path.getmtime(f) for f in deps):
+        return DRIVER
+    gxx = shutil.which("g++") or "g++"
+    cmd = [gxx, "-O2", "-std=c++17", "-Wall", "-I", INCLUDE, src, "-L", HERE, "-llbm_gb300",
+           "-Wl,-rpath,$ORIGIN", "-o", DRIVER + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"g++ failed on lbm_run.cpp:\n{r.stderr}")
+    os.replace(DRIVER + ".tmp", DRIVER)
+    return DRIVER
+
+
 def build(force=False, verbose=False):
     os.makedirs(BUILD, exist_ok=True)
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps_mtime():
+        build_driver()
         return LIB
     exe = nvcc()
 
@@ -54,6 +72,7 @@ def build(force=False, verbose=False):
     if r.returncode != 0:
         raise RuntimeError(f"nvcc link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_driver(force=True)
     return LIB
 
 

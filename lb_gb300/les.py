@@ -77,6 +77,11 @@ class MlpModel:
         np.savez(path, params=self.params, in_mean=self.in_mean, in_std=self.in_std, in_lo=self.in_lo,
                  in_hi=self.in_hi, out_scale=np.float32(self.out_scale))
 
+    def save_raw(self, path):
+        """The lbm_mlp_model struct as raw bytes (the C++ driver's --mlp file)."""
+        with open(path, "wb") as fh:
+            fh.write(bytes(self.struct()))
+
     @classmethod
     def load(cls, path):
         d = np.load(path)

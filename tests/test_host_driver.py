@@ -1,0 +1,93 @@
+"""The C++ host side: include/lbm_solver.hpp (the reference's SolverTurbulentLES policy interface over the
+C ABI) and the driver lb_gb300/host/lbm_run.cpp built on it."""
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from lb_gb300 import build, cases
+from lb_gb300.solver import OmegaLES, OmegaNo, Solver
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_driver_is_built_and_reports_the_abi(built_lib):
+    r = subprocess.run([build.DRIVER, "--help"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0
+    assert "ABI version 2" in r.stdout
+
+
+def test_unsupported_policy_does_not_compile():
+    """A policy the fused kernel does not implement is a compile error, not a silent substitute."""
+    src = r'''
+#include "lbm_solver.hpp"
+using namespace lbm_gb300;
+struct BounceSymmetryHalf {};
+int main() {
+    LBMConstants C; LBMData D;
+    SolverTurbulentLES<D3Q27, InitializationEquilibriumConstVector, CollisionCumD3Q27Turbulent2015, StreamingAB,
+                       BounceBackWallHalf, BounceSymmetryHalf, NoPeriodic, InletVelocityMovingWall,
+                       OutletDensityInterpolated, MomentDensityVelocityN27, OmegaLES, ErrorQuadratic,
+                       NonDimensiolnaliseFactorsVelocity, MomentTimeAvg> s(C, D);
+    return 0;
+}
+'''
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "t.cpp")
+        with open(p, "w") as fh:
+            fh.write(src)
+        r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), p],
+                           capture_output=True, text=True)
+    assert r.returncode != 0
+    assert "symmetry planes are not implemented" in r.stderr
+
+
+@pytest.mark.gpu
+def test_driver_cavity_equals_python_api(built_lib):
+    n, steps = 24, 300
+    with tempfile.TemporaryDirectory() as d:
+        r = subprocess.run([build.DRIVER, "cavity", "--n", str(n), "--steps", str(steps), "--storage", "f64",
+                            "--err-every", "100", "--out", d], capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+        prof = np.loadtxt(os.path.join(d, "centerline_ux_y.txt"))
+    c = cases.cavity(n)
+    s = Solver((n, n, n), turbulence=OmegaNo, storage="f64", nu=c["nu"])
+    s.set_flags(c["flags"])
+    s.set_bc(c["inlets"])
+    s.init_equilibrium(1.0, (0.0, 0.0, 0.0))
+    s.step(steps)
+    _, u = s.moments()
+    s.close()
+    ux = u[0].reshape(n, n, n)[n // 2, :, n // 2] / 0.05
+    assert np.array_equal(prof[:, 1], ux)
+
+
+@pytest.mark.gpu
+def test_driver_channel_profile_equals_python_api(built_lib):
+    nx, ny, nz, steps, avg = 64, 34, 32, 200, 50
+    with tempfile.TemporaryDirectory() as d:
+        r = subprocess.run([build.DRIVER, "channel", "--nx", str(nx), "--ny", str(ny), "--nz", str(nz), "--steps",
+                            str(steps), "--avg", str(avg), "--storage", "f32", "--out", d],
+                           capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+        prof = np.loadtxt(os.path.join(d, "mean_profile.txt"))
+    c = cases.channel(nx, ny, nz, re_tau=180.0, u_max=0.05, amp=0.05)
+    s = Solver((nx, ny, nz), turbulence=OmegaLES, storage="f32", nu=c["nu"], cles=0.17, periodic=c["periodic"],
+               force=c["force"])
+    s.set_flags(c["flags"])
+    s.set_bc()
+    s.init_fields(c["rho"], c["u"])
+    s.step(steps - avg + 1)
+    s.timeavg_begin()
+    s.step(avg - 1)
+    s.timeavg_end()
+    _, um, uu, _ = s.timeavg_get()
+    s.close()
+    um = um.reshape(3, nz, ny, nx)
+    uu = uu.reshape(6, nz, ny, nx)
+    mean_ux = um[0].mean(axis=(0, 2))
+    rxy = (uu[3] - um[0] * um[1]).mean(axis=(0, 2))
+    assert np.allclose(prof[:, 1], mean_ux, rtol=1e-12, atol=1e-15)
+    assert np.allclose(prof[:, 5], rxy, rtol=1e-9, atol=1e-15)

@@ -1,0 +1,176 @@
+"""Validation runs of the benchmark configurations on the GPU (long; not collected by pytest).
+
+    python -m tests.validate_configs c1 [--n 64 --steps 10000]
+    python -m tests.validate_configs c3 [--shape 512,256,256 --steps 20000 --avg 5000]
+    python -m tests.validate_configs c4 [--shape 384,192,192 --steps 4000]
+
+c1: lid-driven cavity 64^3, FP64 cumulant on the GPU against the CPU oracle's FP64 run of the same case
+    (parity of the whole 10k-step trajectory), FP32 against FP64; centre-line profiles.
+c3: channel at 512x256x256 (laminar profile + 5 % seeded noise, Re_tau 180 forcing, Smagorinsky CLES
+    0.17) in FP64, FP32 and FP16-deviation storage: relative L2 error of the x-z-time-averaged mean
+    velocity and of the Reynolds stresses against FP64.
+c4: flow past the voxelized seeded body at 384x192x192: GPU voxelizer against the CPU oracle (bit for
+    bit), FP32 against FP64 drag (momentum exchange, FP64 sums).
+Each prints one JSON line.
+"""
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+from lb_gb300 import cases  # noqa: E402
+from lb_gb300.solver import OmegaLES, OmegaNo, Solver, InletVelocityEquilibrium  # noqa: E402
+
+
+def c1(n, steps):
+    from lb_gb300 import capi
+    from oracle import oracle as O
+    c = cases.cavity(n)
+    out = {"config": "C1 cavity", "n": n, "steps": steps, "nu": c["nu"]}
+    res = {}
+    for st in ("f64", "f32"):
+        s = Solver((n, n, n), turbulence=OmegaNo, storage=st, nu=c["nu"])
+        s.set_flags(c["flags"])
+        s.set_bc(c["inlets"])
+        s.init_equilibrium(1.0, (0.0, 0.0, 0.0))
+        ms = s.step_timed(steps)
+        res[st] = s.moments()[1]
+        out[f"gpu_{st}_seconds"] = ms * 1e-3
+        s.close()
+    cfg = capi.make_config(n, n, n, collision=capi.LBM_COLLISION_CUMULANT2015, closure=capi.LBM_CLOSURE_NONE,
+                           nu=c["nu"])
+    t0 = time.time()
+    o = O.OracleSim(cfg, 64)
+    o.set_flags(c["flags"])
+    o.set_bc(c["inlets"])
+    o.init_equilibrium(1.0, (0.0, 0.0, 0.0))
+    o.step(steps)
+    uo = o.moments()[1]
+    o.close()
+    out["oracle_seconds"] = time.time() - t0
+    ulid = 0.05
+    out["max_abs_du_over_ulid_gpu64_vs_oracle64"] = float(np.max(np.abs(res["f64"] - uo)) / ulid)
+    out["max_abs_du_over_ulid_gpu32_vs_gpu64"] = float(np.max(np.abs(res["f32"] - res["f64"])) / ulid)
+    u = res["f64"].reshape(3, n, n, n)
+    out["centerline_ux_y"] = (u[0, n // 2, :, n // 2] / ulid).round(6).tolist()
+    out["centerline_uy_x"] = (u[1, n // 2, n // 2, :] / ulid).round(6).tolist()
+    return out
+
+
+def _channel_stats(shape, storage, steps, avg, case):
+    nx, ny, nz = shape
+    s = Solver(shape, turbulence=OmegaLES, storage=storage, nu=case["nu"], cles=0.17, periodic=case["periodic"],
+               force=case["force"])
+    s.set_flags(case["flags"])
+    s.set_bc()
+    s.init_fields(case["rho"], case["u"])
+    t0 = time.time()
+    s.step(steps - avg + 1)
+    s.timeavg_begin()
+    s.step(avg - 1)
+    s.timeavg_end()
+    _, um, uu, cnt = s.timeavg_get()
+    d = s.reduce()
+    s.close()
+    um = um.reshape(3, nz, ny, nx)
+    uu = uu.reshape(6, nz, ny, nx)
+    mean = um[0].mean(axis=(0, 2))
+    R = np.stack([(uu[0] - um[0] ** 2).mean(axis=(0, 2)), (uu[1] - um[1] ** 2).mean(axis=(0, 2)),
+                  (uu[2] - um[2] ** 2).mean(axis=(0, 2)), (uu[3] - um[0] * um[1]).mean(axis=(0, 2))])
+    return mean, R, time.time() - t0, d, cnt
+
+
+def c3(shape, steps, avg):
+    case = cases.channel(*shape, re_tau=180.0, u_max=0.05, amp=0.05)
+    out = {"config": "C3 channel precision", "shape": list(shape), "steps": steps, "avg_steps": avg,
+           "nu": case["nu"], "force": case["force"][0]}
+    stats = {st: _channel_stats(shape, st, steps, avg, case) for st in ("f64", "f32", "f16dev")}
+    m64, R64 = stats["f64"][0], stats["f64"][1]
+    for st in ("f32", "f16dev"):
+        m, R = stats[st][0], stats[st][1]
+        out[f"{st}_mean_velocity_rel_l2_vs_f64"] = float(np.linalg.norm(m - m64) / np.linalg.norm(m64))
+        out[f"{st}_reynolds_stress_rel_l2_vs_f64"] = float(np.linalg.norm(R - R64) / max(np.linalg.norm(R64), 1e-300))
+    for st in stats:
+        out[f"{st}_seconds"] = stats[st][2]
+        out[f"{st}_max_speed"] = stats[st][3].max_speed
+        out[f"{st}_nonfinite"] = stats[st][3].nonfinite
+    out["f64_reynolds_stress_norm"] = float(np.linalg.norm(R64))
+    out["f64_mean_profile"] = m64.round(7).tolist()
+    return out
+
+
+def c4(shape, steps):
+    import ctypes as C
+    from lb_gb300 import capi
+    from oracle import oracle as O
+    nx, ny, nz = shape
+    v, f = cases.perturbed_icosphere(radius=24.0)
+    vv, ff = np.ascontiguousarray(v), np.ascontiguousarray(f)
+    dims = np.zeros(3, np.int32)
+    bbox = np.zeros(6)
+    L = capi.lib()
+    args = (vv.ctypes.data_as(C.POINTER(C.c_double)), len(vv), ff.ctypes.data_as(C.POINTER(C.c_int32)), len(ff),
+            1.0, 2.0)
+    t0 = time.time()
+    capi.check(L.lbm_voxelize_mesh(*args, None, dims.ctypes.data_as(C.POINTER(C.c_int32)),
+                                   bbox.ctypes.data_as(C.POINTER(C.c_double)), 0))
+    g = np.zeros(int(np.prod(dims)), np.int32)
+    capi.check(L.lbm_voxelize_mesh(*args, g.ctypes.data_as(C.POINTER(C.c_int32)), dims.ctypes.data_as(C.POINTER(C.c_int32)),
+                                   bbox.ctypes.data_as(C.POINTER(C.c_double)), 0))
+    t_gpu = time.time() - t0
+    t0 = time.time()
+    ref, _ = O.voxelize_mesh(v, f, 1.0, 2.0, (-300.0, -270.0, -240.0))
+    t_orc = time.time() - t0
+    out = {"config": "C4 body", "shape": list(shape), "steps": steps, "triangles": len(f),
+           "voxel_dims": dims.tolist(), "solid_voxels": int(g.sum()),
+           "voxelizer_bit_exact": bool(np.array_equal(g.reshape(ref.shape), ref)),
+           "gpu_voxelizer_seconds": t_gpu, "oracle_voxelizer_seconds": t_orc}
+    body = g.reshape(dims[2], dims[1], dims[0]).astype(bool)
+    center = (nx // 4 - dims[0] // 2, ny // 2 - dims[1] // 2, nz // 2 - dims[2] // 2)
+    case = cases.body_in_channel(nx, ny, nz, body_flags=body, center=center)
+    drag = {}
+    for st in ("f64", "f32"):
+        s = Solver(shape, turbulence=OmegaLES, inlet=InletVelocityEquilibrium, storage=st, nu=case["nu"], cles=0.17,
+                   periodic=case["periodic"])
+        s.set_flags(case["flags"])
+        s.set_bc(case["inlets"], case["outlets"])
+        s.init_equilibrium(1.0, (0.04, 0.0, 0.0))
+        t0 = time.time()
+        s.step(steps)
+        d = s.reduce()
+        drag[st] = np.array(d.drag)
+        out[f"{st}_seconds"] = time.time() - t0
+        out[f"{st}_drag"] = list(d.drag)
+        out[f"{st}_nonfinite"] = d.nonfinite
+        s.close()
+    out["drag_x_rel_diff_f32_vs_f64"] = float(abs(drag["f32"][0] - drag["f64"][0]) / abs(drag["f64"][0]))
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("which", choices=["c1", "c3", "c4"])
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--avg", type=int, default=5000)
+    ap.add_argument("--shape", default=None)
+    a = ap.parse_args()
+    if a.which == "c1":
+        r = c1(a.n, a.steps or 10000)
+    elif a.which == "c3":
+        shape = tuple(int(x) for x in (a.shape or "512,256,256").split(","))
+        r = c3(shape, a.steps or 20000, a.avg)
+    else:
+        shape = tuple(int(x) for x in (a.shape or "384,192,192").split(","))
+        r = c4(shape, a.steps or 4000)
+    print(json.dumps(r))
+
+
+if __name__ == "__main__":
+    main()
