@@ -80,8 +80,14 @@ typedef struct lbm_config {
                                  in between each cell relaxes with its last nu_t (kept in FP16) */
 } lbm_config;
 
-/* implementation options (results are identical either way) */
-#define LBM_OPT_ROW_STAGING  1  /* FP16 storage: rows of bulk cells through the shared-memory row-staged step */
+/* implementation options */
+#define LBM_OPT_ROW_STAGING  1  /* FP16 storage: rows of bulk cells through the shared-memory row-staged step
+                                   (identical results) */
+#define LBM_OPT_F16_ROUND_NEAREST 2  /* FP16 storage: round stores to nearest (ties away from zero).  Default:
+                                   stochastic rounding
+                                   (unbiased; keeps per-step increments below one FP16 step, such as a weak
+                                   body force, in expectation; reproducible: the random bits are a hash of
+                                   the element and the step) */
 
 /* boundary-condition records, mirroring LBMTraits.h:17-43 */
 typedef struct lbm_vertex { int32_t x, y, z; } lbm_vertex;

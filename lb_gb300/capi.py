@@ -48,6 +48,7 @@ class LbmConfig(C.Structure):
 
 
 LBM_OPT_ROW_STAGING = 1
+LBM_OPT_F16_ROUND_NEAREST = 2
 
 
 LBM_MLP_INPUTS = 7

@@ -72,6 +72,7 @@ struct Params {
     float omega0f;
     int has_force;
     float rho0, scale, inv_scale;  // FP16-deviation encoding
+    int f16_sr;              // FP16 stores round stochastically (else to nearest)
     float wr[27];            // w_v rho0            (decode f = h 2^-s + w_v rho0)
     float nwrs[27];          // -w_v rho0 2^s       (encode h = f 2^s - w_v rho0 2^s)
     float2 wr2[27], nwrs2[27];  // the same as (x, x) pairs for the packed two-cell path
@@ -113,6 +114,41 @@ template <class R> LBM_D R p_cles18(const Params& p) { if constexpr (std::is_sam
 template <class R> LBM_D R p_nu(const Params& p) { if constexpr (std::is_same<R, float>::value) return p.nuf; else return p.nu; }
 template <class R> LBM_D R p_F(const Params& p, int a) { if constexpr (std::is_same<R, float>::value) return p.Ff[a]; else return p.F[a]; }
 
+// ---- stochastic rounding of FP16 stores ---------------------------------------------------------------
+// A value is rounded up or down to a neighbouring FP16 number with probability proportional to its
+// distance to the other one, so increments far below one FP16 step (a body force of 1e-8 per step
+// against a step of ~1e-5 in f) survive in expectation instead of being rounded away every time.
+// Method: add 13 random bits below the FP16 mantissa of the FP32 bit pattern (23 - 10 = 13 bits are
+// dropped) and truncate toward zero; unbiased for results in the FP16 normal range.  The random bits
+// are a function of (element, step) only, so runs, resumes and kernel variants are reproducible.
+// Hash: the "lowbias32" 32-bit integer finaliser (C. Wellons, hash-prospector).
+LBM_D uint32_t mix32(uint32_t h) {
+    h ^= h >> 16; h *= 0x7FEB352Du;
+    h ^= h >> 15; h *= 0x846CA68Bu;
+    h ^= h >> 16;
+    return h;
+}
+LBM_D uint32_t sr_seed(unsigned long long e, int m) {
+    return mix32((uint32_t)e ^ mix32((uint32_t)m * 0x9E3779B9u + (uint32_t)(e >> 32)));
+}
+// next 32 random bits of a per-thread stream (32-bit LCG of Numerical Recipes; the high bits are used)
+LBM_D uint32_t lcg_next(uint32_t& s) {
+    s = s * 1664525u + 1013904223u;
+    return s;
+}
+LBM_D __half half_sr(float v, uint32_t r13) { return __float2half_rz(__uint_as_float(__float_as_uint(v) + r13)); }
+// the same dither with a fixed half step instead of random bits rounds to nearest (ties away from zero)
+constexpr uint32_t kHalfStep13 = 0x1000u;                        // for half_sr
+constexpr uint32_t kHalfStep2x = (0x1000u << 19) | (0x1000u << 6);  // for half2_sr
+// two values from one 32-bit random: bits 19..31 for .x, bits 6..18 for .y
+LBM_D __half2 half2_sr(float2 v, uint32_t r) {
+    const float a = __uint_as_float(__float_as_uint(v.x) + (r >> 19));
+    const float b = __uint_as_float(__float_as_uint(v.y) + ((r >> 6) & 0x1FFFu));
+    uint32_t h;
+    asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(h) : "f"(b), "f"(a));  // high half b, low half a
+    return *reinterpret_cast<__half2*>(&h);
+}
+
 // ---- population codecs ------------------------------------------------------------------------------
 template <class S>
 struct Codec;
@@ -133,7 +169,9 @@ struct Codec<StF16> {
         return fmaf(__half2float(__ldg(a)), p.inv_scale, p.wr[V]);
     }
     template <int V> LBM_D static void enc(__half* a, float v, const Params& p) {
-        *a = __float2half_rn(fmaf(v, p.scale, p.nwrs[V]));
+        const float e = fmaf(v, p.scale, p.nwrs[V]);
+        const uint32_t r = sr_seed((unsigned long long)(a - (const __half*)p.f), p.m) >> 19;
+        *a = half_sr(e, p.f16_sr ? r : kHalfStep13);
     }
 };
 

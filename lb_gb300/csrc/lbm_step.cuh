@@ -216,6 +216,8 @@ LBM_D void load_pair(const Params& p, const PairIdx& q, const PairCodec& k, F2 (
 template <class S, bool ODD>
 LBM_D void store_pair(const Params& p, const PairIdx& q, const PairCodec& k, const F2 (&f)[27]) {
     using T = typename S::T;
+    uint32_t rs = 0;  // stochastic-rounding stream of the pair (FP16)
+    if constexpr (S::kind == 2) rs = sr_seed((unsigned long long)q.e0, p.m);
     sfor<0, 27>([&](auto vc) {
         constexpr int V = decltype(vc)::value;
         T* a = (T*)(ODD ? p.wr_odd[V] : p.wr_even[V]);
@@ -226,7 +228,8 @@ LBM_D void store_pair(const Params& p, const PairIdx& q, const PairCodec& k, con
             else *(float2*)(a + q.e0) = f[V].v;
         } else {
             const F2 e = lfma(f[V], k.scale, k.nwrs[csq(V)]);
-            const __half2 h = __float22half2_rn(e.v);
+            const uint32_t rr = lcg_next(rs);
+            const __half2 h = half2_sr(e.v, p.f16_sr ? rr : kHalfStep2x);
             if constexpr (split) { a[i0] = __low2half(h); a[i1] = __high2half(h); }
             else *(__half2*)(a + q.e0) = h;
         }
@@ -277,6 +280,8 @@ template <class S, bool ODD>
 LBM_D void store_pair_rows(const Params& p, const PairRows& w, const PairCodec& k, const F2 (&f)[27]) {
     using T = typename S::T;
     T* A = (T*)p.f;
+    uint32_t rs = 0;  // stochastic-rounding stream of the pair (FP16), seeded by the pair's first cell
+    if constexpr (S::kind == 2) rs = sr_seed((unsigned long long)(w.R[1][1] + w.x0), p.m);
     sfor<0, 27>([&](auto vc) {
         constexpr int V = decltype(vc)::value;
         constexpr int slot = ODD ? V : opp(V);
@@ -289,7 +294,8 @@ LBM_D void store_pair_rows(const Params& p, const PairRows& w, const PairCodec& 
             else *(float2*)(a + w.x0) = f[V].v;
         } else {
             const F2 e = lfma(f[V], k.scale, k.nwrs[csq(V)]);
-            const __half2 h = __float22half2_rn(e.v);
+            const uint32_t rr = lcg_next(rs);
+            const __half2 h = half2_sr(e.v, p.f16_sr ? rr : kHalfStep2x);
             if constexpr (split) { a[i0] = __low2half(h); a[i1] = __high2half(h); }
             else *(__half2*)(a + w.x0) = h;
         }

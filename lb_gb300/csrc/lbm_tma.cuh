@@ -136,7 +136,10 @@ LBM_D void row_from_stage(const Params& p, typename S::T* buf, int y, int z, con
             f[V] = lfma(F2(t), k.inv_scale, k.wr[csq(V)]);
         }
     });
-    collide_pair<COLL, CLOS>(p, f, ((long long)z * p.ny + y) * nx + x0);
+    const long long idx0 = ((long long)z * p.ny + y) * nx + x0;
+    collide_pair<COLL, CLOS>(p, f, idx0);
+    uint32_t rs = 0;  // stochastic-rounding stream of the pair, as store_pair
+    if constexpr (S::kind == 2) rs = sr_seed((unsigned long long)idx0, p.m);
     __syncthreads();  // every pair has read its inputs before any segment is overwritten
     sfor<0, 27>([&](auto vc) {
         constexpr int V = decltype(vc)::value;
@@ -147,7 +150,8 @@ LBM_D void row_from_stage(const Params& p, typename S::T* buf, int y, int z, con
             else *(float2*)a = f[V].v;
         } else {
             const F2 e = lfma(f[V], k.scale, k.nwrs[csq(V)]);
-            const __half2 h = __float22half2_rn(e.v);
+            const uint32_t rr = lcg_next(rs);
+            const __half2 h = half2_sr(e.v, p.f16_sr ? rr : kHalfStep2x);
             if constexpr (sh != 0) { a[0] = __low2half(h); a[1] = __high2half(h); }
             else *(__half2*)a = h;
         }

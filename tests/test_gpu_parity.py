@@ -224,6 +224,34 @@ def test_fp16_deviation_storage_tracks_fp64(built_lib, oracle_lib):
     assert np.abs(rg[fl] - ro[fl]).max() < 2e-3
 
 
+def test_fp16_stochastic_rounding_keeps_a_weak_body_force(built_lib):
+    """Laminar channel driven by twice the force of its initial (steady) profile, so it accelerates by
+    ~1.5e-6 per step: the change of a stored population per step (~3e-7) is below half an FP16 step of
+    the deviation (~2e-6), so rounding every store to nearest freezes the flow, while stochastic
+    rounding (the default) keeps the increments in expectation and tracks FP64.  Tolerance: 2e-3
+    relative L2 of the x-z mean velocity profile after 4000 steps."""
+    shape = (64, 34, 32)
+    nx, ny, nz = shape
+    c = cases.channel(*shape, re_tau=8.0, u_max=0.02, amp=0.0, nu=0.01)  # steady at F = 2 nu u_max / h^2
+    force = (2.0 * c["force"][0], 0.0, 0.0)
+    prof = {}
+    for name, storage, opt in (("f64", "f64", 0), ("sr", "f16dev", 0), ("rn", "f16dev", capi.LBM_OPT_F16_ROUND_NEAREST)):
+        s = Solver(shape, turbulence=OmegaNo, storage=storage, nu=c["nu"], periodic=c["periodic"], force=force,
+                   options=opt)
+        s.set_flags(c["flags"])
+        s.set_bc()
+        s.init_fields(c["rho"], c["u"])
+        s.step(4000)
+        u = s.moments()[1].reshape(3, nz, ny, nx)
+        prof[name] = u[0].mean(axis=(0, 2))[1:-1]
+        s.close()
+    gain = np.linalg.norm(prof["f64"] - c["u"][0].reshape(nz, ny, nx).mean(axis=(0, 2))[1:-1])
+    assert gain > 0.1 * np.linalg.norm(prof["f64"])  # the flow did accelerate
+    err = {k: np.linalg.norm(prof[k] - prof["f64"]) / np.linalg.norm(prof["f64"]) for k in ("sr", "rn")}
+    assert err["sr"] < 2e-3, err
+    assert err["rn"] > 3 * err["sr"], err
+
+
 def test_populations_fp64_match_oracle(built_lib, oracle_lib):
     c = small_body_case()
     shape = (40, 16, 14)

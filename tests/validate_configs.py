@@ -7,8 +7,9 @@
 c1: lid-driven cavity 64^3, FP64 cumulant on the GPU against the CPU oracle's FP64 run of the same case
     (parity of the whole 10k-step trajectory), FP32 against FP64; centre-line profiles.
 c3: channel at 512x256x256 (laminar profile + 5 % seeded noise, Re_tau 180 forcing, Smagorinsky CLES
-    0.17) in FP64, FP32 and FP16-deviation storage: relative L2 error of the x-z-time-averaged mean
-    velocity and of the Reynolds stresses against FP64.
+    0.17) in FP64, FP32 and FP16-deviation storage (stochastic rounding, and round-to-nearest for
+    comparison): relative L2 error of the x-z-time-averaged mean velocity and of the Reynolds stresses
+    against FP64.
 c4: flow past the voxelized seeded body at 384x192x192: GPU voxelizer against the CPU oracle (bit for
     bit), FP32 against FP64 drag (momentum exchange, FP64 sums).
 Each prints one JSON line.
@@ -64,9 +65,13 @@ def c1(n, steps):
 
 
 def _channel_stats(shape, storage, steps, avg, case):
+    from lb_gb300 import capi
     nx, ny, nz = shape
+    opt = 0
+    if storage == "f16dev_rn":  # FP16 storage with round-to-nearest stores instead of stochastic rounding
+        storage, opt = "f16dev", capi.LBM_OPT_F16_ROUND_NEAREST
     s = Solver(shape, turbulence=OmegaLES, storage=storage, nu=case["nu"], cles=0.17, periodic=case["periodic"],
-               force=case["force"])
+               force=case["force"], options=opt)
     s.set_flags(case["flags"])
     s.set_bc()
     s.init_fields(case["rho"], case["u"])
@@ -90,9 +95,9 @@ def c3(shape, steps, avg):
     case = cases.channel(*shape, re_tau=180.0, u_max=0.05, amp=0.05)
     out = {"config": "C3 channel precision", "shape": list(shape), "steps": steps, "avg_steps": avg,
            "nu": case["nu"], "force": case["force"][0]}
-    stats = {st: _channel_stats(shape, st, steps, avg, case) for st in ("f64", "f32", "f16dev")}
+    stats = {st: _channel_stats(shape, st, steps, avg, case) for st in ("f64", "f32", "f16dev", "f16dev_rn")}
     m64, R64 = stats["f64"][0], stats["f64"][1]
-    for st in ("f32", "f16dev"):
+    for st in ("f32", "f16dev", "f16dev_rn"):
         m, R = stats[st][0], stats[st][1]
         out[f"{st}_mean_velocity_rel_l2_vs_f64"] = float(np.linalg.norm(m - m64) / np.linalg.norm(m64))
         out[f"{st}_reynolds_stress_rel_l2_vs_f64"] = float(np.linalg.norm(R - R64) / max(np.linalg.norm(R64), 1e-300))
