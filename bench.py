@@ -325,10 +325,10 @@ def main():
     glups16s = cells / (ms16s * 1e-3) / 1e9
     glups32 = cells / (ms32 * 1e-3) / 1e9
 
-    def roof(kind, ms):
+    def roof(kind, ms, traffic_kind=None):
         per_launch = BYTES_PER_CELL[kind] * N
         achieved = per_launch / (ms * 1e-3 / args.steps) / 1e9
-        t = traffic.get(kind)
+        t = traffic.get(traffic_kind or kind)
         return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                 "peak_kind": peak_kind, "traffic": (t["dram_bytes_per_cell"] * N) if t else None,
                 "algorithmic_bytes_per_launch": per_launch}
@@ -361,7 +361,7 @@ def main():
                        "closure": "learned MLP (tensor cores, fused), Smagorinsky fallback" if model else "smagorinsky",
                        "l2": "state 1.8 GB (f16) / 3.6 GB (f32) >> 129 MB L2; no flush needed",
                        "parallelism": f"{ws} independent replica(s)", "options": args.options},
-            "roofline": roof("f16dev", ms16),
+            "roofline": roof("f16dev", ms16, "f16dev_mlp" if model else None),
             "fp32_plain": {"value": glups32, "ms_per_step": ms32 / args.steps, "roofline": roof("f32", ms32),
                            "closure": "smagorinsky", "speedup_f16_over_f32": glups16 / glups32},
             "f16_smagorinsky": {"value": glups16s, "ms_per_step": ms16s / args.steps, "roofline": roof("f16dev", ms16s),
