@@ -231,3 +231,33 @@ def body_in_channel(nx=384, ny=192, nz=192, u_in=0.04, rho_out=1.0, nu=None, bod
     if nu is None:
         nu = u_in * 48.0 / 200.0
     return {"flags": f, "inlets": inl, "outlets": out, "nu": nu, "periodic": (0, 1, 1)}
+
+
+# ---- config 5: periodic decaying turbulence ------------------------------------------------------------
+def decay_field(n, k0=8.0, urms=0.04, seed=SEED):
+    """Random-phase solenoidal field on n^3 (box wavenumbers k = 2 pi m / n): amplitude
+    sqrt(E(k) / (4 pi k^2)), E ~ k^4 exp(-2 (k/k0)^2), random complex vector projected normal to k,
+    scaled to urms per component.  Returns u (3, n, n, n) float64 [z, y, x]."""
+    try:
+        from scipy import fft as sfft
+        irfftn = lambda a: sfft.irfftn(a, s=(n, n, n), axes=(1, 2, 3), workers=-1)  # noqa: E731
+    except ImportError:
+        irfftn = lambda a: np.fft.irfftn(a, s=(n, n, n), axes=(1, 2, 3))  # noqa: E731
+    rng = np.random.default_rng(seed)
+    kz = np.fft.fftfreq(n, 1.0 / n).astype(np.float32)[:, None, None]
+    ky = np.fft.fftfreq(n, 1.0 / n).astype(np.float32)[None, :, None]
+    kx = np.fft.rfftfreq(n, 1.0 / n).astype(np.float32)[None, None, :]
+    k2 = kx * kx + ky * ky + kz * kz
+    k = np.sqrt(k2)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        amp = np.where(k2 > 0, np.sqrt(k ** 4 * np.exp(-2.0 * (k / k0) ** 2) / (4.0 * np.pi * k2)), 0.0).astype(np.float32)
+    shape = (n, n, n // 2 + 1)
+    a = (rng.standard_normal((3,) + shape, dtype=np.float32) + 1j * rng.standard_normal((3,) + shape, dtype=np.float32))
+    kv = (np.broadcast_to(kx, shape), np.broadcast_to(ky, shape), np.broadcast_to(kz, shape))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        dot = (kv[0] * a[0] + kv[1] * a[1] + kv[2] * a[2]) / np.where(k2 > 0, k2, 1.0)
+    for c in range(3):
+        a[c] = (a[c] - kv[c] * dot) * amp
+    u = irfftn(a)  # components x, y, z on [z, y, x]
+    u *= urms / np.sqrt(np.mean(u * u))
+    return u.astype(np.float64)

@@ -12,6 +12,12 @@ c3: channel at 512x256x256 (laminar profile + 5 % seeded noise, Re_tau 180 forci
     against FP64.
 c4: flow past the voxelized seeded body at 384x192x192: GPU voxelizer against the CPU oracle (bit for
     bit), FP32 against FP64 drag (momentum exchange, FP64 sums).
+c5: periodic decaying turbulence, coarse n^3 (default 128; the configuration's 256 with --n 256) and a
+    4x-finer run of the same seeded random-phase field (E(k) ~ k^4 exp(-2 (k/k0)^2), k0 = 8,
+    divergence-free, u_rms = 0.04 per component).  A priori: the learned closure's and Smagorinsky's
+    subgrid-stress and dissipation errors on the filtered fine field.  A posteriori: coarse LES in
+    FP16-deviation storage with each closure from the filtered initial field, against the filtered
+    fine field after the same physical time.  Throughput of both closures on the coarse lattice.
 Each prints one JSON line.
 """
 import argparse
@@ -158,9 +164,84 @@ def c4(shape, steps):
     return out
 
 
+def _box(f, w):
+    nz, ny, nx = f.shape
+    return f.reshape(nz // w, w, ny // w, w, nx // w, w).mean(axis=(1, 3, 5))
+
+
+def c5(n, steps, k, models):
+    """models: {name: path of an lb_gb300.les.MlpModel}."""
+    from lb_gb300 import les
+    from lb_gb300.solver import OmegaMLP
+    nf = 4 * n
+    nets = {name: les.MlpModel.load(path) for name, path in models.items() if os.path.exists(path)}
+    nu_c = 1e-3 * (n / 128.0)  # coarse lattice viscosity; the fine run has 4x this (acoustic scaling)
+    nu_f = 4.0 * nu_c
+    out = {"config": "C5 decaying turbulence", "coarse": n, "fine": nf, "coarse_steps": steps,
+           "fine_steps": 4 * steps, "nu_coarse": nu_c, "nu_fine": nu_f, "k0": 8, "u_rms": 0.04,
+           "models": {name: os.path.relpath(models[name], ROOT) for name in nets}}
+    t0 = time.time()
+    uf = cases.decay_field(nf)
+    out["field_seconds"] = time.time() - t0
+    uc0 = np.stack([_box(uf[c], 4) for c in range(3)])
+    # fine run (FP32, cumulant + Smagorinsky)
+    s = Solver((nf, nf, nf), turbulence=OmegaLES, storage="f32", nu=nu_f, cles=0.17, periodic=(1, 1, 1))
+    s.set_flags(np.ones((nf, nf, nf), np.int32))
+    s.set_bc()
+    s.init_fields(np.ones(nf ** 3), uf.reshape(3, -1))
+    del uf
+    out["fine_seconds"] = s.step_timed(4 * steps) * 1e-3
+    samples = s.les_samples(4)
+    u_fine = s.moments()[1]
+    s.close()
+    u_ref = np.stack([_box(u_fine[c].reshape(nf, nf, nf), 4) for c in range(3)])
+    del u_fine
+    # a priori on the filtered fine field
+    nu_s = les.smagorinsky_nu(samples, 0.17)
+    cb = les.best_constant(samples)
+    out["samples"] = int(samples.shape[0])
+    sgs = {"smagorinsky_cles_0.17": les.sgs_error(nu_s, samples),
+           "smagorinsky_best_constant_of_this_field": les.sgs_error(les.smagorinsky_nu(samples, cb), samples),
+           "no_model": 1.0}
+    dis = {"smagorinsky_cles_0.17": les.sgs_dissipation_error(nu_s, samples), "no_model": 1.0}
+    for name, m in nets.items():
+        nu_net, ok = les.evaluate(m, samples[:, :7])
+        nu_m = np.where(ok, nu_net, nu_s)
+        out[f"in_range_fraction_{name}"] = float(ok.mean())
+        sgs[f"mlp_{name}"] = les.sgs_error(nu_m, samples)
+        dis[f"mlp_{name}"] = les.sgs_dissipation_error(nu_m, samples)
+    out["a_priori_sgs_error"] = sgs
+    out["a_priori_dissipation_error"] = dis
+    # a posteriori: coarse FP16 LES from the filtered initial field
+    runs = [("smagorinsky", None, 1)]
+    for name in nets:
+        runs += [(f"mlp_{name}", name, 1), (f"mlp_{name}_every_{k}", name, k)]
+    post, thr = {}, {}
+    for label, name, interval in runs:
+        g = Solver((n, n, n), turbulence=OmegaMLP if name else OmegaLES, storage="f16dev", nu=nu_c, cles=0.17,
+                   periodic=(1, 1, 1), mlp_interval=interval)
+        g.set_flags(np.ones((n, n, n), np.int32))
+        g.set_bc()
+        g.init_fields(np.ones(n ** 3), uc0.reshape(3, -1))
+        if name:
+            g.load_mlp(nets[name])
+        ms = g.step_timed(steps)
+        u = g.moments()[1].reshape(3, n, n, n)
+        g.close()
+        post[label] = float(np.linalg.norm(u - u_ref) / np.linalg.norm(u_ref))
+        thr[label] = n ** 3 * steps / (ms * 1e-3) / 1e9
+    out["a_posteriori_rel_l2_vs_filtered_fine"] = post
+    out["a_posteriori_initial_field_vs_filtered_fine"] = float(np.linalg.norm(uc0 - u_ref) / np.linalg.norm(u_ref))
+    out["coarse_glups_fp16"] = thr
+    out["energy_ratio_filtered_fine_T_over_0"] = float(np.sum(u_ref ** 2) / np.sum(uc0 ** 2))
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("which", choices=["c1", "c3", "c4"])
+    ap.add_argument("which", choices=["c1", "c3", "c4", "c5"])
+    ap.add_argument("--interval", type=int, default=8)
+    ap.add_argument("--model", default=None, help="c5: evaluate this model file only")
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--avg", type=int, default=5000)
@@ -171,9 +252,16 @@ def main():
     elif a.which == "c3":
         shape = tuple(int(x) for x in (a.shape or "512,256,256").split(","))
         r = c3(shape, a.steps or 20000, a.avg)
-    else:
+    elif a.which == "c4":
         shape = tuple(int(x) for x in (a.shape or "384,192,192").split(","))
         r = c4(shape, a.steps or 4000)
+    else:
+        data = os.path.join(ROOT, "lb_gb300", "data")
+        models = {"channel": os.path.join(data, "les_mlp_channel.npz"),
+                  "channel_decay": os.path.join(data, "les_mlp_channel_decay.npz")}
+        if a.model:
+            models = {"given": a.model}
+        r = c5(a.n if a.n != 64 else 128, a.steps or 200, a.interval, models)
     print(json.dumps(r))
 
 
