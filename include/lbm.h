@@ -62,7 +62,7 @@ typedef int32_t lbm_status;
 #define LBM_INLET_EQUILIBRIUM  1  /* Inlet/InletVelocityEquilibrium.h:18-108 */
 
 typedef struct lbm_config {
-    int32_t nx, ny, nz;       /* lattice size */
+    int32_t nx, ny, nz;       /* lattice size: at most 2^31 - 2^21 cells, nx <= 2^21, ny, nz <= 65535 */
     int32_t periodic[3];      /* 1 = wrap this axis by index (replaces Periodic.h ghost planes) */
     int32_t collision;        /* LBM_COLLISION_* */
     int32_t closure;          /* LBM_CLOSURE_* */

@@ -193,8 +193,12 @@ lbm_status lbm_create(const lbm_config* cfg, lbm_ctx** out) {
     if (cfg->nx < 3 || cfg->ny < 3 || cfg->nz < 3)
         return fail(nullptr, LBM_ERR_INVALID, "lattice must be at least 3 cells per axis (got %d %d %d)", cfg->nx, cfg->ny, cfg->nz);
     long long N = (long long)cfg->nx * cfg->ny * cfg->nz;
-    if (27LL * N >= (1LL << 31) * 4LL)
-        return fail(nullptr, LBM_ERR_UNSUPPORTED, "lattice of %lld cells is too large", N);
+    // cell indices are 32-bit in the kernels (signed in the pair path, where an x-wrapped index may
+    // exceed the cell by up to nx): N + nx must stay below 2^31; y and z are launch-grid dimensions
+    if (cfg->nx > (1 << 21) || N > (1LL << 31) - (1LL << 21) || cfg->ny > 65535 || cfg->nz > 65535)
+        return fail(nullptr, LBM_ERR_UNSUPPORTED,
+                    "lattice %d x %d x %d: at most 2^31 - 2^21 cells, nx <= 2^21, ny and nz <= 65535",
+                    cfg->nx, cfg->ny, cfg->nz);
     if (cfg->collision != LBM_COLLISION_SRT && cfg->collision != LBM_COLLISION_CUMULANT2015)
         return fail(nullptr, LBM_ERR_UNSUPPORTED, "collision %d not implemented", cfg->collision);
     if (cfg->closure != LBM_CLOSURE_NONE && cfg->closure != LBM_CLOSURE_SMAGORINSKY && cfg->closure != LBM_CLOSURE_MLP)

@@ -44,6 +44,10 @@ def test_create_rejects_bad_config_before_touching_the_gpu(built_lib):
     assert L.lbm_create(C.byref(cfg), C.byref(ctx)) == capi.LBM_ERR_INVALID
     cfg = capi.make_config(8, 8, 8, closure=7)
     assert L.lbm_create(C.byref(cfg), C.byref(ctx)) == capi.LBM_ERR_UNSUPPORTED
+    cfg = capi.make_config(2048, 1024, 1024)  # 2^31 cells: beyond the 32-bit cell index
+    assert L.lbm_create(C.byref(cfg), C.byref(ctx)) == capi.LBM_ERR_UNSUPPORTED
+    cfg = capi.make_config(8, 70000, 8)  # beyond the launch grid's y extent
+    assert L.lbm_create(C.byref(cfg), C.byref(ctx)) == capi.LBM_ERR_UNSUPPORTED
 
 
 def test_mesher_wall_pass_host_only(built_lib):
