@@ -174,6 +174,20 @@ lbm_status lbm_checkpoint_load(lbm_ctx* ctx, const char* path);
 /* in place: every fluid cell (>0) gets 1 + number of solid cells in its 26-neighbourhood */
 lbm_status lbm_mesher_wall_pass(int32_t* flags, int32_t nx, int32_t ny, int32_t nz);
 
+/* ---- mesh-matrix text files (postprocesors/outputerMesh.h:19-211) ------------ */
+/* Writes the reference's format (outputerMesh::MeshMatrixOut): the header "Dimensions: nx ny nz ",
+ * resolution and additional factors, BBmax x/y/z, BBmin x/y/z (as the reference's float fields print
+ * through an ostream, 6 significant digits), then the flags with x fastest, one line per (y, z) with a
+ * space after every value, an empty line after every z slice.  bbox: xmin, ymin, zmin, xmax, ymax,
+ * zmax (the order of lbm_voxelize_off).  The path is used as given (the reference prepends results/). */
+lbm_status lbm_mesh_matrix_write(const char* path, const int32_t* flags, const int32_t dims[3],
+                                 double resolution, double additional, const double bbox[6]);
+/* Reads it back (outputerMesh::MeshMatrixIn): header fields by keyword, then nx*ny*nz integers into
+ * flags (nullable: header only; capacity in elements).  resolution, additional, bbox are nullable. */
+lbm_status lbm_mesh_matrix_read(const char* path, int32_t* flags, int64_t capacity, int32_t dims[3],
+                                double* resolution, double* additional, double bbox[6]);
+const char* lbm_mesh_matrix_last_error(void);
+
 /* ---- OFF voxelizer on the GPU (preprocess geometryMesherOFF.h:45-112) -------- */
 /* Reads an OFF/NOFF file; dims_out = ceil((BBmax-BBmin)*res + 2*add) per axis and bbox_out
  * (xmin,ymin,zmin,xmax,ymax,zmax).  flags_out (nullable: query dims only) receives

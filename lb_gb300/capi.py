@@ -178,6 +178,9 @@ def lib():
         "lbm_mlp_gradient": ([vp, C.POINTER(LbmMlpModel), i64, i64, fp, dp], i32),
         "lbm_mlp_train": ([vp, C.POINTER(LbmMlpModel), i32, i32, C.c_float, C.c_uint64, fp], i32),
         "lbm_mlp_last_error": ([], C.c_char_p),
+        "lbm_mesh_matrix_write": ([C.c_char_p, ip, ip, f64, f64, dp], i32),
+        "lbm_mesh_matrix_read": ([C.c_char_p, ip, i64, ip, dp, dp, dp], i32),
+        "lbm_mesh_matrix_last_error": ([], C.c_char_p),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

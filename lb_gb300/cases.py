@@ -42,6 +42,39 @@ def wall_pass(flags):
     return f
 
 
+def write_mesh_matrix(path, flags, resolution, additional, bbox):
+    """flags [z, y, x] to the reference's mesh-matrix text file (lbm_mesh_matrix_write)."""
+    import ctypes as C
+    f = np.ascontiguousarray(flags, dtype=np.int32)
+    nz, ny, nx = f.shape
+    dims = np.array([nx, ny, nz], np.int32)
+    bb = np.ascontiguousarray(bbox, dtype=np.float64)
+    L = capi.lib()
+    st = L.lbm_mesh_matrix_write(path.encode(), f.ctypes.data_as(C.POINTER(C.c_int32)),
+                                 dims.ctypes.data_as(C.POINTER(C.c_int32)), float(resolution), float(additional),
+                                 bb.ctypes.data_as(C.POINTER(C.c_double)))
+    if st:
+        raise capi.LbmError(st, L.lbm_mesh_matrix_last_error().decode())
+
+
+def read_mesh_matrix(path):
+    """The reference's mesh-matrix text file: (flags [z, y, x] int32, resolution, additional, bbox)."""
+    import ctypes as C
+    L = capi.lib()
+    dims = np.zeros(3, np.int32)
+    res, add = C.c_double(0), C.c_double(0)
+    bb = np.zeros(6)
+    args = (dims.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(res), C.byref(add), bb.ctypes.data_as(C.POINTER(C.c_double)))
+    st = L.lbm_mesh_matrix_read(path.encode(), None, 0, *args)
+    if st:
+        raise capi.LbmError(st, L.lbm_mesh_matrix_last_error().decode())
+    f = np.zeros(int(dims.prod()), np.int32)
+    st = L.lbm_mesh_matrix_read(path.encode(), f.ctypes.data_as(C.POINTER(C.c_int32)), f.size, *args)
+    if st:
+        raise capi.LbmError(st, L.lbm_mesh_matrix_last_error().decode())
+    return f.reshape(dims[2], dims[1], dims[0]), res.value, add.value, bb
+
+
 def wall_pass_numpy(flags):
     """Same count in numpy (no library needed): fluid cells get 1 + #solid 26-neighbours."""
     f = np.asarray(flags, dtype=np.int32).copy()

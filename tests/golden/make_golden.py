@@ -6,13 +6,15 @@ Reads (in the reference checkout, read-only):
 and writes, next to this script:
   BackwardStepLaminar.off                        - the input mesh, byte-for-byte
   backward_step_laminar.npz                      - dims, header values and the 0/1 matrix,
-                                                   bit-packed (x fastest, then y, then z)
+                                                   bit-packed (x fastest, then y, then z), and the
+                                                   SHA-256 of the matrix text file
 
 The mesh-matrix text format is the reference's outputerMesh::MeshMatrixOut
 (3D/preprocess/src/postprocesors/outputerMesh.h:19-56): a 9-line header, then the values
 with x fastest, one row per (y, z) and a blank line after every z slice.
 Run:  python tests/golden/make_golden.py [reference_root]
 """
+import hashlib
 import os
 import shutil
 import sys
@@ -54,6 +56,8 @@ def main(ref_root):
         bbmax=np.asarray([float(header[k][0]) for k in ("BBmaxx", "BBmaxy", "BBmaxz")]),
         packed=np.packbits(arr.astype(np.uint8)),
         count_inside=np.int64(arr.sum()),
+        # SHA-256 of the reference's matrix file: the mesh-matrix writer must reproduce it byte for byte
+        txt_sha256=np.array(hashlib.sha256(open(txt, "rb").read()).hexdigest()),
     )
     print("dims", dims, "inside", int(arr.sum()), "of", arr.size)
 
