@@ -345,8 +345,14 @@ LBM_D void step_pair(const Params& p, int x0, int y, int z) {
     }
 }
 
+// minimum resident CTAs per SM requested from the register allocator.  6 (at most 85 registers, a few
+// spilled to L1) measured fastest on a GB300 at 512x256x256: FP16 40.0 GLUPS against 36.7 with no
+// request (128 registers, 4 CTAs), FP32 30.9 against 30.2; 5, 7 and 8 were slower.
+#ifndef LBM_STEP2_MIN_BLOCKS
+#define LBM_STEP2_MIN_BLOCKS 6
+#endif
 template <class S, int COLL, int CLOS, bool ODD>
-__global__ void __launch_bounds__(128) k_step2(Params p) {
+__global__ void __launch_bounds__(128, LBM_STEP2_MIN_BLOCKS) k_step2(Params p) {
     const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     if (x0 >= p.nx) return;
     step_pair<S, COLL, CLOS, ODD>(p, x0, blockIdx.y, blockIdx.z);
