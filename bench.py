@@ -263,7 +263,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--options", type=int, default=0, help="LBM_OPT_* bits passed to lbm_create")
-    ap.add_argument("--mlp-interval", type=int, default=8,
+    ap.add_argument("--mlp-interval", type=int, default=16,
                     help="also time the learned closure with nu_t refreshed every k-th step")
     ap.add_argument("--mlp", default=os.path.join(ROOT, "lb_gb300", "data", "les_mlp_channel.npz"),
                     help="learned-closure model (lb_gb300.les_train); the headline runs FP16 storage with it")
