@@ -147,10 +147,16 @@ def channel_case(shape):
     return cases.channel(*shape, re_tau=180.0, u_max=0.05, amp=0.05)
 
 
-def make_solver(shape, case, storage, device, options=0, model=None, interval=1):
+def collision_policy(name):
+    from lb_gb300 import solver
+    return {"cumulant2015": solver.CollisionCumD3Q27Turbulent2015, "cumulant2017": solver.CollisionCumD3Q27Turbulent2017,
+            "combined": solver.CollisionCumD3Q27TurbulentCombined, "srt": solver.CollisionSRTTurbulent}[name]
+
+
+def make_solver(shape, case, storage, device, options=0, model=None, interval=1, collision="cumulant2015"):
     """Cumulant collision with the Smagorinsky closure, or with the learned closure when a model is given."""
-    from lb_gb300.solver import CollisionCumD3Q27Turbulent2015, OmegaLES, OmegaMLP, Solver
-    s = Solver(shape, collision=CollisionCumD3Q27Turbulent2015, turbulence=OmegaMLP if model else OmegaLES,
+    from lb_gb300.solver import OmegaLES, OmegaMLP, Solver
+    s = Solver(shape, collision=collision_policy(collision), turbulence=OmegaMLP if model else OmegaLES,
                storage=storage, nu=case["nu"], cles=0.17, periodic=case["periodic"], force=case["force"],
                device=device, options=options, mlp_interval=interval)
     s.set_flags(case["flags"])
@@ -161,8 +167,9 @@ def make_solver(shape, case, storage, device, options=0, model=None, interval=1)
     return s
 
 
-def time_storage(shape, case, storage, steps, warmup, device, dist, with_clocks, options=0, model=None, interval=1):
-    s = make_solver(shape, case, storage, device, options, model, interval)
+def time_storage(shape, case, storage, steps, warmup, device, dist, with_clocks, options=0, model=None, interval=1,
+                 collision="cumulant2015"):
+    s = make_solver(shape, case, storage, device, options, model, interval, collision)
     s.step(warmup)
     s.synchronize()
     barrier(dist)
@@ -262,6 +269,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for the CPU arms")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-collisions", action="store_true",
+                    help="skip the SRT / cumulant-2017 / combined throughput lines")
     ap.add_argument("--options", type=int, default=0, help="LBM_OPT_* bits passed to lbm_create")
     ap.add_argument("--mlp-interval", type=int, default=16,
                     help="also time the learned closure with nu_t refreshed every k-th step")
@@ -342,6 +351,22 @@ def main():
                "h2d_bytes_per_step": h2d / k, "d2h_bytes_per_step": d2h, "steps": k,
                "includes": "lbm_set_flags + lbm_set_bc + lbm_init_fields (+ lbm_mlp_load) from host buffers, "
                            "then per step lbm_step + lbm_probe (device->host read of u, rho)"}
+    # the other collision operators on the same case (Smagorinsky closure), FP16 and FP32 storage
+    colls = None
+    if not args.no_collisions:
+        colls = {}
+        kc = min(args.steps, 200)
+        for name in ("srt", "cumulant2017", "combined"):
+            colls[name] = {}
+            for st in ("f16dev", "f32"):
+                msc, dc, _ = time_storage(shape, case, st, kc, args.warmup, device, dist, False, args.options,
+                                          collision=name)
+                msc = dist_max(dist, msc)
+                colls[name][st] = {"value": dist_sum(dist, float(N) * kc) / (msc * 1e-3) / 1e9,
+                                   "frac": BYTES_PER_CELL[st] * N / (msc * 1e-3 / kc) / 1e9 / hbm,
+                                   "nonfinite": dc.nonfinite}
+        colls["steps"] = kc
+        colls["unit"] = "GLUPS"
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         from oracle import build as obuild
@@ -369,6 +394,7 @@ def main():
             "learned_closure": learned_block(args.mlp, model, glups16, glups16s,
                                              (args.mlp_interval, cells / (ms16k * 1e-3) / 1e9) if ms16k else None),
             # one fused step kernel per step; the row-staged step adds the launch over the wall rows
+            "collisions": colls,
             "gpu_launches": args.steps * (2 if args.options & 1 else 1), "clocks": clk, "cpu_baseline": cpu, "e2e": e2e,
             "check": {"f16_mass": d16.mass, "f32_mass": d32.mass,
                       "nonfinite": d16.nonfinite + d32.nonfinite + d16s.nonfinite}}

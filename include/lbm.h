@@ -46,6 +46,14 @@ typedef int32_t lbm_status;
 /* collision operator (reference: solvers/collisions/) */
 #define LBM_COLLISION_SRT            0  /* CollisionSRTTurbulent.h:20-81 */
 #define LBM_COLLISION_CUMULANT2015   1  /* CollisionCumD3Q27Turbulent2015.h:19-537 */
+#define LBM_COLLISION_CUMULANT2017   2  /* CollisionCumD3Q27Turbulent2017.h:19-594, with the omega_210
+                                           limiters on C210 +- C012, the bulk term -k000 and eq. 44 driven
+                                           by Dyv + Dzw - 2 Dxu (the reference reads C120 +- C102, -(rho - 1)
+                                           and Dxu + Dyv - 2 Dzw, :256-266, :295, :351) */
+#define LBM_COLLISION_CUMULANT_COMBINED 3  /* CollisionCumD3Q27TurbulentCombined.h:19-1087: cumulant-2015 on
+                                           cells of flag 1, cumulant-2017 (corrected as above) on every other
+                                           fluid or boundary cell (:1066-1078); the reference's 2017 copy
+                                           there subtracts 1 + rho in Dxu (:295) */
 
 /* eddy-viscosity closure (reference: solvers/turbulence/) */
 #define LBM_CLOSURE_NONE         0  /* OmegaNo.h:25-48 : omega = 1/tau */

@@ -26,6 +26,8 @@ namespace lbm_gb300 {
 // ---- policy tags (reference file of each in the comment) ----------------------------------------------
 struct D3Q27 { static constexpr int numberOfDiscreteVelocities = 27; };           // models/D3Q27/D3Q27.h
 struct CollisionCumD3Q27Turbulent2015 { static constexpr int32_t code = LBM_COLLISION_CUMULANT2015; };
+struct CollisionCumD3Q27Turbulent2017 { static constexpr int32_t code = LBM_COLLISION_CUMULANT2017; };
+struct CollisionCumD3Q27TurbulentCombined { static constexpr int32_t code = LBM_COLLISION_CUMULANT_COMBINED; };
 struct CollisionSRTTurbulent { static constexpr int32_t code = LBM_COLLISION_SRT; };  // collisions/CollisionSRTTurbulent.h
 struct OmegaLES { static constexpr int32_t code = LBM_CLOSURE_SMAGORINSKY; };      // turbulence/OmegaLES.h
 struct OmegaNo { static constexpr int32_t code = LBM_CLOSURE_NONE; };             // turbulence/OmegaNo.h

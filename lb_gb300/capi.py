@@ -21,6 +21,8 @@ LBM_ERR_UNSUPPORTED = -8
 
 LBM_COLLISION_SRT = 0
 LBM_COLLISION_CUMULANT2015 = 1
+LBM_COLLISION_CUMULANT2017 = 2
+LBM_COLLISION_CUMULANT_COMBINED = 3
 LBM_CLOSURE_NONE = 0
 LBM_CLOSURE_SMAGORINSKY = 1
 LBM_CLOSURE_MLP = 2

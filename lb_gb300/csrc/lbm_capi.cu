@@ -199,7 +199,11 @@ lbm_status lbm_create(const lbm_config* cfg, lbm_ctx** out) {
         return fail(nullptr, LBM_ERR_UNSUPPORTED,
                     "lattice %d x %d x %d: at most 2^31 - 2^21 cells, nx <= 2^21, ny and nz <= 65535",
                     cfg->nx, cfg->ny, cfg->nz);
-    if (cfg->collision != LBM_COLLISION_SRT && cfg->collision != LBM_COLLISION_CUMULANT2015)
+    if ((cfg->collision == LBM_COLLISION_CUMULANT2017 || cfg->collision == LBM_COLLISION_CUMULANT_COMBINED) &&
+        cfg->closure == LBM_CLOSURE_MLP)
+        return fail(nullptr, LBM_ERR_UNSUPPORTED, "the learned closure runs with the SRT or cumulant-2015 collision");
+    if (cfg->collision != LBM_COLLISION_SRT && cfg->collision != LBM_COLLISION_CUMULANT2015 &&
+        cfg->collision != LBM_COLLISION_CUMULANT2017 && cfg->collision != LBM_COLLISION_CUMULANT_COMBINED)
         return fail(nullptr, LBM_ERR_UNSUPPORTED, "collision %d not implemented", cfg->collision);
     if (cfg->closure != LBM_CLOSURE_NONE && cfg->closure != LBM_CLOSURE_SMAGORINSKY && cfg->closure != LBM_CLOSURE_MLP)
         return fail(nullptr, LBM_ERR_UNSUPPORTED, "closure %d not implemented", cfg->closure);

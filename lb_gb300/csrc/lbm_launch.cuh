@@ -43,9 +43,14 @@ template <class S>
 cudaError_t launch_step(const Params& p, int collision, int closure, cudaStream_t st) {
     if (closure == 2) {
         if constexpr (S::kind == 0) return cudaErrorInvalidValue;
-        else return collision == 0 ? step_parity<S, 0, 2>(p, st) : step_parity<S, 1, 2>(p, st);
+        else {
+            if (collision >= 2) return cudaErrorInvalidValue;  // learned closure: SRT or cumulant-2015
+            return collision == 0 ? step_parity<S, 0, 2>(p, st) : step_parity<S, 1, 2>(p, st);
+        }
     }
     if (collision == 0) return closure == 0 ? step_parity<S, 0, 0>(p, st) : step_parity<S, 0, 1>(p, st);
+    if (collision == 2) return closure == 0 ? step_parity<S, 2, 0>(p, st) : step_parity<S, 2, 1>(p, st);
+    if (collision == 3) return closure == 0 ? step_parity<S, 3, 0>(p, st) : step_parity<S, 3, 1>(p, st);
     return closure == 0 ? step_parity<S, 1, 0>(p, st) : step_parity<S, 1, 1>(p, st);
 }
 

@@ -315,4 +315,187 @@ LBM_D void collide_cum15(L (&f)[27], L rho, L ri, L ux, L uy, L uz, L om, const 
     });
 }
 
+
+// ---- cumulant collision with the 2017 parametrisation (CollisionCumD3Q27Turbulent2017.h:241-376) -----
+// Full forward chimera transform (G2015 eq. 43-45) to the 27 central moments, cumulants (eq. 47-54),
+// relaxation with omega_1 local and omega_2 = 1: third-order rates from G2017 eq. 14-16 limited by
+// |C| / (rho lambda + |C|), lambda = 0.01 (section 7); fourth-order cumulants driven by the velocity
+// gradients through A and B (G2017 eq. 43-48); omega_6..10 = 1; then eq. 81-87 and the backward
+// transform.  The three reference defects (the omega_210 limiters reading C120 +- C102, the bulk part
+// of Dxu subtracting rho - 1 instead of k000, and eq. 44 driven by Dxu + Dyv - 2 Dzw, which breaks the
+// operator's invariance under axis relabelling) are corrected here; the oracle reproduces them on request.
+LBM_D float labs_(float x) { return fabsf(x); }
+LBM_D double labs_(double x) { return fabs(x); }
+LBM_D F2 labs_(F2 x) { return F2(fabsf(x.v.x), fabsf(x.v.y)); }
+
+// forward triplet: populations (m, z, p) along one axis -> central moments (k0, k1, k2)
+template <class L>
+LBM_D void tri_fwd(L m, L z, L p, L u, L& k0, L& k1, L& k2) {
+    const L s = p + m, d = p - m;
+    k0 = s + z;
+    k1 = lfma(-u, k0, d);
+    k2 = lfma(u, lfma(u, k0, (L)-2.0f * d), s);  // s - 2u d + u^2 k0
+}
+
+template <class L>
+LBM_D void collide_cum17(L (&f)[27], L rho, L ri, L ux, L uy, L uz, L om) {
+    L k[3][3][3];
+    // z pass, y pass, x pass (indices: slot c+1 before the pass, moment order after it)
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            const int vm = vid(a - 1, b - 1, -1), vz = vid(a - 1, b - 1, 0), vp = vid(a - 1, b - 1, 1);
+            tri_fwd(f[vm], f[vz], f[vp], uz, k[a][b][0], k[a][b][1], k[a][b][2]);
+        }
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            L k0, k1, k2;
+            tri_fwd(k[a][0][c], k[a][1][c], k[a][2][c], uy, k0, k1, k2);
+            k[a][0][c] = k0; k[a][1][c] = k1; k[a][2][c] = k2;
+        }
+#pragma unroll
+    for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            L k0, k1, k2;
+            tri_fwd(k[0][b][c], k[1][b][c], k[2][b][c], ux, k0, k1, k2);
+            k[0][b][c] = k0; k[1][b][c] = k1; k[2][b][c] = k2;
+        }
+    const L one = (L)1.0f, two = (L)2.0f, four = (L)4.0f, half = (L)0.5f, third = (L)(1.0 / 3.0);
+    // cumulants of order 4 to 6 (G2015 eq. 51-54); orders 2 and 3 equal the central moments
+    const L K000 = k[0][0][0], K100 = k[1][0][0], K010 = k[0][1][0], K001 = k[0][0][1];
+    const L C110 = k[1][1][0], C101 = k[1][0][1], C011 = k[0][1][1];
+    const L C200 = k[2][0][0], C020 = k[0][2][0], C002 = k[0][0][2];
+    const L C120 = k[1][2][0], C102 = k[1][0][2], C210 = k[2][1][0], C012 = k[0][1][2], C201 = k[2][0][1],
+            C021 = k[0][2][1], C111 = k[1][1][1];
+    const L C211 = k[2][1][1] - lfma(C200, C011, two * C101 * C110) * ri;
+    const L C121 = k[1][2][1] - lfma(C020, C101, two * C110 * C011) * ri;
+    const L C112 = k[1][1][2] - lfma(C002, C110, two * C011 * C101) * ri;
+    const L C220 = k[2][2][0] - lfma(C020, C200, two * C110 * C110) * ri;
+    const L C022 = k[0][2][2] - lfma(C002, C020, two * C011 * C011) * ri;
+    const L C202 = k[2][0][2] - lfma(C200, C002, two * C101 * C101) * ri;
+    const L C122 = k[1][2][2] - (lfma(C020, C102, lfma(C002, C120, four * C011 * C111)) +
+                                 two * lfma(C110, C012, C101 * C021)) * ri;
+    const L C212 = k[2][1][2] - (lfma(C002, C210, lfma(C200, C012, four * C101 * C111)) +
+                                 two * lfma(C011, C201, C110 * C102)) * ri;
+    const L C221 = k[2][2][1] - (lfma(C200, C021, lfma(C020, C201, four * C110 * C111)) +
+                                 two * lfma(C101, C120, C011 * C210)) * ri;
+    const L m4sum = lfma(C011, k[2][1][1], lfma(C101, k[1][2][1], C110 * k[1][1][2]));
+    const L m3sum = lfma(C120, C102, lfma(C210, C012, C201 * C021));
+    const L C222 = k[2][2][2] -
+                   (lfma(four * C111, C111, lfma(C200, k[0][2][2], lfma(C020, k[2][0][2], C002 * k[2][2][0]))) +
+                    lfma(four, m4sum, two * m3sum)) * ri +
+                   lfma((L)16.0f * C110, C101 * C011,
+                        lfma(four, lfma(C101 * C101, C020, lfma(C011 * C011, C200, C110 * C110 * C002)),
+                             two * C200 * C020 * C002)) * ri * ri;
+    // rates: omega_2 = 1, G2017 eq. 14-16 with o = omega_1
+    const L o = om;
+    const L w3 = (L)8.0f * (o - two) * lfma((L)3.0f, o, (L)-1.0f - (L)5.0f * o) *
+                 rcp(lfma((L)8.0f * lfma((L)-2.0f, o, (L)5.0f), o, lfma(o, lfma((L)9.0f, o, (L)-26.0f), (L)8.0f)));
+    const L w4 = (L)8.0f * (o - two) * lfma((L)3.0f, o, o - (L)7.0f) *
+                 rcp(lfma(o, lfma((L)8.0f, o, (L)-42.0f), (L)56.0f) - (L)8.0f * o);
+    const L w5 = (L)24.0f * (o - two) *
+                 lfma((L)4.0f * o, o, lfma(o, lfma((L)-13.0f, o, (L)18.0f), lfma(o, lfma((L)6.0f, o, (L)-11.0f), two))) *
+                 rcp((L)16.0f * o * o * (o - (L)6.0f) - two * o * lfma((L)5.0f * o, lfma((L)9.0f, o, (L)-46.0f), (L)216.0f) +
+                     lfma(o * lfma((L)3.0f, o, (L)-10.0f), lfma((L)15.0f, o, (L)-28.0f), (L)-48.0f));
+    const L rl = rho * (L)0.01;  // lambda; a double literal, so FP64 lanes get 0.01 exactly
+    auto lim = [&](L w, L c) {
+        const L a = labs_(c);
+        return lfma(one - w, a * rcp(rl + a), w);
+    };
+    const L den = (o - one) * lfma((L)3.0f, o, two - (L)8.0f * o);
+    const L rden = rcp(den);
+    const L A4 = lfma((L)4.0f * o, o, lfma(two * o, o - (L)6.0f, lfma(o, lfma((L)-3.0f, o, (L)10.0f), (L)-4.0f))) * rden;
+    const L B4 = (lfma((L)4.0f * o, lfma((L)9.0f, o, (L)-16.0f), (L)-4.0f * o * o) -
+                  two * lfma((L)9.0f * o, o - two, two)) * rden * third;
+    // second order (G2015 eq. 55-65)
+    const L h = half * ri;
+    const L d20 = C200 - C020, d02 = C200 - C002;
+    const L Dxu = -h * lfma(o, d20 + d02, C200 + C020 + C002 - K000);
+    const L t3oh = (L)3.0f * o * h;
+    const L Dyv = lfma(t3oh, d20, Dxu), Dzw = lfma(t3oh, d02, Dxu);
+    const L m3o = (L)-3.0f * o * ri;
+    const L DxvDyu = m3o * C110, DxwDzu = m3o * C101, DywDzv = m3o * C011;
+    const L o1 = one - o;
+    const L a3 = rho * lfma((L)-1.5f, o, (L)3.0f);  // 3 rho (1 - o/2)
+    const L xD = ux * ux * Dxu, yD = uy * uy * Dyv, zD = uz * uz * Dzw;
+    const L E61 = lfma(o1, d20, a3 * (yD - xD));
+    const L E64 = lfma(o1, d02, a3 * (zD - xD));
+    const L E65 = lfma((L)-1.5f * rho, xD + yD + zD, K000);
+    const L s200 = (E61 + E64 + E65) * third;
+    const L s020 = lfma((L)-2.0f, E61, E64 + E65) * third;
+    const L s002 = lfma((L)-2.0f, E64, E61 + E65) * third;
+    const L s110 = o1 * C110, s101 = o1 * C101, s011 = o1 * C011;
+    // third order (G2017 eq. 37-42)
+    const L P1 = (one - lim(w3, C120 + C102)) * (C120 + C102), M1 = (one - lim(w4, C120 - C102)) * (C120 - C102);
+    const L P2 = (one - lim(w3, C210 + C012)) * (C210 + C012), M2 = (one - lim(w4, C210 - C012)) * (C210 - C012);
+    const L P3 = (one - lim(w3, C201 + C021)) * (C201 + C021), M3 = (one - lim(w4, C201 - C021)) * (C201 - C021);
+    const L s120 = half * (P1 + M1), s102 = half * (P1 - M1);
+    const L s210 = half * (P2 + M2), s012 = half * (P2 - M2);
+    const L s201 = half * (P3 + M3), s021 = half * (P3 - M3);
+    const L s111 = (one - lim(w5, C111)) * C111;
+    // fourth order (G2017 eq. 43-48 with omega_6..8 = 1); fifth and sixth order relax to zero
+    const L vis = rcp(o) - half;
+    const L gA = vis * A4 * rho * (L)(2.0 / 3.0), gB = vis * B4 * rho * (L)(-1.0 / 3.0);
+    // eq. 43-45 solved for the three cumulants, with eq. 44 driven by Dyv + Dzw - 2 Dxu (its axis
+    // image of eq. 43): each C_abc with two 2-indices follows the gradients of those two axes
+    const L c220 = -gA * (Dxu + Dyv), c202 = -gA * (Dxu + Dzw), c022 = -gA * (Dyv + Dzw);
+    const L c211 = gB * DywDzv, c121 = gB * DxwDzu, c112 = gB * DxvDyu;
+    // back to central moments (G2015 eq. 81-87)
+    L q[3][3][3];
+    q[0][0][0] = K000;
+    q[1][0][0] = -K100; q[0][1][0] = -K010; q[0][0][1] = -K001;
+    q[1][1][0] = s110; q[1][0][1] = s101; q[0][1][1] = s011;
+    q[2][0][0] = s200; q[0][2][0] = s020; q[0][0][2] = s002;
+    q[1][2][0] = s120; q[1][0][2] = s102; q[2][1][0] = s210; q[0][1][2] = s012; q[2][0][1] = s201; q[0][2][1] = s021;
+    q[1][1][1] = s111;
+    q[2][1][1] = c211 + lfma(s200, s011, two * s101 * s110) * ri;
+    q[1][2][1] = c121 + lfma(s020, s101, two * s110 * s011) * ri;
+    q[1][1][2] = c112 + lfma(s002, s110, two * s011 * s101) * ri;
+    q[2][2][0] = c220 + lfma(s020, s200, two * s110 * s110) * ri;
+    q[0][2][2] = c022 + lfma(s002, s020, two * s011 * s011) * ri;
+    q[2][0][2] = c202 + lfma(s200, s002, two * s101 * s101) * ri;
+    q[1][2][2] = (lfma(s020, s102, lfma(s002, s120, four * s011 * s111)) + two * lfma(s110, s012, s101 * s021)) * ri;
+    q[2][1][2] = (lfma(s002, s210, lfma(s200, s012, four * s101 * s111)) + two * lfma(s011, s201, s110 * s102)) * ri;
+    q[2][2][1] = (lfma(s200, s021, lfma(s020, s201, four * s110 * s111)) + two * lfma(s101, s120, s011 * s210)) * ri;
+    const L n4sum = lfma(s011, q[2][1][1], lfma(s101, q[1][2][1], s110 * q[1][1][2]));
+    const L n3sum = lfma(s120, s102, lfma(s210, s012, s201 * s021));
+    q[2][2][2] = (lfma(four * s111, s111, lfma(s200, q[0][2][2], lfma(s020, q[2][0][2], s002 * q[2][2][0]))) +
+                  lfma(four, n4sum, two * n3sum)) * ri -
+                 lfma((L)16.0f * s110, s101 * s011,
+                      lfma(four, lfma(s101 * s101, s020, lfma(s011 * s011, s200, s110 * s110 * s002)),
+                           two * s200 * s020 * s002)) * ri * ri;
+    // backward transform: x pass, y pass, z pass (G2015 eq. 88-96)
+    const Axis<L> ax = make_axis(ux, ux * ux), ay = make_axis(uy, uy * uy), az = make_axis(uz, uz * uz);
+#pragma unroll
+    for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            L m, z, p;
+            tri(q[0][b][c], q[1][b][c], q[2][b][c], ax, m, z, p);
+            q[0][b][c] = m; q[1][b][c] = z; q[2][b][c] = p;
+        }
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            L m, z, p;
+            tri(q[a][0][c], q[a][1][c], q[a][2][c], ay, m, z, p);
+            q[a][0][c] = m; q[a][1][c] = z; q[a][2][c] = p;
+        }
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            L m, z, p;
+            tri(q[a][b][0], q[a][b][1], q[a][b][2], az, m, z, p);
+            f[vid(a - 1, b - 1, -1)] = m;
+            f[vid(a - 1, b - 1, 0)] = z;
+            f[vid(a - 1, b - 1, 1)] = p;
+        }
+}
+
 }  // namespace lbm

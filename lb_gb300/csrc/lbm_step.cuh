@@ -31,6 +31,8 @@ LBM_D void collide_lane(L (&f)[27], const Mom<L>& mm, L ri, L ux, L uy, L uz, L 
     if constexpr (COLL == 0) {
         collide_srt(f, mm.rho, ux, uy, uz, om);
         if (force) srt_force(f, ux, uy, uz, om, Fx, Fy, Fz);
+    } else if constexpr (COLL == 2) {
+        collide_cum17(f, mm.rho, ri, ux, uy, uz, om);
     } else {
         collide_cum15(f, mm.rho, ri, ux, uy, uz, om, mm);
     }
@@ -78,8 +80,18 @@ LBM_D void step_cell(const Params& p, int x, int y, int z) {
         else pr[2 * p.n_in + id] = ux;
     }
     if (p.acc) acc_add(p, idx, rho, ux, uy, uz);
-    collide_lane<COLL, CLOS>(f, mm, ri, ux, uy, uz, p_tau<R>(p), p_cles18<R>(p), p_om0<R>(p), p.has_force != 0,
-                             p_F<R>(p, 0), p_F<R>(p, 1), p_F<R>(p, 2));
+    if constexpr (COLL == 3) {
+        // CollisionCumD3Q27TurbulentCombined.h:1066-1078: reference flag 1 -> 2015, other flags -> 2017
+        if (fl & BIT_REFBULK)
+            collide_lane<1, CLOS>(f, mm, ri, ux, uy, uz, p_tau<R>(p), p_cles18<R>(p), p_om0<R>(p), false, (R)0, (R)0,
+                                  (R)0);
+        else
+            collide_lane<2, CLOS>(f, mm, ri, ux, uy, uz, p_tau<R>(p), p_cles18<R>(p), p_om0<R>(p), false, (R)0, (R)0,
+                                  (R)0);
+    } else {
+        collide_lane<COLL, CLOS>(f, mm, ri, ux, uy, uz, p_tau<R>(p), p_cles18<R>(p), p_om0<R>(p), p.has_force != 0,
+                                 p_F<R>(p, 0), p_F<R>(p, 1), p_F<R>(p, 2));
+    }
     if (fl & BIT_OUTUP) {
         const int id = p.aux[idx];
         const int s = p.out_dir[id];
@@ -134,7 +146,8 @@ __device__ __noinline__ void step_cell_call(const Params& p, int x, int y, int z
     step_cell<S, COLL, CLOS, ODD>(p, x, y, z);
 }
 
-// COLL: 0 SRT, 1 cumulant-2015.  CLOS: 0 none, 1 Smagorinsky.
+// COLL: 0 SRT, 1 cumulant-2015, 2 cumulant-2017, 3 combined (2015 on reference flag 1, else 2017).
+// CLOS: 0 none, 1 Smagorinsky.
 template <class S, int COLL, int CLOS, bool ODD>
 __global__ void __launch_bounds__(128) k_step(Params p) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -308,9 +321,13 @@ LBM_D void step_pair(const Params& p, int x0, int y, int z) {
     static_assert(S::kind != 0, "packed pairs are FP32 arithmetic");
     const bool two = x0 + 1 < p.nx;
     const unsigned idx0 = (unsigned)x0 + (unsigned)p.nx * ((unsigned)y + (unsigned)p.ny * (unsigned)z);
-    const uint8_t f0 = p.cls[idx0] & (uint8_t)~BIT_REFBULK;
-    const uint8_t f1 = two ? (p.cls[idx0 + 1] & (uint8_t)~BIT_REFBULK) : (uint8_t)0;
-    const bool pair = two && f0 == CLS_BULK && f1 == CLS_BULK && (p.nx & 1) == 0;
+    // the combined collision packs only pairs of reference-flag-1 cells (both take the 2015 branch)
+    constexpr uint8_t keep = COLL == 3 ? (uint8_t)0xff : (uint8_t)~BIT_REFBULK;
+    constexpr uint8_t want = COLL == 3 ? (uint8_t)(CLS_BULK | BIT_REFBULK) : (uint8_t)CLS_BULK;
+    constexpr int PC = COLL == 3 ? 1 : COLL;
+    const uint8_t f0 = p.cls[idx0] & keep;
+    const uint8_t f1 = two ? (p.cls[idx0 + 1] & keep) : (uint8_t)0;
+    const bool pair = two && f0 == want && f1 == want && (p.nx & 1) == 0;
     if (!pair) {
         step_cell_call<S, COLL, CLOS, ODD>(p, x0, y, z);
         if (two) step_cell_call<S, COLL, CLOS, ODD>(p, x0 + 1, y, z);
@@ -334,25 +351,45 @@ LBM_D void step_pair(const Params& p, int x0, int y, int z) {
         q.eL = (p.wrap[0] && x0 == 0) ? q.e0 + p.nx : q.e0;
         q.eR = (p.wrap[0] && x0 + 2 == p.nx) ? q.e1 - p.nx : q.e1;
         load_pair<S, ODD>(p, q, k, f);
-        collide_pair<COLL, CLOS>(p, f, idx0);
+        collide_pair<PC, CLOS>(p, f, idx0);
         store_pair<S, ODD>(p, q, k, f);
     } else {
         PairRows w;
         make_pair_rows(p, x0, y, z, w);
         load_pair_rows<S, ODD>(p, w, k, f);
-        collide_pair<COLL, CLOS>(p, f, idx0);
+        collide_pair<PC, CLOS>(p, f, idx0);
         store_pair_rows<S, ODD>(p, w, k, f);
     }
 }
 
-// minimum resident CTAs per SM requested from the register allocator.  6 (at most 85 registers, a few
-// spilled to L1) measured fastest on a GB300 at 512x256x256: FP16 40.0 GLUPS against 36.7 with no
-// request (128 registers, 4 CTAs), FP32 30.9 against 30.2; 5, 7 and 8 were slower.
+// minimum resident CTAs per SM requested from the register allocator, per collision (0: no request),
+// measured on a GB300 on the 512x256x256 channel (GLUPS, FP16-deviation / FP32 storage):
+//   cumulant-2015: 6 (at most 85 registers, a few spilled to L1): 40.0 / 30.9, against 36.7 / 30.2 with
+//                  no request (128 registers); 5, 7 and 8 slower;
+//   SRT:           4 (128 registers): 31.8 / 26.7, against 22.9 / 21.9 with none (250 registers),
+//                  29.9 / 26.6 at 3, 23.2 / 18.9 at 5, 16.2 / 13.8 at 6 (1.8 KB spilled);
+//   cumulant-2017: 4: 29.5 / 28.3, against 26.9 / 24.8 with none (166 registers), 29.5 / 27.9 at 5,
+//                  26.8 / 23.6 at 6.
 #ifndef LBM_STEP2_MIN_BLOCKS
 #define LBM_STEP2_MIN_BLOCKS 6
 #endif
+#ifndef LBM_STEP2_MIN_BLOCKS_SRT
+#define LBM_STEP2_MIN_BLOCKS_SRT 4
+#endif
+#ifndef LBM_STEP2_MIN_BLOCKS_CUM17
+#define LBM_STEP2_MIN_BLOCKS_CUM17 4
+#endif
+#ifndef LBM_STEP2_MIN_BLOCKS_COMBINED
+#define LBM_STEP2_MIN_BLOCKS_COMBINED LBM_STEP2_MIN_BLOCKS
+#endif
+constexpr int step2_min_blocks(int coll) {
+    return coll == 1 ? LBM_STEP2_MIN_BLOCKS
+         : coll == 0 ? LBM_STEP2_MIN_BLOCKS_SRT
+         : coll == 2 ? LBM_STEP2_MIN_BLOCKS_CUM17
+                     : LBM_STEP2_MIN_BLOCKS_COMBINED;
+}
 template <class S, int COLL, int CLOS, bool ODD>
-__global__ void __launch_bounds__(128, LBM_STEP2_MIN_BLOCKS) k_step2(Params p) {
+__global__ void __launch_bounds__(128, step2_min_blocks(COLL)) k_step2(Params p) {
     const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     if (x0 >= p.nx) return;
     step_pair<S, COLL, CLOS, ODD>(p, x0, blockIdx.y, blockIdx.z);

@@ -20,12 +20,12 @@
 namespace lbm {
 
 // resident CTAs per SM requested from the register allocator: none for the steps that run the network
-// (6 and 7 measured no faster), as k_step2 (LBM_STEP2_MIN_BLOCKS) for the steps that reuse kept nu_t
+// (6 and 7 measured no faster), as k_step2 (step2_min_blocks) for the steps that reuse kept nu_t
 #ifndef LBM_MLP_MIN_BLOCKS
 #define LBM_MLP_MIN_BLOCKS 0
 #endif
 template <class S, int COLL, bool ODD, int MODE>
-__global__ void __launch_bounds__(128, MODE == 2 ? LBM_STEP2_MIN_BLOCKS : LBM_MLP_MIN_BLOCKS) k_step2_mlp(Params p) {
+__global__ void __launch_bounds__(128, MODE == 2 ? step2_min_blocks(COLL) : LBM_MLP_MIN_BLOCKS) k_step2_mlp(Params p) {
     static_assert(S::kind != 0, "the learned closure runs on the packed FP32 path");
     __shared__ uint4 wf[MODE == 2 ? 1 : kMlpFragRows][32];
     __shared__ uint4 stage[MODE == 2 ? 1 : 4][64];

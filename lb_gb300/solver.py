@@ -28,6 +28,14 @@ class CollisionCumD3Q27Turbulent2015:           # collisions/CollisionCumD3Q27Tu
     code = capi.LBM_COLLISION_CUMULANT2015
 
 
+class CollisionCumD3Q27Turbulent2017:           # collisions/CollisionCumD3Q27Turbulent2017.h
+    code = capi.LBM_COLLISION_CUMULANT2017
+
+
+class CollisionCumD3Q27TurbulentCombined:       # collisions/CollisionCumD3Q27TurbulentCombined.h
+    code = capi.LBM_COLLISION_CUMULANT_COMBINED
+
+
 class CollisionSRTTurbulent:                    # collisions/CollisionSRTTurbulent.h
     code = capi.LBM_COLLISION_SRT
 

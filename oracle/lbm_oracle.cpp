@@ -16,7 +16,9 @@
 //   * c_rev[20] = 21 instead of 19 (models/D3Q27/D3Q27.h:120-124);
 //   * wall nodes need > 2 on the wall-pass count, i.e. >= 2 solid neighbours
 //     (geometry/geometryMesherBoundary.h:459), so single-corner-contact cells are skipped;
-//   * ErrorQuadratic's z term uses uStat.y - uErr.z (errorEvaluations/ErrorQuadratic.h:43-44).
+//   * ErrorQuadratic's z term uses uStat.y - uErr.z (errorEvaluations/ErrorQuadratic.h:43-44);
+//   * cumulant-2017: the third-order limiter arguments, the bulk reference and eq. 44's gradient
+//     term (solvers/collisions/CollisionCumD3Q27Turbulent2017.h:256-266, :295, :351).
 //
 // Extensions with no reference counterpart (off unless requested): body force (Guo term for
 // SRT, velocity shift for the cumulant, where G2015 eq. 85-87 carry it), native index-wrap
@@ -231,7 +233,13 @@ struct Sim {
         m = (k0 * (uu * uu - uu) + k1 * ((R)2 * uu - (R)1) + k2) * (R)0.5;
         p = (k0 * (uu * uu + uu) + k1 * ((R)2 * uu + (R)1) + k2) * (R)0.5;
     }
-    void cumulant_cell(size_t c) {
+    // G17 = false: CollisionCumD3Q27Turbulent2015 (all rates but omega_1 equal to 1);
+    // G17 = true: CollisionCumD3Q27Turbulent2017.h:241-376 (limited third-order rates, fourth-order
+    // cumulants driven by the velocity gradients).  With ref_compat the 2017 operator keeps two
+    // reference defects: omega210p012 / omega210m012 are limited by C120 +- C102 instead of
+    // C210 +- C012 (:256-266), the bulk part of Dxu subtracts (-1 + rho) instead of k000 (:295), and
+    // eq. 44's gradient term is not the axis image of eq. 43's (:351).
+    void cumulant_cell(size_t c, bool G17 = false, bool combined = false) {
         R f[3][3][3];
         for (int v = 0; v < 27; v++) f[C[v][0] + 1][C[v][1] + 1][C[v][2] + 1] = df[v * N + c];
         const R ux = u[0][c], uy = u[1][c], uz = u[2][c], r = rho[c], omg = omega[c];
@@ -274,11 +282,41 @@ struct Sim {
                    (R)2 * K(2,0,0) * K(0,2,0) * K(0,0,2)) / r / r;
         const R k000 = K(0,0,0), k100 = K(1,0,0), k010 = K(0,1,0), k001 = K(0,0,1);
 #undef K
-        // relaxation, G2015 eq. 55-73 (reference :240-316): omega1 = local, all others 1
-        const R o1 = omg, o2 = 1, o3 = 1, o4 = 1, o5 = 1, o6 = 1, o7 = 1, o8 = 1, o9 = 1, o10 = 1;
-        const R Dxu = -o1 * (R)0.5 / r * ((R)2 * C200 - C020 - C002) - o2 * (R)0.5 / r * (C200 + C020 + C002 - k000);
+        // relaxation, G2015 eq. 55-73 (reference 2015 :240-316; 2017 :241-376)
+        const R o1 = omg, o2 = 1, o6 = 1, o7 = 1, o8 = 1, o9 = 1, o10 = 1;
+        R w120p102 = 1, w210p012 = 1, w201p021 = 1, w120m102 = 1, w210m012 = 1, w201m021 = 1, w111 = 1;
+        R A4 = 0, B4 = 0;
+        if (G17) {
+            // G2017 eq. 14-16 and the limiter of its section 7 (lambda = 0.01)
+            const R w3 = (R)8 * (o1 - (R)2) * (o2 * ((R)3 * o1 - (R)1) - (R)5 * o1) /
+                         ((R)8 * ((R)5 - (R)2 * o1) * o1 + o2 * ((R)8 + o1 * ((R)9 * o1 - (R)26)));
+            const R w4 = (R)8 * (o1 - (R)2) * (o1 + o2 * ((R)3 * o1 - (R)7)) /
+                         (o2 * ((R)56 - (R)42 * o1 + (R)8 * o1 * o1) - (R)8 * o1);
+            const R w5 = (R)24 * (o1 - (R)2) *
+                         ((R)4 * o1 * o1 + o1 * o2 * ((R)18 - (R)13 * o1) + o2 * o2 * ((R)2 + o1 * ((R)6 * o1 - (R)11))) /
+                         ((R)16 * o1 * o1 * (o1 - (R)6) - (R)2 * o1 * o2 * ((R)216 + (R)5 * o1 * ((R)9 * o1 - (R)46)) +
+                          o2 * o2 * (o1 * ((R)3 * o1 - (R)10) * ((R)15 * o1 - (R)28) - (R)48));
+            const R lam = (R)0.01;
+            auto lim = [&](R w, R cc) { const R a = std::fabs(cc); return w + ((R)1 - w) * a / (r * lam + a); };
+            w120p102 = lim(w3, C120 + C102);
+            w210p012 = lim(w3, ref_compat ? C120 + C102 : C210 + C012);
+            w201p021 = lim(w3, C201 + C021);
+            w120m102 = lim(w4, C120 - C102);
+            w210m012 = lim(w4, ref_compat ? C120 - C102 : C210 - C012);
+            w201m021 = lim(w4, C201 - C021);
+            w111 = lim(w5, C111);
+            const R den = (o1 - o2) * (o2 * ((R)2 + (R)3 * o1) - (R)8 * o1);
+            A4 = ((R)4 * o1 * o1 + (R)2 * o1 * o2 * (o1 - (R)6) + o2 * o2 * (o1 * ((R)10 - (R)3 * o1) - (R)4)) / den;
+            B4 = ((R)4 * o1 * o2 * ((R)9 * o1 - (R)16) - (R)4 * o1 * o1 - (R)2 * o2 * o2 * ((R)2 + (R)9 * o1 * (o1 - (R)2))) /
+                 ((R)3 * den);
+        }
+        // the 2017 header writes - (-1 + rho) (:295), the combined header's 2017 copy - -(-1 - rho)
+        // (CollisionCumD3Q27TurbulentCombined.h:295)
+        const R bulk0 = (G17 && ref_compat) ? (combined ? r + (R)1 : r - (R)1) : k000;
+        const R Dxu = -o1 * (R)0.5 / r * ((R)2 * C200 - C020 - C002) - o2 * (R)0.5 / r * (C200 + C020 + C002 - bulk0);
         const R Dyv = Dxu + (R)3 * o1 * (R)0.5 / r * (C200 - C020);
         const R Dzw = Dxu + (R)3 * o1 * (R)0.5 / r * (C200 - C002);
+        const R DxvDyu = -(R)3 * o1 / r * C110, DxwDzu = -(R)3 * o1 / r * C101, DywDzv = -(R)3 * o1 / r * C011;
         const R S110 = ((R)1 - o1) * C110, S101 = ((R)1 - o1) * C101, S011 = ((R)1 - o1) * C011;
         const R E61 = ((R)1 - o1) * (C200 - C020) - (R)3 * r * ((R)1 - o1 * (R)0.5) * (ux * ux * Dxu - uy * uy * Dyv);
         const R E64 = ((R)1 - o1) * (C200 - C002) - (R)3 * r * ((R)1 - o1 * (R)0.5) * (ux * ux * Dxu - uz * uz * Dzw);
@@ -287,20 +325,30 @@ struct Sim {
         const R S200 = (R)1 / (R)3 * (E61 + E64 + E65);
         const R S020 = (R)1 / (R)3 * (E64 - (R)2 * E61 + E65);
         const R S002 = (R)1 / (R)3 * (E61 - (R)2 * E64 + E65);
-        const R S120 = (-C102 - C120) * o3 * (R)0.5 + (C102 - C120) * o4 * (R)0.5 + C120;
-        const R S102 = (-C102 - C120) * o3 * (R)0.5 + (-C102 + C120) * o4 * (R)0.5 + C102;
-        const R S210 = (-C012 - C210) * o3 * (R)0.5 + (C012 - C210) * o4 * (R)0.5 + C210;
-        const R S012 = (-C012 - C210) * o3 * (R)0.5 + (-C012 + C210) * o4 * (R)0.5 + C012;
-        const R S021 = (-C021 - C201) * o3 * (R)0.5 + (-C021 + C201) * o4 * (R)0.5 + C021;
-        const R S201 = (-C021 - C201) * o3 * (R)0.5 + (C021 - C201) * o4 * (R)0.5 + C201;
-        const R S111 = ((R)1 - o5) * C111;
-        const R E71 = ((R)1 - o6) * (C220 - (R)2 * C202 + C022);
-        const R E72 = ((R)1 - o6) * (C220 + C202 - (R)2 * C022);
-        const R E73 = ((R)1 - o7) * (C220 + C202 + C022);
-        const R S220 = (R)1 / (R)3 * (E71 + E72 + E73);
-        const R S202 = (R)1 / (R)3 * (-E71 + E73);
-        const R S022 = (R)1 / (R)3 * (-E72 + E73);
-        const R S211 = ((R)1 - o8) * C211, S121 = ((R)1 - o8) * C121, S112 = ((R)1 - o8) * C112;
+        // third order: sums and differences relax with their own rates (G2015 eq. 61-66, G2017 eq. 37-42)
+        const R P1 = ((R)1 - w120p102) * (C120 + C102), P2 = ((R)1 - w210p012) * (C210 + C012),
+                P3 = ((R)1 - w201p021) * (C201 + C021);
+        const R M1 = ((R)1 - w120m102) * (C120 - C102), M2 = ((R)1 - w210m012) * (C210 - C012),
+                M3 = ((R)1 - w201m021) * (C201 - C021);
+        const R S120 = (R)0.5 * (P1 + M1), S102 = (R)0.5 * (P1 - M1);
+        const R S210 = (R)0.5 * (P2 + M2), S012 = (R)0.5 * (P2 - M2);
+        const R S201 = (R)0.5 * (P3 + M3), S021 = (R)0.5 * (P3 - M3);
+        const R S111 = ((R)1 - w111) * C111;
+        // fourth order (G2017 eq. 43-48; A = B = 0 in the 2015 operator)
+        const R vis = (R)1 / o1 - (R)0.5;
+        const R E43 = (R)2 / (R)3 * vis * o6 * A4 * r * (Dxu - (R)2 * Dyv + Dzw) + ((R)1 - o6) * (C220 - (R)2 * C202 + C022);
+        // C220 + C202 - 2 C022 follows 2 Dxu - Dyv - Dzw under an axis relabelling (each C_abc
+        // with two 2-indices tracks the gradients of those two axes), so the isotropic driving
+        // term is Dyv + Dzw - 2 Dxu; the reference writes Dxu + Dyv - 2 Dzw (:351).
+        const R D44 = ref_compat ? Dxu + Dyv - (R)2 * Dzw : Dyv + Dzw - (R)2 * Dxu;
+        const R E44 = (R)2 / (R)3 * vis * o6 * A4 * r * D44 + ((R)1 - o6) * (C220 + C202 - (R)2 * C022);
+        const R E45 = -(R)4 / (R)3 * vis * o7 * A4 * r * (Dxu + Dyv + Dzw) + ((R)1 - o7) * (C220 + C202 + C022);
+        const R S220 = (R)1 / (R)3 * (E43 + E44 + E45);
+        const R S202 = (R)1 / (R)3 * (-E43 + E45);
+        const R S022 = (R)1 / (R)3 * (-E44 + E45);
+        const R S211 = -(R)1 / (R)3 * vis * o8 * B4 * r * DywDzv + ((R)1 - o8) * C211;
+        const R S121 = -(R)1 / (R)3 * vis * o8 * B4 * r * DxwDzu + ((R)1 - o8) * C121;
+        const R S112 = -(R)1 / (R)3 * vis * o8 * B4 * r * DxvDyu + ((R)1 - o8) * C112;
         const R S221 = ((R)1 - o9) * C221, S212 = ((R)1 - o9) * C212, S122 = ((R)1 - o9) * C122;
         const R S222 = ((R)1 - o10) * C222;
         // cumulants -> central moments, G2015 eq. 81-87 (reference :322-380)
@@ -351,6 +399,23 @@ struct Sim {
 #pragma omp parallel for schedule(static)
         for (long long c = 0; c < (long long)N; c++)
             if (mesh[c] != 0) cumulant_cell((size_t)c);
+    }
+    void collision_cum2017() {
+#pragma omp parallel for schedule(static)
+        for (long long c = 0; c < (long long)N; c++)
+            if (mesh[c] != 0) cumulant_cell((size_t)c, true);
+    }
+    // CollisionCumD3Q27TurbulentCombined.h:1066-1084: flag 1 -> the 2015 operator, other flags -> 2017
+    void collision_combined() {
+#pragma omp parallel for schedule(static)
+        for (long long c = 0; c < (long long)N; c++)
+            if (mesh[c] != 0) cumulant_cell((size_t)c, mesh[c] != 1, true);
+    }
+    void collide_all() {
+        if (collision == LBM_COLLISION_SRT) collision_srt();
+        else if (collision == LBM_COLLISION_CUMULANT2017) collision_cum2017();
+        else if (collision == LBM_COLLISION_CUMULANT_COMBINED) collision_combined();
+        else collision_cum2015();
     }
 
     // ---- StreamingAB.h:38-68 (+ index wrap) ------------------------------------------------
@@ -526,7 +591,7 @@ struct Sim {
     // ---- SolverTurbulentLES::runSimulation loop body, SolverTurbulentLES.h:186-226 --------
     void step() {
         if (closure == LBM_CLOSURE_SMAGORINSKY) omega_les(); else omega_no();
-        if (collision == LBM_COLLISION_SRT) collision_srt(); else collision_cum2015();
+        collide_all();
         streaming_ab();
         bounce_back_wall();
         if (!inlets.empty()) { if (inlet_kind == LBM_INLET_MOVING_WALL) inlet_moving_wall(); else inlet_equilibrium(); }
@@ -785,23 +850,24 @@ int orc_wall_list_size(void* p) {
     return n;
 }
 void orc_mesher_wall_pass(int32_t* flags, int nx, int ny, int nz) { wall_pass(flags, nx, ny, nz); }
-// one cumulant collision of a single cell, for known-answer tests: f_in/f_out 27 doubles
+// one cumulant collision of a single cell of the given reference flag, for known-answer tests:
+// f_in/f_out 27 doubles
 void orc_collide_cell(int precision, int collision, const double* f_in, double rho, const double* u,
-                      double omega, const double* force, double* f_out) {
+                      double omega, const double* force, double* f_out, int ref_compat, int flag) {
     lbm_config cfg;
     std::memset(&cfg, 0, sizeof(cfg));
     cfg.nx = cfg.ny = cfg.nz = 1; cfg.nu = 1.0 / 6.0; cfg.collision = collision;
     for (int a = 0; a < 3; a++) cfg.force[a] = force ? force[a] : 0.0;
     auto run = [&](auto* S) {
-        S->mesh[0] = 1;
+        S->mesh[0] = flag;
         for (int v = 0; v < 27; v++) S->df[v] = f_in[v];
         S->rho[0] = rho; for (int a = 0; a < 3; a++) S->u[a][0] = u[a];
         S->omega[0] = omega;
-        if (collision == LBM_COLLISION_SRT) S->collision_srt(); else S->collision_cum2015();
+        S->collide_all();
         for (int v = 0; v < 27; v++) f_out[v] = S->dfp[v];
     };
-    if (precision == 32) { Sim<float> S(cfg, 0); run(&S); }
-    else { Sim<double> S(cfg, 0); run(&S); }
+    if (precision == 32) { Sim<float> S(cfg, ref_compat); run(&S); }
+    else { Sim<double> S(cfg, ref_compat); run(&S); }
 }
 
 }  // extern "C"

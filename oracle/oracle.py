@@ -45,7 +45,7 @@ def lib():
         L.orc_wall_list_size.argtypes = [vp]
         L.orc_wall_list_size.restype = i32
         L.orc_mesher_wall_pass.argtypes = [ip, i32, i32, i32]
-        L.orc_collide_cell.argtypes = [i32, i32, dp, f64, dp, f64, dp, dp]
+        L.orc_collide_cell.argtypes = [i32, i32, dp, f64, dp, f64, dp, dp, i32, i32]
         L.orc_voxelize_off.argtypes = [C.c_char_p, f64, f64, dp, ip, ip, dp]
         L.orc_voxelize_mesh.argtypes = [dp, i32, ip, i32, f64, f64, dp, ip, ip, dp]
         _lib = L
@@ -172,12 +172,15 @@ def wall_pass(flags):
     return f
 
 
-def collide_cell(f_in, rho, u, omega, collision, precision=64, force=(0.0, 0.0, 0.0)):
+def collide_cell(f_in, rho, u, omega, collision, precision=64, force=(0.0, 0.0, 0.0), ref_compat=False, flag=1):
+    """One collision of a single cell whose reference flag is `flag` (the combined collision picks its
+    operator by flag: 1 -> cumulant-2015, other -> cumulant-2017)."""
     fi = np.ascontiguousarray(f_in, dtype=np.float64)
     uu = np.ascontiguousarray(u, dtype=np.float64)
     ff = np.ascontiguousarray(force, dtype=np.float64)
     out = np.empty(27)
-    lib().orc_collide_cell(precision, collision, _d(fi), float(rho), _d(uu), float(omega), _d(ff), _d(out))
+    lib().orc_collide_cell(precision, collision, _d(fi), float(rho), _d(uu), float(omega), _d(ff), _d(out),
+                           int(ref_compat), int(flag))
     return out
 
 

@@ -48,6 +48,11 @@ def test_create_rejects_bad_config_before_touching_the_gpu(built_lib):
     assert L.lbm_create(C.byref(cfg), C.byref(ctx)) == capi.LBM_ERR_UNSUPPORTED
     cfg = capi.make_config(8, 70000, 8)  # beyond the launch grid's y extent
     assert L.lbm_create(C.byref(cfg), C.byref(ctx)) == capi.LBM_ERR_UNSUPPORTED
+    cfg = capi.make_config(8, 8, 8, collision=5)
+    assert L.lbm_create(C.byref(cfg), C.byref(ctx)) == capi.LBM_ERR_UNSUPPORTED
+    cfg = capi.make_config(8, 8, 8, collision=capi.LBM_COLLISION_CUMULANT2017, closure=capi.LBM_CLOSURE_MLP,
+                           storage=capi.LBM_STORAGE_F32)  # the learned closure: SRT or cumulant-2015
+    assert L.lbm_create(C.byref(cfg), C.byref(ctx)) == capi.LBM_ERR_UNSUPPORTED
 
 
 def test_mesher_wall_pass_host_only(built_lib):

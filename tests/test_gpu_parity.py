@@ -11,13 +11,15 @@ import numpy as np
 import pytest
 
 from lb_gb300 import capi, cases
-from lb_gb300.solver import (CollisionCumD3Q27Turbulent2015, CollisionSRTTurbulent, InletVelocityEquilibrium,
+from lb_gb300.solver import (CollisionCumD3Q27Turbulent2015, CollisionCumD3Q27Turbulent2017,
+                             CollisionCumD3Q27TurbulentCombined, CollisionSRTTurbulent, InletVelocityEquilibrium,
                              InletVelocityMovingWall, OmegaLES, OmegaNo, Solver)
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-COLL = {"cum": CollisionCumD3Q27Turbulent2015, "srt": CollisionSRTTurbulent}
+COLL = {"cum": CollisionCumD3Q27Turbulent2015, "cum17": CollisionCumD3Q27Turbulent2017,
+        "comb": CollisionCumD3Q27TurbulentCombined, "srt": CollisionSRTTurbulent}
 CLOS = {"smag": OmegaLES, "none": OmegaNo}
 
 
@@ -56,7 +58,8 @@ def compare(g, o, uscale, tol_rho, tol_u, mask=None):
     return dr, du
 
 
-@pytest.mark.parametrize("coll,clos", [("cum", "smag"), ("cum", "none"), ("srt", "smag"), ("srt", "none")])
+@pytest.mark.parametrize("coll,clos", [("cum", "smag"), ("cum", "none"), ("cum17", "smag"), ("cum17", "none"),
+                                       ("comb", "smag"), ("srt", "smag"), ("srt", "none")])
 def test_cavity_fp64_matches_oracle(built_lib, oracle_lib, coll, clos):
     n = 20
     c = cases.cavity(n, u_lid=0.05, re=400.0)
@@ -68,7 +71,8 @@ def test_cavity_fp64_matches_oracle(built_lib, oracle_lib, coll, clos):
         compare(g, o, 0.05, 1e-12, 1e-12)
 
 
-@pytest.mark.parametrize("coll,re", [("cum", 1000.0), ("srt", 400.0), ("srt", 1000.0)])
+@pytest.mark.parametrize("coll,re", [("cum", 1000.0), ("cum17", 1000.0), ("comb", 1000.0), ("srt", 400.0),
+                                     ("srt", 1000.0)])
 def test_cavity_fp32_matches_oracle_fp32(built_lib, oracle_lib, coll, re):
     """FP32 parity after 100 steps at tau = 0.5036 / 0.509.  The FP32 oracle itself drifts
     0.9-1.4e-5 (of u_lid) from the FP64 oracle here (rounding noise that over-relaxation at
@@ -99,10 +103,11 @@ def fp32_parity(g, o, o64, uscale, steps):
     assert e_gpu <= 1.5 * e_orc + 1e-6, (e_gpu, e_orc)
 
 
-def test_channel_periodic_force_fp64(built_lib, oracle_lib):
+@pytest.mark.parametrize("coll", ["cum", "cum17", "comb"])
+def test_channel_periodic_force_fp64(built_lib, oracle_lib, coll):
     nx, ny, nz = 24, 14, 12
     c = cases.channel(nx, ny, nz, re_tau=3.0, u_max=0.05, nu=0.01)  # u_tau = 0.005, F = 4e-6
-    g, o = pair((nx, ny, nz), c, "cum", "smag", "f64", 64, force=c["force"])
+    g, o = pair((nx, ny, nz), c, coll, "smag", "f64", 64, force=c["force"])
     init_both(g, o, c)
     for _ in range(3):
         g.step(33)
@@ -111,13 +116,14 @@ def test_channel_periodic_force_fp64(built_lib, oracle_lib):
 
 
 @pytest.mark.parametrize("storage", ["f32", "f16dev"])
-def test_channel_packed_pairs(built_lib, oracle_lib, storage):
+@pytest.mark.parametrize("coll", ["cum", "cum17", "comb"])
+def test_channel_packed_pairs(built_lib, oracle_lib, storage, coll):
     """Periodic channel with force on an even-width lattice: interior cells run the packed
     two-cell path, the seams and wall rows the per-cell path."""
     nx, ny, nz = 32, 14, 12
     c = cases.channel(nx, ny, nz, re_tau=3.0, u_max=0.05, nu=0.01)
-    g, o = pair((nx, ny, nz), c, "cum", "smag", storage, 32, force=c["force"])
-    _, o64 = pair((nx, ny, nz), c, "cum", "smag", "f64", 64, force=c["force"])
+    g, o = pair((nx, ny, nz), c, coll, "smag", storage, 32, force=c["force"])
+    _, o64 = pair((nx, ny, nz), c, coll, "smag", "f64", 64, force=c["force"])
     init_both(g, o, c)
     o64.init_fields(c["rho"], c["u"])
     if storage == "f32":

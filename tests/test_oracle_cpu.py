@@ -53,7 +53,8 @@ def feq(r, u):
     return W * r * (1 + 3 * cu + 4.5 * cu * cu - 1.5 * u @ u)
 
 
-@pytest.mark.parametrize("coll", [capi.LBM_COLLISION_SRT, capi.LBM_COLLISION_CUMULANT2015])
+@pytest.mark.parametrize("coll", [capi.LBM_COLLISION_SRT, capi.LBM_COLLISION_CUMULANT2015,
+                                  capi.LBM_COLLISION_CUMULANT2017, capi.LBM_COLLISION_CUMULANT_COMBINED])
 def test_collision_conserves_mass_and_momentum(oracle_lib, coll):
     rng = np.random.default_rng(1)
     for _ in range(5):
@@ -61,7 +62,7 @@ def test_collision_conserves_mass_and_momentum(oracle_lib, coll):
         f = feq(1 + rng.uniform(-0.02, 0.02), u) * (1 + 0.02 * rng.standard_normal(27))
         r = f.sum()
         uu = CV.T @ f / r
-        out = O.collide_cell(f, r, uu, rng.uniform(0.6, 1.9), coll)
+        out = O.collide_cell(f, r, uu, rng.uniform(0.6, 1.9), coll, flag=3)  # combined: its 2017 branch
         assert abs(out.sum() - f.sum()) < 1e-14
         assert np.abs(CV.T @ out - CV.T @ f).max() < 1e-14
 
@@ -162,3 +163,76 @@ def test_cavity_mass_conserved_and_lid_drives_flow(oracle_lib):
     assert d.nonfinite == 0
     assert ux[6, 10, 6] > 0.005          # flow under the lid moves with it
     assert abs(d.mass - m0) / m0 < 1e-3  # moving-wall nodes exchange little mass
+
+
+def feq_factorised(r, u):
+    """The product-form D3Q27 equilibrium: every cumulant above second order is zero."""
+    def phi(c, a):
+        return np.where(c == 0, 2.0 / 3.0 - a * a, 0.5 * (1.0 / 3.0 + a * a + c * a))
+    return r * phi(CV[:, 0], u[0]) * phi(CV[:, 1], u[1]) * phi(CV[:, 2], u[2])
+
+
+@pytest.mark.parametrize("coll", [capi.LBM_COLLISION_CUMULANT2015, capi.LBM_COLLISION_CUMULANT2017])
+def test_cumulant_equilibrium_is_fixed_point(oracle_lib, coll):
+    """CollisionCumD3Q27Turbulent2015/2017: the cumulant equilibrium of a moving fluid is left unchanged.
+    The 2017 reference's bulk term (-(rho - 1) in Dxu, CollisionCumD3Q27Turbulent2017.h:295) breaks this:
+    it reads a velocity gradient of -1/(2 rho) into a fluid at rest in its own frame."""
+    u = np.array([0.04, -0.03, 0.02])
+    f = feq_factorised(1.02, u)
+    out = O.collide_cell(f, f.sum(), CV.T @ f / f.sum(), 1.7, coll)
+    assert np.abs(out - f).max() < 1e-15
+    if coll == capi.LBM_COLLISION_CUMULANT2017:
+        ref = O.collide_cell(f, f.sum(), CV.T @ f / f.sum(), 1.7, coll, ref_compat=True)
+        assert np.abs(ref - f).max() > 1e-5
+
+
+def _permute_axes(f, perm):
+    """Populations of the same state with axes relabelled: new axis a is old axis perm[a]."""
+    idx = {tuple(c): v for v, c in enumerate(CV)}
+    g = np.empty(27)
+    for v, c in enumerate(CV):
+        g[idx[tuple(c[list(perm)])]] = f[v]
+    return g
+
+
+def test_cumulant2017_commutes_with_axis_relabelling(oracle_lib):
+    """The corrected 2017 operator is isotropic: relabelling x, y, z before or after the collision gives
+    the same populations, for a rotation and for the three transpositions.  Two reference lines break
+    this and ref_compat reproduces them: the limiters of the 210/012 pair read C120 +- C102
+    (CollisionCumD3Q27Turbulent2017.h:256-266), and eq. 44 pairs C220 + C202 - 2 C022 with
+    Dxu + Dyv - 2 Dzw (:351), whose axis image is Dyv + Dzw - 2 Dxu."""
+    rng = np.random.default_rng(5)
+    u = np.array([0.03, -0.01, 0.02])
+    f = feq(1.0, u) * (1 + 0.05 * rng.standard_normal(27))
+    r = f.sum()
+    uu = CV.T @ f / r
+    for perm in ((1, 2, 0), (1, 0, 2), (0, 2, 1), (2, 1, 0)):
+        fp = _permute_axes(f, perm)
+        up = uu[list(perm)]
+        for ref, expect_equal in ((False, True), (True, False)):
+            a = _permute_axes(O.collide_cell(f, r, uu, 1.8, capi.LBM_COLLISION_CUMULANT2017, ref_compat=ref), perm)
+            b = O.collide_cell(fp, r, up, 1.8, capi.LBM_COLLISION_CUMULANT2017, ref_compat=ref)
+            assert (np.abs(a - b).max() < 1e-15) == expect_equal, (perm, ref, np.abs(a - b).max())
+
+
+def test_combined_collision_picks_the_operator_by_flag(oracle_lib):
+    """CollisionCumD3Q27TurbulentCombined: cells of flag 1 take the 2015 operator, every other nonzero
+    flag (wall-pass counts, boundary nodes) the 2017 one (CollisionCumD3Q27TurbulentCombined.h:1066-1078).
+    Its 2017 copy differs from the 2017 header in one reference line only, the bulk term of Dxu
+    (:295, - -(-1 - rho) against - (-1 + rho)), so the two agree when corrected and differ with
+    ref_compat."""
+    rng = np.random.default_rng(9)
+    u = np.array([0.02, 0.03, -0.01])
+    f = feq(1.01, u) * (1 + 0.03 * rng.standard_normal(27))
+    r = f.sum()
+    uu = CV.T @ f / r
+    comb = capi.LBM_COLLISION_CUMULANT_COMBINED
+    c15 = O.collide_cell(f, r, uu, 1.9, capi.LBM_COLLISION_CUMULANT2015)
+    c17 = O.collide_cell(f, r, uu, 1.9, capi.LBM_COLLISION_CUMULANT2017)
+    assert np.abs(c15 - c17).max() > 1e-8
+    assert np.array_equal(O.collide_cell(f, r, uu, 1.9, comb, flag=1), c15)
+    for flag in (2, 7, -1, -2, -3):
+        assert np.array_equal(O.collide_cell(f, r, uu, 1.9, comb, flag=flag), c17)
+    ref17 = O.collide_cell(f, r, uu, 1.9, capi.LBM_COLLISION_CUMULANT2017, ref_compat=True)
+    refc = O.collide_cell(f, r, uu, 1.9, comb, ref_compat=True, flag=7)
+    assert np.abs(refc - ref17).max() > 1e-6
