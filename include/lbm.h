@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define LBM_ABI_VERSION 2
+#define LBM_ABI_VERSION 3
 
 typedef int32_t lbm_status;
 #define LBM_OK                 0
@@ -68,6 +68,25 @@ typedef int32_t lbm_status;
 /* what the reference's flag -1 nodes are (its INLETTYPE policy) */
 #define LBM_INLET_MOVING_WALL  0  /* Inlet/InletVelocityMovingWall.h:18-60 */
 #define LBM_INLET_EQUILIBRIUM  1  /* Inlet/InletVelocityEquilibrium.h:18-108 */
+#define LBM_INLET_ZOU_HE       2  /* Inlet/InletVelocityZouHe.h:18-104: the node is collided, never streamed
+                                     into, and for n.c_v > 0 sets df(opp v) = f*_v - f_eq_v(rho, u)
+                                     + f_eq_{opp v}(rho, u_b) (rho, u: the node's moments) */
+
+/* what the reference's flag -2 outlet nodes do (its OUTLETTYPE policy); outlet normals +-x */
+#define LBM_OUTLET_DENSITY_INTERPOLATED        0  /* Outlet/OutletDensityInterpolated.h:20-257 */
+#define LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM       1  /* Outlet/OutletNeighbourEquilibrium.h:20-127: for the 9
+                                                     links entering against the normal, f_v = f_eq_v(u, rho_b)
+                                                     + (f_eq_v - f_v)(x+c_v), u the node's velocity and
+                                                     f_v(x+c_v) the value the node streamed there */
+#define LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA 2  /* the same + the sponge of OutletNeighbourEquilibriumOmega.h:
+                                                     18-79: over the last ceil(10 %) of the lattice along the
+                                                     first outlet's normal axis, omega -= (high - low) / width
+                                                     * (distance from the sponge's start) */
+#define LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA_RF 3  /* the same + OutletNeighbourEquilibriumOmegaRF.h:151-155:
+                                                     rho_b *= 1 - u_x^2 / 2 where the node's u_x < 0 */
+#define LBM_OUTLET_DENSITY_EQUILIBRIUM         4  /* Outlet/OutletDensityEquilibrium.h:20-79: the 9 entering
+                                                     links set to f_eq(u, rho_b) of their own direction (the
+                                                     reference writes f_eq of the opposite, outgoing one, :66) */
 
 typedef struct lbm_config {
     int32_t nx, ny, nz;       /* lattice size: at most 2^31 - 2^21 cells, nx <= 2^21, ny, nz <= 65535 */
@@ -86,6 +105,9 @@ typedef struct lbm_config {
     int32_t options;          /* LBM_OPT_* bits (0: defaults) */
     int32_t mlp_interval;     /* learned closure: the network runs every k-th step (0, 1: every step);
                                  in between each cell relaxes with its last nu_t (kept in FP16) */
+    int32_t outlet_kind;      /* LBM_OUTLET_* */
+    double  omega_dumping_low;   /* sponge of LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA(_RF): omegaDumpingLow, */
+    double  omega_dumping_high;  /* omegaDumpingHigh (LBMConstants.h:74-76, set in main.cu:137-138) */
 } lbm_config;
 
 /* implementation options */
@@ -113,6 +135,13 @@ typedef struct lbm_bc_outlet {      /* boundaryConditionOutlet, LBMTraits.h:38-4
     float density;                  /* lattice units */
     int32_t regular;
 } lbm_bc_outlet;
+
+typedef struct lbm_bc_symmetry {    /* boundaryConditionSymmetry, LBMTraits.h:45-49 */
+    lbm_vertex vertex;
+    float normal[3];                /* outward normal, +-y only (the reference's x and z branches are
+                                       commented out, BounceSymmetryHalf.h:58-81, :135-157) */
+    int32_t regular;                /* 1: the node's wall-pass flag was 10 (a flat face) */
+} lbm_bc_symmetry;
 
 /* diagnostics of the current state, reduced in FP64 on the device */
 typedef struct lbm_diag {
@@ -142,6 +171,12 @@ lbm_status lbm_set_flags(lbm_ctx* ctx, const int32_t* flags);
 /* per-node records of the -1 and -2 nodes (compileBoundaryArrayInlets/Outlets). */
 lbm_status lbm_set_bc(lbm_ctx* ctx, const lbm_bc_inlet* inlets, int32_t n_inlets,
                       const lbm_bc_outlet* outlets, int32_t n_outlets);
+/* half-way specular reflection on -2 nodes listed here (Symmetry/BounceSymmetryHalf.h:18-178,
+ * compileBoundaryArraySymmetry, geometryMesherBoundary.h:563-580): for the links entering across the
+ * plane, f_v(x) = f*_{sym v}(x - c_v parallel), sym mirroring the normal component.  The cell across
+ * the plane must be solid; a link whose in-plane source is solid bounces back.  Call after lbm_set_bc
+ * (which clears the list). */
+lbm_status lbm_set_symmetry(lbm_ctx* ctx, const lbm_bc_symmetry* records, int32_t n);
 
 /* ---- initialisation (InitializationEquilibriumConstVector.h:103-224) ---------- */
 lbm_status lbm_init_equilibrium(lbm_ctx* ctx, double rho0, const double u0[3]);

@@ -34,12 +34,19 @@ struct OmegaNo { static constexpr int32_t code = LBM_CLOSURE_NONE; };           
 struct OmegaMLP { static constexpr int32_t code = LBM_CLOSURE_MLP; };             // learned closure (no reference policy)
 struct StreamingAB {};                     // streamings/StreamingAB.h (AA pattern in place here)
 struct BounceBackWallHalf {};              // boundaryConditions/Wall/BounceBackWallHalf.h
-struct NoSymmetry {};                      // boundaryConditions/Symmetry/NoSymmetry.h
+struct NoSymmetry { static constexpr bool on = false; };           // boundaryConditions/Symmetry/NoSymmetry.h
+struct BounceSymmetryHalf { static constexpr bool on = true; };    // boundaryConditions/Symmetry/BounceSymmetryHalf.h
 struct Periodic { static constexpr bool on = true; };    // boundaryConditions/Periodic/Periodic.h (index wrap)
 struct NoPeriodic { static constexpr bool on = false; };
 struct InletVelocityMovingWall { static constexpr int32_t code = LBM_INLET_MOVING_WALL; };
 struct InletVelocityEquilibrium { static constexpr int32_t code = LBM_INLET_EQUILIBRIUM; };
-struct OutletDensityInterpolated {};       // boundaryConditions/Outlet/OutletDensityInterpolated.h
+struct InletVelocityZouHe { static constexpr int32_t code = LBM_INLET_ZOU_HE; };  // Inlet/InletVelocityZouHe.h
+// boundaryConditions/Outlet/*.h
+struct OutletDensityInterpolated { static constexpr int32_t code = LBM_OUTLET_DENSITY_INTERPOLATED; };
+struct OutletNeighbourEquilibrium { static constexpr int32_t code = LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM; };
+struct OutletNeighbourEquilibriumOmega { static constexpr int32_t code = LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA; };
+struct OutletNeighbourEquilibriumOmegaRF { static constexpr int32_t code = LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA_RF; };
+struct OutletDensityEquilibrium { static constexpr int32_t code = LBM_OUTLET_DENSITY_EQUILIBRIUM; };
 struct MomentDensityVelocityN27 {};        // moments/MomentDensityVelocityN27.h
 struct MomentTimeAvg {};                   // moments/MomentTimeAvg.h
 struct ErrorQuadratic {};                  // errorEvaluations/ErrorQuadratic.h
@@ -68,12 +75,15 @@ struct LBMConstants {
     int32_t device = 0;
     int32_t mlp_interval = 1;
     const lbm_mlp_model* mlp = nullptr;
+    // outlet sponge of OutletNeighbourEquilibriumOmega(RF) (LBMConstants.h:74-76; -1: none)
+    double omegaDumpingLow = -1.0, omegaDumpingHigh = -1.0;
 };
 
 struct LBMData {
     std::vector<int32_t> meshFluid;            // reference flag encoding, x fastest
     std::vector<lbm_bc_inlet> meshBoundaryInlet;
     std::vector<lbm_bc_outlet> meshBoundaryOutlet;
+    std::vector<lbm_bc_symmetry> meshBoundarySymmetry;  // used with BounceSymmetryHalf
     std::vector<double> rhoInit, uInit;        // optional initial fields (else VelocityInit everywhere)
     std::vector<double> rho, u;                // host copies after the run (u: ux[N], uy[N], uz[N])
     std::vector<double> rhoTimeAvg, uTimeAvg, uuTimeAvg;
@@ -99,8 +109,15 @@ class SolverTurbulentLES {
     static_assert(MODELTYPE::numberOfDiscreteVelocities == 27, "the kernels are D3Q27");
     static_assert(std::is_same<STREAMINGTYPE, StreamingAB>::value, "streaming: StreamingAB (AA pattern in place)");
     static_assert(std::is_same<BOUNCEBACKWALLTYPE, BounceBackWallHalf>::value, "wall: BounceBackWallHalf");
-    static_assert(std::is_same<SYMMETRYTYPE, NoSymmetry>::value, "symmetry planes are not implemented");
-    static_assert(std::is_same<OUTLETTYPE, OutletDensityInterpolated>::value, "outlet: OutletDensityInterpolated");
+    static_assert(std::is_same<SYMMETRYTYPE, NoSymmetry>::value || std::is_same<SYMMETRYTYPE, BounceSymmetryHalf>::value,
+                  "symmetry: NoSymmetry or BounceSymmetryHalf");
+    static_assert(std::is_same<OUTLETTYPE, OutletDensityInterpolated>::value ||
+                      std::is_same<OUTLETTYPE, OutletNeighbourEquilibrium>::value ||
+                      std::is_same<OUTLETTYPE, OutletNeighbourEquilibriumOmega>::value ||
+                      std::is_same<OUTLETTYPE, OutletNeighbourEquilibriumOmegaRF>::value ||
+                      std::is_same<OUTLETTYPE, OutletDensityEquilibrium>::value,
+                  "outlet: OutletDensityInterpolated, OutletNeighbourEquilibrium(Omega, OmegaRF) or "
+                  "OutletDensityEquilibrium");
     static_assert(std::is_same<MOMENTTYPE, MomentDensityVelocityN27>::value, "moments: MomentDensityVelocityN27");
     static_assert(std::is_same<ERRORTYPE, ErrorQuadratic>::value, "error: ErrorQuadratic");
     static_assert(std::is_same<INITIALIZATIONTYPE, InitializationEquilibriumConstVector>::value,
@@ -138,6 +155,9 @@ public:
         c.f16_scale_log2 = 10;
         c.device = Constants.device;
         c.mlp_interval = Constants.mlp_interval;
+        c.outlet_kind = OUTLETTYPE::code;
+        c.omega_dumping_low = Constants.omegaDumpingLow;
+        c.omega_dumping_high = Constants.omegaDumpingHigh;
         if (ctx) lbm_destroy(ctx);
         ctx = nullptr;
         check(lbm_create(&c, &ctx), nullptr, "lbm_create");
@@ -147,6 +167,9 @@ public:
         check(lbm_set_bc(ctx, Data.meshBoundaryInlet.data(), (int32_t)Data.meshBoundaryInlet.size(),
                          Data.meshBoundaryOutlet.data(), (int32_t)Data.meshBoundaryOutlet.size()),
               ctx, "lbm_set_bc");
+        if (SYMMETRYTYPE::on)
+            check(lbm_set_symmetry(ctx, Data.meshBoundarySymmetry.data(), (int32_t)Data.meshBoundarySymmetry.size()),
+                  ctx, "lbm_set_symmetry");
         if (!Data.rhoInit.empty()) {
             if (Data.rhoInit.size() != N || Data.uInit.size() != 3 * N)
                 throw Error(LBM_ERR_INVALID, "rhoInit / uInit have the wrong size");

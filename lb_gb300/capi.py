@@ -31,6 +31,12 @@ LBM_STORAGE_F32 = 1
 LBM_STORAGE_F16DEV = 2
 LBM_INLET_MOVING_WALL = 0
 LBM_INLET_EQUILIBRIUM = 1
+LBM_INLET_ZOU_HE = 2
+LBM_OUTLET_DENSITY_INTERPOLATED = 0
+LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM = 1
+LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA = 2
+LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA_RF = 3
+LBM_OUTLET_DENSITY_EQUILIBRIUM = 4
 
 
 class LbmConfig(C.Structure):
@@ -46,6 +52,8 @@ class LbmConfig(C.Structure):
         ("device", C.c_int32),
         ("options", C.c_int32),
         ("mlp_interval", C.c_int32),
+        ("outlet_kind", C.c_int32),
+        ("omega_dumping_low", C.c_double), ("omega_dumping_high", C.c_double),
     ]
 
 
@@ -80,6 +88,10 @@ class LbmBcOutlet(C.Structure):
                 ("regular", C.c_int32)]
 
 
+class LbmBcSymmetry(C.Structure):
+    _fields_ = [("vertex", LbmVertex), ("normal", C.c_float * 3), ("regular", C.c_int32)]
+
+
 class LbmDiag(C.Structure):
     _fields_ = [("mass", C.c_double), ("momentum", C.c_double * 3), ("drag", C.c_double * 3),
                 ("max_speed", C.c_double), ("nonfinite", C.c_int64), ("fluid_cells", C.c_int64),
@@ -89,7 +101,8 @@ class LbmDiag(C.Structure):
 def make_config(nx, ny, nz, periodic=(0, 0, 0), collision=LBM_COLLISION_CUMULANT2015,
                 closure=LBM_CLOSURE_NONE, storage=LBM_STORAGE_F32, inlet_kind=LBM_INLET_MOVING_WALL,
                 nu=1.0 / 6.0, tau=0.0, cles=0.173, force=(0.0, 0.0, 0.0), rho0=1.0,
-                f16_scale_log2=10, device=0, options=0, mlp_interval=1):
+                f16_scale_log2=10, device=0, options=0, mlp_interval=1, outlet_kind=LBM_OUTLET_DENSITY_INTERPOLATED,
+                omega_dumping=(-1.0, -1.0)):
     c = LbmConfig()
     c.nx, c.ny, c.nz = int(nx), int(ny), int(nz)
     for a in range(3):
@@ -99,6 +112,8 @@ def make_config(nx, ny, nz, periodic=(0, 0, 0), collision=LBM_COLLISION_CUMULANT
     c.nu, c.tau, c.cles, c.rho0 = float(nu), float(tau), float(cles), float(rho0)
     c.f16_scale_log2, c.device, c.options = int(f16_scale_log2), int(device), int(options)
     c.mlp_interval = int(mlp_interval)
+    c.outlet_kind = int(outlet_kind)
+    c.omega_dumping_low, c.omega_dumping_high = float(omega_dumping[0]), float(omega_dumping[1])
     return c
 
 
@@ -118,6 +133,15 @@ def make_outlet(x, y, z, normal, density, regular=1):
     for a in range(3):
         r.normal[a] = float(normal[a])
     r.density = float(density)
+    r.regular = int(regular)
+    return r
+
+
+def make_symmetry(x, y, z, normal, regular=1):
+    r = LbmBcSymmetry()
+    r.vertex = LbmVertex(int(x), int(y), int(z))
+    for a in range(3):
+        r.normal[a] = float(normal[a])
     r.regular = int(regular)
     return r
 
@@ -151,6 +175,7 @@ def lib():
         "lbm_abi_version": ([], i32),
         "lbm_set_flags": ([vp, ip], i32),
         "lbm_set_bc": ([vp, C.POINTER(LbmBcInlet), i32, C.POINTER(LbmBcOutlet), i32], i32),
+        "lbm_set_symmetry": ([vp, C.POINTER(LbmBcSymmetry), i32], i32),
         "lbm_init_equilibrium": ([vp, f64, dp], i32),
         "lbm_init_fields": ([vp, dp, dp], i32),
         "lbm_step": ([vp, i32], i32),

@@ -177,6 +177,70 @@ def channel(nx, ny, nz, re_tau=180.0, u_max=0.05, amp=0.05, seed=SEED, nu=None, 
             "rho": rho, "u": u, "h": h, "u_tau": u_tau}
 
 
+def symmetric_channel(nx, h_rows, nz, u_max=0.05, amp=0.05, seed=SEED, nu=0.02, re_tau=3.0, wall=wall_pass_numpy):
+    """A periodic (x, z) channel cut at its mid-plane by a BounceSymmetryHalf plane, and the full channel
+    it stands for.  Half: solid row y=0, fluid rows 1..h_rows with the last one -2 symmetry nodes (normal
+    +y; regular when the wall pass gave them 10), solid row h_rows+1 across the plane.  Full: fluid rows
+    1..2 h_rows between solid rows 0 and 2 h_rows+1; its initial field is the half's mirrored about
+    y = h_rows + 1/2 (u_y changes sign), so the two runs agree on rows 0..h_rows.  Laminar profile plus
+    seeded noise, body force F_x = u_tau^2 / h for Re_tau = u_tau h / nu.  Returns (half, full)."""
+    H = int(h_rows)
+    h = float(H)
+    u_tau = re_tau * nu / h
+    force = (u_tau * u_tau / h, 0.0, 0.0)
+    fh = np.ones((nz, H + 2, nx), dtype=np.int32)
+    fh[:, 0, :] = 0
+    fh[:, H + 1, :] = 0
+    fh = wall(fh)
+    regular = fh[:, H, :] == 10
+    fh[:, H, :] = -2
+    sym = [capi.make_symmetry(i, H, k, (0, 1, 0), int(regular[k, i])) for k in range(nz) for i in range(nx)]
+    y = np.arange(H + 2, dtype=np.float64)
+    prof = u_max * (1.0 - ((y - (H + 0.5)) / h) ** 2)
+    prof[[0, -1]] = 0.0
+    Nh = nx * (H + 2) * nz
+    idx = np.arange(Nh, dtype=np.uint64)
+    uh = np.zeros((3, Nh))
+    for a in range(3):
+        uh[a] = (uniform(seed, idx, a) * 2.0 - 1.0) * amp * u_max
+    uh[0] += np.broadcast_to(prof[None, :, None], (nz, H + 2, nx)).reshape(-1)
+    uh[:, (fh.reshape(-1) == 0)] = 0.0
+    half = {"flags": fh, "inlets": [], "outlets": [], "symmetry": sym, "nu": nu, "periodic": (1, 0, 1),
+            "force": force, "rho": np.ones(Nh), "u": uh}
+    ff = np.ones((nz, 2 * H + 2, nx), dtype=np.int32)
+    ff[:, 0, :] = 0
+    ff[:, -1, :] = 0
+    ff = wall(ff)
+    u3 = uh.reshape(3, nz, H + 2, nx)
+    uf = np.zeros((3, nz, 2 * H + 2, nx))
+    uf[:, :, :H + 1, :] = u3[:, :, :H + 1, :]
+    mir = u3[:, :, H:0:-1, :].copy()        # rows H..1 -> rows H+1..2H
+    mir[1] *= -1.0
+    uf[:, :, H + 1:2 * H + 1, :] = mir
+    full = {"flags": ff, "inlets": [], "outlets": [], "nu": nu, "periodic": (1, 0, 1), "force": force,
+            "rho": np.ones(nx * (2 * H + 2) * nz), "u": uf.reshape(3, -1)}
+    return half, full
+
+
+def duct(nx, ny, nz, u_in=0.04, rho_out=1.0, nu=0.02, amp=0.3, seed=SEED):
+    """Inlet plane x=0 (-1 nodes, normal -x, u=(u_in,0,0)), outlet plane x=nx-1 (-2 nodes, normal +x,
+    rho_out), periodic y and z, no walls; initial field u_in plus seeded noise of amplitude amp * u_in
+    per component (enough for some outlet nodes to start with u_x < 0)."""
+    f = np.ones((nz, ny, nx), dtype=np.int32)
+    f[:, :, 0] = -1
+    f[:, :, -1] = -2
+    inl = [capi.make_inlet(0, j, k, (-1, 0, 0), (u_in, 0, 0)) for k in range(nz) for j in range(ny)]
+    out = [capi.make_outlet(nx - 1, j, k, (1, 0, 0), rho_out) for k in range(nz) for j in range(ny)]
+    N = nx * ny * nz
+    idx = np.arange(N, dtype=np.uint64)
+    u = np.zeros((3, N))
+    for a in range(3):
+        u[a] = (uniform(seed, idx, a) * 2.0 - 1.0) * amp * u_in
+    u[0] += u_in
+    rho = 1.0 + 0.01 * (uniform(seed + 1, idx, 0) * 2.0 - 1.0)
+    return {"flags": f, "inlets": inl, "outlets": out, "nu": nu, "periodic": (0, 1, 1), "rho": rho, "u": u}
+
+
 # ---- config 4: flow past a seeded body ------------------------------------------------------------------
 def icosphere(subdiv):
     t = (1.0 + math.sqrt(5.0)) / 2.0

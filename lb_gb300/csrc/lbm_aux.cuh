@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(128) k_read(Params p, ReadOut o) {
         a[7 * N + c.idx] += (double)ux * uy; a[8 * N + c.idx] += (double)ux * uz; a[9 * N + c.idx] += (double)uy * uz;
     }
     if (o.mode & READ_DIAG) {
-        const bool tgt = live && (cl == CLS_BULK || cl == CLS_EDGE || cl == CLS_OUTLET);
+        const bool tgt = live && (cl == CLS_BULK || cl == CLS_EDGE || cl == CLS_OUTLET || cl == CLS_SYM);
         double v[RED_COUNT] = {0};
         if (tgt) {
             bool ok = true;

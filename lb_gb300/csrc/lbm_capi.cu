@@ -21,6 +21,12 @@
 
 using namespace lbm;
 
+static_assert(OUT_INTERPOLATED == LBM_OUTLET_DENSITY_INTERPOLATED && OUT_NEQ == LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM &&
+                  OUT_NEQ_OMEGA == LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA &&
+                  OUT_NEQ_OMEGA_RF == LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA_RF &&
+                  OUT_DENSITY_EQ == LBM_OUTLET_DENSITY_EQUILIBRIUM,
+              "device outlet kinds follow lbm.h");
+
 struct lbm_ctx {
     lbm_config cfg{};
     cudaStream_t st = nullptr;
@@ -32,6 +38,7 @@ struct lbm_ctx {
     std::vector<int32_t> flags;
     std::vector<lbm_bc_inlet> inlets;
     std::vector<lbm_bc_outlet> outlets;
+    std::vector<lbm_bc_symmetry> syms;
     bool have_flags = false, have_geom = false, initialized = false;
     // side tables
     int n_lid = 0, n_in = 0, n_out = 0;
@@ -43,6 +50,13 @@ struct lbm_ctx {
     void* d_out_save = nullptr;
     float* d_out_rho = nullptr;
     int32_t* d_out_dir = nullptr;
+    int n_ms = 0;                    // neighbour-equilibrium outlets: cells that keep their moments
+    void* d_out_msave = nullptr;
+    int32_t* d_out_nb = nullptr;
+    int n_sym = 0;
+    int32_t* d_sym_dir = nullptr;
+    int sponge_axis = -1, sponge_begin = 0;
+    double sponge_slope = 0.0;
     long long m = 0;  // steps done
     // monitors
     double* d_acc = nullptr;
@@ -130,6 +144,12 @@ static Params make_params(const lbm_ctx* c) {
     p.lid_state = c->d_lid_state; p.lid_n = c->d_lid_n; p.lid_u = c->d_lid_u; p.n_lid = c->n_lid;
     p.in_probe = c->d_in_probe; p.in_u = c->d_in_u; p.in_dir = c->d_in_dir; p.n_in = c->n_in;
     p.out_save = c->d_out_save; p.out_rho = c->d_out_rho; p.out_dir = c->d_out_dir; p.n_out = c->n_out;
+    p.outlet_kind = c->cfg.outlet_kind;
+    p.out_msave = c->d_out_msave; p.out_nb = c->d_out_nb; p.n_ms = c->n_ms;
+    p.inlet_zouhe = c->cfg.inlet_kind == LBM_INLET_ZOU_HE ? 1 : 0;
+    p.sym_dir = c->d_sym_dir; p.n_sym = c->n_sym;
+    p.sponge_axis = c->sponge_axis; p.sponge_begin = c->sponge_begin;
+    p.sponge_slope = c->sponge_slope; p.sponge_slopef = (float)c->sponge_slope;
     p.mlp_frag = c->d_mlp_frag;
     p.mlp = c->mlp_norm;
     p.nut = c->d_nut;
@@ -208,6 +228,13 @@ lbm_status lbm_create(const lbm_config* cfg, lbm_ctx** out) {
     if (cfg->closure != LBM_CLOSURE_NONE && cfg->closure != LBM_CLOSURE_SMAGORINSKY && cfg->closure != LBM_CLOSURE_MLP)
         return fail(nullptr, LBM_ERR_UNSUPPORTED, "closure %d not implemented", cfg->closure);
     if (cfg->mlp_interval < 0) return fail(nullptr, LBM_ERR_INVALID, "mlp_interval %d < 0", cfg->mlp_interval);
+    if (cfg->inlet_kind < LBM_INLET_MOVING_WALL || cfg->inlet_kind > LBM_INLET_ZOU_HE)
+        return fail(nullptr, LBM_ERR_UNSUPPORTED, "inlet kind %d not implemented", cfg->inlet_kind);
+    if (cfg->outlet_kind < LBM_OUTLET_DENSITY_INTERPOLATED || cfg->outlet_kind > LBM_OUTLET_DENSITY_EQUILIBRIUM)
+        return fail(nullptr, LBM_ERR_UNSUPPORTED, "outlet kind %d not implemented", cfg->outlet_kind);
+    if ((cfg->outlet_kind == LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA ||
+         cfg->outlet_kind == LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA_RF) && cfg->closure == LBM_CLOSURE_MLP)
+        return fail(nullptr, LBM_ERR_UNSUPPORTED, "the outlet sponge runs with the Smagorinsky or no closure");
     if (cfg->closure == LBM_CLOSURE_MLP && cfg->storage == LBM_STORAGE_F64)
         return fail(nullptr, LBM_ERR_UNSUPPORTED, "the learned closure runs with FP32 or FP16-deviation storage");
     if (cfg->storage < LBM_STORAGE_F64 || cfg->storage > LBM_STORAGE_F16DEV)
@@ -248,10 +275,12 @@ static void free_side(lbm_ctx* c) {
     dfree(c->d_lid_state); dfree(c->d_lid_n); dfree(c->d_lid_u);
     dfree(c->d_in_probe); dfree(c->d_in_u); dfree(c->d_in_dir);
     dfree(c->d_out_save); dfree(c->d_out_rho); dfree(c->d_out_dir);
-    c->d_lid_state = c->d_in_probe = c->d_out_save = nullptr;
+    dfree(c->d_out_msave); dfree(c->d_out_nb); dfree(c->d_sym_dir);
+    c->d_lid_state = c->d_in_probe = c->d_out_save = c->d_out_msave = nullptr;
     c->d_lid_n = c->d_lid_u = c->d_in_u = c->d_out_rho = nullptr;
-    c->d_in_dir = c->d_out_dir = nullptr;
-    c->n_lid = c->n_in = c->n_out = 0;
+    c->d_in_dir = c->d_out_dir = c->d_out_nb = c->d_sym_dir = nullptr;
+    c->n_lid = c->n_in = c->n_out = c->n_ms = c->n_sym = 0;
+    c->sponge_axis = -1;
 }
 
 lbm_status lbm_destroy(lbm_ctx* c) {
@@ -282,6 +311,15 @@ lbm_status lbm_set_bc(lbm_ctx* c, const lbm_bc_inlet* in, int32_t nin, const lbm
         return fail(c, LBM_ERR_INVALID, "lbm_set_bc: bad argument");
     c->inlets.assign(in, in + nin);
     c->outlets.assign(out, out + nout);
+    c->syms.clear();
+    c->have_geom = false;
+    c->initialized = false;
+    return LBM_OK;
+}
+
+lbm_status lbm_set_symmetry(lbm_ctx* c, const lbm_bc_symmetry* recs, int32_t n) {
+    if (!c || n < 0 || (n && !recs)) return fail(c, LBM_ERR_INVALID, "lbm_set_symmetry: bad argument");
+    c->syms.assign(recs, recs + n);
     c->have_geom = false;
     c->initialized = false;
     return LBM_OK;
@@ -299,13 +337,27 @@ static lbm_status build_geometry(lbm_ctx* c) {
     };
     std::vector<uint8_t> cls((size_t)N);
     std::vector<int32_t> aux((size_t)N, -1);
-    const bool lid_kind = c->cfg.inlet_kind == LBM_INLET_MOVING_WALL;
+    // moving-wall and Zou/He nodes share the 3-level side table: collided, never streamed into
+    const bool lid_kind = c->cfg.inlet_kind == LBM_INLET_MOVING_WALL || c->cfg.inlet_kind == LBM_INLET_ZOU_HE;
+    const int okind = c->cfg.outlet_kind;
+    const bool neq_kind = okind == LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM || okind == LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA ||
+                          okind == LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA_RF;
+    std::vector<char> is_sym((size_t)N, 0);
+    for (const auto& r : c->syms) {
+        int i = r.vertex.x, j = r.vertex.y, k = r.vertex.z;
+        if (i < 0 || j < 0 || k < 0 || i >= nx || j >= ny || k >= nz)
+            return fail(c, LBM_ERR_INVALID, "symmetry record at (%d,%d,%d) is outside the lattice", i, j, k);
+        if (c->flags[id(i, j, k)] != -2)
+            return fail(c, LBM_ERR_INVALID, "symmetry record at (%d,%d,%d) is not a -2 cell", i, j, k);
+        if (is_sym[id(i, j, k)]) return fail(c, LBM_ERR_INVALID, "two symmetry records for (%d,%d,%d)", i, j, k);
+        is_sym[id(i, j, k)] = 1;
+    }
     for (long long q = 0; q < N; q++) {
         int32_t f = c->flags[q];
         uint8_t k;
         if (f == 0) k = CLS_SOLID;
         else if (f == -1) k = lid_kind ? CLS_LID : CLS_INLET;
-        else if (f == -2) k = CLS_OUTLET;
+        else if (f == -2) k = is_sym[q] ? CLS_SYM : CLS_OUTLET;
         else if (f > 0 || f == -3) k = CLS_BULK;
         else return fail(c, LBM_ERR_INVALID, "flag %d at cell %lld is not in the reference encoding", f, q);
         cls[q] = k | (f == 1 ? BIT_REFBULK : 0);
@@ -341,6 +393,7 @@ static lbm_status build_geometry(lbm_ctx* c) {
         long long q = id(i, j, k);
         if (c->flags[q] != -2) return fail(c, LBM_ERR_INVALID, "outlet record at (%d,%d,%d) is not a -2 cell", i, j, k);
         if (aux[q] >= 0) return fail(c, LBM_ERR_INVALID, "two outlet records for (%d,%d,%d)", i, j, k);
+        if (is_sym[q]) return fail(c, LBM_ERR_INVALID, "(%d,%d,%d) has an outlet and a symmetry record", i, j, k);
         int s = (r.normal[0] == 1.f && r.normal[1] == 0.f && r.normal[2] == 0.f) ? 1
               : (r.normal[0] == -1.f && r.normal[1] == 0.f && r.normal[2] == 0.f) ? -1 : 0;
         if (!s) return fail(c, LBM_ERR_UNSUPPORTED, "outlet at (%d,%d,%d): only +-x normals (as the reference)", i, j, k);
@@ -349,11 +402,42 @@ static lbm_status build_geometry(lbm_ctx* c) {
         out_dir.push_back(s);
         out_rho.push_back(r.density);
     }
+    // symmetry records: +-y normals only (BounceSymmetryHalf.h:84-133; the x and z branches are commented
+    // out), a solid cell across the plane, in-plane sources inside the lattice and streaming normally
+    std::vector<int32_t> sym_dir;
+    int n_sym = 0;
+    for (const auto& r : c->syms) {
+        int i = r.vertex.x, j = r.vertex.y, k = r.vertex.z;
+        long long q = id(i, j, k);
+        int sg = (r.normal[0] == 0.f && r.normal[1] == 1.f && r.normal[2] == 0.f) ? 1
+               : (r.normal[0] == 0.f && r.normal[1] == -1.f && r.normal[2] == 0.f) ? -1 : 0;
+        if (!sg) return fail(c, LBM_ERR_UNSUPPORTED, "symmetry at (%d,%d,%d): only +-y normals (as the reference)", i, j, k);
+        if (wrap[1]) return fail(c, LBM_ERR_UNSUPPORTED, "symmetry planes need a non-periodic y axis");
+        if (j + sg < 0 || j + sg >= ny)
+            return fail(c, LBM_ERR_UNSUPPORTED, "symmetry at (%d,%d,%d): the row across the plane must be solid", i, j, k);
+        for (int dz = -1; dz <= 1; dz++)
+            for (int dx = -1; dx <= 1; dx++) {
+                bool ok = true;
+                int a = wrapc(i + dx, nx, 0, ok), e = wrapc(k + dz, nz, 2, ok);
+                if (!ok) return fail(c, LBM_ERR_UNSUPPORTED, "symmetry at (%d,%d,%d) mirrors from outside the lattice", i, j, k);
+                if (c->flags[id(a, j + sg, e)] != 0)
+                    return fail(c, LBM_ERR_UNSUPPORTED, "symmetry at (%d,%d,%d): the row across the plane must be solid",
+                                i, j, k);
+                int32_t fs = c->flags[id(a, j, e)];
+                if (fs == -1) return fail(c, LBM_ERR_UNSUPPORTED, "symmetry at (%d,%d,%d) mirrors an inlet node", i, j, k);
+                if (r.regular && fs == 0)
+                    return fail(c, LBM_ERR_INVALID, "symmetry at (%d,%d,%d) is marked regular but has a solid in-plane neighbour", i, j, k);
+            }
+        aux[q] = n_sym++;
+        sym_dir.push_back(sg);
+    }
     for (long long q = 0; q < N; q++) {
         int k = cls[q] & CLS_MASK;
         if ((k == CLS_LID || k == CLS_INLET || k == CLS_OUTLET) && aux[q] < 0)
             return fail(c, LBM_ERR_INVALID, "cell %lld has flag %d but no boundary record", q, c->flags[q]);
     }
+    std::vector<int32_t> out_nb(neq_kind ? 9 * (size_t)n_out : 0, -1);
+    int n_ms = 0;
     // helper roles: probes of the equilibrium inlets, upstream cells of the outlets
     auto set_role = [&](long long q, uint8_t bit, int node, const char* what) -> lbm_status {
         int k = cls[q] & CLS_MASK;
@@ -376,13 +460,35 @@ static lbm_status build_geometry(lbm_ctx* c) {
                 lbm_status st = set_role(id(ii, j, kk), d == 1 ? BIT_PROBE1 : BIT_PROBE2, aux[q], "inlet probe");
                 if (st) return st;
             }
-        } else if (k == CLS_OUTLET) {
+        } else if (k == CLS_OUTLET && okind == LBM_OUTLET_DENSITY_INTERPOLATED) {
             int s = out_dir[aux[q]];
             bool ok = true;
             int ii = wrapc(i - s, nx, 0, ok);
             if (!ok) return fail(c, LBM_ERR_INVALID, "outlet at (%d,%d,%d) has no upstream cell", i, j, kk);
             lbm_status st = set_role(id(ii, j, kk), BIT_OUTUP, aux[q], "outlet upstream");
             if (st) return st;
+        } else if (k == CLS_OUTLET && neq_kind) {
+            // neighbour-equilibrium outlets read the moments of the 9 cells x + c_v (c_x = -s), which keep
+            // them in a side table (one entry per cell, shared by the outlet nodes around it)
+            int s = out_dir[aux[q]];
+            for (int dz = -1; dz <= 1; dz++)
+                for (int dy = -1; dy <= 1; dy++) {
+                    bool ok = true;
+                    int ii = wrapc(i - s, nx, 0, ok), jj = wrapc(j + dy, ny, 1, ok), ze = wrapc(kk + dz, nz, 2, ok);
+                    if (!ok) return fail(c, LBM_ERR_INVALID, "outlet at (%d,%d,%d) has no upstream cell", i, j, kk);
+                    long long r = id(ii, jj, ze);
+                    if (c->flags[r] <= 0)
+                        return fail(c, LBM_ERR_UNSUPPORTED,
+                                    "neighbour-equilibrium outlet at (%d,%d,%d): upstream cell (%d,%d,%d) must be fluid",
+                                    i, j, kk, ii, jj, ze);
+                    if (cls[r] & (BIT_PROBE1 | BIT_PROBE2))
+                        return fail(c, LBM_ERR_UNSUPPORTED, "cell %lld would serve two boundary nodes", r);
+                    if (!(cls[r] & BIT_OUTUP)) {
+                        cls[r] |= BIT_OUTUP;
+                        aux[r] = n_ms++;
+                    }
+                    out_nb[(size_t)outlet_slot(vid(-s, dy, dz)) * n_out + aux[q]] = aux[r];
+                }
         }
     }
     // BULK/EDGE split: fluid cells next to a solid, moving-wall or inlet node stream through
@@ -405,7 +511,7 @@ static lbm_status build_geometry(lbm_ctx* c) {
     // outlets may only do so on their interpolated links, and must not touch solid cells
     auto check_links = [&](long long q) -> lbm_status {
         int k = cls[q] & CLS_MASK;
-        if (k != CLS_BULK && k != CLS_EDGE && k != CLS_OUTLET) return LBM_OK;
+        if (k != CLS_BULK && k != CLS_EDGE && k != CLS_OUTLET && k != CLS_SYM) return LBM_OK;
         int i = (int)(q % nx), j = (int)((q / nx) % ny), kk = (int)(q / ((long long)nx * ny));
         for (int dz = -1; dz <= 1; dz++)
             for (int dy = -1; dy <= 1; dy++)
@@ -444,9 +550,26 @@ static lbm_status build_geometry(lbm_ctx* c) {
             lbm_status st = check_links(q);
             if (st) return st;
         }
+    // sponge of OutletNeighbourEquilibriumOmega(RF)::outletOmega (:18-79): along the first outlet's normal
+    // axis, the last ceil(0.1 n) planes (the reference's float ceil(n * 0.1f), equal for every n) lose
+    // (high - low) / width * (plane - first plane) of their relaxation rate; those cells take the
+    // per-cell path (the bit keeps them off the packed pair path)
+    int sp_axis = -1, sp_begin = 0;
+    double sp_slope = 0.0;
+    if ((okind == LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA || okind == LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA_RF) &&
+        !c->outlets.empty()) {
+        sp_axis = 0;  // outlet normals are +-x (checked above)
+        const int width = (int)std::ceil((float)nx * 0.1f);
+        sp_begin = nx - width;
+        sp_slope = (c->cfg.omega_dumping_high - c->cfg.omega_dumping_low) / (double)width;
+        if (sp_slope != 0.0)
+            for (long long q = 0; q < N; q++)
+                if ((int)(q % nx) >= sp_begin && (cls[q] & CLS_MASK) != CLS_SOLID) cls[q] |= BIT_SPONGE;
+    }
     // upload
     cudaSetDevice(c->cfg.device);
     free_side(c);
+    c->sponge_axis = sp_axis; c->sponge_begin = sp_begin; c->sponge_slope = sp_slope;
     CU(c, cudaMemcpyAsync(c->d_cls, cls.data(), (size_t)N, cudaMemcpyHostToDevice, c->st));
     CU(c, cudaMemcpyAsync(c->d_aux, aux.data(), (size_t)N * 4, cudaMemcpyHostToDevice, c->st));
     const size_t rs = real_size(c);
@@ -479,6 +602,18 @@ static lbm_status build_geometry(lbm_ctx* c) {
         CU(c, cudaMalloc(&c->d_out_dir, (size_t)n_out * 4));
         CU(c, cudaMemcpy(c->d_out_rho, out_rho.data(), (size_t)n_out * 4, cudaMemcpyHostToDevice));
         CU(c, cudaMemcpy(c->d_out_dir, out_dir.data(), (size_t)n_out * 4, cudaMemcpyHostToDevice));
+    }
+    c->n_ms = n_ms;
+    if (n_ms) {
+        CU(c, cudaMalloc(&c->d_out_msave, 2 * 4 * (size_t)n_ms * rs));
+        CU(c, cudaMemset(c->d_out_msave, 0, 2 * 4 * (size_t)n_ms * rs));
+        CU(c, cudaMalloc(&c->d_out_nb, out_nb.size() * 4));
+        CU(c, cudaMemcpy(c->d_out_nb, out_nb.data(), out_nb.size() * 4, cudaMemcpyHostToDevice));
+    }
+    c->n_sym = n_sym;
+    if (n_sym) {
+        CU(c, cudaMalloc(&c->d_sym_dir, (size_t)n_sym * 4));
+        CU(c, cudaMemcpy(c->d_sym_dir, sym_dir.data(), (size_t)n_sym * 4, cudaMemcpyHostToDevice));
     }
     CU(c, cudaStreamSynchronize(c->st));
     // rows the row-staged step may take (FP16-deviation storage): every cell bulk fluid, x periodic,
@@ -542,6 +677,7 @@ static lbm_status init_common(lbm_ctx* c, const double* rho, const double* u, do
     dfree(dr); dfree(du); dfree(dp);
     if (e != cudaSuccess) return fail(c, LBM_ERR_CUDA, "init kernel: %s", cudaGetErrorString(e));
     if (c->d_out_save) CU(c, cudaMemset(c->d_out_save, 0, 2 * 18 * (size_t)c->n_out * real_size(c)));
+    if (c->d_out_msave) CU(c, cudaMemset(c->d_out_msave, 0, 2 * 4 * (size_t)c->n_ms * real_size(c)));
     c->avg_on = false; c->avg_count = 0; c->avg_last = -1;
     if (c->d_uerr) CU(c, cudaMemset(c->d_uerr, 0, 3 * N * 8));
     c->initialized = true;
@@ -815,14 +951,17 @@ lbm_status lbm_checkpoint_save(lbm_ctx* c, const char* path) {
         return put(h.data(), n);
     };
     int32_t ver = LBM_ABI_VERSION;
-    int64_t m = c->m, nin = (int64_t)c->inlets.size(), nout = (int64_t)c->outlets.size();
+    int64_t m = c->m, nin = (int64_t)c->inlets.size(), nout = (int64_t)c->outlets.size(),
+            nsym = (int64_t)c->syms.size();
     bool ok = put(kMagic, 8) && put(&ver, 4) && put(&c->cfg, sizeof(c->cfg)) && put(&m, 8) &&
               put(c->flags.data(), N * 4) && put(&nin, 8) && put(c->inlets.data(), nin * sizeof(lbm_bc_inlet)) &&
               put(&nout, 8) && put(c->outlets.data(), nout * sizeof(lbm_bc_outlet)) &&
+              put(&nsym, 8) && put(c->syms.data(), nsym * sizeof(lbm_bc_symmetry)) &&
               put_dev(c->d_f, 27 * N * c->esize) &&
               put_dev(c->d_lid_state, 3 * 27 * (size_t)c->n_lid * rs) &&
               put_dev(c->d_in_probe, 9 * (size_t)c->n_in * rs) &&
-              put_dev(c->d_out_save, 36 * (size_t)c->n_out * rs);
+              put_dev(c->d_out_save, 36 * (size_t)c->n_out * rs) &&
+              put_dev(c->d_out_msave, 8 * (size_t)c->n_ms * rs);
     std::fclose(fp);
     if (!ok) return fail(c, LBM_ERR_IO, "writing %s failed", path);
     return LBM_OK;
@@ -836,7 +975,7 @@ lbm_status lbm_checkpoint_load(lbm_ctx* c, const char* path) {
     char mg[8];
     int32_t ver = 0;
     lbm_config cfg;
-    int64_t m = 0, nin = 0, nout = 0;
+    int64_t m = 0, nin = 0, nout = 0, nsym = 0;
     if (!get(mg, 8) || std::memcmp(mg, kMagic, 8) != 0 || !get(&ver, 4) || ver != LBM_ABI_VERSION ||
         !get(&cfg, sizeof(cfg)) || !get(&m, 8)) {
         std::fclose(fp);
@@ -852,12 +991,14 @@ lbm_status lbm_checkpoint_load(lbm_ctx* c, const char* path) {
     std::vector<lbm_bc_inlet> in(ok ? (size_t)nin : 0);
     ok = ok && get(in.data(), nin * sizeof(lbm_bc_inlet)) && get(&nout, 8);
     std::vector<lbm_bc_outlet> out(ok ? (size_t)nout : 0);
-    ok = ok && get(out.data(), nout * sizeof(lbm_bc_outlet));
+    ok = ok && get(out.data(), nout * sizeof(lbm_bc_outlet)) && get(&nsym, 8);
+    std::vector<lbm_bc_symmetry> sy(ok ? (size_t)nsym : 0);
+    ok = ok && get(sy.data(), nsym * sizeof(lbm_bc_symmetry));
     if (!ok) { std::fclose(fp); return fail(c, LBM_ERR_IO, "truncated checkpoint %s", path); }
     int dev = c->cfg.device;
     c->cfg = cfg;
     c->cfg.device = dev;
-    c->flags = fl; c->inlets = in; c->outlets = out;
+    c->flags = fl; c->inlets = in; c->outlets = out; c->syms = sy;
     c->have_flags = true; c->have_geom = false;
     cudaSetDevice(dev);
     lbm_status s = build_geometry(c);
@@ -870,7 +1011,8 @@ lbm_status lbm_checkpoint_load(lbm_ctx* c, const char* path) {
         return cudaMemcpy(d, h.data(), n, cudaMemcpyHostToDevice) == cudaSuccess;
     };
     ok = get_dev(c->d_f, 27 * N * c->esize) && get_dev(c->d_lid_state, 81 * (size_t)c->n_lid * rs) &&
-         get_dev(c->d_in_probe, 9 * (size_t)c->n_in * rs) && get_dev(c->d_out_save, 36 * (size_t)c->n_out * rs);
+         get_dev(c->d_in_probe, 9 * (size_t)c->n_in * rs) && get_dev(c->d_out_save, 36 * (size_t)c->n_out * rs) &&
+         get_dev(c->d_out_msave, 8 * (size_t)c->n_ms * rs);
     std::fclose(fp);
     if (!ok) return fail(c, LBM_ERR_IO, "reading %s failed", path);
     c->m = m;

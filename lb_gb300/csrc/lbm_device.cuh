@@ -35,14 +35,19 @@
 namespace lbm {
 
 // ---- cell class byte ---------------------------------------------------------------------------
-enum : uint8_t { CLS_SOLID = 0, CLS_BULK = 1, CLS_EDGE = 2, CLS_LID = 3, CLS_INLET = 4, CLS_OUTLET = 5 };
+enum : uint8_t { CLS_SOLID = 0, CLS_BULK = 1, CLS_EDGE = 2, CLS_LID = 3, CLS_INLET = 4, CLS_OUTLET = 5, CLS_SYM = 6 };
 enum : uint8_t {
     BIT_PROBE1 = 1u << 3,   // interior neighbour 1 of an equilibrium inlet: stores rho, ux
     BIT_PROBE2 = 1u << 4,   // interior neighbour 2: stores ux
     BIT_OUTUP = 1u << 5,    // upstream neighbour of an outlet: stores its incoming-direction f*
+                            // (density-interpolated) or its moments (neighbour-equilibrium outlets)
     BIT_REFBULK = 1u << 6,  // reference flag == 1 (cells the error monitor sums over)
+    BIT_SPONGE = 1u << 7,   // inside the outlet sponge: the relaxation rate is lowered
 };
 constexpr uint8_t CLS_MASK = 7;
+
+// outlet kinds (the values of LBM_OUTLET_* in lbm.h)
+constexpr int OUT_INTERPOLATED = 0, OUT_NEQ = 1, OUT_NEQ_OMEGA = 2, OUT_NEQ_OMEGA_RF = 3, OUT_DENSITY_EQ = 4;
 
 // velocity set, lane types and collision math: lbm_math.cuh
 // the 9 directions with c_x = -s (s = +1: outlet facing +x) as used by the outlet side table
@@ -98,6 +103,18 @@ struct Params {
     const float* out_rho;    // prescribed density
     const int32_t* out_dir;  // +1: normal +x, -1: normal -x
     int n_out;
+    int outlet_kind;         // LBM_OUTLET_*
+    void* out_msave;         // [2][4][n_ms] of S::R : parity, {rho, ux, uy, uz}, cell (neighbour-equilibrium)
+    const int32_t* out_nb;   // [9][n_out] : out_msave entry of the cell x + c_v, per entering direction
+    int n_ms;
+    int inlet_zouhe;         // flag -1 nodes follow InletVelocityZouHe (else the moving wall)
+    // symmetry nodes (half-way specular reflection across a +-y plane)
+    const int32_t* sym_dir;  // [n_sym] : +1 normal +y, -1 normal -y
+    int n_sym;
+    // outlet sponge: cells with BIT_SPONGE relax with omega - slope * (coordinate - begin)
+    int sponge_axis, sponge_begin;
+    double sponge_slope;
+    float sponge_slopef;
     // learned closure (LBM_CLOSURE_MLP): fragment table [kMlpFragRows][32] and input normalisation
     const uint4* mlp_frag;
     MlpNorm mlp;
@@ -275,11 +292,12 @@ LBM_D void gather(const Params& p, const Cell& c, int cl, typename S::R (&f)[27]
         });
         return;
     }
-    // EDGE or OUTLET, m >= 1: per-link rules
+    // EDGE, OUTLET or SYM, m >= 1: per-link rules
     const int osgn = (cl == CLS_OUTLET) ? p.out_dir[p.aux[c.idx]] : 0;
+    const int ysgn = (cl == CLS_SYM) ? p.sym_dir[p.aux[c.idx]] : 0;
     sfor<0, 27>([&](auto vc) {
         constexpr int V = decltype(vc)::value;
-        if (osgn != 0 && cx(V) == -osgn) { f[V] = (R)0; return; }  // interpolated below
+        if (osgn != 0 && cx(V) == -osgn) { f[V] = (R)0; return; }  // outlet rule below
         if (nbr_oob<-cx(V), -cy(V), -cz(V)>(c)) {  // a link from outside the box (rejected at set-up)
             f[V] = (R)0;
             return;
@@ -290,7 +308,9 @@ LBM_D void gather(const Params& p, const Cell& c, int cl, typename S::R (&f)[27]
             // half-way bounce-back: f_v(x) = f*_{opp v}(x) of the previous step
             R b = ODD ? load_at<S, V>(p, V * N + c.idx) : load_at<S, opp(V)>(p, opp(V) * N + nb);
             f[V] = b;
-            if (DRAG) {  // fluid momentum lost through the link: b*c_{opp v} - b*c_v = -2 b c_v
+            // fluid momentum lost through the link: b*c_{opp v} - b*c_v = -2 b c_v (not on the links a
+            // symmetry node takes from across its plane)
+            if (DRAG && !(cy(V) != 0 && cy(V) == -ysgn)) {
                 drag[0] -= (R)(2 * cx(V)) * b; drag[1] -= (R)(2 * cy(V)) * b; drag[2] -= (R)(2 * cz(V)) * b;
             }
         } else if (ncl == CLS_LID) {
@@ -311,7 +331,47 @@ LBM_D void gather(const Params& p, const Cell& c, int cl, typename S::R (&f)[27]
             else     f[V] = load_at<S, V>(p, V * N + c.idx);
         }
     });
-    if (osgn != 0) {
+    if (ysgn != 0) {
+        // BounceSymmetryHalf.h:84-131: a link entering across the plane (c_y = -sign of the normal; the
+        // loop above bounced it back from the solid cell across) carries f*_{sym v} of the in-plane cell
+        // s = x - (c_x, 0, c_z) from the previous step, sym mirroring c_y; a solid s keeps the bounce-back.
+        // The value sits where s streamed it: after an even step in s's own slot opp(sym v), after an
+        // odd one in slot sym v of the solid cell across the plane.
+        sfor<0, 27>([&](auto vc) {
+            constexpr int V = decltype(vc)::value;
+            if constexpr (cy(V) != 0) {
+                if (cy(V) == -ysgn) {
+                    constexpr int SV = vid(cx(V), -cy(V), cz(V));
+                    const long long sc = nbr<-cx(V), 0, -cz(V)>(c);
+                    if ((p.cls[sc] & CLS_MASK) != CLS_SOLID)
+                        f[V] = ODD ? load_at<S, opp(SV)>(p, opp(SV) * N + sc) : load_at<S, SV>(p, SV * N + nbr<0, -cy(V), 0>(c));
+                }
+            }
+        });
+    }
+    if (osgn != 0 && p.outlet_kind != OUT_INTERPOLATED) {
+        // values kept by the node in the previous step: g_v = f_eq_v(u, rho_b) (- f*_v for the
+        // neighbour-equilibrium outlets, which then add f_eq_v of the cell x + c_v)
+        const int id = p.aux[c.idx];
+        const R* sv = (const R*)p.out_save + (long long)((p.m - 1) & 1) * 18 * p.n_out;
+        const R* ms = (const R*)p.out_msave + (long long)((p.m - 1) & 1) * 4 * p.n_ms;
+        const bool neq = p.outlet_kind != OUT_DENSITY_EQ;
+        sfor<0, 27>([&](auto vc) {
+            constexpr int V = decltype(vc)::value;
+            if constexpr (cx(V) != 0) {
+                if (cx(V) == -osgn) {
+                    const int k = outlet_slot(V);
+                    R g = sv[(9 + k) * p.n_out + id];
+                    if (neq) {
+                        const int e = p.out_nb[k * p.n_out + id];
+                        const R r = ms[e], ux = ms[p.n_ms + e], uy = ms[2 * p.n_ms + e], uz = ms[3 * p.n_ms + e];
+                        g += feq<V>(r, ux, uy, uz, ux * ux + uy * uy + uz * uz);
+                    }
+                    f[V] = g;
+                }
+            }
+        });
+    } else if (osgn != 0) {
         // OutletDensityInterpolated.h:200-221: incoming = cs f*(x-n) + (1-cs) f*(x); then
         // f += f_eq(u, 1) - f_eq(u, rho) with u from the prescribed density
         const int id = p.aux[c.idx];

@@ -21,13 +21,15 @@ LBM_D void acc_add(const Params& p, long long i, double rho, double ux, double u
     a[7 * N + i] += ux * uy; a[8 * N + i] += ux * uz; a[9 * N + i] += uy * uz;
 }
 
-// relaxation rate and collision of one lane (a cell, or a pair of cells)
-template <int COLL, int CLOS, class L>
+// relaxation rate and collision of one lane (a cell, or a pair of cells); SP: the rate is lowered by
+// dom afterwards (the outlet sponge, OutletNeighbourEquilibriumOmega.h:69-74 after TURBULENCETYPE::omega)
+template <int COLL, int CLOS, bool SP = false, class L>
 LBM_D void collide_lane(L (&f)[27], const Mom<L>& mm, L ri, L ux, L uy, L uz, L tau, L cles18, L om0,
-                        bool force, L Fx, L Fy, L Fz) {
+                        bool force, L Fx, L Fy, L Fz, L dom = L(0.0f)) {
     L om;
     if constexpr (CLOS == 0) om = om0;
     else om = omega_smagorinsky(tau, cles18, mm.rho, ri, ux, uy, uz, mm);
+    if constexpr (SP) om = om - dom;
     if constexpr (COLL == 0) {
         collide_srt(f, mm.rho, ux, uy, uz, om);
         if (force) srt_force(f, ux, uy, uz, om, Fx, Fy, Fz);
@@ -36,6 +38,15 @@ LBM_D void collide_lane(L (&f)[27], const Mom<L>& mm, L ri, L ux, L uy, L uz, L 
     } else {
         collide_cum15(f, mm.rho, ri, ux, uy, uz, om, mm);
     }
+}
+
+// the outlet sponge's reduction of the relaxation rate at (x, y, z): slope * (coordinate - begin),
+// as OutletNeighbourEquilibriumOmega.h:66-71 forms it (real type times the integer distance)
+template <class R>
+LBM_D R sponge_rate(const Params& p, int x, int y, int z) {
+    const int pos = (p.sponge_axis == 0 ? x : p.sponge_axis == 1 ? y : z) - p.sponge_begin;
+    if constexpr (std::is_same<R, float>::value) return p.sponge_slopef * (float)pos;
+    else return p.sponge_slope * (double)pos;
 }
 
 // ---- one cell (scalar lane) --------------------------------------------------------------------------
@@ -80,19 +91,29 @@ LBM_D void step_cell(const Params& p, int x, int y, int z) {
         else pr[2 * p.n_in + id] = ux;
     }
     if (p.acc) acc_add(p, idx, rho, ux, uy, uz);
+    // outlet sponge: omega -= slope * (coordinate - first sponge plane), in the storage's real type
+    const R dom = (fl & BIT_SPONGE) ? sponge_rate<R>(p, x, y, z) : (R)0;
     if constexpr (COLL == 3) {
         // CollisionCumD3Q27TurbulentCombined.h:1066-1078: reference flag 1 -> 2015, other flags -> 2017
         if (fl & BIT_REFBULK)
-            collide_lane<1, CLOS>(f, mm, ri, ux, uy, uz, p_tau<R>(p), p_cles18<R>(p), p_om0<R>(p), false, (R)0, (R)0,
-                                  (R)0);
+            collide_lane<1, CLOS, true>(f, mm, ri, ux, uy, uz, p_tau<R>(p), p_cles18<R>(p), p_om0<R>(p), false, (R)0,
+                                        (R)0, (R)0, dom);
         else
-            collide_lane<2, CLOS>(f, mm, ri, ux, uy, uz, p_tau<R>(p), p_cles18<R>(p), p_om0<R>(p), false, (R)0, (R)0,
-                                  (R)0);
+            collide_lane<2, CLOS, true>(f, mm, ri, ux, uy, uz, p_tau<R>(p), p_cles18<R>(p), p_om0<R>(p), false, (R)0,
+                                        (R)0, (R)0, dom);
     } else {
-        collide_lane<COLL, CLOS>(f, mm, ri, ux, uy, uz, p_tau<R>(p), p_cles18<R>(p), p_om0<R>(p), p.has_force != 0,
-                                 p_F<R>(p, 0), p_F<R>(p, 1), p_F<R>(p, 2));
+        collide_lane<COLL, CLOS, true>(f, mm, ri, ux, uy, uz, p_tau<R>(p), p_cles18<R>(p), p_om0<R>(p),
+                                       p.has_force != 0, p_F<R>(p, 0), p_F<R>(p, 1), p_F<R>(p, 2), dom);
     }
-    if (fl & BIT_OUTUP) {
+    // upstream roles exist for the density-interpolated outlet (f* of the cell) and the neighbour-
+    // equilibrium outlets (moments); the density-equilibrium outlet has none
+    if ((fl & BIT_OUTUP) && p.outlet_kind != OUT_INTERPOLATED && p.outlet_kind != OUT_DENSITY_EQ) {
+        // neighbour-equilibrium outlets: the moments this step's collision used (the reference's
+        // u_view / rho_view when the outlet pass of this step runs)
+        const int e = p.aux[idx];
+        R* ms = (R*)p.out_msave + (long long)(p.m & 1) * 4 * p.n_ms;
+        ms[e] = rho; ms[p.n_ms + e] = ux; ms[2 * p.n_ms + e] = uy; ms[3 * p.n_ms + e] = uz;
+    } else if ((fl & BIT_OUTUP) && p.outlet_kind == OUT_INTERPOLATED) {
         const int id = p.aux[idx];
         const int s = p.out_dir[id];
         R* sv = (R*)p.out_save + (long long)(p.m & 1) * 18 * p.n_out;
@@ -114,18 +135,43 @@ LBM_D void step_cell(const Params& p, int x, int y, int z) {
         R* nxt = (R*)p.lid_state + (long long)lvl3(p.m + 1) * 27 * nl;
         const R n0 = p.lid_n[id], n1 = p.lid_n[nl + id], n2 = p.lid_n[2 * nl + id];
         const R w0 = p.lid_u[id], w1 = p.lid_u[nl + id], w2 = p.lid_u[2 * nl + id];
+        const R u2 = ux * ux + uy * uy + uz * uz, w2s = w0 * w0 + w1 * w1 + w2 * w2;
+        const bool zh = p.inlet_zouhe != 0;
         sfor<0, 27>([&](auto vc) {
             constexpr int V = decltype(vc)::value;
             constexpr int O = opp(V);
             // component O is set from f*_V when n.c_V > 0, else it keeps its value
-            if (n0 * (R)cx(V) + n1 * (R)cy(V) + n2 * (R)cz(V) > (R)0)
-                nxt[O * nl + id] = f[V] - (R)6 * (R)wgt(V) * rho * ((R)cx(V) * w0 + (R)cy(V) * w1 + (R)cz(V) * w2);
-            else
+            if (n0 * (R)cx(V) + n1 * (R)cy(V) + n2 * (R)cz(V) > (R)0) {
+                if (zh)  // InletVelocityZouHe.h:85-97: f*_V - f_eq_V(rho, u) + f_eq_O(rho, u_b)
+                    nxt[O * nl + id] = f[V] - feq<V>(rho, ux, uy, uz, u2) + feq<O>(rho, w0, w1, w2, w2s);
+                else
+                    nxt[O * nl + id] = f[V] - (R)6 * (R)wgt(V) * rho * ((R)cx(V) * w0 + (R)cy(V) * w1 + (R)cz(V) * w2);
+            } else {
                 nxt[O * nl + id] = cur[O * nl + id];
+            }
         });
         return;
     }
-    if (cl == CLS_OUTLET) {
+    if (cl == CLS_OUTLET && p.outlet_kind != OUT_INTERPOLATED) {
+        // the node's part of the next state's entering links (gathered in the next step):
+        //   density-equilibrium  f_eq_v(u, rho_b)            (OutletDensityEquilibrium.h:63-67)
+        //   neighbour-equilibrium f_eq_v(u, rho_b) - f*_v     (OutletNeighbourEquilibrium.h:104-110: the
+        //                         neighbour x + c_v holds f*_v after streaming; its f_eq_v is added in
+        //                         the gather)
+        // OmegaRF: rho_b (1 - u_x^2 / 2) where u_x < 0 (OutletNeighbourEquilibriumOmegaRF.h:151-155)
+        const int id = p.aux[idx];
+        const int s = p.out_dir[id];
+        R* sv = (R*)p.out_save + (long long)(p.m & 1) * 18 * p.n_out;
+        R rb = (R)p.out_rho[id];
+        if (p.outlet_kind == OUT_NEQ_OMEGA_RF && ux < (R)0) rb = (R)((double)rb - 0.5 * (double)ux * (double)ux * (double)rb);
+        const R u2 = ux * ux + uy * uy + uz * uz;
+        const bool neq = p.outlet_kind != OUT_DENSITY_EQ;
+        sfor<0, 27>([&](auto vc) {
+            constexpr int V = decltype(vc)::value;
+            if constexpr (cx(V) != 0)
+                if (cx(V) == -s) sv[(9 + outlet_slot(V)) * p.n_out + id] = feq<V>(rb, ux, uy, uz, u2) - (neq ? f[V] : (R)0);
+        });
+    } else if (cl == CLS_OUTLET) {
         const int id = p.aux[idx];
         const int s = p.out_dir[id];
         R* sv = (R*)p.out_save + (long long)(p.m & 1) * 18 * p.n_out;

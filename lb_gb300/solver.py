@@ -72,6 +72,10 @@ class NoSymmetry:                               # boundaryConditions/Symmetry/No
     pass
 
 
+class BounceSymmetryHalf:                       # boundaryConditions/Symmetry/BounceSymmetryHalf.h (+-y normals)
+    pass
+
+
 class Periodic:                                 # boundaryConditions/Periodic/Periodic.h (index wrap here)
     pass
 
@@ -88,8 +92,28 @@ class InletVelocityEquilibrium:                 # boundaryConditions/Inlet/Inlet
     code = capi.LBM_INLET_EQUILIBRIUM
 
 
+class InletVelocityZouHe:                       # boundaryConditions/Inlet/InletVelocityZouHe.h
+    code = capi.LBM_INLET_ZOU_HE
+
+
 class OutletDensityInterpolated:                # boundaryConditions/Outlet/OutletDensityInterpolated.h
-    pass
+    code = capi.LBM_OUTLET_DENSITY_INTERPOLATED
+
+
+class OutletNeighbourEquilibrium:               # boundaryConditions/Outlet/OutletNeighbourEquilibrium.h
+    code = capi.LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM
+
+
+class OutletNeighbourEquilibriumOmega:          # .../Outlet/OutletNeighbourEquilibriumOmega.h (+ sponge)
+    code = capi.LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA
+
+
+class OutletNeighbourEquilibriumOmegaRF:        # .../Outlet/OutletNeighbourEquilibriumOmegaRF.h
+    code = capi.LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA_RF
+
+
+class OutletDensityEquilibrium:                 # boundaryConditions/Outlet/OutletDensityEquilibrium.h
+    code = capi.LBM_OUTLET_DENSITY_EQUILIBRIUM
 
 
 class MomentDensityVelocityN27:                 # moments/MomentDensityVelocityN27.h
@@ -150,7 +174,7 @@ class Solver:
     def __init__(self, shape, collision=CollisionCumD3Q27Turbulent2015, turbulence=OmegaNo,
                  inlet=InletVelocityMovingWall, storage="f32", nu=1.0 / 6.0, tau=0.0, cles=0.173,
                  periodic=(0, 0, 0), force=(0.0, 0.0, 0.0), rho0=1.0, f16_scale_log2=10, device=0, options=0,
-                 mlp_interval=1):
+                 mlp_interval=1, outlet=OutletDensityInterpolated, omega_dumping=(-1.0, -1.0)):
         nx, ny, nz = shape
         self.shape = (int(nx), int(ny), int(nz))
         self.N = nx * ny * nz
@@ -158,7 +182,7 @@ class Solver:
                                     closure=turbulence.code, storage=STORAGE[storage],
                                     inlet_kind=inlet.code, nu=nu, tau=tau, cles=cles, force=force,
                                     rho0=rho0, f16_scale_log2=f16_scale_log2, device=device, options=options,
-                                    mlp_interval=mlp_interval)
+                                    mlp_interval=mlp_interval, outlet_kind=outlet.code, omega_dumping=omega_dumping)
         self._ctx = C.c_void_p()
         check(lib().lbm_create(C.byref(self.cfg), C.byref(self._ctx)))
 
@@ -195,6 +219,12 @@ class Solver:
         ai = (capi.LbmBcInlet * max(ni, 1))(*inlets)
         ao = (capi.LbmBcOutlet * max(no, 1))(*outlets)
         self._check(lib().lbm_set_bc(self._ctx, ai, ni, ao, no))
+
+    def set_symmetry(self, records=()):
+        """BounceSymmetryHalf records (capi.make_symmetry) of -2 nodes; call after set_bc."""
+        n = len(records)
+        a = (capi.LbmBcSymmetry * max(n, 1))(*records)
+        self._check(lib().lbm_set_symmetry(self._ctx, a, n))
 
     def init_equilibrium(self, rho0=1.0, u0=(0.0, 0.0, 0.0)):
         u = np.asarray(u0, dtype=np.float64)
@@ -301,11 +331,12 @@ class SolverTurbulentLES:
                  NonDim=NonDimensiolnaliseFactorsVelocity, TimeAvg=MomentTimeAvg, *, constants, data):
         if Model is not D3Q27:
             raise NotImplementedError("only D3Q27 is implemented")
-        if Symmetry is not NoSymmetry:
-            raise NotImplementedError("symmetry boundaries are not implemented")
+        if Symmetry not in (NoSymmetry, BounceSymmetryHalf):
+            raise NotImplementedError(f"symmetry policy {Symmetry.__name__} is not implemented")
         self.C = constants
         self.data = data
-        self.policies = dict(Collision=Collision, Turbulence=Turbulence, Inlet=Inlet)
+        self.policies = dict(Collision=Collision, Turbulence=Turbulence, Inlet=Inlet, Outlet=Outlet,
+                             Symmetry=Symmetry)
         self.solver = None
 
     def convertToLattice(self, verbose=False):
@@ -316,9 +347,13 @@ class SolverTurbulentLES:
         self.solver = Solver(d["flags"].shape[::-1], collision=self.policies["Collision"],
                              turbulence=self.policies["Turbulence"], inlet=self.policies["Inlet"],
                              storage=c.get("storage", "f32"), nu=c["nu"], cles=c.get("CLES", 0.173),
-                             periodic=c.get("periodic", (0, 0, 0)), force=c.get("force", (0.0, 0.0, 0.0)))
+                             periodic=c.get("periodic", (0, 0, 0)), force=c.get("force", (0.0, 0.0, 0.0)),
+                             outlet=self.policies["Outlet"],
+                             omega_dumping=(c.get("omegaDumpingLow", -1.0), c.get("omegaDumpingHigh", -1.0)))
         self.solver.set_flags(d["flags"])
         self.solver.set_bc(d.get("inlets", ()), d.get("outlets", ()))
+        if self.policies["Symmetry"] is BounceSymmetryHalf:
+            self.solver.set_symmetry(d.get("symmetry", ()))
         self.solver.init_equilibrium(c.get("rho0", 1.0), c.get("VelocityInit", (0.0, 0.0, 0.0)))
 
     def runSimulation(self):

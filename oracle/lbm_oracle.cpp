@@ -56,12 +56,28 @@ static const int CREV_OK[27] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14,
 static const int CREV_REF[27] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14,
                                  13, 16, 15, 18, 17, 20, 21, 22, 21, 24, 23, 26, 25};
 
+// the y mirror of each direction: (c_x, -c_y, c_z).  The reference's c_sym_y (D3Q27.h:162-190) maps
+// seven directions elsewhere; ref_compat uses its entries there.
+static int sym_y_ok(int v) {
+    for (int w = 0; w < 27; w++)
+        if (C[w][0] == C[v][0] && C[w][1] == -C[v][1] && C[w][2] == C[v][2]) return w;
+    return -1;
+}
+static int sym_y_ref(int v) {
+    switch (v) {
+        case 11: return 16; case 12: return 15; case 19: return 19; case 20: return 23;
+        case 22: return 22; case 23: return 21; case 24: return 20;
+        default: return sym_y_ok(v);
+    }
+}
+
 template <class R>
 struct Sim {
     int nx, ny, nz;
     size_t N;
     int wrap[3];
-    int collision, closure, inlet_kind, ref_compat;
+    int collision, closure, inlet_kind, outlet_kind, ref_compat;
+    double dump_low, dump_high;
     R tau, nu, cles, F[3], cs;
     R w[27];
     const int* crev;
@@ -78,16 +94,19 @@ struct Sim {
     struct Inlet { int x, y, z; R n[3], v[3]; int regular; };
     struct Outlet { int x, y, z; R n[3], density; int regular; };
     struct Per { int x, y, z; R n[3]; int idx, regular; };
+    struct Sym { int x, y, z; R n[3]; int regular; };
     std::vector<Wall> walls;
     std::vector<Inlet> inlets;
     std::vector<Outlet> outlets;
     std::vector<Per> pers;
+    std::vector<Sym> syms;
 
     Sim(const lbm_config& c, int refc) {
         nx = c.nx; ny = c.ny; nz = c.nz;
         N = (size_t)nx * ny * nz;
         for (int a = 0; a < 3; a++) wrap[a] = c.periodic[a];
         collision = c.collision; closure = c.closure; inlet_kind = c.inlet_kind; ref_compat = refc;
+        outlet_kind = c.outlet_kind; dump_low = c.omega_dumping_low; dump_high = c.omega_dumping_high;
         nu = (R)c.nu;
         tau = c.tau > 0 ? (R)c.tau : (R)(3.0 * c.nu + 0.5);
         cles = (R)c.cles;
@@ -133,6 +152,11 @@ struct Sim {
                     int32_t m = mesh[id(i, j, k)];
                     if (m > thr) walls.push_back({i, j, k, m > 10 ? 0 : 1});
                 }
+        // -2 nodes are not wall nodes in the reference (compileBoundaryArrayWall erases them,
+        // geometryMesherBoundary.h:533-550), so their links from solid cells keep their old value;
+        // corrected: symmetry nodes bounce back on those links
+        if (!ref_compat)
+            for (const Sym& sy : syms) walls.push_back({sy.x, sy.y, sy.z, 0});
     }
 
     // ---- InitializationEquilibriumConstVector.h:103-224 (lattice units) ------------------
@@ -532,6 +556,127 @@ struct Sim {
         }
     }
 
+    // ---- OutletNeighbourEquilibriumOmega(RF)::outletOmega, :18-79 ----------------------------
+    // omega -= (high - low) / width * (distance from the sponge's first plane) over the last
+    // ceil(10 %) of the lattice along the first outlet's normal axis (always at the high end)
+    void outlet_omega() {
+        const Outlet& o0 = outlets[0];
+        float n[3], pl[3];
+        for (int a = 0; a < 3; a++) { n[a] = (float)o0.n[a]; pl[a] = std::fabs(std::fabs(n[a]) - 1.f); }
+        const int dims[3] = {nx, ny, nz};
+        int d01[3], dimA[3], beg[3];
+        for (int a = 0; a < 3; a++) {
+            d01[a] = (int)std::ceil((float)dims[a] * 0.1f);
+            dimA[a] = (int)((float)d01[a] * std::fabs(n[a]) + (float)dims[a] * std::fabs(pl[a]));
+            beg[a] = dims[a] - dimA[a];
+        }
+        const int interval = (int)std::fabs((float)d01[0] * n[0] + (float)d01[1] * n[1] + (float)d01[2] * n[2]);
+        const R der = ((R)dump_high - (R)dump_low) / (R)interval;
+#pragma omp parallel for collapse(2) schedule(static)
+        for (int k = beg[2]; k < nz; k++)
+            for (int j = beg[1]; j < ny; j++)
+                for (int i = beg[0]; i < nx; i++) {
+                    const int pos = (int)((float)(i - beg[0]) * n[0] * n[0] + (float)(j - beg[1]) * n[1] * n[1] +
+                                          (float)(k - beg[2]) * n[2] * n[2]);
+                    omega[id(i, j, k)] = omega[id(i, j, k)] - der * (R)pos;
+                }
+    }
+
+    // ---- InletVelocityZouHe.h:85-97 -------------------------------------------------------
+    void inlet_zou_he() {
+#pragma omp parallel for schedule(static)
+        for (long long e = 0; e < (long long)inlets.size(); e++) {
+            const Inlet& in = inlets[e];
+            size_t c = id(in.x, in.y, in.z);
+            for (int v = 0; v < 27; v++)
+                if (in.n[0] * C[v][0] + in.n[1] * C[v][1] + in.n[2] * C[v][2] > 0) {
+                    R fneq = dfp[v * N + c] - feq(u[0][c], u[1][c], u[2][c], rho[c], v);
+                    df[crev[v] * N + c] = fneq + feq(in.v[0], in.v[1], in.v[2], rho[c], crev[v]);
+                }
+        }
+    }
+
+    // ---- OutletNeighbourEquilibrium.h:93-125 (RF: OutletNeighbourEquilibriumOmegaRF.h:151-155) ----
+    // entering links f_v = f_eq_v(u, rho_b) + (f_eq_v - f_v)(x + c_v), f_v(x + c_v) being the
+    // population that x itself streamed there: its non-equilibrium part enters with the opposite sign,
+    // which damps it (with the same sign the outlet feeds each link its own last value, and a perturbed
+    // duct diverges within 50 steps)
+    void outlet_neighbour_equilibrium(bool rf) {
+#pragma omp parallel for schedule(static)
+        for (long long e = 0; e < (long long)outlets.size(); e++) {
+            const Outlet& ot = outlets[e];
+            size_t c = id(ot.x, ot.y, ot.z);
+            R dens = ot.density;
+            if (rf && u[0][c] < 0) dens = (R)((double)dens - 0.5 * (double)u[0][c] * (double)u[0][c] * (double)dens);
+            for (int v = 0; v < 27; v++) {
+                if (!(ot.n[0] * C[v][0] + ot.n[1] * C[v][1] + ot.n[2] * C[v][2] < 0)) continue;
+                int a = nb(ot.x, C[v][0], 0), b = nb(ot.y, C[v][1], 1), g = nb(ot.z, C[v][2], 2);
+                if (!ot.regular && !(mesh_at(a, b, g) > 0)) continue;
+                size_t q = id(a, b, g);
+                R fen = feq(u[0][q], u[1][q], u[2][q], rho[q], v);
+                R fn = df[v * N + q];
+                R fbc = feq(u[0][c], u[1][c], u[2][c], dens, v);
+                df[v * N + c] = fbc + (fen - fn);
+            }
+        }
+    }
+
+    // ---- OutletDensityEquilibrium.h:57-70: entering links at f_eq(u, rho_b); the reference takes the
+    // equilibrium of the outgoing direction v for slot c_rev[v] (:66), reproduced with ref_compat
+    void outlet_density_equilibrium() {
+#pragma omp parallel for schedule(static)
+        for (long long e = 0; e < (long long)outlets.size(); e++) {
+            const Outlet& ot = outlets[e];
+            size_t c = id(ot.x, ot.y, ot.z);
+            for (int v = 0; v < 27; v++)
+                if (ot.n[0] * C[v][0] + ot.n[1] * C[v][1] + ot.n[2] * C[v][2] > 0)
+                    df[crev[v] * N + c] = feq(u[0][c], u[1][c], u[2][c], ot.density, ref_compat ? v : crev[v]);
+        }
+    }
+
+    // ---- BounceSymmetryHalf.h:84-131 (y normals; the x and z branches are commented out) ---------
+    // links entering across the plane take f*_{sym v} of the in-plane cell s = x - (c_x, 0, c_z).
+    // Irregular nodes: a solid s bounces back; with ref_compat also on every link whose in-plane
+    // projection is solid (:127-130), and a -2 s gets the extra write df(s, sym(c_rev v)) = f*(s, c_rev v)
+    // (:117-121), which races with s's own rule in the reference; here it runs after all rules.
+    void symmetry_half() {
+        std::vector<char> done(syms.size(), 0);
+#pragma omp parallel for schedule(static)
+        for (long long e = 0; e < (long long)syms.size(); e++) {
+            const Sym& sy = syms[e];
+            if (!(sy.n[0] == 0 && std::fabs((double)sy.n[1]) == 1 && sy.n[2] == 0)) continue;  // "Fail." (:158-161)
+            done[e] = 1;
+            size_t c = id(sy.x, sy.y, sy.z);
+            for (int v = 0; v < 27; v++) {
+                int a = nb(sy.x, -C[v][0], 0), g = nb(sy.z, -C[v][2], 2);
+                int sv = ref_compat ? sym_y_ref(v) : sym_y_ok(v);
+                bool across = sy.n[1] * C[v][1] < 0;
+                if (sy.regular) {
+                    if (across) df[v * N + c] = dfp[sv * N + id(a, sy.y, g)];
+                    continue;
+                }
+                int32_t m = mesh_at(a, sy.y, g);
+                if (m != 0) {
+                    if (across) df[v * N + c] = dfp[sv * N + id(a, sy.y, g)];
+                } else if (across || ref_compat) {
+                    df[v * N + c] = dfp[crev[v] * N + c];
+                }
+            }
+        }
+        if (!ref_compat) return;
+        for (size_t e = 0; e < syms.size(); e++) {
+            const Sym& sy = syms[e];
+            if (!done[e] || sy.regular) continue;
+            for (int v = 0; v < 27; v++) {
+                int a = nb(sy.x, -C[v][0], 0), g = nb(sy.z, -C[v][2], 2);
+                if (sy.n[1] * C[v][1] < 0 && mesh_at(a, sy.y, g) == -2) {
+                    size_t sc = id(a, sy.y, g);
+                    df[sym_y_ref(crev[v]) * N + sc] = dfp[crev[v] * N + sc];
+                }
+            }
+        }
+    }
+
     // ---- Periodic.h:43-138 (ghost-plane form) ----------------------------------------------
     void periodic_ghost() {
 #pragma omp parallel for schedule(static)
@@ -591,11 +736,23 @@ struct Sim {
     // ---- SolverTurbulentLES::runSimulation loop body, SolverTurbulentLES.h:186-226 --------
     void step() {
         if (closure == LBM_CLOSURE_SMAGORINSKY) omega_les(); else omega_no();
+        if (!outlets.empty() && (outlet_kind == LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA ||
+                                 outlet_kind == LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA_RF))
+            outlet_omega();
         collide_all();
         streaming_ab();
         bounce_back_wall();
-        if (!inlets.empty()) { if (inlet_kind == LBM_INLET_MOVING_WALL) inlet_moving_wall(); else inlet_equilibrium(); }
-        if (!outlets.empty()) outlet_density_interpolated();
+        if (!inlets.empty()) {
+            if (inlet_kind == LBM_INLET_MOVING_WALL) inlet_moving_wall();
+            else if (inlet_kind == LBM_INLET_ZOU_HE) inlet_zou_he();
+            else inlet_equilibrium();
+        }
+        if (!outlets.empty()) {
+            if (outlet_kind == LBM_OUTLET_DENSITY_INTERPOLATED) outlet_density_interpolated();
+            else if (outlet_kind == LBM_OUTLET_DENSITY_EQUILIBRIUM) outlet_density_equilibrium();
+            else outlet_neighbour_equilibrium(outlet_kind == LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA_RF);
+        }
+        if (!syms.empty()) symmetry_half();
         if (!pers.empty()) periodic_ghost();
         moment_update();
         if (a_on) timeavg_add();
@@ -712,7 +869,8 @@ int orc_set_bc(void* p, const lbm_bc_inlet* in, int nin, const lbm_bc_outlet* ou
     Handle* h = (Handle*)p;
     DISPATCH(h, {
         using SR = std::remove_pointer_t<decltype(S)>;
-        S->inlets.clear(); S->outlets.clear();
+        S->inlets.clear(); S->outlets.clear(); S->syms.clear();
+        S->build_wall_list();
         for (int e = 0; e < nin; e++) {
             typename SR::Inlet r;
             r.x = in[e].vertex.x; r.y = in[e].vertex.y; r.z = in[e].vertex.z;
@@ -727,6 +885,22 @@ int orc_set_bc(void* p, const lbm_bc_inlet* in, int nin, const lbm_bc_outlet* ou
             r.density = out[e].density; r.regular = out[e].regular;
             S->outlets.push_back(r);
         }
+    });
+    return 0;
+}
+int orc_set_symmetry(void* p, const lbm_bc_symmetry* rec, int n) {
+    Handle* h = (Handle*)p;
+    DISPATCH(h, {
+        using SR = std::remove_pointer_t<decltype(S)>;
+        S->syms.clear();
+        for (int e = 0; e < n; e++) {
+            typename SR::Sym r;
+            r.x = rec[e].vertex.x; r.y = rec[e].vertex.y; r.z = rec[e].vertex.z;
+            for (int a = 0; a < 3; a++) r.n[a] = rec[e].normal[a];
+            r.regular = rec[e].regular;
+            S->syms.push_back(r);
+        }
+        S->build_wall_list();
     });
     return 0;
 }
@@ -757,7 +931,7 @@ int orc_init_equilibrium(void* p, double rho0, const double* u0) {
     });
     return 0;
 }
-// rho: N, u: 3N component-major; then df = df_post = feq (init_df)
+// rho: N, u: 3N component-major (inlet nodes take their record velocity); then df = df_post = feq (init_df)
 int orc_init_fields(void* p, const double* rho, const double* u) {
     Handle* h = (Handle*)p;
     DISPATCH(h, {
@@ -766,6 +940,10 @@ int orc_init_fields(void* p, const double* rho, const double* u) {
                 S->rho[c] = rho[c];
                 for (int a = 0; a < 3; a++) S->u[a][c] = u[a * S->N + c];
             } else { S->rho[c] = 0; for (int a = 0; a < 3; a++) S->u[a][c] = 0; }
+        }
+        for (auto& in : S->inlets) {  // inletVelocities, InitializationEquilibriumVariables.h:140-154
+            size_t c = S->id(in.x, in.y, in.z);
+            for (int a = 0; a < 3; a++) S->u[a][c] = in.v[a];
         }
         S->init_df_from_moments();
         S->force_consistent_moments();

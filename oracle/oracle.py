@@ -9,7 +9,7 @@ import os
 import numpy as np
 
 from . import build as _build
-from lb_gb300.capi import LbmConfig, LbmBcInlet, LbmBcOutlet, LbmDiag  # plain ctypes structs
+from lb_gb300.capi import LbmConfig, LbmBcInlet, LbmBcOutlet, LbmBcSymmetry, LbmDiag  # plain ctypes structs
 
 _lib = None
 
@@ -30,6 +30,7 @@ def lib():
         L.orc_set_flags.argtypes = [vp, ip]
         L.orc_set_bc.argtypes = [vp, C.POINTER(LbmBcInlet), i32, C.POINTER(LbmBcOutlet), i32]
         L.orc_set_periodic_list.argtypes = [vp, ip, i32]
+        L.orc_set_symmetry.argtypes = [vp, C.POINTER(LbmBcSymmetry), i32]
         L.orc_init_equilibrium.argtypes = [vp, f64, dp]
         L.orc_init_fields.argtypes = [vp, dp, dp]
         L.orc_step.argtypes = [vp, i32]
@@ -92,6 +93,11 @@ class OracleSim:
         ai = (LbmBcInlet * max(ni, 1))(*inlets)
         ao = (LbmBcOutlet * max(no, 1))(*outlets)
         lib().orc_set_bc(self.h, ai, ni, ao, no)
+
+    def set_symmetry(self, records=()):
+        n = len(records)
+        a = (LbmBcSymmetry * max(n, 1))(*records)
+        lib().orc_set_symmetry(self.h, a, n)
 
     def set_periodic_list(self, recs):
         r = np.ascontiguousarray(recs, dtype=np.int32).reshape(-1, 8)

@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol(built_lib):
 
 def test_status_strings_and_abi(built_lib):
     L = capi.lib()
-    assert L.lbm_abi_version() == 2
+    assert L.lbm_abi_version() == 3
     assert L.lbm_status_string(capi.LBM_ERR_NONFINITE) == b"non-finite populations"
 
 

@@ -16,7 +16,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def test_driver_is_built_and_reports_the_abi(built_lib):
     r = subprocess.run([build.DRIVER, "--help"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0
-    assert "ABI version 2" in r.stdout
+    assert "ABI version 3" in r.stdout
 
 
 def test_unsupported_policy_does_not_compile():
@@ -24,11 +24,11 @@ def test_unsupported_policy_does_not_compile():
     src = r'''
 #include "lbm_solver.hpp"
 using namespace lbm_gb300;
-struct BounceSymmetryHalf {};
+struct BounceSymmetryFull {};
 int main() {
     LBMConstants C; LBMData D;
     SolverTurbulentLES<D3Q27, InitializationEquilibriumConstVector, CollisionCumD3Q27Turbulent2015, StreamingAB,
-                       BounceBackWallHalf, BounceSymmetryHalf, NoPeriodic, InletVelocityMovingWall,
+                       BounceBackWallHalf, BounceSymmetryFull, NoPeriodic, InletVelocityMovingWall,
                        OutletDensityInterpolated, MomentDensityVelocityN27, OmegaLES, ErrorQuadratic,
                        NonDimensiolnaliseFactorsVelocity, MomentTimeAvg> s(C, D);
     return 0;
@@ -41,7 +41,7 @@ int main() {
         r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), p],
                            capture_output=True, text=True)
     assert r.returncode != 0
-    assert "symmetry planes are not implemented" in r.stderr
+    assert "symmetry: NoSymmetry or BounceSymmetryHalf" in r.stderr
 
 
 @pytest.mark.gpu
