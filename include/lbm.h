@@ -231,6 +231,32 @@ lbm_status lbm_mesh_matrix_read(const char* path, int32_t* flags, int64_t capaci
                                 double* resolution, double* additional, double bbox[6]);
 const char* lbm_mesh_matrix_last_error(void);
 
+/* ---- legacy VTK field files and the probe CSV (postprocesors/outputerVTK.h:26-851) ----------------
+ * lbm_vtk_write gives the reference's structured-points layout: "# vtk DataFile Version 2.0", the title
+ * (the reference writes "LBE variables", or "LBE <name>" for the mesh), "ASCII", "DATASET
+ * STRUCTURED_POINTS", "DIMENSIONS nx ny nz", "ASPECT_RATIO" 1/resolution three times, "ORIGIN"
+ * bbmin - (additional - 0.5)/resolution per axis, "POINT_DATA N", then per field "SCALARS <name> double 1"
+ * + "LOOKUP_TABLE default" or "VECTORS <name> double", one point per line, x fastest.  Each value is
+ * the field rounded to float times the float scale (the reference's Crho, Cpressure, Cu; 1 for lattice
+ * units), printed as an ostream prints a float (6 significant digits).  The writers of the reference map
+ * onto fields as: MeshVTK {object: flags}; variablesVTK {rho*Crho, p*Cpressure, U*Cu};
+ * variablesLatticeVTK {rho, pressure, U}; the time-averaged ones the same on the means, with pressure
+ * rho*cs2; omegaVTK {Omega}; distributionFunctionVTK and tauVTK one scalar each. */
+typedef struct lbm_vtk_field {
+    const char* name;        /* no spaces */
+    int32_t components;      /* 1: SCALARS; 3: VECTORS, data component-major (x[N], y[N], z[N]) */
+    const double* data;      /* N (or 3N) values, x fastest */
+    double scale;
+} lbm_vtk_field;
+lbm_status lbm_vtk_write(const char* path, const char* title, const int32_t dims[3], double resolution,
+                         double additional, const double bbmin[3], const lbm_vtk_field* fields, int32_t nfields);
+/* probeWriteOut: appends "ux,uy,uz,rho,pressure" of one lbm_probe sample (u_x, u_y, u_z, rho) times Cu,
+ * Crho and cs2*Cpressure; a new file starts with "Sampling frequency is: <Ct * probe_every_it>" and the
+ * column line.  The path is used as given (the reference writes ./results/probeData.csv). */
+lbm_status lbm_probe_csv_append(const char* path, double sampling_period, const double sample[4], double cu,
+                                double crho, double cpressure);
+const char* lbm_vtk_last_error(void);
+
 /* ---- OFF voxelizer on the GPU (preprocess geometryMesherOFF.h:45-112) -------- */
 /* Reads an OFF/NOFF file; dims_out = ceil((BBmax-BBmin)*res + 2*add) per axis and bbox_out
  * (xmin,ymin,zmin,xmax,ymax,zmax).  flags_out (nullable: query dims only) receives

@@ -77,6 +77,14 @@ struct LBMConstants {
     const lbm_mlp_model* mlp = nullptr;
     // outlet sponge of OutletNeighbourEquilibriumOmega(RF) (LBMConstants.h:74-76; -1: none)
     double omegaDumpingLow = -1.0, omegaDumpingHigh = -1.0;
+    // output as the reference's loop writes it (SolverTurbulentLES.h:225-263): results/variables.<k/plot>.vtk
+    // every plot_every_it steps, results/variablesTimeAvg.vtk after the average, results/probeData.csv per
+    // probe sample.  No files while results_dir is empty.
+    int plot_every_it = -1;
+    std::string results_dir;
+    double Crho = 1.0, Cpressure = 1.0, Cu = 1.0, Ct = 1.0;     // conversion factors (physical / lattice)
+    double resolution_factor = 1.0, additional_factor = 0.5;   // VTK header geometry (geometry mesher)
+    double BBmin[3] = {0.0, 0.0, 0.0};
 };
 
 struct LBMData {
@@ -191,6 +199,27 @@ public:
                         Constants.ProbeLocationLat[2], out),
               ctx, "lbm_probe");
         Data.probe.insert(Data.probe.end(), out, out + 4);
+        if (!Constants.results_dir.empty()) {
+            const std::string path = Constants.results_dir + "/probeData.csv";
+            const lbm_status st = lbm_probe_csv_append(path.c_str(), Constants.Ct * Constants.probe_every_it, out,
+                                                       Constants.Cu, Constants.Crho, Constants.Cpressure);
+            if (st != LBM_OK) throw Error(st, std::string("lbm_probe_csv_append: ") + lbm_vtk_last_error());
+        }
+    }
+
+    // outputerVTK::variablesVTK / variablesTimeAvgVTK (outputerVTK.h:59-187, :318-447): rho Crho,
+    // p Cpressure (p = rho cs2) and U Cu, structured points
+    void writeVTK(const std::string& path, const std::vector<double>& rho, const std::vector<double>& u,
+                  bool time_avg) {
+        std::vector<double> p(rho.size());
+        for (size_t i = 0; i < rho.size(); i++) p[i] = rho[i] / 3.0;
+        const lbm_vtk_field f[3] = {{"rho", 1, rho.data(), Constants.Crho},
+                                    {time_avg ? "pressure" : "p", 1, p.data(), Constants.Cpressure},
+                                    {"U", 3, u.data(), Constants.Cu}};
+        const int32_t dims[3] = {Constants.dimX_int, Constants.dimY_int, Constants.dimZ_int};
+        const lbm_status st = lbm_vtk_write(path.c_str(), "LBE variables", dims, Constants.resolution_factor,
+                                            Constants.additional_factor, Constants.BBmin, f, 3);
+        if (st != LBM_OK) throw Error(st, std::string("lbm_vtk_write: ") + lbm_vtk_last_error());
     }
 
     // the reference's step loop (SolverTurbulentLES.h:179-268).  After step k: the state is added to the
@@ -208,6 +237,11 @@ public:
                    k >= it - Constants.probe_iterations;
         };
         auto err_after = [&](int k) { return Constants.err_every_it > 0 && k % Constants.err_every_it == 0 && k != 0; };
+        auto plot_after = [&](int k) {
+            return !Constants.results_dir.empty() && Constants.plot_every_it > 0 && k % Constants.plot_every_it == 0 &&
+                   k != 0;
+        };
+        const size_t N = (size_t)Constants.dimX_int * Constants.dimY_int * Constants.dimZ_int;
         bool averaging = false;
         int k = 0;  // steps done
         while (k < it) {
@@ -216,7 +250,9 @@ public:
                 averaging = true;
             }
             int j = k;  // the last step of this batch: the first with an event after it
-            while (j < it - 1 && !probe_after(j) && !err_after(j) && !(avg > 0 && !averaging && j + 1 >= avg_begin)) j++;
+            while (j < it - 1 && !probe_after(j) && !err_after(j) && !plot_after(j) &&
+                   !(avg > 0 && !averaging && j + 1 >= avg_begin))
+                j++;
             check(lbm_step(ctx, j - k + 1), ctx, "lbm_step");
             k = j + 1;
             if (probe_after(j)) probeWrite();
@@ -227,10 +263,16 @@ public:
                 Data.errors.push_back(e);
                 if (std::isnan(e)) break;
             }
+            if (plot_after(j)) {
+                Data.rho.resize(N);
+                Data.u.resize(3 * N);
+                check(lbm_get_moments(ctx, Data.rho.data(), Data.u.data()), ctx, "lbm_get_moments");
+                writeVTK(Constants.results_dir + "/variables." + std::to_string(j / Constants.plot_every_it) + ".vtk",
+                         Data.rho, Data.u, false);
+            }
         }
         if (averaging) check(lbm_timeavg_end(ctx), ctx, "lbm_timeavg_end");
         check(lbm_synchronize(ctx), ctx, "lbm_synchronize");
-        const size_t N = (size_t)Constants.dimX_int * Constants.dimY_int * Constants.dimZ_int;
         Data.rho.resize(N);
         Data.u.resize(3 * N);
         check(lbm_get_moments(ctx, Data.rho.data(), Data.u.data()), ctx, "lbm_get_moments");
@@ -240,6 +282,8 @@ public:
             Data.uuTimeAvg.resize(6 * N);
             check(lbm_timeavg_get(ctx, Data.rhoTimeAvg.data(), Data.uTimeAvg.data(), Data.uuTimeAvg.data(), nullptr),
                   ctx, "lbm_timeavg_get");
+            if (!Constants.results_dir.empty())
+                writeVTK(Constants.results_dir + "/variablesTimeAvg.vtk", Data.rhoTimeAvg, Data.uTimeAvg, true);
         }
     }
 

@@ -92,6 +92,11 @@ class LbmBcSymmetry(C.Structure):
     _fields_ = [("vertex", LbmVertex), ("normal", C.c_float * 3), ("regular", C.c_int32)]
 
 
+class LbmVtkField(C.Structure):
+    _fields_ = [("name", C.c_char_p), ("components", C.c_int32), ("data", C.POINTER(C.c_double)),
+                ("scale", C.c_double)]
+
+
 class LbmDiag(C.Structure):
     _fields_ = [("mass", C.c_double), ("momentum", C.c_double * 3), ("drag", C.c_double * 3),
                 ("max_speed", C.c_double), ("nonfinite", C.c_int64), ("fluid_cells", C.c_int64),
@@ -208,6 +213,9 @@ def lib():
         "lbm_mesh_matrix_write": ([C.c_char_p, ip, ip, f64, f64, dp], i32),
         "lbm_mesh_matrix_read": ([C.c_char_p, ip, i64, ip, dp, dp, dp], i32),
         "lbm_mesh_matrix_last_error": ([], C.c_char_p),
+        "lbm_vtk_write": ([C.c_char_p, C.c_char_p, ip, f64, f64, dp, C.POINTER(LbmVtkField), i32], i32),
+        "lbm_probe_csv_append": ([C.c_char_p, f64, dp, f64, f64, f64], i32),
+        "lbm_vtk_last_error": ([], C.c_char_p),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

@@ -3,6 +3,8 @@
 // which sets LBMConstants, meshes the geometry and calls initializeSimulation / runSimulation.
 //
 //   lbm_run cavity  [--n 64] [--steps 10000] [--re 1000] [--ulid 0.05] [--storage f64|f32|f16dev] [--out DIR]
+//                   [--plot K]  (both cases: DIR/variables.<i>.vtk every K steps, DIR/variablesTimeAvg.vtk after
+//                                the average, in lattice units, as the reference's outputerVTK writes them)
 //   lbm_run channel [--nx 256 --ny 130 --nz 128] [--steps 20000] [--avg 5000] [--storage ...]
 //                   [--re-tau 180] [--umax 0.05] [--amp 0.05] [--mlp model.bin] [--mlp-interval 1] [--out DIR]
 //
@@ -83,6 +85,8 @@ int run_cavity(const Args& a) {
     C.iterations = a.inum("steps", 10000);
     C.storage = storage_of(a.get("storage", "f64"));
     C.err_every_it = a.inum("err-every", 1000);
+    C.plot_every_it = a.inum("plot", -1);
+    if (C.plot_every_it > 0) C.results_dir = a.get("out", ".");
     const size_t N = (size_t)n * n * n;
     D.meshFluid.assign(N, 1);
     auto at = [&](int i, int j, int k) -> int32_t& { return D.meshFluid[(size_t)i + (size_t)n * ((size_t)j + (size_t)n * k)]; };
@@ -143,6 +147,8 @@ int run_channel(const Args& a) {
     C.iterationsMomentAvg = a.inum("avg", C.iterations / 4);
     C.storage = storage_of(a.get("storage", "f32"));
     C.mlp_interval = a.inum("mlp-interval", 1);
+    C.plot_every_it = a.inum("plot", -1);
+    if (C.plot_every_it > 0) C.results_dir = a.get("out", ".");
     const size_t N = (size_t)nx * ny * nz;
     D.meshFluid.assign(N, 1);
     for (int k = 0; k < nz; k++)

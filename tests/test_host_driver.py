@@ -65,6 +65,33 @@ def test_driver_cavity_equals_python_api(built_lib):
 
 
 @pytest.mark.gpu
+def test_driver_writes_the_reference_vtk_dumps(built_lib):
+    """runSimulation with plot_every_it = 10 writes variables.1.vtk after step index 10 (11 steps) and
+    variables.2.vtk after 21 steps, as SolverTurbulentLES.h:246-252 does; the dumped U equals the Python
+    API's state after the same steps to the file's 6 digits."""
+    n, steps = 12, 21
+    with tempfile.TemporaryDirectory() as d:
+        r = subprocess.run([build.DRIVER, "cavity", "--n", str(n), "--steps", str(steps), "--storage", "f64",
+                            "--err-every", "0", "--plot", "10", "--out", d], capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+        assert sorted(f for f in os.listdir(d) if f.endswith(".vtk")) == ["variables.1.vtk", "variables.2.vtk"]
+        lines = open(os.path.join(d, "variables.2.vtk")).read().splitlines()
+    N = n ** 3
+    assert lines[0] == "# vtk DataFile Version 2.0" and lines[4] == f"DIMENSIONS {n} {n} {n}"
+    i = lines.index("VECTORS U double")
+    U = np.array([[float(t) for t in l.split()] for l in lines[i + 1:i + 1 + N]]).T
+    c = cases.cavity(n)
+    s = Solver((n, n, n), turbulence=OmegaNo, storage="f64", nu=c["nu"])
+    s.set_flags(c["flags"])
+    s.set_bc(c["inlets"])
+    s.init_equilibrium(1.0, (0.0, 0.0, 0.0))
+    s.step(steps)
+    _, u = s.moments()
+    s.close()
+    assert np.allclose(U, u, rtol=6e-6, atol=1e-12)  # 6 significant digits: up to 5e-6 relative
+
+
+@pytest.mark.gpu
 def test_driver_channel_profile_equals_python_api(built_lib):
     nx, ny, nz, steps, avg = 64, 34, 32, 200, 50
     with tempfile.TemporaryDirectory() as d:

@@ -1,0 +1,77 @@
+"""The legacy VTK writer and probe CSV (outputerVTK.h:26-851) on the CPU: the bytes of a small file equal
+the layout restated independently here (float values, 6 significant digits, x fastest), and the
+outputerVTK helpers name their fields as the reference does."""
+import numpy as np
+
+from lb_gb300 import output
+
+
+def g6(v):
+    return "%.6g" % float(np.float32(v))
+
+
+def expected(title, dims, res, add, bbmin, fields):
+    nx, ny, nz = dims
+    N = nx * ny * nz
+    r = np.float32(res)
+    asp = g6(np.float32(1.0) / r)
+    org = ["%.6g" % (float(np.float32(b)) - (float(np.float32(add)) - 0.5) / float(r)) for b in bbmin]
+    s = ["# vtk DataFile Version 2.0", title, "ASCII", "DATASET STRUCTURED_POINTS",
+         "DIMENSIONS %d %d %d" % dims, "ASPECT_RATIO %s %s %s" % (asp, asp, asp), "ORIGIN " + " ".join(org),
+         "POINT_DATA %d" % N]
+    for name, a, sc in fields:
+        a = np.asarray(a, dtype=np.float64).reshape(-1)
+        vals = (a.astype(np.float32) * np.float32(sc)).astype(np.float32)
+        if a.size == N:
+            s += ["SCALARS %s double 1" % name, "LOOKUP_TABLE default"] + [g6(v) for v in vals]
+        else:
+            v3 = vals.reshape(3, N)
+            s += ["VECTORS %s double" % name] + [" ".join(g6(v3[c, q]) for c in range(3)) for q in range(N)]
+    return "\n".join(s) + "\n"
+
+
+def test_vtk_bytes_follow_the_reference_layout(built_lib, tmp_path):
+    dims = (3, 2, 2)
+    N = 12
+    rng = np.random.default_rng(4)
+    rho = 1.0 + 0.01 * rng.standard_normal(N)
+    u = 0.05 * rng.standard_normal(3 * N)
+    grid = output.Grid(dims, resolution=75.0, additional=3.0, bbmin=(-0.1, 0.0, 0.02))
+    conv = {"Crho": 1.293, "Cpressure": 2.5e3, "Cu": 46.78}
+    p = tmp_path / "variables.1.vtk"
+    output.outputerVTK.variablesVTK(p, grid, rho, u, conv)
+    want = expected("LBE variables", dims, 75.0, 3.0, (-0.1, 0.0, 0.02),
+                    [("rho", rho, 1.293), ("p", rho / 3.0, 2.5e3), ("U", u, 46.78)])
+    assert p.read_text() == want
+
+
+def test_mesh_and_scalar_writers(built_lib, tmp_path):
+    dims = (4, 3, 2)
+    flags = np.array([0, 1, 10, -2] * 6, dtype=np.int32)
+    grid = output.Grid(dims)
+    p = tmp_path / "mesh.vtk"
+    output.outputerVTK.MeshVTK(p, grid, flags, "BackwardStep")
+    lines = p.read_text().splitlines()
+    assert lines[1] == "LBE BackwardStep" and lines[8] == "SCALARS object double 1"
+    assert lines[10:14] == ["0", "1", "10", "-2"] and len(lines) == 10 + 24
+    f = np.arange(27 * 24, dtype=np.float64).reshape(27, 24) * 1e-3
+    output.outputerVTK.distributionFunctionVTK(p, grid, f, 19)
+    lines = p.read_text().splitlines()
+    assert lines[8] == "SCALARS DFunciton_19 double 1" and lines[10] == g6(f[19, 0])
+    output.outputerVTK.tauVTK(p, grid, np.full(24, 1.8))
+    lines = p.read_text().splitlines()
+    assert lines[8] == "SCALARS Tau double 1" and lines[10] == g6(np.float32(1) / np.float32(1.8))
+
+
+def test_probe_csv_appends_rows(built_lib, tmp_path):
+    p = tmp_path / "probeData.csv"
+    conv = {"Crho": 1.293, "Cpressure": 2.5e3, "Cu": 46.78}
+    output.outputerVTK.probeWriteOut(p, (0.01, -0.002, 0.0005, 1.001), conv, 1.25e-5)
+    output.outputerVTK.probeWriteOut(p, (0.02, 0.0, 0.0, 0.999), conv, 1.25e-5)
+    lines = p.read_text().splitlines()
+    assert lines[0] == "Sampling frequency is: " + g6(1.25e-5) and lines[1] == "ux,uy,uz,rho,pressure"
+    f = np.float32
+    row = [f(f(0.01) * f(46.78)), f(f(-0.002) * f(46.78)), f(f(0.0005) * f(46.78)), f(f(1.001) * f(1.293)),
+           f(f(f(1.001) * f(f(1.0) / f(3.0))) * f(2.5e3))]
+    assert lines[2] == ",".join(g6(v) for v in row)
+    assert len(lines) == 4
