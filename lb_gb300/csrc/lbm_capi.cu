@@ -450,6 +450,7 @@ static lbm_status build_geometry(lbm_ctx* c) {
     };
     for (long long q = 0; q < N; q++) {
         int k = cls[q] & CLS_MASK;
+        if (k != CLS_INLET && k != CLS_OUTLET) continue;  // coordinates only for the boundary nodes
         int i = (int)(q % nx), j = (int)((q / nx) % ny), kk = (int)(q / ((long long)nx * ny));
         if (k == CLS_INLET) {
             int s = in_dir[aux[q]];  // interior at -s
@@ -563,8 +564,11 @@ static lbm_status build_geometry(lbm_ctx* c) {
         sp_begin = nx - width;
         sp_slope = (c->cfg.omega_dumping_high - c->cfg.omega_dumping_low) / (double)width;
         if (sp_slope != 0.0)
-            for (long long q = 0; q < N; q++)
-                if ((int)(q % nx) >= sp_begin && (cls[q] & CLS_MASK) != CLS_SOLID) cls[q] |= BIT_SPONGE;
+            for (long long r = 0; r < (long long)ny * nz; r++)
+                for (int i = sp_begin; i < nx; i++) {
+                    const long long q = r * nx + i;
+                    if ((cls[q] & CLS_MASK) != CLS_SOLID) cls[q] |= BIT_SPONGE;
+                }
     }
     // upload
     cudaSetDevice(c->cfg.device);
