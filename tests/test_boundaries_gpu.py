@@ -178,3 +178,36 @@ def test_checkpoint_resume_with_side_tables_is_bit_identical(built_lib, tmp_path
     s2.checkpoint_load(p)
     s2.step(5)
     assert np.array_equal(s2.populations(), f1)
+
+
+def test_unsupported_boundary_setups_are_rejected(built_lib):
+    """Set-up checks (host side, before any kernel): symmetry normals other than +-y, a symmetry plane
+    without a solid row across it, a neighbour-equilibrium outlet whose upstream cell is not fluid."""
+    half, _ = cases.symmetric_channel(16, 6, 8)
+
+    def sym_status(records):
+        s = Solver((16, 8, 8), turbulence=OmegaLES, storage="f32", nu=half["nu"], periodic=half["periodic"])
+        s.set_flags(half["flags"])
+        s.set_bc()
+        s.set_symmetry(records)
+        with pytest.raises(capi.LbmError) as e:
+            s.init_fields(half["rho"], half["u"])
+        s.close()
+        return e.value.status
+
+    recs = half["symmetry"]
+    assert sym_status([capi.make_symmetry(r.vertex.x, r.vertex.y, r.vertex.z, (1, 0, 0), 1) for r in recs]) == \
+        capi.LBM_ERR_UNSUPPORTED
+    # normal -y: the row "across" is the fluid row below the plane
+    assert sym_status([capi.make_symmetry(r.vertex.x, r.vertex.y, r.vertex.z, (0, -1, 0), 1) for r in recs]) == \
+        capi.LBM_ERR_UNSUPPORTED
+    c = cases.duct(24, 10, 8)
+    f = c["flags"].copy()
+    f[3, 4, 22] = 0  # a solid cell upstream of the outlet plane
+    s = Solver((24, 10, 8), turbulence=OmegaLES, inlet=InletVelocityZouHe, outlet=OutletNeighbourEquilibrium,
+               storage="f32", nu=c["nu"], periodic=c["periodic"])
+    s.set_flags(f)
+    s.set_bc(c["inlets"], c["outlets"])
+    with pytest.raises(capi.LbmError) as e:
+        s.init_fields(c["rho"], c["u"])
+    assert e.value.status == capi.LBM_ERR_UNSUPPORTED

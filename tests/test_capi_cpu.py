@@ -53,6 +53,13 @@ def test_create_rejects_bad_config_before_touching_the_gpu(built_lib):
     cfg = capi.make_config(8, 8, 8, collision=capi.LBM_COLLISION_CUMULANT2017, closure=capi.LBM_CLOSURE_MLP,
                            storage=capi.LBM_STORAGE_F32)  # the learned closure: SRT or cumulant-2015
     assert L.lbm_create(C.byref(cfg), C.byref(ctx)) == capi.LBM_ERR_UNSUPPORTED
+    cfg = capi.make_config(8, 8, 8, inlet_kind=3)
+    assert L.lbm_create(C.byref(cfg), C.byref(ctx)) == capi.LBM_ERR_UNSUPPORTED
+    cfg = capi.make_config(8, 8, 8, outlet_kind=5)
+    assert L.lbm_create(C.byref(cfg), C.byref(ctx)) == capi.LBM_ERR_UNSUPPORTED
+    cfg = capi.make_config(8, 8, 8, closure=capi.LBM_CLOSURE_MLP, storage=capi.LBM_STORAGE_F16DEV,
+                           outlet_kind=capi.LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA)  # sponge + learned closure
+    assert L.lbm_create(C.byref(cfg), C.byref(ctx)) == capi.LBM_ERR_UNSUPPORTED
 
 
 def test_mesher_wall_pass_host_only(built_lib):
