@@ -34,6 +34,7 @@ struct OmegaNo { static constexpr int32_t code = LBM_CLOSURE_NONE; };           
 struct OmegaMLP { static constexpr int32_t code = LBM_CLOSURE_MLP; };             // learned closure (no reference policy)
 struct StreamingAB {};                     // streamings/StreamingAB.h (AA pattern in place here)
 struct BounceBackWallHalf {};              // boundaryConditions/Wall/BounceBackWallHalf.h
+struct BounceBackWallHalfMesh {};          // .../Wall/BounceBackWallHalfMesh.h (the same rule on every fluid cell)
 struct NoSymmetry { static constexpr bool on = false; };           // boundaryConditions/Symmetry/NoSymmetry.h
 struct BounceSymmetryHalf { static constexpr bool on = true; };    // boundaryConditions/Symmetry/BounceSymmetryHalf.h
 struct Periodic { static constexpr bool on = true; };    // boundaryConditions/Periodic/Periodic.h (index wrap)
@@ -116,7 +117,9 @@ template <typename MODELTYPE, typename INITIALIZATIONTYPE, typename COLLISIONTYP
 class SolverTurbulentLES {
     static_assert(MODELTYPE::numberOfDiscreteVelocities == 27, "the kernels are D3Q27");
     static_assert(std::is_same<STREAMINGTYPE, StreamingAB>::value, "streaming: StreamingAB (AA pattern in place)");
-    static_assert(std::is_same<BOUNCEBACKWALLTYPE, BounceBackWallHalf>::value, "wall: BounceBackWallHalf");
+    static_assert(std::is_same<BOUNCEBACKWALLTYPE, BounceBackWallHalf>::value ||
+                      std::is_same<BOUNCEBACKWALLTYPE, BounceBackWallHalfMesh>::value,
+                  "wall: BounceBackWallHalf or BounceBackWallHalfMesh");
     static_assert(std::is_same<SYMMETRYTYPE, NoSymmetry>::value || std::is_same<SYMMETRYTYPE, BounceSymmetryHalf>::value,
                   "symmetry: NoSymmetry or BounceSymmetryHalf");
     static_assert(std::is_same<OUTLETTYPE, OutletDensityInterpolated>::value ||

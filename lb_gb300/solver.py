@@ -68,6 +68,10 @@ class BounceBackWallHalf:                       # boundaryConditions/Wall/Bounce
     pass
 
 
+class BounceBackWallHalfMesh(BounceBackWallHalf):  # boundaryConditions/Wall/BounceBackWallHalfMesh.h: the same
+    pass                                           # rule on every fluid cell with a solid neighbour
+
+
 class NoSymmetry:                               # boundaryConditions/Symmetry/NoSymmetry.h
     pass
 

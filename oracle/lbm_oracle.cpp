@@ -143,6 +143,10 @@ struct Sim {
     }
 
     // ---- wall list: geometryMesherBoundary.h:439-484 + compileBoundaryArrayWall :514-550
+    // wall_mesh: the BounceBackWallHalfMesh policy, which bounces back on the cells of flag exactly 2
+    // (BounceBackWallHalfMesh.h:38) instead of the list; corrected, both take every fluid cell with a
+    // solid neighbour
+    int wall_mesh = 0;
     void build_wall_list() {
         walls.clear();
         int thr = ref_compat ? 2 : 1;  // reference: > 2 (:459); corrected: any solid neighbour
@@ -150,7 +154,8 @@ struct Sim {
             for (int j = 0; j < ny; j++)
                 for (int i = 0; i < nx; i++) {
                     int32_t m = mesh[id(i, j, k)];
-                    if (m > thr) walls.push_back({i, j, k, m > 10 ? 0 : 1});
+                    bool on = (wall_mesh && ref_compat) ? m == 2 : m > thr;
+                    if (on) walls.push_back({i, j, k, m > 10 ? 0 : 1});
                 }
         // -2 nodes are not wall nodes in the reference (compileBoundaryArrayWall erases them,
         // geometryMesherBoundary.h:533-550), so their links from solid cells keep their old value;
@@ -886,6 +891,11 @@ int orc_set_bc(void* p, const lbm_bc_inlet* in, int nin, const lbm_bc_outlet* ou
             S->outlets.push_back(r);
         }
     });
+    return 0;
+}
+int orc_set_wall_policy(void* p, int mesh_variant) {
+    Handle* h = (Handle*)p;
+    DISPATCH(h, { S->wall_mesh = mesh_variant; S->build_wall_list(); });
     return 0;
 }
 int orc_set_symmetry(void* p, const lbm_bc_symmetry* rec, int n) {

@@ -31,6 +31,7 @@ def lib():
         L.orc_set_bc.argtypes = [vp, C.POINTER(LbmBcInlet), i32, C.POINTER(LbmBcOutlet), i32]
         L.orc_set_periodic_list.argtypes = [vp, ip, i32]
         L.orc_set_symmetry.argtypes = [vp, C.POINTER(LbmBcSymmetry), i32]
+        L.orc_set_wall_policy.argtypes = [vp, i32]
         L.orc_init_equilibrium.argtypes = [vp, f64, dp]
         L.orc_init_fields.argtypes = [vp, dp, dp]
         L.orc_step.argtypes = [vp, i32]
@@ -93,6 +94,10 @@ class OracleSim:
         ai = (LbmBcInlet * max(ni, 1))(*inlets)
         ao = (LbmBcOutlet * max(no, 1))(*outlets)
         lib().orc_set_bc(self.h, ai, ni, ao, no)
+
+    def set_wall_policy(self, mesh_variant):
+        """1: BounceBackWallHalfMesh (flag-2 cells under ref_compat), 0: BounceBackWallHalf (the list)."""
+        lib().orc_set_wall_policy(self.h, int(mesh_variant))
 
     def set_symmetry(self, records=()):
         n = len(records)

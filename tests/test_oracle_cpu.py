@@ -236,3 +236,28 @@ def test_combined_collision_picks_the_operator_by_flag(oracle_lib):
     ref17 = O.collide_cell(f, r, uu, 1.9, capi.LBM_COLLISION_CUMULANT2017, ref_compat=True)
     refc = O.collide_cell(f, r, uu, 1.9, comb, ref_compat=True, flag=7)
     assert np.abs(refc - ref17).max() > 1e-6
+
+
+def test_wall_policies_differ_only_in_the_reference_selection(oracle_lib):
+    """BounceBackWallHalf bounces back on the wall list (flag > 2 in the reference,
+    geometryMesherBoundary.h:459), BounceBackWallHalfMesh on the cells of flag exactly 2
+    (BounceBackWallHalfMesh.h:38); corrected, both take every fluid cell with a solid neighbour."""
+    from lb_gb300 import cases
+    f0 = np.ones((10, 10, 10), np.int32)
+    f0[[0, -1], :, :] = 0
+    f0[:, [0, -1], :] = 0
+    f0[:, :, [0, -1]] = 0
+    f0[5, 5, 5] = 0  # an isolated solid cell: its 26 neighbours have flag 2
+    flags = cases.wall_pass_numpy(f0)
+    assert np.sum(flags == 2) == 26
+    cfg = capi.make_config(10, 10, 10, nu=0.05)
+    sizes = {}
+    for ref in (False, True):
+        for mesh in (0, 1):
+            o = O.OracleSim(cfg, 64, ref_compat=ref)
+            o.set_flags(flags)
+            o.set_wall_policy(mesh)
+            sizes[(ref, mesh)] = o.wall_list_size()
+    f = flags.reshape(-1)
+    assert sizes[(False, 0)] == sizes[(False, 1)] == int(np.sum(f > 1))
+    assert sizes[(True, 0)] == int(np.sum(f > 2)) and sizes[(True, 1)] == int(np.sum(f == 2))
