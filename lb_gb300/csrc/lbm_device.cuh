@@ -78,6 +78,8 @@ struct Params {
     int has_force;
     float rho0, scale, inv_scale;  // FP16-deviation encoding
     int f16_sr;              // FP16 stores round stochastically (else to nearest)
+    uint32_t lcg_a, lcg_c;   // the packed path's dither stream s -> a s + c: the LCG below when rounding
+                             // stochastically, a = 0 and c = the fixed half-step dither when to nearest
     float wr[27];            // w_v rho0            (decode f = h 2^-s + w_v rho0)
     float nwrs[27];          // -w_v rho0 2^s       (encode h = f 2^s - w_v rho0 2^s)
     float2 wr2[27], nwrs2[27];  // the same as (x, x) pairs for the packed two-cell path
@@ -148,9 +150,12 @@ LBM_D uint32_t mix32(uint32_t h) {
 LBM_D uint32_t sr_seed(unsigned long long e, int m) {
     return mix32((uint32_t)e ^ mix32((uint32_t)m * 0x9E3779B9u + (uint32_t)(e >> 32)));
 }
-// next 32 random bits of a per-thread stream (32-bit LCG of Numerical Recipes; the high bits are used)
-LBM_D uint32_t lcg_next(uint32_t& s) {
-    s = s * 1664525u + 1013904223u;
+// next 32 random bits of a per-thread stream (32-bit LCG of Numerical Recipes, a = 1664525,
+// c = 1013904223; the high bits are used); a and c come from the parameters, so rounding to nearest
+// (a = 0, c = kHalfStep2x) takes the same instructions without a select
+constexpr uint32_t kLcgA = 1664525u, kLcgC = 1013904223u;
+LBM_D uint32_t lcg_next(uint32_t& s, const Params& p) {
+    s = s * p.lcg_a + p.lcg_c;
     return s;
 }
 LBM_D __half half_sr(float v, uint32_t r13) { return __float2half_rz(__uint_as_float(__float_as_uint(v) + r13)); }

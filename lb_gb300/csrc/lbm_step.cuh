@@ -287,8 +287,7 @@ LBM_D void store_pair(const Params& p, const PairIdx& q, const PairCodec& k, con
             else *(float2*)(a + q.e0) = f[V].v;
         } else {
             const F2 e = lfma(f[V], k.scale, k.nwrs[csq(V)]);
-            const uint32_t rr = lcg_next(rs);
-            const __half2 h = half2_sr(e.v, p.f16_sr ? rr : kHalfStep2x);
+            const __half2 h = half2_sr(e.v, lcg_next(rs, p));
             if constexpr (split) { a[i0] = __low2half(h); a[i1] = __high2half(h); }
             else *(__half2*)(a + q.e0) = h;
         }
@@ -353,8 +352,7 @@ LBM_D void store_pair_rows(const Params& p, const PairRows& w, const PairCodec& 
             else *(float2*)(a + w.x0) = f[V].v;
         } else {
             const F2 e = lfma(f[V], k.scale, k.nwrs[csq(V)]);
-            const uint32_t rr = lcg_next(rs);
-            const __half2 h = half2_sr(e.v, p.f16_sr ? rr : kHalfStep2x);
+            const __half2 h = half2_sr(e.v, lcg_next(rs, p));
             if constexpr (split) { a[i0] = __low2half(h); a[i1] = __high2half(h); }
             else *(__half2*)(a + w.x0) = h;
         }
