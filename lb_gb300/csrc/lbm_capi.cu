@@ -344,7 +344,7 @@ static lbm_status build_geometry(lbm_ctx* c) {
     const int okind = c->cfg.outlet_kind;
     const bool neq_kind = okind == LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM || okind == LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA ||
                           okind == LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA_RF;
-    std::vector<char> is_sym((size_t)N, 0);
+    std::vector<char> is_sym(c->syms.empty() ? 0 : (size_t)N, 0);
     for (const auto& r : c->syms) {
         int i = r.vertex.x, j = r.vertex.y, k = r.vertex.z;
         if (i < 0 || j < 0 || k < 0 || i >= nx || j >= ny || k >= nz)
@@ -354,12 +354,13 @@ static lbm_status build_geometry(lbm_ctx* c) {
         if (is_sym[id(i, j, k)]) return fail(c, LBM_ERR_INVALID, "two symmetry records for (%d,%d,%d)", i, j, k);
         is_sym[id(i, j, k)] = 1;
     }
+    long long n_flag1 = 0, n_flag2 = 0;  // cells of flag -1 and -2 (each needs one record)
     for (long long q = 0; q < N; q++) {
         int32_t f = c->flags[q];
         uint8_t k;
         if (f == 0) k = CLS_SOLID;
-        else if (f == -1) k = lid_kind ? CLS_LID : CLS_INLET;
-        else if (f == -2) k = is_sym[q] ? CLS_SYM : CLS_OUTLET;
+        else if (f == -1) { k = lid_kind ? CLS_LID : CLS_INLET; n_flag1++; }
+        else if (f == -2) { k = (!is_sym.empty() && is_sym[q]) ? CLS_SYM : CLS_OUTLET; n_flag2++; }
         else if (f > 0 || f == -3) k = CLS_BULK;
         else return fail(c, LBM_ERR_INVALID, "flag %d at cell %lld is not in the reference encoding", f, q);
         cls[q] = k | (f == 1 ? BIT_REFBULK : 0);
@@ -395,7 +396,8 @@ static lbm_status build_geometry(lbm_ctx* c) {
         long long q = id(i, j, k);
         if (c->flags[q] != -2) return fail(c, LBM_ERR_INVALID, "outlet record at (%d,%d,%d) is not a -2 cell", i, j, k);
         if (aux[q] >= 0) return fail(c, LBM_ERR_INVALID, "two outlet records for (%d,%d,%d)", i, j, k);
-        if (is_sym[q]) return fail(c, LBM_ERR_INVALID, "(%d,%d,%d) has an outlet and a symmetry record", i, j, k);
+        if (!is_sym.empty() && is_sym[q])
+            return fail(c, LBM_ERR_INVALID, "(%d,%d,%d) has an outlet and a symmetry record", i, j, k);
         int s = (r.normal[0] == 1.f && r.normal[1] == 0.f && r.normal[2] == 0.f) ? 1
               : (r.normal[0] == -1.f && r.normal[1] == 0.f && r.normal[2] == 0.f) ? -1 : 0;
         if (!s) return fail(c, LBM_ERR_UNSUPPORTED, "outlet at (%d,%d,%d): only +-x normals (as the reference)", i, j, k);
@@ -433,11 +435,14 @@ static lbm_status build_geometry(lbm_ctx* c) {
         aux[q] = n_sym++;
         sym_dir.push_back(sg);
     }
-    for (long long q = 0; q < N; q++) {
-        int k = cls[q] & CLS_MASK;
-        if ((k == CLS_LID || k == CLS_INLET || k == CLS_OUTLET) && aux[q] < 0)
-            return fail(c, LBM_ERR_INVALID, "cell %lld has flag %d but no boundary record", q, c->flags[q]);
-    }
+    // every record names a distinct cell of its flag (checked above), so equal counts mean every -1 and
+    // -2 cell has its record; the scan for the culprit runs only when they differ
+    if (n_flag1 != (long long)c->inlets.size() || n_flag2 != (long long)(c->outlets.size() + c->syms.size()))
+        for (long long q = 0; q < N; q++) {
+            int k = cls[q] & CLS_MASK;
+            if ((k == CLS_LID || k == CLS_INLET || k == CLS_OUTLET) && aux[q] < 0)
+                return fail(c, LBM_ERR_INVALID, "cell %lld has flag %d but no boundary record", q, c->flags[q]);
+        }
     std::vector<int32_t> out_nb(neq_kind ? 9 * (size_t)n_out : 0, -1);
     int n_ms = 0;
     // helper roles: probes of the equilibrium inlets, upstream cells of the outlets
@@ -450,9 +455,13 @@ static lbm_status build_geometry(lbm_ctx* c) {
         aux[q] = node;
         return LBM_OK;
     };
-    for (long long q = 0; q < N; q++) {
+    std::vector<long long> bnodes;  // the inlet and outlet nodes, from their records
+    bnodes.reserve(c->inlets.size() + c->outlets.size());
+    for (const auto& r : c->inlets) bnodes.push_back(id(r.vertex.x, r.vertex.y, r.vertex.z));
+    for (const auto& r : c->outlets) bnodes.push_back(id(r.vertex.x, r.vertex.y, r.vertex.z));
+    for (long long q : bnodes) {
         int k = cls[q] & CLS_MASK;
-        if (k != CLS_INLET && k != CLS_OUTLET) continue;  // coordinates only for the boundary nodes
+        if (k != CLS_INLET && k != CLS_OUTLET) continue;  // moving-wall and Zou/He nodes have no helpers
         int i = (int)(q % nx), j = (int)((q / nx) % ny), kk = (int)(q / ((long long)nx * ny));
         if (k == CLS_INLET) {
             int s = in_dir[aux[q]];  // interior at -s
@@ -548,11 +557,10 @@ static lbm_status build_geometry(lbm_ctx* c) {
                 }
         }
     }
-    for (long long q = 0; q < N; q++)
-        if ((cls[q] & CLS_MASK) == CLS_OUTLET) {
-            lbm_status st = check_links(q);
-            if (st) return st;
-        }
+    for (const auto& r : c->outlets) {
+        lbm_status st = check_links(id(r.vertex.x, r.vertex.y, r.vertex.z));
+        if (st) return st;
+    }
     // sponge of OutletNeighbourEquilibriumOmega(RF)::outletOmega (:18-79): along the first outlet's normal
     // axis, the last ceil(0.1 n) planes (the reference's float ceil(n * 0.1f), equal for every n) lose
     // (high - low) / width * (plane - first plane) of their relaxation rate; those cells take the
