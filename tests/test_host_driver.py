@@ -44,6 +44,39 @@ int main() {
     assert "symmetry: NoSymmetry or BounceSymmetryHalf" in r.stderr
 
 
+def test_supported_policies_compile():
+    """Every policy tag the kernels implement composes into SolverTurbulentLES (the reference's
+    declaration in main.cu reads the same with these names)."""
+    src = r'''
+#include "lbm_solver.hpp"
+using namespace lbm_gb300;
+int main() {
+    LBMConstants C; LBMData D;
+    SolverTurbulentLES<D3Q27, InitializationEquilibriumConstVector, CollisionCumD3Q27Turbulent2017, StreamingAB,
+                       BounceBackWallHalfMesh, BounceSymmetryHalf, Periodic, InletVelocityZouHe,
+                       OutletNeighbourEquilibriumOmega, MomentDensityVelocityN27, OmegaLES, ErrorQuadratic,
+                       NonDimensiolnaliseFactorsVelocity, MomentTimeAvg> a(C, D);
+    SolverTurbulentLES<D3Q27, InitializationEquilibriumConstVector, CollisionCumD3Q27TurbulentCombined, StreamingAB,
+                       BounceBackWallHalf, NoSymmetry, NoPeriodic, InletVelocityEquilibrium,
+                       OutletDensityEquilibrium, MomentDensityVelocityN27, OmegaNo, ErrorQuadratic,
+                       NonDimensiolnaliseFactorsVelocity, MomentTimeAvg> b(C, D);
+    SolverTurbulentLES<D3Q27, InitializationEquilibriumConstVector, CollisionSRTTurbulent, StreamingAB,
+                       BounceBackWallHalf, NoSymmetry, Periodic, InletVelocityMovingWall,
+                       OutletNeighbourEquilibriumOmegaRF, MomentDensityVelocityN27, OmegaMLP, ErrorQuadratic,
+                       NonDimensiolnaliseFactorsVelocity, MomentTimeAvg> c(C, D);
+    (void)a; (void)b; (void)c;
+    return 0;
+}
+'''
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "t.cpp")
+        with open(p, "w") as fh:
+            fh.write(src)
+        r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), p],
+                           capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 @pytest.mark.gpu
 def test_driver_cavity_equals_python_api(built_lib):
     n, steps = 24, 300
