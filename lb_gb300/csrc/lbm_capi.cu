@@ -111,6 +111,7 @@ static Params make_params(const lbm_ctx* c) {
     for (int a = 0; a < 3; a++) p.wrap[a] = c->cfg.periodic[a] ? 1 : 0;
     p.N = c->N;
     p.m = (int)c->m;
+    p.sr_step_seed = step_seed(p.m);
     p.tau = c->cfg.tau > 0 ? c->cfg.tau : 3.0 * c->cfg.nu + 0.5;
     p.cles18 = 18.0 * c->cfg.cles;
     p.nu = c->cfg.nu;

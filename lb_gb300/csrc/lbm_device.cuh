@@ -78,6 +78,7 @@ struct Params {
     int has_force;
     float rho0, scale, inv_scale;  // FP16-deviation encoding
     int f16_sr;              // FP16 stores round stochastically (else to nearest)
+    uint32_t sr_step_seed;   // step_seed(m)
     uint32_t lcg_a, lcg_c;   // the packed path's dither stream s -> a s + c: the LCG below when rounding
                              // stochastically, a = 0 and c = the fixed half-step dither when to nearest
     float wr[27];            // w_v rho0            (decode f = h 2^-s + w_v rho0)
@@ -141,7 +142,7 @@ template <class R> LBM_D R p_F(const Params& p, int a) { if constexpr (std::is_s
 // dropped) and truncate toward zero; unbiased for results in the FP16 normal range.  The random bits
 // are a function of (element, step) only, so runs, resumes and kernel variants are reproducible.
 // Hash: the "lowbias32" 32-bit integer finaliser (C. Wellons, hash-prospector).
-LBM_D uint32_t mix32(uint32_t h) {
+LBM_HD uint32_t mix32(uint32_t h) {
     h ^= h >> 16; h *= 0x7FEB352Du;
     h ^= h >> 15; h *= 0x846CA68Bu;
     h ^= h >> 16;
@@ -150,6 +151,10 @@ LBM_D uint32_t mix32(uint32_t h) {
 LBM_D uint32_t sr_seed(unsigned long long e, int m) {
     return mix32((uint32_t)e ^ mix32((uint32_t)m * 0x9E3779B9u + (uint32_t)(e >> 32)));
 }
+// the step's part of sr_seed for indices below 2^32 (the packed paths' pair indices), hashed once per
+// launch on the host: sr_seed(e, m) == mix32(e ^ step_seed(m)) for such e
+LBM_HD uint32_t step_seed(int m) { return mix32((uint32_t)m * 0x9E3779B9u); }
+LBM_D uint32_t sr_seed_pair(uint32_t e, const Params& p) { return mix32(e ^ p.sr_step_seed); }
 // next 32 random bits of a per-thread stream (32-bit LCG of Numerical Recipes, a = 1664525,
 // c = 1013904223; the high bits are used); a and c come from the parameters, so rounding to nearest
 // (a = 0, c = kHalfStep2x) takes the same instructions without a select

@@ -276,7 +276,7 @@ template <class S, bool ODD>
 LBM_D void store_pair(const Params& p, const PairIdx& q, const PairCodec& k, const F2 (&f)[27]) {
     using T = typename S::T;
     uint32_t rs = 0;  // stochastic-rounding stream of the pair (FP16)
-    if constexpr (S::kind == 2) rs = sr_seed((unsigned long long)q.e0, p.m);
+    if constexpr (S::kind == 2) rs = sr_seed_pair((uint32_t)q.e0, p);
     sfor<0, 27>([&](auto vc) {
         constexpr int V = decltype(vc)::value;
         T* a = (T*)(ODD ? p.wr_odd[V] : p.wr_even[V]);
@@ -339,7 +339,7 @@ LBM_D void store_pair_rows(const Params& p, const PairRows& w, const PairCodec& 
     using T = typename S::T;
     T* A = (T*)p.f;
     uint32_t rs = 0;  // stochastic-rounding stream of the pair (FP16), seeded by the pair's first cell
-    if constexpr (S::kind == 2) rs = sr_seed((unsigned long long)(w.R[1][1] + w.x0), p.m);
+    if constexpr (S::kind == 2) rs = sr_seed_pair((uint32_t)(w.R[1][1] + w.x0), p);
     sfor<0, 27>([&](auto vc) {
         constexpr int V = decltype(vc)::value;
         constexpr int slot = ODD ? V : opp(V);

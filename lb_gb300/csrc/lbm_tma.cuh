@@ -139,7 +139,7 @@ LBM_D void row_from_stage(const Params& p, typename S::T* buf, int y, int z, con
     const long long idx0 = ((long long)z * p.ny + y) * nx + x0;
     collide_pair<COLL, CLOS>(p, f, idx0);
     uint32_t rs = 0;  // stochastic-rounding stream of the pair, as store_pair
-    if constexpr (S::kind == 2) rs = sr_seed((unsigned long long)idx0, p.m);
+    if constexpr (S::kind == 2) rs = sr_seed_pair((uint32_t)idx0, p);
     __syncthreads();  // every pair has read its inputs before any segment is overwritten
     sfor<0, 27>([&](auto vc) {
         constexpr int V = decltype(vc)::value;
