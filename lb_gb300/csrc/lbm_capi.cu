@@ -132,18 +132,23 @@ static Params make_params(const lbm_ctx* c) {
     // per-direction addresses of the fast path (bulk cells off the periodic seams)
     const unsigned long long base = (unsigned long long)c->d_f, es = (unsigned long long)c->esize;
     const long long nx = c->cfg.nx, nxy = (long long)c->cfg.nx * c->cfg.ny;
+    double raw_rho = 0.0, raw_mdiag = 0.0;
     for (int v = 0; v < 27; v++) {
         const int o = opp(v);
         const long long off = cx(v) + cy(v) * nx + cz(v) * nxy;  // element offset of x + c_v
         p.wr[v] = (float)(wgt(v) * c->cfg.rho0);
         p.nwrs[v] = -(float)(wgt(v) * c->cfg.rho0) * p.scale;
         p.wr2[v] = make_float2(p.wr[v], p.wr[v]);
+        raw_rho += (double)p.wr[v];
+        raw_mdiag += (double)p.wr[v] * cx(v) * cx(v);
         p.nwrs2[v] = make_float2(p.nwrs[v], p.nwrs[v]);
         p.rd_even[v] = base + (unsigned long long)(v * c->N) * es;
         p.rd_odd[v] = base + (unsigned long long)(o * c->N - off) * es;
         p.wr_even[v] = base + (unsigned long long)(o * c->N) * es;
         p.wr_odd[v] = base + (unsigned long long)(v * c->N + off) * es;
     }
+    p.raw_rho = (float)raw_rho;
+    p.raw_mdiag = (float)raw_mdiag;
     p.lid_state = c->d_lid_state; p.lid_n = c->d_lid_n; p.lid_u = c->d_lid_u; p.n_lid = c->n_lid;
     p.in_probe = c->d_in_probe; p.in_u = c->d_in_u; p.in_dir = c->d_in_dir; p.n_in = c->n_in;
     p.out_save = c->d_out_save; p.out_rho = c->d_out_rho; p.out_dir = c->d_out_dir; p.n_out = c->n_out;

@@ -79,6 +79,7 @@ struct Params {
     float rho0, scale, inv_scale;  // FP16-deviation encoding
     int f16_sr;              // FP16 stores round stochastically (else to nearest)
     uint32_t sr_step_seed;   // step_seed(m)
+    float raw_rho, raw_mdiag;  // sum_v w_v rho0 and sum_v w_v rho0 c_vx^2 of the FP16 codec's references
     uint32_t lcg_a, lcg_c;   // the packed path's dither stream s -> a s + c: the LCG below when rounding
                              // stochastically, a = 0 and c = the fixed half-step dither when to nearest
     float wr[27];            // w_v rho0            (decode f = h 2^-s + w_v rho0)

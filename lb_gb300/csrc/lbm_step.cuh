@@ -216,11 +216,27 @@ LBM_D void collide_with_rate(L (&f)[27], const Mom<L>& mm, L ri, L ux, L uy, L u
 // rate where the kept value is negative (fallback mark) or not a number
 LBM_D float rate_kept(float nu, float tau, float om_s) { return nu >= 0.0f ? __fdividef(1.0f, lfma(3.0f, nu, tau)) : om_s; }
 
+// moments of the populations from those of the stored FP16 deviations, f_v = h_v 2^-s + w_v rho0:
+// rho = 2^-s sum h + sum w rho0, j = 2^-s j_h, M_ab = 2^-s M_ab,h + delta_ab sum w rho0 c_x^2 (the
+// weights are symmetric, so the odd and mixed sums of w_v rho0 vanish)
+LBM_D Mom<F2> moments_from_raw(const Mom<F2>& m, const Params& p) {
+    const F2 s = F2(p.inv_scale), d = F2(p.raw_mdiag);
+    Mom<F2> o;
+    o.rho = lfma(m.rho, s, F2(p.raw_rho));
+    o.jx = m.jx * s; o.jy = m.jy * s; o.jz = m.jz * s;
+    o.Mxx = lfma(m.Mxx, s, d); o.Myy = lfma(m.Myy, s, d); o.Mzz = lfma(m.Mzz, s, d);
+    o.Mxy = m.Mxy * s; o.Mxz = m.Mxz * s; o.Myz = m.Myz * s;
+    return o;
+}
+
 // moments, relaxation rate and collision of a packed pair of bulk cells
-// (time-average accumulation of the two cells idx0, idx0+1 when p.acc is set)
-template <int COLL, int CLOS>
+// (time-average accumulation of the two cells idx0, idx0+1 when p.acc is set).  RAW: f holds the FP16
+// deviations (the cumulant-2015 collision rebuilds every population from the moments)
+template <int COLL, int CLOS, bool RAW = false>
 LBM_D void collide_pair(const Params& p, F2 (&f)[27], long long idx0) {
-    const Mom<F2> mm = raw_moments(f);
+    static_assert(!RAW || COLL == 1, "only the cumulant-2015 step needs no decoded populations");
+    Mom<F2> mm = raw_moments(f);
+    if constexpr (RAW) mm = moments_from_raw(mm, p);
     const F2 ri = rcp(mm.rho);
     F2 ux = mm.jx * ri, uy = mm.jy * ri, uz = mm.jz * ri;
     if (p.has_force) {
@@ -253,7 +269,9 @@ struct PairCodec {
     F2 inv_scale, scale, wr[4], nwrs[4];
 };
 
-template <class S, bool ODD>
+// RAW (FP16 storage): f[v] receives the stored deviation h_v itself (the caller then takes the moments of
+// f from those of h, moments_from_raw); else the population h_v 2^-s + w_v rho0
+template <class S, bool ODD, bool RAW = false>
 LBM_D void load_pair(const Params& p, const PairIdx& q, const PairCodec& k, F2 (&f)[27]) {
     using T = typename S::T;
     sfor<0, 27>([&](auto vc) {
@@ -268,7 +286,8 @@ LBM_D void load_pair(const Params& p, const PairIdx& q, const PairCodec& k, F2 (
             float2 t;
             if constexpr (split) t = make_float2(__half2float(__ldg(a + i0)), __half2float(__ldg(a + i1)));
             else t = __half22float2(__ldg((const __half2*)(a + q.e0)));
-            f[V] = lfma(F2(t), k.inv_scale, k.wr[csq(V)]);
+            if constexpr (RAW) f[V] = F2(t);
+            else f[V] = lfma(F2(t), k.inv_scale, k.wr[csq(V)]);
         }
     });
 }
@@ -312,7 +331,7 @@ LBM_D void make_pair_rows(const Params& p, int x0, int y, int z, PairRows& w) {
     w.xm = x0 == 0 ? p.nx - 1 : x0 - 1;
     w.x2 = x0 + 2 == p.nx ? 0 : x0 + 2;
 }
-template <class S, bool ODD>
+template <class S, bool ODD, bool RAW = false>
 LBM_D void load_pair_rows(const Params& p, const PairRows& w, const PairCodec& k, F2 (&f)[27]) {
     using T = typename S::T;
     const T* A = (const T*)p.f;
@@ -330,7 +349,8 @@ LBM_D void load_pair_rows(const Params& p, const PairRows& w, const PairCodec& k
             float2 t;
             if constexpr (split) t = make_float2(__half2float(__ldg(a + i0)), __half2float(__ldg(a + i1)));
             else t = __half22float2(__ldg((const __half2*)(a + w.x0)));
-            f[V] = lfma(F2(t), k.inv_scale, k.wr[csq(V)]);
+            if constexpr (RAW) f[V] = F2(t);
+            else f[V] = lfma(F2(t), k.inv_scale, k.wr[csq(V)]);
         }
     });
 }
@@ -369,6 +389,7 @@ LBM_D void step_pair(const Params& p, int x0, int y, int z) {
     constexpr uint8_t keep = COLL == 3 ? (uint8_t)0xff : (uint8_t)~BIT_REFBULK;
     constexpr uint8_t want = COLL == 3 ? (uint8_t)(CLS_BULK | BIT_REFBULK) : (uint8_t)CLS_BULK;
     constexpr int PC = COLL == 3 ? 1 : COLL;
+    constexpr bool RAW = S::kind == 2 && PC == 1;  // FP16 + cumulant-2015: moments from the deviations
     const uint8_t f0 = p.cls[idx0] & keep;
     const uint8_t f1 = two ? (p.cls[idx0 + 1] & keep) : (uint8_t)0;
     const bool pair = two && f0 == want && f1 == want && (p.nx & 1) == 0;
@@ -394,14 +415,14 @@ LBM_D void step_pair(const Params& p, int x0, int y, int z) {
         q.e1 = q.e0 + 1;
         q.eL = (p.wrap[0] && x0 == 0) ? q.e0 + p.nx : q.e0;
         q.eR = (p.wrap[0] && x0 + 2 == p.nx) ? q.e1 - p.nx : q.e1;
-        load_pair<S, ODD>(p, q, k, f);
-        collide_pair<PC, CLOS>(p, f, idx0);
+        load_pair<S, ODD, RAW>(p, q, k, f);
+        collide_pair<PC, CLOS, RAW>(p, f, idx0);
         store_pair<S, ODD>(p, q, k, f);
     } else {
         PairRows w;
         make_pair_rows(p, x0, y, z, w);
-        load_pair_rows<S, ODD>(p, w, k, f);
-        collide_pair<PC, CLOS>(p, f, idx0);
+        load_pair_rows<S, ODD, RAW>(p, w, k, f);
+        collide_pair<PC, CLOS, RAW>(p, f, idx0);
         store_pair_rows<S, ODD>(p, w, k, f);
     }
 }

@@ -133,11 +133,12 @@ LBM_D void row_from_stage(const Params& p, typename S::T* buf, int y, int z, con
             float2 t;
             if constexpr (sh != 0) t = make_float2(__half2float(a[0]), __half2float(a[1]));
             else t = __half22float2(*(const __half2*)a);
-            f[V] = lfma(F2(t), k.inv_scale, k.wr[csq(V)]);
+            if constexpr (COLL == 1) f[V] = F2(t);  // moments from the deviations, as step_pair
+            else f[V] = lfma(F2(t), k.inv_scale, k.wr[csq(V)]);
         }
     });
     const long long idx0 = ((long long)z * p.ny + y) * nx + x0;
-    collide_pair<COLL, CLOS>(p, f, idx0);
+    collide_pair<COLL, CLOS, S::kind == 2 && COLL == 1>(p, f, idx0);
     uint32_t rs = 0;  // stochastic-rounding stream of the pair, as store_pair
     if constexpr (S::kind == 2) rs = sr_seed_pair((uint32_t)idx0, p);
     __syncthreads();  // every pair has read its inputs before any segment is overwritten
