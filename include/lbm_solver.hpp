@@ -25,10 +25,16 @@ namespace lbm_gb300 {
 
 // ---- policy tags (reference file of each in the comment) ----------------------------------------------
 struct D3Q27 { static constexpr int numberOfDiscreteVelocities = 27; };           // models/D3Q27/D3Q27.h
-struct CollisionCumD3Q27Turbulent2015 { static constexpr int32_t code = LBM_COLLISION_CUMULANT2015; };
-struct CollisionCumD3Q27Turbulent2017 { static constexpr int32_t code = LBM_COLLISION_CUMULANT2017; };
-struct CollisionCumD3Q27TurbulentCombined { static constexpr int32_t code = LBM_COLLISION_CUMULANT_COMBINED; };
-struct CollisionSRTTurbulent { static constexpr int32_t code = LBM_COLLISION_SRT; };  // collisions/CollisionSRTTurbulent.h
+struct CollisionCumD3Q27Turbulent2015 { static constexpr int32_t code = LBM_COLLISION_CUMULANT2015; static constexpr bool laminar = false; };
+struct CollisionCumD3Q27Turbulent2017 { static constexpr int32_t code = LBM_COLLISION_CUMULANT2017; static constexpr bool laminar = false; };
+struct CollisionCumD3Q27TurbulentCombined { static constexpr int32_t code = LBM_COLLISION_CUMULANT_COMBINED; static constexpr bool laminar = false; };
+struct CollisionSRTTurbulent { static constexpr int32_t code = LBM_COLLISION_SRT; static constexpr bool laminar = false; };  // collisions/CollisionSRTTurbulent.h
+// the laminar collisions relax with the global omega = 1/tau (Constants->omega:
+// CollisionCumD3Q27Laminar.h:27, CollisionSRTLaminar.h:28, CollisionSRTunroll.h:27) and ignore the per-cell
+// field, so the solver runs them with no closure and no outlet sponge whatever the other tags say
+struct CollisionCumD3Q27Laminar { static constexpr int32_t code = LBM_COLLISION_CUMULANT2015; static constexpr bool laminar = true; };
+struct CollisionSRTLaminar { static constexpr int32_t code = LBM_COLLISION_SRT; static constexpr bool laminar = true; };
+struct CollisionSRTunroll { static constexpr int32_t code = LBM_COLLISION_SRT; static constexpr bool laminar = true; };  // CollisionSRTLaminar unrolled
 struct OmegaLES { static constexpr int32_t code = LBM_CLOSURE_SMAGORINSKY; };      // turbulence/OmegaLES.h
 struct OmegaNo { static constexpr int32_t code = LBM_CLOSURE_NONE; };             // turbulence/OmegaNo.h
 struct OmegaMLP { static constexpr int32_t code = LBM_CLOSURE_MLP; };             // learned closure (no reference policy)
@@ -155,7 +161,7 @@ public:
         c.nx = Constants.dimX_int; c.ny = Constants.dimY_int; c.nz = Constants.dimZ_int;
         for (int a = 0; a < 3; a++) c.periodic[a] = PERIODICTYPE::on ? Constants.periodic[a] : 0;
         c.collision = COLLISIONTYPE::code;
-        c.closure = TURBULENCETYPE::code;
+        c.closure = COLLISIONTYPE::laminar ? LBM_CLOSURE_NONE : TURBULENCETYPE::code;
         c.storage = Constants.storage;
         c.inlet_kind = INLETTYPE::code;
         c.nu = Constants.ny;
@@ -167,8 +173,8 @@ public:
         c.device = Constants.device;
         c.mlp_interval = Constants.mlp_interval;
         c.outlet_kind = OUTLETTYPE::code;
-        c.omega_dumping_low = Constants.omegaDumpingLow;
-        c.omega_dumping_high = Constants.omegaDumpingHigh;
+        c.omega_dumping_low = COLLISIONTYPE::laminar ? 0.0 : Constants.omegaDumpingLow;    // a sponge of slope 0
+        c.omega_dumping_high = COLLISIONTYPE::laminar ? 0.0 : Constants.omegaDumpingHigh;
         if (ctx) lbm_destroy(ctx);
         ctx = nullptr;
         check(lbm_create(&c, &ctx), nullptr, "lbm_create");
@@ -188,7 +194,7 @@ public:
         } else {
             check(lbm_init_equilibrium(ctx, Constants.rho0, Constants.VelocityInit), ctx, "lbm_init_equilibrium");
         }
-        if (std::is_same<TURBULENCETYPE, OmegaMLP>::value) {
+        if (std::is_same<TURBULENCETYPE, OmegaMLP>::value && !COLLISIONTYPE::laminar) {
             if (!Constants.mlp) throw Error(LBM_ERR_STATE, "OmegaMLP needs LBMConstants::mlp");
             check(lbm_mlp_load(ctx, Constants.mlp), ctx, "lbm_mlp_load");
         }

@@ -40,12 +40,20 @@ class CollisionSRTTurbulent:                    # collisions/CollisionSRTTurbule
     code = capi.LBM_COLLISION_SRT
 
 
-class CollisionSRTLaminar(CollisionSRTTurbulent):          # same update with a global omega
+class CollisionSRTLaminar(CollisionSRTTurbulent):
+    """collisions/CollisionSRTLaminar.h: the SRT update with the global omega = 1/tau (Constants->omega,
+    :28); the solver then runs no closure and no outlet sponge, which the reference's laminar collisions
+    ignore as they never read the per-cell field."""
+    laminar = True
+
+
+class CollisionSRTunroll(CollisionSRTLaminar):  # collisions/CollisionSRTunroll.h: CollisionSRTLaminar unrolled
     pass
 
 
 class CollisionCumD3Q27Laminar(CollisionCumD3Q27Turbulent2015):
-    pass
+    """collisions/CollisionCumD3Q27Laminar.h: the 2015 cumulant with omega1 = the global 1/tau (:27)."""
+    laminar = True
 
 
 class OmegaLES:                                 # turbulence/OmegaLES.h
@@ -172,6 +180,14 @@ def _dp(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+def effective_closure(collision, turbulence, omega_dumping):
+    """The closure and sponge a collision policy runs with: a laminar collision relaxes with the global
+    1/tau whatever the turbulence and outlet policies compute, so it gets OmegaNo and a sponge of slope 0."""
+    if getattr(collision, "laminar", False):
+        return OmegaNo, (0.0, 0.0)
+    return turbulence, omega_dumping
+
+
 class Solver:
     """One lattice on one GPU (one lbm_ctx)."""
 
@@ -179,6 +195,7 @@ class Solver:
                  inlet=InletVelocityMovingWall, storage="f32", nu=1.0 / 6.0, tau=0.0, cles=0.173,
                  periodic=(0, 0, 0), force=(0.0, 0.0, 0.0), rho0=1.0, f16_scale_log2=10, device=0, options=0,
                  mlp_interval=1, outlet=OutletDensityInterpolated, omega_dumping=(-1.0, -1.0)):
+        turbulence, omega_dumping = effective_closure(collision, turbulence, omega_dumping)
         nx, ny, nz = shape
         self.shape = (int(nx), int(ny), int(nz))
         self.N = nx * ny * nz

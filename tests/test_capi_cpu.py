@@ -68,3 +68,20 @@ def test_mesher_wall_pass_host_only(built_lib):
     ptr = f.ctypes.data_as(C.POINTER(C.c_int32))
     assert capi.lib().lbm_mesher_wall_pass(ptr, 6, 5, 4) == 0
     assert f[1, 1, 2] == 1 + 9 and f[1, 2, 2] == 1 and f[0, 1, 2] == 1 + 6
+
+
+def test_laminar_collisions_run_with_the_global_omega():
+    """CollisionSRTLaminar, CollisionSRTunroll and CollisionCumD3Q27Laminar read Constants->omega
+    (CollisionSRTLaminar.h:28, CollisionSRTunroll.h:27, CollisionCumD3Q27Laminar.h:27), never the
+    per-cell field that OmegaLES and the outlet sponge write: the mirror gives them no closure and a
+    sponge of slope 0, and keeps the turbulent collisions' choices."""
+    from lb_gb300 import solver as S
+    for coll, code in ((S.CollisionSRTLaminar, capi.LBM_COLLISION_SRT), (S.CollisionSRTunroll, capi.LBM_COLLISION_SRT),
+                       (S.CollisionCumD3Q27Laminar, capi.LBM_COLLISION_CUMULANT2015)):
+        assert coll.code == code
+        for turb in (S.OmegaLES, S.OmegaMLP, S.OmegaNo):
+            t, d = S.effective_closure(coll, turb, (0.0, 0.05))
+            assert t is S.OmegaNo and d == (0.0, 0.0)
+    for coll in (S.CollisionSRTTurbulent, S.CollisionCumD3Q27Turbulent2015, S.CollisionCumD3Q27Turbulent2017,
+                 S.CollisionCumD3Q27TurbulentCombined):
+        assert S.effective_closure(coll, S.OmegaLES, (0.0, 0.05)) == (S.OmegaLES, (0.0, 0.05))

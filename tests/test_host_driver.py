@@ -64,7 +64,21 @@ int main() {
                        BounceBackWallHalf, NoSymmetry, Periodic, InletVelocityMovingWall,
                        OutletNeighbourEquilibriumOmegaRF, MomentDensityVelocityN27, OmegaMLP, ErrorQuadratic,
                        NonDimensiolnaliseFactorsVelocity, MomentTimeAvg> c(C, D);
-    (void)a; (void)b; (void)c;
+    SolverTurbulentLES<D3Q27, InitializationEquilibriumConstVector, CollisionSRTunroll, StreamingAB,
+                       BounceBackWallHalf, NoSymmetry, Periodic, InletVelocityZouHe,
+                       OutletNeighbourEquilibriumOmega, MomentDensityVelocityN27, OmegaLES, ErrorQuadratic,
+                       NonDimensiolnaliseFactorsVelocity, MomentTimeAvg> e(C, D);
+    SolverTurbulentLES<D3Q27, InitializationEquilibriumConstVector, CollisionCumD3Q27Laminar, StreamingAB,
+                       BounceBackWallHalf, NoSymmetry, NoPeriodic, InletVelocityMovingWall,
+                       OutletDensityInterpolated, MomentDensityVelocityN27, OmegaMLP, ErrorQuadratic,
+                       NonDimensiolnaliseFactorsVelocity, MomentTimeAvg> f(C, D);
+    SolverTurbulentLES<D3Q27, InitializationEquilibriumConstVector, CollisionSRTLaminar, StreamingAB,
+                       BounceBackWallHalf, NoSymmetry, NoPeriodic, InletVelocityMovingWall,
+                       OutletDensityInterpolated, MomentDensityVelocityN27, OmegaNo, ErrorQuadratic,
+                       NonDimensiolnaliseFactorsVelocity, MomentTimeAvg> g(C, D);
+    static_assert(CollisionSRTunroll::laminar && CollisionCumD3Q27Laminar::laminar &&
+                  !CollisionCumD3Q27Turbulent2015::laminar, "laminar tags");
+    (void)a; (void)b; (void)c; (void)e; (void)f; (void)g;
     return 0;
 }
 '''
