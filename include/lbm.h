@@ -255,6 +255,14 @@ lbm_status lbm_vtk_write(const char* path, const char* title, const int32_t dims
  * column line.  The path is used as given (the reference writes ./results/probeData.csv). */
 lbm_status lbm_probe_csv_append(const char* path, double sampling_period, const double sample[4], double cu,
                                 double crho, double cpressure);
+/* InitializationEquilibriumVariables (initializations/InitializationEquilibriumVariables.h:47-113): the
+ * restart read of a variables file.  Skips lines up to the first one holding "LOOKUP_TABLE default",
+ * reads nx*ny*nz values (x fastest) as float into rho, skips lines up to one holding "VECTORS U double"
+ * and reads three floats per point into u (component-major: x[N], y[N], z[N]).  No conversion factor is
+ * applied (the reference reads the numbers as they stand), so the file to restart from is a lattice-unit
+ * one (variablesLatticeVTK).  A DIMENSIONS line ahead of the data must match dims.  LBM_ERR_IO when the
+ * file does not open, LBM_ERR_INVALID when a marker is missing or the data run short. */
+lbm_status lbm_vtk_read_variables(const char* path, const int32_t dims[3], double* rho, double* u);
 const char* lbm_vtk_last_error(void);
 
 /* ---- OFF voxelizer on the GPU (preprocess geometryMesherOFF.h:45-112) -------- */

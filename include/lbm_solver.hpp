@@ -58,6 +58,9 @@ struct MomentDensityVelocityN27 {};        // moments/MomentDensityVelocityN27.h
 struct MomentTimeAvg {};                   // moments/MomentTimeAvg.h
 struct ErrorQuadratic {};                  // errorEvaluations/ErrorQuadratic.h
 struct InitializationEquilibriumConstVector {};  // initializations/InitializationEquilibriumConstVector.h
+// initializations/InitializationEquilibriumVariables.h: restart from the lattice-unit VTK dump
+// <results_dir or "results">/<InitFileName> (lbm_vtk_read_variables)
+struct InitializationEquilibriumVariables {};
 struct NonDimensiolnaliseFactorsVelocity {};     // nonDimensionalisions/NonDimensiolnaliseFactorsVelocity.h
 
 // ---- state carriers (the fields of LBMConstants / LBMData this path uses) ------------------------------
@@ -89,6 +92,7 @@ struct LBMConstants {
     // probe sample.  No files while results_dir is empty.
     int plot_every_it = -1;
     std::string results_dir;
+    std::string InitFileName;         // InitializationEquilibriumVariables: the VTK file under results_dir
     double Crho = 1.0, Cpressure = 1.0, Cu = 1.0, Ct = 1.0;     // conversion factors (physical / lattice)
     double resolution_factor = 1.0, additional_factor = 0.5;   // VTK header geometry (geometry mesher)
     double BBmin[3] = {0.0, 0.0, 0.0};
@@ -137,8 +141,9 @@ class SolverTurbulentLES {
                   "OutletDensityEquilibrium");
     static_assert(std::is_same<MOMENTTYPE, MomentDensityVelocityN27>::value, "moments: MomentDensityVelocityN27");
     static_assert(std::is_same<ERRORTYPE, ErrorQuadratic>::value, "error: ErrorQuadratic");
-    static_assert(std::is_same<INITIALIZATIONTYPE, InitializationEquilibriumConstVector>::value,
-                  "initialisation: InitializationEquilibriumConstVector");
+    static_assert(std::is_same<INITIALIZATIONTYPE, InitializationEquilibriumConstVector>::value ||
+                      std::is_same<INITIALIZATIONTYPE, InitializationEquilibriumVariables>::value,
+                  "initialisation: InitializationEquilibriumConstVector or InitializationEquilibriumVariables");
     static_assert(std::is_same<MOMENTTIMEAVGTYPE, MomentTimeAvg>::value, "time average: MomentTimeAvg");
 
 public:
@@ -187,7 +192,16 @@ public:
         if (SYMMETRYTYPE::on)
             check(lbm_set_symmetry(ctx, Data.meshBoundarySymmetry.data(), (int32_t)Data.meshBoundarySymmetry.size()),
                   ctx, "lbm_set_symmetry");
-        if (!Data.rhoInit.empty()) {
+        if (std::is_same<INITIALIZATIONTYPE, InitializationEquilibriumVariables>::value) {
+            const std::string path =
+                (Constants.results_dir.empty() ? std::string("results") : Constants.results_dir) + "/" +
+                Constants.InitFileName;
+            std::vector<double> rho(N), u(3 * N);
+            const int32_t dims[3] = {c.nx, c.ny, c.nz};
+            const lbm_status s = lbm_vtk_read_variables(path.c_str(), dims, rho.data(), u.data());
+            if (s != LBM_OK) throw Error(s, std::string("lbm_vtk_read_variables: ") + lbm_vtk_last_error());
+            check(lbm_init_fields(ctx, rho.data(), u.data()), ctx, "lbm_init_fields");
+        } else if (!Data.rhoInit.empty()) {
             if (Data.rhoInit.size() != N || Data.uInit.size() != 3 * N)
                 throw Error(LBM_ERR_INVALID, "rhoInit / uInit have the wrong size");
             check(lbm_init_fields(ctx, Data.rhoInit.data(), Data.uInit.data()), ctx, "lbm_init_fields");

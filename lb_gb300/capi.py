@@ -215,6 +215,7 @@ def lib():
         "lbm_mesh_matrix_last_error": ([], C.c_char_p),
         "lbm_vtk_write": ([C.c_char_p, C.c_char_p, ip, f64, f64, dp, C.POINTER(LbmVtkField), i32], i32),
         "lbm_probe_csv_append": ([C.c_char_p, f64, dp, f64, f64, f64], i32),
+        "lbm_vtk_read_variables": ([C.c_char_p, ip, dp, dp], i32),
         "lbm_vtk_last_error": ([], C.c_char_p),
     }
     for name, (args, res) in sig.items():

@@ -1,6 +1,7 @@
 // vtk_io.cu - host code: the reference's legacy VTK field files (outputerVTK, postprocesors/outputerVTK.h:
 // 26-823) and its probe CSV (outputerVTK::probeWriteOut, :824-851), so field dumps open in the same
-// post-processing as the reference's.
+// post-processing as the reference's; and the restart read of InitializationEquilibriumVariables
+// (initializations/InitializationEquilibriumVariables.h:47-113).
 //
 // VTK layout (every writer of the reference): "# vtk DataFile Version 2.0", a title line, "ASCII",
 // "DATASET STRUCTURED_POINTS", "DIMENSIONS nx ny nz", "ASPECT_RATIO" 1/res three times (float),
@@ -13,6 +14,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
+#include <sstream>
 #include <string>
 
 namespace {
@@ -144,6 +147,48 @@ lbm_status lbm_probe_csv_append(const char* path, double sampling_period, const 
     const bool ok = std::fwrite(s.data(), 1, s.size(), f) == s.size();
     std::fclose(f);
     if (!ok) return vtk_fail(LBM_ERR_IO, std::string("appending to ") + path + " failed");
+    return LBM_OK;
+}
+
+lbm_status lbm_vtk_read_variables(const char* path, const int32_t dims[3], double* rho, double* u) {
+    if (!path || !dims || !rho || !u || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0)
+        return vtk_fail(LBM_ERR_INVALID, "lbm_vtk_read_variables: bad argument");
+    std::ifstream in(path);
+    if (!in.is_open()) return vtk_fail(LBM_ERR_IO, std::string("cannot open ") + path);
+    const long long N = (long long)dims[0] * dims[1] * dims[2];
+    std::string line;
+    bool found = false;
+    while (std::getline(in, line)) {
+        if (line.compare(0, 10, "DIMENSIONS") == 0) {
+            std::istringstream d(line.substr(10));
+            long long a = 0, b = 0, c = 0;
+            if (!(d >> a >> b >> c) || a != dims[0] || b != dims[1] || c != dims[2])
+                return vtk_fail(LBM_ERR_INVALID, std::string(path) + ": " + line + " does not match the lattice");
+        }
+        if (line.find("LOOKUP_TABLE default") != std::string::npos) {
+            found = true;
+            break;
+        }
+    }
+    if (!found) return vtk_fail(LBM_ERR_INVALID, std::string(path) + ": no LOOKUP_TABLE default line");
+    // the reference reads into its float RealType (operator>> on float)
+    float v = 0.f;
+    for (long long q = 0; q < N; q++) {
+        if (!(in >> v)) return vtk_fail(LBM_ERR_INVALID, std::string(path) + ": short density data");
+        rho[q] = v;
+    }
+    found = false;
+    while (std::getline(in, line))
+        if (line.find("VECTORS U double") != std::string::npos) {
+            found = true;
+            break;
+        }
+    if (!found) return vtk_fail(LBM_ERR_INVALID, std::string(path) + ": no VECTORS U double line");
+    float x = 0.f, y = 0.f, z = 0.f;
+    for (long long q = 0; q < N; q++) {
+        if (!(in >> x >> y >> z)) return vtk_fail(LBM_ERR_INVALID, std::string(path) + ": short velocity data");
+        u[q] = x; u[N + q] = y; u[2 * N + q] = z;
+    }
     return LBM_OK;
 }
 

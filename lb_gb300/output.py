@@ -50,6 +50,23 @@ def write_vtk(path, grid, fields, title="LBE variables"):
         raise capi.LbmError(st, L.lbm_vtk_last_error().decode())
 
 
+def read_variables_vtk(path, dims):
+    """InitializationEquilibriumVariables' read (InitializationEquilibriumVariables.h:47-113): the first
+    LOOKUP_TABLE block as rho and the "VECTORS U double" block as u (3, N), each value parsed as float,
+    no conversion factor (restart from a variablesLatticeVTK file)."""
+    nx, ny, nz = (int(d) for d in dims)
+    N = nx * ny * nz
+    rho = np.empty(N, np.float64)
+    u = np.empty(3 * N, np.float64)
+    d = np.array([nx, ny, nz], np.int32)
+    L = capi.lib()
+    st = L.lbm_vtk_read_variables(str(path).encode(), d.ctypes.data_as(C.POINTER(C.c_int32)),
+                                  rho.ctypes.data_as(C.POINTER(C.c_double)), u.ctypes.data_as(C.POINTER(C.c_double)))
+    if st:
+        raise capi.LbmError(st, L.lbm_vtk_last_error().decode())
+    return rho, u.reshape(3, N)
+
+
 class outputerVTK:
     """The reference's writer names; paths are used as given (the reference writes under results/)."""
 

@@ -12,6 +12,7 @@ thin object over one lbm_ctx; `SolverTurbulentLES` keeps the reference's method 
 there is no CPU fallback.
 """
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -142,6 +143,11 @@ class MomentTimeAvg:                            # moments/MomentTimeAvg.h
 
 class InitializationEquilibriumConstVector:     # initializations/InitializationEquilibriumConstVector.h
     pass
+
+
+class InitializationEquilibriumVariables:       # initializations/InitializationEquilibriumVariables.h
+    """Restart: rho and u from the VTK file <results_dir>/<InitFileName> (a variablesLatticeVTK dump),
+    inlet nodes at their record velocity, populations at equilibrium."""
 
 
 class NonDimensiolnaliseFactorsVelocity:        # nonDimensionalisions/NonDimensiolnaliseFactorsVelocity.h
@@ -356,8 +362,10 @@ class SolverTurbulentLES:
             raise NotImplementedError(f"symmetry policy {Symmetry.__name__} is not implemented")
         self.C = constants
         self.data = data
+        if Initialisation not in (InitializationEquilibriumConstVector, InitializationEquilibriumVariables):
+            raise NotImplementedError(f"initialisation policy {Initialisation.__name__} is not implemented")
         self.policies = dict(Collision=Collision, Turbulence=Turbulence, Inlet=Inlet, Outlet=Outlet,
-                             Symmetry=Symmetry)
+                             Symmetry=Symmetry, Initialisation=Initialisation)
         self.solver = None
 
     def convertToLattice(self, verbose=False):
@@ -375,7 +383,13 @@ class SolverTurbulentLES:
         self.solver.set_bc(d.get("inlets", ()), d.get("outlets", ()))
         if self.policies["Symmetry"] is BounceSymmetryHalf:
             self.solver.set_symmetry(d.get("symmetry", ()))
-        self.solver.init_equilibrium(c.get("rho0", 1.0), c.get("VelocityInit", (0.0, 0.0, 0.0)))
+        if self.policies["Initialisation"] is InitializationEquilibriumVariables:
+            from .output import read_variables_vtk
+            path = os.path.join(c.get("results_dir") or "results", c["InitFileName"])
+            rho, u = read_variables_vtk(path, self.solver.shape)
+            self.solver.init_fields(rho, u)
+        else:
+            self.solver.init_equilibrium(c.get("rho0", 1.0), c.get("VelocityInit", (0.0, 0.0, 0.0)))
 
     def runSimulation(self):
         c = self.C

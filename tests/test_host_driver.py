@@ -72,7 +72,7 @@ int main() {
                        BounceBackWallHalf, NoSymmetry, NoPeriodic, InletVelocityMovingWall,
                        OutletDensityInterpolated, MomentDensityVelocityN27, OmegaMLP, ErrorQuadratic,
                        NonDimensiolnaliseFactorsVelocity, MomentTimeAvg> f(C, D);
-    SolverTurbulentLES<D3Q27, InitializationEquilibriumConstVector, CollisionSRTLaminar, StreamingAB,
+    SolverTurbulentLES<D3Q27, InitializationEquilibriumVariables, CollisionSRTLaminar, StreamingAB,
                        BounceBackWallHalf, NoSymmetry, NoPeriodic, InletVelocityMovingWall,
                        OutletDensityInterpolated, MomentDensityVelocityN27, OmegaNo, ErrorQuadratic,
                        NonDimensiolnaliseFactorsVelocity, MomentTimeAvg> g(C, D);

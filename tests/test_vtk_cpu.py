@@ -75,3 +75,49 @@ def test_probe_csv_appends_rows(built_lib, tmp_path):
            f(f(f(1.001) * f(f(1.0) / f(3.0))) * f(2.5e3))]
     assert lines[2] == ",".join(g6(v) for v in row)
     assert len(lines) == 4
+
+
+def test_restart_read_takes_the_lattice_dump_back(built_lib, tmp_path):
+    """InitializationEquilibriumVariables.h:47-113: the first LOOKUP_TABLE block is rho and the
+    "VECTORS U double" block u, each value read as a float.  A variablesLatticeVTK dump comes back as
+    the float of its 6-digit text; a variablesVTK dump comes back scaled (the reference applies no
+    conversion factor on this read)."""
+    dims = (4, 3, 2)
+    N = 24
+    rng = np.random.default_rng(7)
+    rho = 1.0 + 0.01 * rng.standard_normal(N)
+    u = 0.05 * rng.standard_normal((3, N))
+    grid = output.Grid(dims)
+    p = tmp_path / "variables.vtk"
+    output.outputerVTK.variablesLatticeVTK(p, grid, rho, u)
+    r2, u2 = output.read_variables_vtk(p, dims)
+    as_text = lambda a: np.array([float(np.float32(g6(v))) for v in np.asarray(a).reshape(-1)])
+    assert np.array_equal(r2, as_text(rho)) and np.array_equal(u2.reshape(-1), as_text(u))
+    assert np.abs(r2 - rho).max() < 1e-5 and np.abs(u2 - u).max() < 1e-6
+    q = tmp_path / "physical.vtk"
+    output.outputerVTK.variablesVTK(q, grid, rho, u, {"Crho": 2.0, "Cpressure": 1.0, "Cu": 10.0})
+    r3, u3 = output.read_variables_vtk(q, dims)
+    assert np.allclose(r3, 2.0 * rho, rtol=1e-5) and np.allclose(u3, 10.0 * u, rtol=1e-5, atol=1e-6)
+
+
+def test_restart_read_rejects_bad_files(built_lib, tmp_path):
+    import pytest
+    from lb_gb300 import capi
+    dims = (4, 3, 2)
+    with pytest.raises(capi.LbmError) as e:
+        output.read_variables_vtk(tmp_path / "missing.vtk", dims)
+    assert e.value.status == capi.LBM_ERR_IO
+    p = tmp_path / "v.vtk"
+    output.outputerVTK.variablesLatticeVTK(p, output.Grid(dims), np.ones(24), np.zeros((3, 24)))
+    with pytest.raises(capi.LbmError) as e:
+        output.read_variables_vtk(p, (4, 3, 3))  # DIMENSIONS 4 3 2 in the file
+    assert e.value.status == capi.LBM_ERR_INVALID
+    text = p.read_text().splitlines()
+    (tmp_path / "short.vtk").write_text("\n".join(text[:-3]) + "\n")
+    with pytest.raises(capi.LbmError) as e:
+        output.read_variables_vtk(tmp_path / "short.vtk", dims)
+    assert e.value.status == capi.LBM_ERR_INVALID and "short velocity" in str(e.value)
+    (tmp_path / "nou.vtk").write_text("\n".join(t for t in text if not t.startswith("VECTORS")) + "\n")
+    with pytest.raises(capi.LbmError) as e:
+        output.read_variables_vtk(tmp_path / "nou.vtk", dims)
+    assert e.value.status == capi.LBM_ERR_INVALID
