@@ -61,7 +61,6 @@ struct InitializationEquilibriumConstVector {};  // initializations/Initializati
 // initializations/InitializationEquilibriumVariables.h: restart from the lattice-unit VTK dump
 // <results_dir or "results">/<InitFileName> (lbm_vtk_read_variables)
 struct InitializationEquilibriumVariables {};
-struct NonDimensiolnaliseFactorsVelocity {};     // nonDimensionalisions/NonDimensiolnaliseFactorsVelocity.h
 
 // ---- state carriers (the fields of LBMConstants / LBMData this path uses) ------------------------------
 struct LBMConstants {
@@ -96,6 +95,17 @@ struct LBMConstants {
     double Crho = 1.0, Cpressure = 1.0, Cu = 1.0, Ct = 1.0;     // conversion factors (physical / lattice)
     double resolution_factor = 1.0, additional_factor = 0.5;   // VTK header geometry (geometry mesher)
     double BBmin[3] = {0.0, 0.0, 0.0};
+    // physical inputs of NonDimensiolnaliseFactorsVelocity (LBMConstants.h:12-64); convertToLattice
+    // converts when ny_fyz > 0, else the lattice-unit fields above are used as given
+    double BBmax[3] = {0.0, 0.0, 0.0};
+    double rho_fyz = 1.0, ny_fyz = 0.0, u_guess_fyz = 0.0, conversion_factor_fyz = 1.0, U_lb = 0.05;
+    double L_fyz = 0.0, Cl = 1.0, Cm = 1.0, Cu_inverse = 1.0, Re = 0.0, omega = 0.0;  // set by the conversion
+    // the reference sets tau = ny / 3 + 1/2 (NonDimensiolnaliseFactorsVelocity.h:66); nu = (tau - 1/2) / 3
+    // gives 3 ny + 1/2, used unless tau_ref_compat
+    bool tau_ref_compat = false;
+    // initializeSimulationData (SolverTurbulentLES.h:276-323): step counts from physical times (-1: unset)
+    double time = -1.0, plot_every = -1.0, err_every = -1.0;
+    double ProbeLocation[3] = {0.0, 0.0, 0.0};
 };
 
 struct LBMData {
@@ -114,6 +124,45 @@ class Error : public std::runtime_error {
 public:
     Error(lbm_status s, const std::string& m) : std::runtime_error(m), status(s) {}
     lbm_status status;
+};
+
+// nonDimensionalisions/NonDimensiolnaliseFactorsVelocity.h: lattice units from the physical inputs, in
+// the reference's float arithmetic (RealType = float, LBMTraits.h:72)
+struct NonDimensiolnaliseFactorsVelocity {
+    // :20-85.  Cl = L_x / nx with L_x = |BBmax_x - BBmin_x| * conversion_factor_fyz; Cu = u_guess / U_lb;
+    // Ct = Cl / Cu; Crho = rho_fyz; Cm = Crho Cl^3; Cpressure = Cm / Cl / Ct^2; Re = u_guess L_x / nu_fyz;
+    // ny = nu_fyz Ct / Cl^2; tau, omega = 1 / tau.  The reference asserts U_lb < cs and 0.5 < tau < 0.99
+    // (:29, :81): both raise here.
+    static void nonDimensionalize(LBMConstants& C) {
+        using R = float;
+        const R cs = 1.f / std::sqrt(3.f);
+        if (!((R)C.U_lb < cs)) throw Error(LBM_ERR_INVALID, "U_lb must be below the speed of sound");
+        const R L = std::fabs((R)C.BBmax[0] - (R)C.BBmin[0]) * (R)C.conversion_factor_fyz;
+        const R Cl = L / (R)C.dimX_int;
+        const R Cu = (R)C.u_guess_fyz / (R)C.U_lb;
+        const R Ct = Cl / Cu;
+        const R Crho = (R)C.rho_fyz;
+        const R Cm = Crho * Cl * Cl * Cl;
+        const R ny = (R)C.ny_fyz * Ct / Cl / Cl;
+        const R tau = C.tau_ref_compat ? ny / 3.f + 0.5f : 3.f * ny + 0.5f;
+        if (!(tau > 0.5f && tau < 0.99f))
+            throw Error(LBM_ERR_INVALID, "tau = " + std::to_string(tau) + " outside (0.5, 0.99): change the "
+                                         "resolution or the lattice speed");
+        C.L_fyz = L; C.Cl = Cl; C.Cu = Cu; C.Cu_inverse = (R)1 / Cu; C.Ct = Ct; C.Crho = Crho; C.Cm = Cm;
+        C.Cpressure = Cm / Cl / Ct / Ct;
+        C.Re = (R)C.u_guess_fyz * L / (R)C.ny_fyz;
+        C.ny = ny; C.tau = tau; C.omega = 1.f / tau;
+    }
+    // :87-108: inlet velocities times Cu_inverse
+    static void nonDimensionalizeInlet(std::vector<lbm_bc_inlet>& in, const LBMConstants& C) {
+        for (auto& r : in)
+            for (int a = 0; a < 3; a++) r.velocity[a] = (float)((float)r.velocity[a] * (float)C.Cu_inverse);
+    }
+    // :110-130: outlet densities / Cm * Cl^3
+    static void nonDimensionalizeOutlet(std::vector<lbm_bc_outlet>& out, const LBMConstants& C) {
+        const float Cm = (float)C.Cm, Cl = (float)C.Cl;
+        for (auto& r : out) r.density = (float)r.density / Cm * Cl * Cl * Cl;
+    }
 };
 
 inline void check(lbm_status s, const lbm_ctx* ctx, const char* what) {
@@ -155,9 +204,46 @@ public:
         if (ctx) lbm_destroy(ctx);
     }
 
-    // NonDimensiolnaliseFactorsVelocity converts physical inputs to lattice units; the constants here
-    // are lattice units already (as after the reference's convertToLattice)
-    void convertToLattice(bool /*verbose*/) {}
+    // SolverTurbulentLES.h:270-274: NONDYM::nonDimensionalize when physical inputs are given (ny_fyz > 0);
+    // with lattice-unit constants (ny_fyz = 0) nothing changes.  After a conversion, initializeSimulation
+    // also converts the inlet velocities and outlet densities (SolverTurbulentLES.h:118, :124) and the
+    // initial state (rho_fyz / Cm Cl^3, VelocityInit / Cu: InitializationEquilibriumConstVector.h:79-82).
+    void convertToLattice(bool verbose) {
+        if (!(Constants.ny_fyz > 0)) return;
+        NONDYM::nonDimensionalize(Constants);
+        converted = true;
+        if (verbose)
+            std::printf("Cl %g Cu %g Ct %g Re %g ny %g tau %g\n", Constants.Cl, Constants.Cu, Constants.Ct,
+                        Constants.Re, Constants.ny, Constants.tau);
+    }
+
+    // SolverTurbulentLES.h:276-323: step counts from physical times (plot_every, err_every, time over Ct)
+    // and the probe position in lattice cells (round(x / (BBmax - BBmin + 2 additional / resolution) n)).
+    // One of plot_every / plot_every_it and of err_every / err_every_it must be given, as the reference
+    // asserts.  The reference's probe asserts test lat >= dim (:313-315), the reverse of their message; the
+    // probe must lie inside the lattice here.
+    void initializeSimulationData(bool verbose) {
+        using R = float;
+        auto steps = [&](int& it, double every, const char* what) {
+            if (it == -1 && every != -1) it = (int)std::ceil((R)every / (R)Constants.Ct);
+            else if (it == -1) throw Error(LBM_ERR_INVALID, std::string("give ") + what + " or " + what + "_it");
+        };
+        steps(Constants.plot_every_it, Constants.plot_every, "plot_every");
+        steps(Constants.err_every_it, Constants.err_every, "err_every");
+        if (Constants.time >= 0) Constants.iterations = (int)std::ceil((R)Constants.time / (R)Constants.Ct);
+        if (verbose) std::printf("Plotting every %d iterations; %d iterations.\n", Constants.plot_every_it,
+                                 Constants.iterations);
+        if (Constants.probe_every_it != -1) {
+            const int dims[3] = {Constants.dimX_int, Constants.dimY_int, Constants.dimZ_int};
+            const R pad = 2 * ((R)Constants.additional_factor / (R)Constants.resolution_factor);
+            for (int a = 0; a < 3; a++) {
+                const R ext = (R)Constants.BBmax[a] - (R)Constants.BBmin[a] + pad;
+                const int lat = (int)std::round((R)Constants.ProbeLocation[a] / ext * (R)dims[a]);
+                if (lat < 0 || lat >= dims[a]) throw Error(LBM_ERR_INVALID, "Probe must be in the domain!");
+                Constants.ProbeLocationLat[a] = lat;
+            }
+        }
+    }
 
     // the context, geometry, boundary records and the equilibrium initial state
     // (SolverTurbulentLES.h:103-146; InitializationEquilibriumConstVector.h:103-224)
@@ -186,9 +272,19 @@ public:
         const size_t N = (size_t)c.nx * c.ny * c.nz;
         if (Data.meshFluid.size() != N) throw Error(LBM_ERR_INVALID, "meshFluid has the wrong size");
         check(lbm_set_flags(ctx, Data.meshFluid.data()), ctx, "lbm_set_flags");
-        check(lbm_set_bc(ctx, Data.meshBoundaryInlet.data(), (int32_t)Data.meshBoundaryInlet.size(),
-                         Data.meshBoundaryOutlet.data(), (int32_t)Data.meshBoundaryOutlet.size()),
-              ctx, "lbm_set_bc");
+        std::vector<lbm_bc_inlet> inlets = Data.meshBoundaryInlet;
+        std::vector<lbm_bc_outlet> outlets = Data.meshBoundaryOutlet;
+        double rho_init = Constants.rho0, u_init[3] = {Constants.VelocityInit[0], Constants.VelocityInit[1],
+                                                       Constants.VelocityInit[2]};
+        if (converted) {
+            NONDYM::nonDimensionalizeInlet(inlets, Constants);
+            NONDYM::nonDimensionalizeOutlet(outlets, Constants);
+            const float Cl = (float)Constants.Cl;
+            rho_init = (float)Constants.rho_fyz / (float)Constants.Cm * Cl * Cl * Cl;
+            for (int a = 0; a < 3; a++) u_init[a] = (float)Constants.VelocityInit[a] * (float)Constants.Cu_inverse;
+        }
+        check(lbm_set_bc(ctx, inlets.data(), (int32_t)inlets.size(), outlets.data(), (int32_t)outlets.size()), ctx,
+              "lbm_set_bc");
         if (SYMMETRYTYPE::on)
             check(lbm_set_symmetry(ctx, Data.meshBoundarySymmetry.data(), (int32_t)Data.meshBoundarySymmetry.size()),
                   ctx, "lbm_set_symmetry");
@@ -206,7 +302,7 @@ public:
                 throw Error(LBM_ERR_INVALID, "rhoInit / uInit have the wrong size");
             check(lbm_init_fields(ctx, Data.rhoInit.data(), Data.uInit.data()), ctx, "lbm_init_fields");
         } else {
-            check(lbm_init_equilibrium(ctx, Constants.rho0, Constants.VelocityInit), ctx, "lbm_init_equilibrium");
+            check(lbm_init_equilibrium(ctx, rho_init, u_init), ctx, "lbm_init_equilibrium");
         }
         if (std::is_same<TURBULENCETYPE, OmegaMLP>::value && !COLLISIONTYPE::laminar) {
             if (!Constants.mlp) throw Error(LBM_ERR_STATE, "OmegaMLP needs LBMConstants::mlp");
@@ -317,6 +413,7 @@ public:
 
 private:
     lbm_ctx* ctx = nullptr;
+    bool converted = false;  // convertToLattice converted physical inputs
 };
 
 }  // namespace lbm_gb300

@@ -167,6 +167,46 @@ class NonDimensiolnaliseFactorsVelocity:        # nonDimensionalisions/NonDimens
     def reference_tau(nu_lb):
         return nu_lb / 3.0 + 0.5
 
+    @staticmethod
+    def nonDimensionalize(c, nx):
+        """nonDimensionalize (:20-85) on a constants dict, in the reference's float arithmetic: reads BBmin,
+        BBmax, conversion_factor_fyz, u_guess_fyz, U_lb, rho_fyz, ny_fyz; sets L_fyz, Cl, Cu, Cu_inverse, Ct,
+        Crho, Cm, Cpressure, Re, nu, tau, omega.  tau = 3 nu + 1/2 (nu / 3 + 1/2 with tau_ref_compat).
+        U_lb >= cs or tau outside (0.5, 0.99) raise, where the reference asserts (:29, :81)."""
+        f = np.float32
+        with np.errstate(all="ignore"):
+            if not f(c["U_lb"]) < f(1.0) / np.sqrt(f(3.0)):
+                raise ValueError("U_lb must be below the speed of sound")
+            L = f(abs(f(c["BBmax"][0]) - f(c["BBmin"][0]))) * f(c.get("conversion_factor_fyz", 1.0))
+            Cl = L / f(nx)
+            Cu = f(c["u_guess_fyz"]) / f(c["U_lb"])
+            Ct = Cl / Cu
+            Crho = f(c.get("rho_fyz", 1.0))
+            Cm = Crho * Cl * Cl * Cl
+            ny = f(c["ny_fyz"]) * Ct / Cl / Cl
+            tau = ny / f(3.0) + f(0.5) if c.get("tau_ref_compat") else f(3.0) * ny + f(0.5)
+        if not (f(0.5) < tau < f(0.99)):
+            raise ValueError(f"tau = {float(tau)} outside (0.5, 0.99): change the resolution or the lattice speed")
+        c.update(L_fyz=float(L), Cl=float(Cl), Cu=float(Cu), Cu_inverse=float(f(1.0) / Cu), Ct=float(Ct),
+                 Crho=float(Crho), Cm=float(Cm), Cpressure=float(Cm / Cl / Ct / Ct),
+                 Re=float(f(c["u_guess_fyz"]) * L / f(c["ny_fyz"])), nu=float(ny), tau=float(tau),
+                 omega=float(f(1.0) / tau))
+        return c
+
+    @staticmethod
+    def nonDimensionalizeInlet(records, c):
+        """:87-108: inlet velocities times Cu_inverse (float); returns converted copies."""
+        k = np.float32(c["Cu_inverse"])
+        return [capi.make_inlet(r.vertex.x, r.vertex.y, r.vertex.z, tuple(r.normal),
+                                [float(np.float32(v) * k) for v in r.velocity], r.regular) for r in records]
+
+    @staticmethod
+    def nonDimensionalizeOutlet(records, c):
+        """:110-130: outlet densities / Cm * Cl^3 (float); returns converted copies."""
+        Cm, Cl = np.float32(c["Cm"]), np.float32(c["Cl"])
+        return [capi.make_outlet(r.vertex.x, r.vertex.y, r.vertex.z, tuple(r.normal),
+                                 float(np.float32(r.density) / Cm * Cl * Cl * Cl), r.regular) for r in records]
+
 
 STORAGE = {"f64": capi.LBM_STORAGE_F64, "f32": capi.LBM_STORAGE_F32, "f16dev": capi.LBM_STORAGE_F16DEV}
 
@@ -367,20 +407,68 @@ class SolverTurbulentLES:
         self.policies = dict(Collision=Collision, Turbulence=Turbulence, Inlet=Inlet, Outlet=Outlet,
                              Symmetry=Symmetry, Initialisation=Initialisation)
         self.solver = None
+        self._converted = False
 
     def convertToLattice(self, verbose=False):
-        return None  # constants are given in lattice units
+        """SolverTurbulentLES.h:270-274: converts physical inputs when the constants hold ny_fyz > 0
+        (NonDimensiolnaliseFactorsVelocity.nonDimensionalize); lattice-unit constants stay as given."""
+        c = self.C
+        if not c.get("ny_fyz", 0) > 0:
+            return None
+        NonDimensiolnaliseFactorsVelocity.nonDimensionalize(c, self.data["flags"].shape[2])
+        self._converted = True
+        if verbose:
+            print(f"Cl {c['Cl']:g} Cu {c['Cu']:g} Ct {c['Ct']:g} Re {c['Re']:g} ny {c['nu']:g} tau {c['tau']:g}")
+        return None
+
+    def initializeSimulationData(self, verbose=False):
+        """SolverTurbulentLES.h:276-323: plot_every_it, err_every_it and iterations from the physical times
+        over Ct (one of plot_every / plot_every_it and of err_every / err_every_it must be given), and the
+        probe cell round(x / (BBmax - BBmin + 2 additional / resolution) * n), which must lie inside the
+        lattice (the reference's asserts test the reverse of their message, :313-315)."""
+        c = self.C
+        f = np.float32
+        for what in ("plot_every", "err_every"):
+            if c.get(what + "_it", -1) == -1:
+                if c.get(what, -1) == -1:
+                    raise ValueError(f"give {what} or {what}_it")
+                c[what + "_it"] = int(np.ceil(f(c[what]) / f(c["Ct"])))
+        if c.get("time", -1) >= 0:
+            c["iterations"] = int(np.ceil(f(c["time"]) / f(c["Ct"])))
+        if c.get("probe_every_it", -1) != -1:
+            nz, ny, nx = self.data["flags"].shape
+            pad = f(2) * (f(c.get("additional_factor", 0.5)) / f(c.get("resolution_factor", 1.0)))
+            lat = []
+            for a, n in enumerate((nx, ny, nz)):
+                ext = f(c["BBmax"][a]) - f(c["BBmin"][a]) + pad
+                v = int(np.round(f(c["ProbeLocation"][a]) / ext * f(n)))
+                if not 0 <= v < n:
+                    raise ValueError("Probe must be in the domain!")
+                lat.append(v)
+            c["ProbeLocationLat"] = tuple(lat)
+        if verbose:
+            print(f"Plotting every {c['plot_every_it']} iterations; {c.get('iterations')} iterations.")
 
     def initializeSimulation(self, verbose=False):
         c, d = self.C, self.data
         self.solver = Solver(d["flags"].shape[::-1], collision=self.policies["Collision"],
                              turbulence=self.policies["Turbulence"], inlet=self.policies["Inlet"],
-                             storage=c.get("storage", "f32"), nu=c["nu"], cles=c.get("CLES", 0.173),
+                             storage=c.get("storage", "f32"), nu=c["nu"], tau=c.get("tau", 0.0),
+                             cles=c.get("CLES", 0.173),
                              periodic=c.get("periodic", (0, 0, 0)), force=c.get("force", (0.0, 0.0, 0.0)),
                              outlet=self.policies["Outlet"],
                              omega_dumping=(c.get("omegaDumpingLow", -1.0), c.get("omegaDumpingHigh", -1.0)))
         self.solver.set_flags(d["flags"])
-        self.solver.set_bc(d.get("inlets", ()), d.get("outlets", ()))
+        inlets, outlets = d.get("inlets", ()), d.get("outlets", ())
+        rho0, u0 = c.get("rho0", 1.0), c.get("VelocityInit", (0.0, 0.0, 0.0))
+        if self._converted:  # SolverTurbulentLES.h:118, :124; InitializationEquilibriumConstVector.h:79-82
+            inlets = NonDimensiolnaliseFactorsVelocity.nonDimensionalizeInlet(inlets, c)
+            outlets = NonDimensiolnaliseFactorsVelocity.nonDimensionalizeOutlet(outlets, c)
+            f = np.float32
+            Cl = f(c["Cl"])
+            rho0 = float(f(c.get("rho_fyz", 1.0)) / f(c["Cm"]) * Cl * Cl * Cl)
+            u0 = tuple(float(f(v) * f(c["Cu_inverse"])) for v in u0)
+        self.solver.set_bc(inlets, outlets)
         if self.policies["Symmetry"] is BounceSymmetryHalf:
             self.solver.set_symmetry(d.get("symmetry", ()))
         if self.policies["Initialisation"] is InitializationEquilibriumVariables:
@@ -389,7 +477,7 @@ class SolverTurbulentLES:
             rho, u = read_variables_vtk(path, self.solver.shape)
             self.solver.init_fields(rho, u)
         else:
-            self.solver.init_equilibrium(c.get("rho0", 1.0), c.get("VelocityInit", (0.0, 0.0, 0.0)))
+            self.solver.init_equilibrium(rho0, u0)
 
     def runSimulation(self):
         c = self.C

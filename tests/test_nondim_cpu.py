@@ -1,0 +1,131 @@
+"""NonDimensiolnaliseFactorsVelocity (nonDimensionalisions/NonDimensiolnaliseFactorsVelocity.h:20-130) and
+initializeSimulationData (SolverTurbulentLES.h:276-323) of the host mirrors, on the CPU: the factors
+restated here in double agree with the mirrors' float arithmetic to float precision, the C++ and the
+Python mirrors agree bit for bit, and the checks the reference asserts raise."""
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from lb_gb300 import capi
+from lb_gb300.solver import (NonDimensiolnaliseFactorsVelocity as ND, SolverTurbulentLES)
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+# physical inputs of the shape main.cu:142-152 sets (air, U_lb = 0.09), on a 1 m x 0.5 m x 0.5 m box
+PHYS = dict(BBmin=(0.0, 0.0, 0.0), BBmax=(1.0, 0.5, 0.5), conversion_factor_fyz=1.0, u_guess_fyz=4.0, U_lb=0.09,
+            rho_fyz=1.293, ny_fyz=2e-4)
+NX = 128
+
+
+def test_factors_follow_the_definitions():
+    c = ND.nonDimensionalize(dict(PHYS), NX)
+    Cl = 1.0 / NX
+    Cu = 4.0 / 0.09
+    Ct = Cl / Cu
+    nu = 2e-4 * Ct / Cl ** 2
+    ref = dict(L_fyz=1.0, Cl=Cl, Cu=Cu, Cu_inverse=1 / Cu, Ct=Ct, Crho=1.293, Cm=1.293 * Cl ** 3,
+               Cpressure=1.293 * Cl ** 3 / Cl / Ct ** 2, Re=4.0 * 1.0 / 2e-4, nu=nu, tau=3 * nu + 0.5,
+               omega=1 / (3 * nu + 0.5))
+    for k, v in ref.items():
+        assert abs(c[k] - v) <= 3e-7 * abs(v), (k, c[k], v)
+    r = ND.nonDimensionalize(dict(PHYS, tau_ref_compat=True), NX)
+    assert abs(r["tau"] - (nu / 3 + 0.5)) <= 3e-7 and r["tau"] < c["tau"]
+
+
+def test_reference_asserts_raise():
+    with pytest.raises(ValueError):
+        ND.nonDimensionalize(dict(PHYS, U_lb=0.6), NX)  # above cs = 0.577
+    with pytest.raises(ValueError):
+        ND.nonDimensionalize(dict(PHYS, ny_fyz=0.5), NX)  # tau = 4.8
+
+
+def test_records_and_initial_state_convert():
+    c = ND.nonDimensionalize(dict(PHYS), NX)
+    ins = ND.nonDimensionalizeInlet([capi.make_inlet(0, 1, 2, (-1, 0, 0), (1.5, 0.0, -0.25))], c)
+    assert ins[0].velocity[0] == pytest.approx(1.5 / c["Cu"], rel=1e-6)
+    assert ins[0].velocity[2] == pytest.approx(-0.25 / c["Cu"], rel=1e-6)
+    assert (ins[0].vertex.x, ins[0].vertex.y, ins[0].vertex.z, ins[0].normal[0]) == (0, 1, 2, -1.0)
+    outs = ND.nonDimensionalizeOutlet([capi.make_outlet(9, 1, 2, (1, 0, 0), 1.293)], c)
+    assert outs[0].density == pytest.approx(1.0, rel=1e-6)
+
+
+def test_simulation_data_step_counts_and_probe():
+    flags = np.ones((8, 16, NX), np.int32)
+    c = dict(PHYS, nu=0.0, plot_every=0.05, err_every_it=100, time=0.5, probe_every_it=10,
+             ProbeLocation=(0.5, 0.25, 0.125), additional_factor=0.0, resolution_factor=1.0)
+    s = SolverTurbulentLES(constants=c, data={"flags": flags})
+    s.convertToLattice()
+    s.initializeSimulationData()
+    f = np.float32
+    assert c["plot_every_it"] == int(np.ceil(f(0.05) / f(c["Ct"])))
+    assert c["err_every_it"] == 100
+    assert c["iterations"] == int(np.ceil(f(0.5) / f(c["Ct"])))
+    # x: 0.5 / 1.0 * 128 = 64; y: 0.25 / 0.5 * 16 = 8; z: 0.125 / 0.5 * 8 = 2
+    assert c["ProbeLocationLat"] == (64, 8, 2)
+    with pytest.raises(ValueError):
+        SolverTurbulentLES(constants=dict(c, plot_every_it=-1, plot_every=-1), data={"flags": flags}) \
+            .initializeSimulationData()
+    bad = dict(c, ProbeLocation=(1.5, 0.25, 0.125))
+    with pytest.raises(ValueError):
+        SolverTurbulentLES(constants=bad, data={"flags": flags}).initializeSimulationData()
+
+
+def test_cpp_mirror_matches_python_bit_for_bit(built_lib):
+    src = r'''
+#include <cstdio>
+#include "lbm_solver.hpp"
+using namespace lbm_gb300;
+int main() {
+    LBMConstants C;
+    C.dimX_int = %d;
+    C.BBmin[0] = 0.0; C.BBmax[0] = 1.0; C.conversion_factor_fyz = 1.0;
+    C.u_guess_fyz = 4.0; C.U_lb = 0.09; C.rho_fyz = 1.293; C.ny_fyz = 2e-4;
+    NonDimensiolnaliseFactorsVelocity::nonDimensionalize(C);
+    std::printf("%%.9g %%.9g %%.9g %%.9g %%.9g %%.9g %%.9g %%.9g %%.9g\n", C.Cl, C.Cu, C.Ct, C.Cm, C.Cpressure, C.Re, C.ny,
+                C.tau, C.omega);
+    C.tau_ref_compat = true;
+    NonDimensiolnaliseFactorsVelocity::nonDimensionalize(C);
+    std::printf("%%.9g\n", C.tau);
+    LBMConstants K;
+    K.dimX_int = %d; K.dimY_int = 16; K.dimZ_int = 8;
+    K.BBmin[0] = 0.0; K.BBmax[0] = 1.0; K.BBmax[1] = 0.5; K.BBmax[2] = 0.5; K.conversion_factor_fyz = 1.0;
+    K.u_guess_fyz = 4.0; K.U_lb = 0.09; K.rho_fyz = 1.293; K.ny_fyz = 2e-4;
+    K.plot_every = 0.05; K.err_every_it = 100; K.time = 0.5; K.probe_every_it = 10;
+    K.ProbeLocation[0] = 0.5; K.ProbeLocation[1] = 0.25; K.ProbeLocation[2] = 0.125;
+    K.additional_factor = 0.0; K.resolution_factor = 1.0;
+    LBMData D;
+    SolverTurbulentLES<D3Q27, InitializationEquilibriumConstVector, CollisionCumD3Q27Turbulent2015, StreamingAB,
+                       BounceBackWallHalf, NoSymmetry, Periodic, InletVelocityEquilibrium,
+                       OutletDensityInterpolated, MomentDensityVelocityN27, OmegaLES, ErrorQuadratic,
+                       NonDimensiolnaliseFactorsVelocity, MomentTimeAvg> s(K, D);
+    s.convertToLattice(false);
+    s.initializeSimulationData(false);
+    std::printf("%%d %%d %%d %%d %%d %%d\n", K.plot_every_it, K.err_every_it, K.iterations, K.ProbeLocationLat[0],
+                K.ProbeLocationLat[1], K.ProbeLocationLat[2]);
+    return 0;
+}
+''' % (NX, NX)
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "t.cpp")
+        exe = os.path.join(d, "t")
+        with open(p, "w") as fh:
+            fh.write(src)
+        lib = os.path.join(ROOT, "lb_gb300")
+        r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), p,
+                            "-L", lib, "-llbm_gb300", "-Wl,-rpath," + lib, "-o", exe], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    c = ND.nonDimensionalize(dict(PHYS), NX)
+    want = [c[k] for k in ("Cl", "Cu", "Ct", "Cm", "Cpressure", "Re", "nu", "tau", "omega")]
+    want.append(ND.nonDimensionalize(dict(PHYS, tau_ref_compat=True), NX)["tau"])
+    assert [float(v) for v in out[:10]] == [float("%.9g" % w) for w in want]
+    k = dict(PHYS, nu=0.0, plot_every=0.05, err_every_it=100, time=0.5, probe_every_it=10,
+             ProbeLocation=(0.5, 0.25, 0.125), additional_factor=0.0, resolution_factor=1.0)
+    s = SolverTurbulentLES(constants=k, data={"flags": np.ones((8, 16, NX), np.int32)})
+    s.convertToLattice()
+    s.initializeSimulationData()
+    assert [int(v) for v in out[10:]] == [k["plot_every_it"], k["err_every_it"], k["iterations"],
+                                          *k["ProbeLocationLat"]]
