@@ -217,6 +217,65 @@ lbm_status lbm_checkpoint_load(lbm_ctx* ctx, const char* path);
 /* in place: every fluid cell (>0) gets 1 + number of solid cells in its 26-neighbourhood */
 lbm_status lbm_mesher_wall_pass(int32_t* flags, int32_t nx, int32_t ny, int32_t nz);
 
+/* ---- host mesher, cuboid boundary passes (geometryMesherBoundary.h:47-437) ---------------------
+ * The sampling frame of the mesher (LBMConstants): cell (i, j, k) is tested at its centre
+ * (i + 0.5 - additional) / resolution + bbmin per axis (in double, rounded to float for the inlet passes as
+ * the reference's RealType look coordinates are).  A cuboid (geometryObjectCuboid.h:9-52) is the axis box
+ * spanned by three corners, closed on every face; its id (a negative flag: -1 inlet, -2 outlet or
+ * symmetry, -3 periodic) replaces the flag of every cell a pass takes.  Each pass appends records at
+ * records[*n] (room for capacity records in all) and advances *n; LBM_ERR_INVALID when they do not fit
+ * (nothing is written then).  Run the wall pass first: the regular field is read off the wall-pass
+ * count (inlets: 1 unless the flag is above 10; outlets, symmetry, periodic: 1 only for a flag of 10). */
+typedef struct lbm_mesh_frame {
+    int32_t dims[3];
+    float resolution_factor, additional_factor;
+    float bbmin[3];
+} lbm_mesh_frame;
+typedef struct lbm_cuboid {
+    double x1[3], x2[3], x3[3];
+    int32_t id;
+} lbm_cuboid;
+typedef struct lbm_bc_periodic {    /* boundaryConditionPeriodic (LBMTraits.h): mesher output only; the
+                                       kernels wrap periodic axes by index (lbm_config.periodic) */
+    lbm_vertex vertex;
+    float normal[3];
+    int32_t periodic_index;
+    int32_t regular;
+} lbm_bc_periodic;
+/* meshingBoundaryConditionInletUniform (:47-108): cells with flag > 0.  As the reference, a velocity with
+ * three equal components is refused (LBM_ERR_INVALID: the reference's guard against a scalar passed as a
+ * vector). */
+lbm_status lbm_mesher_inlet_uniform(const lbm_mesh_frame* frame, int32_t* flags, const lbm_cuboid* cuboid,
+                                    const float normal[3], const float velocity[3], lbm_bc_inlet* records,
+                                    int64_t capacity, int64_t* n);
+/* meshingBoundaryConditionInletParaboloidCircle (:111-177): the uniform pass at zero velocity, then every
+ * inlet record so far whose cell centre lies in the cuboid and within radius of center gets
+ * -3 u_mean (1 - (d / radius)^2) normal (clipped at 0).  The reference's own zero-velocity call trips the
+ * guard above and throws; the pass here skips that guard. */
+lbm_status lbm_mesher_inlet_paraboloid_circle(const lbm_mesh_frame* frame, int32_t* flags, const lbm_cuboid* cuboid,
+                                              const double center[3], float radius, const float normal[3],
+                                              float mean_velocity, lbm_bc_inlet* records, int64_t capacity,
+                                              int64_t* n);
+/* meshingBoundaryConditionInletParaboloidRectangle (:179-274): as above with the product profile
+ * 2 u_mean prod_a s_a (D_a - s_a) / (prod_a D_a^2 / 16) over the two in-plane axes (s_a measured from the
+ * face's low corner center - D/2); inlet_dims[a] along the normal is set to 1 on return, as the
+ * reference does to its by-reference arguments. */
+lbm_status lbm_mesher_inlet_paraboloid_rectangle(const lbm_mesh_frame* frame, int32_t* flags,
+                                                 const lbm_cuboid* cuboid, const double center[3],
+                                                 float inlet_dims[3], const float normal[3], float mean_velocity,
+                                                 lbm_bc_inlet* records, int64_t capacity, int64_t* n);
+/* meshingBoundaryConditionOutlet (:276-325), ...Symmetry (:327-377), ...Periodic (:379-437): cells with a
+ * nonzero flag (earlier boundary ids included). */
+lbm_status lbm_mesher_outlet(const lbm_mesh_frame* frame, int32_t* flags, const lbm_cuboid* cuboid,
+                             const float normal[3], float density, lbm_bc_outlet* records, int64_t capacity,
+                             int64_t* n);
+lbm_status lbm_mesher_symmetry(const lbm_mesh_frame* frame, int32_t* flags, const lbm_cuboid* cuboid,
+                               const float normal[3], lbm_bc_symmetry* records, int64_t capacity, int64_t* n);
+lbm_status lbm_mesher_periodic(const lbm_mesh_frame* frame, int32_t* flags, const lbm_cuboid* cuboid,
+                               const float normal[3], int32_t periodic_index, lbm_bc_periodic* records,
+                               int64_t capacity, int64_t* n);
+const char* lbm_mesher_last_error(void);
+
 /* ---- mesh-matrix text files (postprocesors/outputerMesh.h:19-211) ------------ */
 /* Writes the reference's format (outputerMesh::MeshMatrixOut): the header "Dimensions: nx ny nz ",
  * resolution and additional factors, BBmax x/y/z, BBmin x/y/z (as the reference's float fields print

@@ -113,6 +113,7 @@ struct LBMData {
     std::vector<lbm_bc_inlet> meshBoundaryInlet;
     std::vector<lbm_bc_outlet> meshBoundaryOutlet;
     std::vector<lbm_bc_symmetry> meshBoundarySymmetry;  // used with BounceSymmetryHalf
+    std::vector<lbm_bc_periodic> meshBoundaryPeriodic;  // mesher output; the kernels wrap periodic axes by index
     std::vector<double> rhoInit, uInit;        // optional initial fields (else VelocityInit everywhere)
     std::vector<double> rho, u;                // host copies after the run (u: ux[N], uy[N], uz[N])
     std::vector<double> rhoTimeAvg, uTimeAvg, uuTimeAvg;
@@ -124,6 +125,119 @@ class Error : public std::runtime_error {
 public:
     Error(lbm_status s, const std::string& m) : std::runtime_error(m), status(s) {}
     lbm_status status;
+};
+
+// geometry/geometryObjectCuboid.h:9-52: the axis box spanned by three corners; id is the negative flag
+// its cells get (-1 inlet, -2 outlet or symmetry, -3 periodic)
+struct geometryObjectCuboid {
+    lbm_cuboid c{};
+    geometryObjectCuboid(const double X1[3], const double X2[3], const double X3[3], int id) {
+        for (int a = 0; a < 3; a++) { c.x1[a] = X1[a]; c.x2[a] = X2[a]; c.x3[a] = X3[a]; }
+        c.id = id;
+    }
+};
+
+// geometry/geometryMesherBoundary.h: the wall pass and the cuboid boundary passes on Data.meshFluid (x
+// fastest, changed in place) with the sampling frame of Constants (dimensions, resolution_factor,
+// additional_factor, BBmin); the records go straight into Data's lists (the reference's
+// compileBoundaryArray* copies, :486-603, are no-ops here).  Host code of the C ABI (lbm_mesher_*).
+class geometryMesherBoundary {
+public:
+    geometryMesherBoundary(LBMConstants& constants, LBMData& data) : C(constants), D(data) {}
+
+    void meshingBoundaryWall(bool /*verbose*/) {
+        run(lbm_mesher_wall_pass(D.meshFluid.data(), C.dimX_int, C.dimY_int, C.dimZ_int));
+    }
+    void meshingBoundaryConditionInletUniform(const geometryObjectCuboid& cub, const float normal[3],
+                                              const float velocity[3], bool /*verbose*/) {
+        grow(D.meshBoundaryInlet, cub.c, [&](lbm_bc_inlet* r, int64_t cap, int64_t* n) {
+            return lbm_mesher_inlet_uniform(&frame_, flags(), &cub.c, normal, velocity, r, cap, n);
+        });
+    }
+    void meshingBoundaryConditionInletParaboloidCircle(const geometryObjectCuboid& cub, const double center[3],
+                                                       float radius, const float normal[3], float mean_velocity,
+                                                       bool /*verbose*/) {
+        grow(D.meshBoundaryInlet, cub.c, [&](lbm_bc_inlet* r, int64_t cap, int64_t* n) {
+            return lbm_mesher_inlet_paraboloid_circle(&frame_, flags(), &cub.c, center, radius, normal, mean_velocity,
+                                                      r, cap, n);
+        });
+    }
+    // the inlet dimensions along the normal are set to 1 on return, as the reference's by-reference arguments
+    void meshingBoundaryConditionInletParaboloidRectangle(const geometryObjectCuboid& cub, const double center[3],
+                                                          float& dimX, float& dimY, float& dimZ, const float normal[3],
+                                                          float mean_velocity, bool /*verbose*/) {
+        float d[3] = {dimX, dimY, dimZ};
+        grow(D.meshBoundaryInlet, cub.c, [&](lbm_bc_inlet* r, int64_t cap, int64_t* n) {
+            return lbm_mesher_inlet_paraboloid_rectangle(&frame_, flags(), &cub.c, center, d, normal, mean_velocity,
+                                                         r, cap, n);
+        });
+        dimX = d[0]; dimY = d[1]; dimZ = d[2];
+    }
+    void meshingBoundaryConditionOutlet(const geometryObjectCuboid& cub, const float normal[3], float density,
+                                        bool /*verbose*/) {
+        grow(D.meshBoundaryOutlet, cub.c, [&](lbm_bc_outlet* r, int64_t cap, int64_t* n) {
+            return lbm_mesher_outlet(&frame_, flags(), &cub.c, normal, density, r, cap, n);
+        });
+    }
+    void meshingBoundaryConditionSymmetry(const geometryObjectCuboid& cub, const float normal[3], bool /*verbose*/) {
+        grow(D.meshBoundarySymmetry, cub.c, [&](lbm_bc_symmetry* r, int64_t cap, int64_t* n) {
+            return lbm_mesher_symmetry(&frame_, flags(), &cub.c, normal, r, cap, n);
+        });
+    }
+    void meshingBoundaryConditionPeriodic(const geometryObjectCuboid& cub, const float normal[3], int periodicIndex,
+                                          bool /*verbose*/) {
+        grow(D.meshBoundaryPeriodic, cub.c, [&](lbm_bc_periodic* r, int64_t cap, int64_t* n) {
+            return lbm_mesher_periodic(&frame_, flags(), &cub.c, normal, periodicIndex, r, cap, n);
+        });
+    }
+    void compileBoundaryArrayInlets(bool) {}
+    void compileBoundaryArrayOutlets(bool) {}
+    void compileBoundaryArraySymmetry(bool) {}
+    void compileBoundaryArrayPeriodic(bool) {}
+    void compileBoundaryArrayWall(bool) {}  // wall links are found from the flags by the kernels
+    void arrayTransfer(bool) {}             // initializeSimulation uploads flags and records
+
+private:
+    LBMConstants& C;
+    LBMData& D;
+    lbm_mesh_frame frame_{};
+
+    int32_t* flags() {
+        const size_t N = (size_t)C.dimX_int * C.dimY_int * C.dimZ_int;
+        if (D.meshFluid.size() != N) throw Error(LBM_ERR_INVALID, "meshFluid has the wrong size");
+        frame_.dims[0] = C.dimX_int; frame_.dims[1] = C.dimY_int; frame_.dims[2] = C.dimZ_int;
+        frame_.resolution_factor = (float)C.resolution_factor;
+        frame_.additional_factor = (float)C.additional_factor;
+        for (int a = 0; a < 3; a++) frame_.bbmin[a] = (float)C.BBmin[a];
+        return D.meshFluid.data();
+    }
+    static void run(lbm_status s) {
+        if (s != LBM_OK) throw Error(s, std::string("mesher: ") + lbm_mesher_last_error());
+    }
+    // room for the cells of the cuboid's index box widened by one cell per side (centre test bound)
+    int64_t bound(const lbm_cuboid& c) const {
+        const int dims[3] = {C.dimX_int, C.dimY_int, C.dimZ_int};
+        int64_t n = 1;
+        for (int a = 0; a < 3; a++) {
+            const double lo = std::fmin(c.x1[a], std::fmin(c.x2[a], c.x3[a]));
+            const double hi = std::fmax(c.x1[a], std::fmax(c.x2[a], c.x3[a]));
+            const double r = C.resolution_factor, ad = C.additional_factor, bb = C.BBmin[a];
+            const double i0 = std::fmax(0.0, std::floor((lo - bb) * r + ad - 0.5) - 1);
+            const double i1 = std::fmin(dims[a] - 1.0, std::ceil((hi - bb) * r + ad - 0.5) + 1);
+            n *= i1 >= i0 ? (int64_t)(i1 - i0) + 1 : 0;
+        }
+        return n;
+    }
+    template <class Rec, class Pass>
+    void grow(std::vector<Rec>& v, const lbm_cuboid& c, Pass pass) {
+        const int64_t have = (int64_t)v.size();
+        const int64_t cap = have + bound(c);
+        v.resize((size_t)cap);
+        int64_t n = have;
+        const lbm_status s = pass(v.data(), cap, &n);
+        v.resize((size_t)(s == LBM_OK ? n : have));
+        run(s);
+    }
 };
 
 // nonDimensionalisions/NonDimensiolnaliseFactorsVelocity.h: lattice units from the physical inputs, in

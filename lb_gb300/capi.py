@@ -92,6 +92,20 @@ class LbmBcSymmetry(C.Structure):
     _fields_ = [("vertex", LbmVertex), ("normal", C.c_float * 3), ("regular", C.c_int32)]
 
 
+class LbmBcPeriodic(C.Structure):
+    _fields_ = [("vertex", LbmVertex), ("normal", C.c_float * 3), ("periodic_index", C.c_int32),
+                ("regular", C.c_int32)]
+
+
+class LbmMeshFrame(C.Structure):
+    _fields_ = [("dims", C.c_int32 * 3), ("resolution_factor", C.c_float), ("additional_factor", C.c_float),
+                ("bbmin", C.c_float * 3)]
+
+
+class LbmCuboid(C.Structure):
+    _fields_ = [("x1", C.c_double * 3), ("x2", C.c_double * 3), ("x3", C.c_double * 3), ("id", C.c_int32)]
+
+
 class LbmVtkField(C.Structure):
     _fields_ = [("name", C.c_char_p), ("components", C.c_int32), ("data", C.POINTER(C.c_double)),
                 ("scale", C.c_double)]
@@ -216,6 +230,19 @@ def lib():
         "lbm_vtk_write": ([C.c_char_p, C.c_char_p, ip, f64, f64, dp, C.POINTER(LbmVtkField), i32], i32),
         "lbm_probe_csv_append": ([C.c_char_p, f64, dp, f64, f64, f64], i32),
         "lbm_vtk_read_variables": ([C.c_char_p, ip, dp, dp], i32),
+        "lbm_mesher_inlet_uniform": ([C.POINTER(LbmMeshFrame), ip, C.POINTER(LbmCuboid), fp, fp,
+                                      C.POINTER(LbmBcInlet), i64, C.POINTER(C.c_int64)], i32),
+        "lbm_mesher_inlet_paraboloid_circle": ([C.POINTER(LbmMeshFrame), ip, C.POINTER(LbmCuboid), dp, C.c_float, fp,
+                                                C.c_float, C.POINTER(LbmBcInlet), i64, C.POINTER(C.c_int64)], i32),
+        "lbm_mesher_inlet_paraboloid_rectangle": ([C.POINTER(LbmMeshFrame), ip, C.POINTER(LbmCuboid), dp, fp, fp,
+                                                   C.c_float, C.POINTER(LbmBcInlet), i64, C.POINTER(C.c_int64)], i32),
+        "lbm_mesher_outlet": ([C.POINTER(LbmMeshFrame), ip, C.POINTER(LbmCuboid), fp, C.c_float,
+                               C.POINTER(LbmBcOutlet), i64, C.POINTER(C.c_int64)], i32),
+        "lbm_mesher_symmetry": ([C.POINTER(LbmMeshFrame), ip, C.POINTER(LbmCuboid), fp, C.POINTER(LbmBcSymmetry), i64,
+                                 C.POINTER(C.c_int64)], i32),
+        "lbm_mesher_periodic": ([C.POINTER(LbmMeshFrame), ip, C.POINTER(LbmCuboid), fp, i32, C.POINTER(LbmBcPeriodic),
+                                 i64, C.POINTER(C.c_int64)], i32),
+        "lbm_mesher_last_error": ([], C.c_char_p),
         "lbm_vtk_last_error": ([], C.c_char_p),
     }
     for name, (args, res) in sig.items():
