@@ -364,7 +364,7 @@ public:
     void initializeSimulation(bool verbose) {
         lbm_config c{};
         c.nx = Constants.dimX_int; c.ny = Constants.dimY_int; c.nz = Constants.dimZ_int;
-        for (int a = 0; a < 3; a++) c.periodic[a] = PERIODICTYPE::on ? Constants.periodic[a] : 0;
+        for (int a = 0; a < 3; a++) c.periodic[a] = PERIODICTYPE::on && !laminar_loop ? Constants.periodic[a] : 0;
         c.collision = COLLISIONTYPE::code;
         c.closure = COLLISIONTYPE::laminar ? LBM_CLOSURE_NONE : TURBULENCETYPE::code;
         c.storage = Constants.storage;
@@ -442,13 +442,14 @@ public:
 
     // outputerVTK::variablesVTK / variablesTimeAvgVTK (outputerVTK.h:59-187, :318-447): rho Crho,
     // p Cpressure (p = rho cs2) and U Cu, structured points
+    // pressure_name: the field is "pressure" (time averages, lattice dumps), else "p"; lattice: factors 1
     void writeVTK(const std::string& path, const std::vector<double>& rho, const std::vector<double>& u,
-                  bool time_avg) {
+                  bool pressure_name, bool lattice = false) {
         std::vector<double> p(rho.size());
         for (size_t i = 0; i < rho.size(); i++) p[i] = rho[i] / 3.0;
-        const lbm_vtk_field f[3] = {{"rho", 1, rho.data(), Constants.Crho},
-                                    {time_avg ? "pressure" : "p", 1, p.data(), Constants.Cpressure},
-                                    {"U", 3, u.data(), Constants.Cu}};
+        const lbm_vtk_field f[3] = {{"rho", 1, rho.data(), lattice ? 1.0 : Constants.Crho},
+                                    {pressure_name ? "pressure" : "p", 1, p.data(), lattice ? 1.0 : Constants.Cpressure},
+                                    {"U", 3, u.data(), lattice ? 1.0 : Constants.Cu}};
         const int32_t dims[3] = {Constants.dimX_int, Constants.dimY_int, Constants.dimZ_int};
         const lbm_status st = lbm_vtk_write(path.c_str(), "LBE variables", dims, Constants.resolution_factor,
                                             Constants.additional_factor, Constants.BBmin, f, 3);
@@ -466,13 +467,13 @@ public:
         const int avg = Constants.iterationsMomentAvg;
         const int avg_begin = it - avg + 1;  // lbm_timeavg counts the states produced after the call
         auto probe_after = [&](int k) {
-            return Constants.probe_every_it > 0 && k % Constants.probe_every_it == 0 &&
+            return !laminar_loop && Constants.probe_every_it > 0 && k % Constants.probe_every_it == 0 &&
                    k >= it - Constants.probe_iterations;
         };
         auto err_after = [&](int k) { return Constants.err_every_it > 0 && k % Constants.err_every_it == 0 && k != 0; };
         auto plot_after = [&](int k) {
             return !Constants.results_dir.empty() && Constants.plot_every_it > 0 && k % Constants.plot_every_it == 0 &&
-                   k != 0;
+                   (k != 0 || laminar_loop);
         };
         const size_t N = (size_t)Constants.dimX_int * Constants.dimY_int * Constants.dimZ_int;
         bool averaging = false;
@@ -500,8 +501,14 @@ public:
                 Data.rho.resize(N);
                 Data.u.resize(3 * N);
                 check(lbm_get_moments(ctx, Data.rho.data(), Data.u.data()), ctx, "lbm_get_moments");
-                writeVTK(Constants.results_dir + "/variables." + std::to_string(j / Constants.plot_every_it) + ".vtk",
-                         Data.rho, Data.u, false);
+                if (laminar_loop)  // outputerVTK::variablesLatticeVTK (outputerVTK.h:189-316): lattice units
+                    writeVTK(Constants.results_dir + "/variablesLattice" + std::to_string(j / Constants.plot_every_it) +
+                                 ".vtk",
+                             Data.rho, Data.u, true, true);
+                else
+                    writeVTK(Constants.results_dir + "/variables." + std::to_string(j / Constants.plot_every_it) +
+                                 ".vtk",
+                             Data.rho, Data.u, false);
             }
         }
         if (averaging) check(lbm_timeavg_end(ctx), ctx, "lbm_timeavg_end");
@@ -525,9 +532,36 @@ public:
     LBMConstants& Constants;
     LBMData& Data;
 
+protected:
+    // SolverLaminar's loop (SolverLaminar.h:127-204): no probe, a lattice-unit dump also after the first
+    // step, and no periodic hook (the reference's laminar loop never calls PERIODICTYPE)
+    bool laminar_loop = false;
+
 private:
     lbm_ctx* ctx = nullptr;
     bool converted = false;  // convertToLattice converted physical inputs
+};
+
+// solvers/SolverLaminar.h:61-237: the same policies without a turbulence model.  The step runs with the
+// global omega = 1/tau (OmegaNo); initializeSimulation first runs initializeSimulationData, as the
+// reference's does (:99).
+template <typename MODELTYPE, typename INITIALIZATIONTYPE, typename COLLISIONTYPE, typename STREAMINGTYPE,
+          typename BOUNCEBACKWALLTYPE, typename SYMMETRYTYPE, typename PERIODICTYPE, typename INLETTYPE,
+          typename OUTLETTYPE, typename MOMENTTYPE, typename ERRORTYPE, typename NONDYM, typename MOMENTTIMEAVGTYPE>
+class SolverLaminar
+    : public SolverTurbulentLES<MODELTYPE, INITIALIZATIONTYPE, COLLISIONTYPE, STREAMINGTYPE, BOUNCEBACKWALLTYPE,
+                                SYMMETRYTYPE, PERIODICTYPE, INLETTYPE, OUTLETTYPE, MOMENTTYPE, OmegaNo, ERRORTYPE, NONDYM,
+                                MOMENTTIMEAVGTYPE> {
+    using Base = SolverTurbulentLES<MODELTYPE, INITIALIZATIONTYPE, COLLISIONTYPE, STREAMINGTYPE, BOUNCEBACKWALLTYPE,
+                                    SYMMETRYTYPE, PERIODICTYPE, INLETTYPE, OUTLETTYPE, MOMENTTYPE, OmegaNo, ERRORTYPE,
+                                    NONDYM, MOMENTTIMEAVGTYPE>;
+
+public:
+    SolverLaminar(LBMConstants& constants, LBMData& data) : Base(constants, data) { this->laminar_loop = true; }
+    void initializeSimulation(bool verbose) {
+        this->initializeSimulationData(verbose);
+        Base::initializeSimulation(verbose);
+    }
 };
 
 }  // namespace lbm_gb300

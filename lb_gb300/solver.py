@@ -501,3 +501,29 @@ class SolverTurbulentLES:
         if navg:
             self.solver.timeavg_end()
         return errors
+
+
+class SolverLaminar(SolverTurbulentLES):
+    """solvers/SolverLaminar.h:61-237: the same policies without a turbulence model (the step relaxes with
+    the global 1/tau) and without the periodic hook, which the reference's laminar loop never calls;
+    initializeSimulation runs initializeSimulationData first (:99)."""
+
+    def __init__(self, Model=D3Q27, Initialisation=InitializationEquilibriumConstVector,
+                 Collision=CollisionCumD3Q27Laminar, Streaming=StreamingAB, BounceBackWall=BounceBackWallHalf,
+                 Symmetry=NoSymmetry, Periodic_=NoPeriodic, Inlet=InletVelocityMovingWall,
+                 Outlet=OutletDensityInterpolated, Moments=MomentDensityVelocityN27, Error=ErrorQuadratic,
+                 NonDim=NonDimensiolnaliseFactorsVelocity, TimeAvg=MomentTimeAvg, *, constants, data):
+        super().__init__(Model, Initialisation, Collision, Streaming, BounceBackWall, Symmetry, Periodic_, Inlet, Outlet,
+                         Moments, OmegaNo, Error, NonDim, TimeAvg, constants=constants, data=data)
+
+    def initializeSimulation(self, verbose=False):
+        self.initializeSimulationData(verbose)
+        saved = self.C.get("periodic")
+        self.C["periodic"] = (0, 0, 0)
+        try:
+            super().initializeSimulation(verbose)
+        finally:
+            if saved is None:
+                self.C.pop("periodic")
+            else:
+                self.C["periodic"] = saved

@@ -76,9 +76,12 @@ int main() {
                        BounceBackWallHalf, NoSymmetry, NoPeriodic, InletVelocityMovingWall,
                        OutletDensityInterpolated, MomentDensityVelocityN27, OmegaNo, ErrorQuadratic,
                        NonDimensiolnaliseFactorsVelocity, MomentTimeAvg> g(C, D);
+    SolverLaminar<D3Q27, InitializationEquilibriumConstVector, CollisionCumD3Q27Laminar, StreamingAB,
+                  BounceBackWallHalf, NoSymmetry, Periodic, InletVelocityEquilibrium, OutletDensityInterpolated,
+                  MomentDensityVelocityN27, ErrorQuadratic, NonDimensiolnaliseFactorsVelocity, MomentTimeAvg> h(C, D);
     static_assert(CollisionSRTunroll::laminar && CollisionCumD3Q27Laminar::laminar &&
                   !CollisionCumD3Q27Turbulent2015::laminar, "laminar tags");
-    (void)a; (void)b; (void)c; (void)e; (void)f; (void)g;
+    (void)a; (void)b; (void)c; (void)e; (void)f; (void)g; (void)h;
     return 0;
 }
 '''

@@ -129,3 +129,14 @@ int main() {
     s.initializeSimulationData()
     assert [int(v) for v in out[10:]] == [k["plot_every_it"], k["err_every_it"], k["iterations"],
                                           *k["ProbeLocationLat"]]
+
+
+def test_laminar_solver_sets_up_like_the_reference():
+    """SolverLaminar (SolverLaminar.h:94-125): no turbulence policy (OmegaNo), and initializeSimulation runs
+    initializeSimulationData first, so missing output intervals are refused before the GPU is touched."""
+    from lb_gb300.solver import OmegaNo, SolverLaminar
+    flags = np.ones((4, 5, 6), np.int32)
+    s = SolverLaminar(constants=dict(nu=0.1, err_every_it=10), data={"flags": flags})
+    assert s.policies["Turbulence"] is OmegaNo
+    with pytest.raises(ValueError, match="plot_every"):
+        s.initializeSimulation()
