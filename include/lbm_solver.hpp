@@ -240,6 +240,86 @@ private:
     }
 };
 
+// postprocesors/outputerVTK.h and outputerMesh.h: the reference's writer and reader names over the C ABI's
+// host code.  Files go under <results_dir or "results">/ with the reference's names; the fields are the
+// host copies in LBMData (rho, u after runSimulation; rhoTimeAvg, uTimeAvg after an average).
+struct outputerVTK {
+    static std::string dir(const LBMConstants& C) { return C.results_dir.empty() ? std::string("results") : C.results_dir; }
+    // one structured-points file with rho, p or pressure (rho cs2) and U, each times its factor
+    static void variables(const std::string& path, const LBMConstants& C, const std::vector<double>& rho,
+                          const std::vector<double>& u, const char* pname, double crho, double cp, double cu) {
+        const size_t N = (size_t)C.dimX_int * C.dimY_int * C.dimZ_int;
+        if (rho.size() != N || u.size() != 3 * N) throw Error(LBM_ERR_INVALID, "outputerVTK: fields not read back");
+        std::vector<double> p(N);
+        for (size_t i = 0; i < N; i++) p[i] = rho[i] / 3.0;
+        const lbm_vtk_field f[3] = {{"rho", 1, rho.data(), crho}, {pname, 1, p.data(), cp}, {"U", 3, u.data(), cu}};
+        write(path, "LBE variables", C, f, 3);
+    }
+    static void write(const std::string& path, const char* title, const LBMConstants& C, const lbm_vtk_field* f,
+                      int n) {
+        const int32_t dims[3] = {C.dimX_int, C.dimY_int, C.dimZ_int};
+        const lbm_status st = lbm_vtk_write(path.c_str(), title, dims, C.resolution_factor, C.additional_factor,
+                                            C.BBmin, f, n);
+        if (st != LBM_OK) throw Error(st, std::string("lbm_vtk_write: ") + lbm_vtk_last_error());
+    }
+    // :26-56: the flag field as "object", title "LBE <filename>"
+    static void MeshVTK(const LBMData& D, const LBMConstants& C, const std::string& filename) {
+        std::vector<double> fl(D.meshFluid.begin(), D.meshFluid.end());
+        const lbm_vtk_field f = {"object", 1, fl.data(), 1.0};
+        write(dir(C) + "/" + filename + ".vtk", ("LBE " + filename).c_str(), C, &f, 1);
+    }
+    // :59-187 (physical units, results/variables.<step>.vtk) and :189-316 (lattice, variablesLattice<step>.vtk)
+    static void variablesVTK(const LBMData& D, const LBMConstants& C, int step, bool /*verbose*/) {
+        variables(dir(C) + "/variables." + std::to_string(step) + ".vtk", C, D.rho, D.u, "p", C.Crho, C.Cpressure,
+                  C.Cu);
+    }
+    static void variablesLatticeVTK(const LBMData& D, const LBMConstants& C, int step, bool /*verbose*/) {
+        variables(dir(C) + "/variablesLattice" + std::to_string(step) + ".vtk", C, D.rho, D.u, "pressure", 1, 1, 1);
+    }
+    // :318-447 and :449-576 (both write results/variablesTimeAvg.vtk)
+    static void variablesTimeAvgVTK(const LBMData& D, const LBMConstants& C, bool /*verbose*/) {
+        variables(dir(C) + "/variablesTimeAvg.vtk", C, D.rhoTimeAvg, D.uTimeAvg, "pressure", C.Crho, C.Cpressure, C.Cu);
+    }
+    static void variablesTimeAvgLatticeVTK(const LBMData& D, const LBMConstants& C, bool /*verbose*/) {
+        variables(dir(C) + "/variablesTimeAvg.vtk", C, D.rhoTimeAvg, D.uTimeAvg, "pressure", 1, 1, 1);
+    }
+    // :824-851: one probe line appended to results/probeData.csv
+    static void probeWriteOut(const LBMConstants& C, double velX, double velY, double velZ, double rho) {
+        const double s[4] = {velX, velY, velZ, rho};
+        const std::string path = dir(C) + "/probeData.csv";
+        const lbm_status st = lbm_probe_csv_append(path.c_str(), C.Ct * C.probe_every_it, s, C.Cu, C.Crho, C.Cpressure);
+        if (st != LBM_OK) throw Error(st, std::string("lbm_probe_csv_append: ") + lbm_vtk_last_error());
+    }
+};
+
+struct outputerMesh {
+    // outputerMesh.h:19-56: results/<filename>.txt from meshFluid and the header constants
+    static void MeshMatrixOut(const LBMData& D, const LBMConstants& C, const std::string& filename) {
+        const int32_t dims[3] = {C.dimX_int, C.dimY_int, C.dimZ_int};
+        const double bbox[6] = {C.BBmin[0], C.BBmin[1], C.BBmin[2], C.BBmax[0], C.BBmax[1], C.BBmax[2]};
+        const std::string path = outputerVTK::dir(C) + "/" + filename + ".txt";
+        const lbm_status st =
+            lbm_mesh_matrix_write(path.c_str(), D.meshFluid.data(), dims, C.resolution_factor, C.additional_factor, bbox);
+        if (st != LBM_OK) throw Error(st, std::string("lbm_mesh_matrix_write: ") + lbm_mesh_matrix_last_error());
+    }
+    // :59-211: dimensions, resolution_factor, additional_factor, BBmin / BBmax and meshFluid from the file
+    static void MeshMatrixIn(LBMData& D, LBMConstants& C, const std::string& filename, bool verbose) {
+        const std::string path = outputerVTK::dir(C) + "/" + filename + ".txt";
+        int32_t dims[3];
+        double res = 0, add = 0, bbox[6];
+        lbm_status st = lbm_mesh_matrix_read(path.c_str(), nullptr, 0, dims, &res, &add, bbox);
+        if (st != LBM_OK) throw Error(st, std::string("lbm_mesh_matrix_read: ") + lbm_mesh_matrix_last_error());
+        D.meshFluid.resize((size_t)dims[0] * dims[1] * dims[2]);
+        st = lbm_mesh_matrix_read(path.c_str(), D.meshFluid.data(), (int64_t)D.meshFluid.size(), dims, nullptr, nullptr,
+                                  nullptr);
+        if (st != LBM_OK) throw Error(st, std::string("lbm_mesh_matrix_read: ") + lbm_mesh_matrix_last_error());
+        C.dimX_int = dims[0]; C.dimY_int = dims[1]; C.dimZ_int = dims[2];
+        C.resolution_factor = res; C.additional_factor = add;
+        for (int a = 0; a < 3; a++) { C.BBmin[a] = bbox[a]; C.BBmax[a] = bbox[3 + a]; }
+        if (verbose) std::printf("Mesh %s read: %d x %d x %d\n", path.c_str(), dims[0], dims[1], dims[2]);
+    }
+};
+
 // nonDimensionalisions/NonDimensiolnaliseFactorsVelocity.h: lattice units from the physical inputs, in
 // the reference's float arithmetic (RealType = float, LBMTraits.h:72)
 struct NonDimensiolnaliseFactorsVelocity {

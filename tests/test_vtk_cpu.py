@@ -121,3 +121,65 @@ def test_restart_read_rejects_bad_files(built_lib, tmp_path):
     with pytest.raises(capi.LbmError) as e:
         output.read_variables_vtk(tmp_path / "nou.vtk", dims)
     assert e.value.status == capi.LBM_ERR_INVALID
+
+
+def test_cpp_outputers_write_the_python_files(built_lib, tmp_path):
+    """outputerVTK / outputerMesh of the C++ mirror (include/lbm_solver.hpp): the same bytes as the Python
+    writers for the same fields and constants, and MeshMatrixIn reads back what MeshMatrixOut wrote."""
+    import os
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = tmp_path / "cpp"
+    out.mkdir()
+    src = r'''
+#include <cstdio>
+#include "lbm_solver.hpp"
+using namespace lbm_gb300;
+int main(int argc, char** argv) {
+    LBMConstants C; LBMData D;
+    C.dimX_int = 3; C.dimY_int = 2; C.dimZ_int = 2; C.results_dir = argv[1];
+    C.resolution_factor = 75.0; C.additional_factor = 3.0; C.BBmin[0] = -0.1; C.BBmin[2] = 0.02;
+    C.BBmax[0] = 0.2; C.BBmax[1] = 0.05; C.BBmax[2] = 0.09;
+    C.Crho = 1.293; C.Cpressure = 2.5e3; C.Cu = 46.78; C.Ct = 1e-4; C.probe_every_it = 5;
+    for (int q = 0; q < 12; q++) {
+        D.rho.push_back(1.0 + 0.001 * q);
+        D.meshFluid.push_back(q % 3 == 0 ? 0 : (q % 5 == 0 ? -1 : 1 + q));
+    }
+    for (int q = 0; q < 36; q++) D.u.push_back(0.01 * (q - 17));
+    D.rhoTimeAvg = D.rho; D.uTimeAvg = D.u;
+    outputerVTK::variablesVTK(D, C, 4, false);
+    outputerVTK::variablesLatticeVTK(D, C, 4, false);
+    outputerVTK::variablesTimeAvgVTK(D, C, false);
+    outputerVTK::MeshVTK(D, C, "meshIN");
+    outputerVTK::probeWriteOut(C, 0.01, -0.02, 0.003, 1.001);
+    outputerMesh::MeshMatrixOut(D, C, "geom");
+    LBMConstants C2; LBMData D2; C2.results_dir = argv[1];
+    outputerMesh::MeshMatrixIn(D2, C2, "geom", false);
+    std::printf("%d %d %d %d\n", (int)(D2.meshFluid == D.meshFluid), C2.dimX_int, C2.dimY_int, C2.dimZ_int);
+    return 0;
+}
+'''
+    p = tmp_path / "t.cpp"
+    exe = tmp_path / "t"
+    p.write_text(src)
+    lib = os.path.join(root, "lb_gb300")
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(root, "include"), str(p), "-L", lib,
+                        "-llbm_gb300", "-Wl,-rpath," + lib, "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    res = subprocess.run([str(exe), str(out)], capture_output=True, text=True, check=True).stdout.split()
+    assert res == ["1", "3", "2", "2"]
+    N = 12
+    rho = 1.0 + 0.001 * np.arange(N)
+    u = 0.01 * (np.arange(3 * N) - 17)
+    flags = np.array([0 if q % 3 == 0 else (-1 if q % 5 == 0 else 1 + q) for q in range(N)])
+    grid = output.Grid((3, 2, 2), resolution=75.0, additional=3.0, bbmin=(-0.1, 0.0, 0.02))
+    conv = {"Crho": 1.293, "Cpressure": 2.5e3, "Cu": 46.78}
+    py = tmp_path / "py"
+    py.mkdir()
+    output.outputerVTK.variablesVTK(py / "variables.4.vtk", grid, rho, u, conv)
+    output.outputerVTK.variablesLatticeVTK(py / "variablesLattice4.vtk", grid, rho, u)
+    output.outputerVTK.variablesTimeAvgVTK(py / "variablesTimeAvg.vtk", grid, rho, u, conv)
+    output.outputerVTK.MeshVTK(py / "meshIN.vtk", grid, flags, "meshIN")
+    output.outputerVTK.probeWriteOut(py / "probeData.csv", [0.01, -0.02, 0.003, 1.001], conv, 1e-4 * 5)
+    for name in ("variables.4.vtk", "variablesLattice4.vtk", "variablesTimeAvg.vtk", "meshIN.vtk", "probeData.csv"):
+        assert (out / name).read_bytes() == (py / name).read_bytes(), name
