@@ -106,6 +106,9 @@ struct LBMConstants {
     // initializeSimulationData (SolverTurbulentLES.h:276-323): step counts from physical times (-1: unset)
     double time = -1.0, plot_every = -1.0, err_every = -1.0;
     double ProbeLocation[3] = {0.0, 0.0, 0.0};
+    // the preprocessor's inputs (preprocess.cpp:41-45): OFF file, output name, the point outside
+    std::string file_name, mesh_name;
+    double point_outside[3] = {-1.0, -1.0, -1.0};
 };
 
 struct LBMData {
@@ -238,6 +241,60 @@ private:
         v.resize((size_t)(s == LBM_OK ? n : have));
         run(s);
     }
+};
+
+// preprocess/src/geometry/geometryHandlerOFF.h and geometryMesherOFF.h: the preprocessor's calls
+// (preprocess.cpp:60-72) over lbm_voxelize_off.  The handler reads the OFF/NOFF file and its bounding box
+// (float, as LBMConstants keeps it); the mesher sizes the lattice, ceil((BBmax - BBmin) res + 2 add) per
+// axis, and fills meshFluid with 1 inside the polyhedron, 0 outside (the GPU voxelizer: ray parity along
+// +x, bit-exact with the reference's segment test on its golden file).
+struct geometryHandlerOFF {
+    std::string path;
+    double bbox[6] = {0, 0, 0, 0, 0, 0};
+    int32_t dims[3] = {0, 0, 0};
+    void polyhedronFromFile(const LBMConstants& C, bool /*verbose*/) {
+        path = C.file_name;
+        const lbm_status s =
+            lbm_voxelize_off(path.c_str(), C.resolution_factor, C.additional_factor, C.point_outside, nullptr, dims, bbox, 0);
+        if (s != LBM_OK) throw Error(s, "cannot read the OFF file " + path);
+    }
+    void polyhedronBbox(bool /*verbose*/) {}  // the bounding box comes with the read
+    void writeToConstants(LBMConstants& C) const {
+        for (int a = 0; a < 3; a++) { C.BBmin[a] = bbox[a]; C.BBmax[a] = bbox[3 + a]; }
+    }
+};
+
+class geometryMesherOFF {
+public:
+    geometryMesherOFF(LBMConstants& constants, LBMData& data) : C(constants), D(data) {}
+    // geometryMesherOFF.h:45-79: lattice dimensions from the bounding box
+    void initialization(bool /*verbose*/) {
+        for (int a = 0; a < 3; a++) {
+            const float ext = (float)C.BBmax[a] - (float)C.BBmin[a];
+            const int n = (int)std::ceil(ext * (float)C.resolution_factor + 2 * (float)C.additional_factor);
+            (a == 0 ? C.dimX_int : a == 1 ? C.dimY_int : C.dimZ_int) = n;
+        }
+        D.meshFluid.assign((size_t)C.dimX_int * C.dimY_int * C.dimZ_int, 0);
+    }
+    // :81-112: 1 inside, 0 outside at every cell centre
+    void meshingPolyhedron(const geometryHandlerOFF& H, const double point_outside[3], bool /*verbose*/) {
+        int32_t dims[3];
+        double bbox[6];
+        // the voxelizer's own dimensions first: it writes that many flags
+        lbm_status s = lbm_voxelize_off(H.path.c_str(), C.resolution_factor, C.additional_factor, point_outside, nullptr,
+                                        dims, bbox, C.device);
+        if (s != LBM_OK) throw Error(s, "cannot read the OFF file " + H.path);
+        if (dims[0] != C.dimX_int || dims[1] != C.dimY_int || dims[2] != C.dimZ_int)
+            throw Error(LBM_ERR_INVALID, "the lattice does not match the polyhedron's bounding box");
+        D.meshFluid.resize((size_t)dims[0] * dims[1] * dims[2]);
+        s = lbm_voxelize_off(H.path.c_str(), C.resolution_factor, C.additional_factor, point_outside, D.meshFluid.data(),
+                             dims, bbox, C.device);
+        if (s != LBM_OK) throw Error(s, "lbm_voxelize_off failed on " + H.path);
+    }
+
+private:
+    LBMConstants& C;
+    LBMData& D;
 };
 
 // postprocesors/outputerVTK.h and outputerMesh.h: the reference's writer and reader names over the C ABI's

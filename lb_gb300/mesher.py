@@ -6,7 +6,8 @@ the reference's method names, building the flag field and the boundary records a
 dimZ_int (or the flag array's shape), resolution_factor, additional_factor and BBmin.  `data["flags"]` is
 the flag field [z, y, x] (int32, changed in place, as the reference changes meshFluidHost); the passes
 collect records, and compileBoundaryArray* put them into data["inlets"], ["outlets"], ["symmetry"],
-["periodic"] for Solver.set_bc / set_symmetry.
+["periodic"] for Solver.set_bc / set_symmetry.  geometryHandlerOFF and geometryMesherOFF are the
+preprocessor's OFF reader and polyhedron mesher (preprocess.cpp:60-72) over lbm_voxelize_off.
 """
 import ctypes as C
 import math
@@ -166,3 +167,68 @@ class geometryMesherBoundary:
 
     def arrayTransfer(self, verbose=False):
         return None  # the Solver uploads flags and records itself
+
+
+class geometryHandlerOFF:
+    """preprocess/src/geometry/geometryHandlerOFF.h: reads the OFF/NOFF file and its bounding box (float, as
+    LBMConstants keeps it) through lbm_voxelize_off's size query (host code, no GPU)."""
+
+    def __init__(self):
+        self.path = None
+        self.bbox = None
+        self.dims = None
+
+    def polyhedronFromFile(self, constants, verbose=False):
+        self.path = str(constants["file_name"])
+        dims = np.zeros(3, np.int32)
+        bbox = np.zeros(6, np.float64)
+        out = np.asarray(constants.get("point_outside", (-1.0, -1.0, -1.0)), np.float64)
+        st = capi.lib().lbm_voxelize_off(self.path.encode(), float(constants["resolution_factor"]),
+                                         float(constants["additional_factor"]), out.ctypes.data_as(C.POINTER(C.c_double)),
+                                         None, dims.ctypes.data_as(C.POINTER(C.c_int32)),
+                                         bbox.ctypes.data_as(C.POINTER(C.c_double)), 0)
+        if st:
+            raise capi.LbmError(st, f"cannot read the OFF file {self.path}")
+        self.bbox, self.dims = bbox, tuple(int(d) for d in dims)
+
+    def polyhedronBbox(self, verbose=False):
+        return None  # the bounding box comes with the read
+
+    def writeToConstants(self, constants):
+        constants["BBmin"] = tuple(float(v) for v in self.bbox[:3])
+        constants["BBmax"] = tuple(float(v) for v in self.bbox[3:])
+
+
+class geometryMesherOFF:
+    """preprocess/src/geometry/geometryMesherOFF.h:45-112: the lattice from the bounding box, then 1 inside
+    the polyhedron and 0 outside at every cell centre (the GPU voxelizer)."""
+
+    def __init__(self, constants, data):
+        self.C = constants
+        self.data = data
+
+    def initialization(self, verbose=False):
+        f = np.float32
+        dims = []
+        for a in range(3):
+            ext = f(self.C["BBmax"][a]) - f(self.C["BBmin"][a])
+            dims.append(int(np.ceil(ext * f(self.C["resolution_factor"]) + f(2) * f(self.C["additional_factor"]))))
+        self.C["dimX_int"], self.C["dimY_int"], self.C["dimZ_int"] = dims
+        self.data["flags"] = np.zeros(dims[::-1], np.int32)
+
+    def meshingPolyhedron(self, handler, point_outside, verbose=False):
+        nx, ny, nz = self.C["dimX_int"], self.C["dimY_int"], self.C["dimZ_int"]
+        if handler.dims != (nx, ny, nz):
+            raise ValueError("the lattice does not match the polyhedron's bounding box")
+        flags = np.zeros((nz, ny, nx), np.int32)
+        dims = np.zeros(3, np.int32)
+        bbox = np.zeros(6, np.float64)
+        out = np.asarray(point_outside, np.float64)
+        st = capi.lib().lbm_voxelize_off(handler.path.encode(), float(self.C["resolution_factor"]),
+                                         float(self.C["additional_factor"]), out.ctypes.data_as(C.POINTER(C.c_double)),
+                                         flags.ctypes.data_as(C.POINTER(C.c_int32)),
+                                         dims.ctypes.data_as(C.POINTER(C.c_int32)),
+                                         bbox.ctypes.data_as(C.POINTER(C.c_double)), int(self.C.get("device", 0)))
+        if st:
+            raise capi.LbmError(st, f"lbm_voxelize_off failed on {handler.path}")
+        self.data["flags"] = flags

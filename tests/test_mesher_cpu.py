@@ -219,3 +219,56 @@ int main() {
     want += ["%d %d %d %.9g %d" % (r.vertex.x, r.vertex.y, r.vertex.z, r.velocity[0], r.regular) for r in m.inlets]
     want += ["%d %d %d %d" % (r.vertex.x, r.vertex.y, r.vertex.z, r.regular) for r in m.outlets]
     assert out == want
+
+
+def test_off_handler_and_mesher_size_the_golden_lattice(built_lib):
+    """geometryHandlerOFF / geometryMesherOFF of both mirrors on the reference's BackwardStepLaminar.off:
+    the bounding box and the lattice dimensions of the golden mesh-matrix file (the flags themselves are
+    the GPU voxelizer's, checked bit for bit on the GPU)."""
+    import os
+    import subprocess
+    import tempfile
+    from lb_gb300.mesher import geometryHandlerOFF, geometryMesherOFF
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    gold = os.path.join(root, "tests", "golden")
+    g = np.load(os.path.join(gold, "backward_step_laminar.npz"))
+    off = os.path.join(gold, "BackwardStepLaminar.off")
+    c = dict(file_name=off, resolution_factor=float(g["resolution"]), additional_factor=float(g["additional"]))
+    h = geometryHandlerOFF()
+    h.polyhedronFromFile(c)
+    h.polyhedronBbox()
+    h.writeToConstants(c)
+    d = {}
+    geometryMesherOFF(c, d).initialization()
+    assert (c["dimX_int"], c["dimY_int"], c["dimZ_int"]) == tuple(int(v) for v in g["dims"]) == h.dims
+    assert d["flags"].shape == tuple(int(v) for v in g["dims"][::-1])
+    assert np.allclose(c["BBmin"], g["bbmin"], rtol=0, atol=1e-6) and np.allclose(c["BBmax"], g["bbmax"], rtol=0, atol=1e-6)
+    src = r'''
+#include <cstdio>
+#include "lbm_solver.hpp"
+using namespace lbm_gb300;
+int main(int argc, char** argv) {
+    LBMConstants C; LBMData D;
+    C.file_name = argv[1]; C.resolution_factor = %r; C.additional_factor = %r;
+    geometryHandlerOFF H;
+    H.polyhedronFromFile(C, false);
+    H.writeToConstants(C);
+    geometryMesherOFF M(C, D);
+    M.initialization(false);
+    std::printf("%%d %%d %%d %%zu %%.9g %%.9g\n", C.dimX_int, C.dimY_int, C.dimZ_int, D.meshFluid.size(), C.BBmin[0], C.BBmax[2]);
+    return 0;
+}
+''' % (float(g["resolution"]), float(g["additional"]))
+    with tempfile.TemporaryDirectory() as t:
+        p = os.path.join(t, "t.cpp")
+        exe = os.path.join(t, "t")
+        with open(p, "w") as fh:
+            fh.write(src)
+        lib = os.path.join(root, "lb_gb300")
+        r = subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(root, "include"), p, "-L", lib, "-llbm_gb300",
+                            "-Wl,-rpath," + lib, "-o", exe], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        out = subprocess.run([exe, off], capture_output=True, text=True, check=True).stdout.split()
+    n = [int(v) for v in g["dims"]]
+    assert out[:4] == [str(n[0]), str(n[1]), str(n[2]), str(n[0] * n[1] * n[2])]
+    assert float(out[4]) == float("%.9g" % c["BBmin"][0]) and float(out[5]) == float("%.9g" % c["BBmax"][2])
