@@ -11,6 +11,7 @@
 // something else.
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -242,6 +243,64 @@ private:
         run(s);
     }
 };
+
+// A lattice made periodic the reference's way (Periodic.h: per axis two planes of -3 nodes whose records
+// point at each other) as the index-wrapped lattice the kernels run: with the pair at planes p < q of an
+// axis, planes p .. q-1 are kept (plane q repeats plane p), the axis wraps (C.periodic), -3 flags become
+// plain fluid and the inlet, outlet and symmetry records move with the planes (those on dropped planes
+// are dropped).  D.meshBoundaryPeriodic is cleared.  The two forms step identically.
+inline void foldPeriodic(LBMConstants& C, LBMData& D) {
+    const int n[3] = {C.dimX_int, C.dimY_int, C.dimZ_int};
+    int lo[3] = {0, 0, 0}, hi[3] = {n[0], n[1], n[2]};
+    for (int a = 0; a < 3; a++) {
+        int planes[2] = {-1, -1}, idx[2] = {-1, -1}, np_ = 0;
+        for (const auto& r : D.meshBoundaryPeriodic) {
+            int axis = -1, cnt = 0;
+            for (int b = 0; b < 3; b++)
+                if (r.normal[b] != 0) { axis = b; cnt++; }
+            if (cnt != 1) throw Error(LBM_ERR_INVALID, "periodic record with a normal off the axes");
+            if (axis != a) continue;
+            const int pl = a == 0 ? r.vertex.x : a == 1 ? r.vertex.y : r.vertex.z;
+            int e = 0;
+            while (e < np_ && !(planes[e] == pl && idx[e] == r.periodic_index)) e++;
+            if (e == np_) {
+                if (np_ == 2) throw Error(LBM_ERR_INVALID, "more than two periodic planes on one axis");
+                planes[np_] = pl; idx[np_] = r.periodic_index; np_++;
+            }
+        }
+        if (np_ == 0) continue;
+        if (np_ != 2) throw Error(LBM_ERR_INVALID, "a periodic plane without its partner");
+        const int p = std::min(planes[0], planes[1]), q = std::max(planes[0], planes[1]);
+        const int ip = planes[0] == p ? idx[0] : idx[1], iq = planes[0] == p ? idx[1] : idx[0];
+        if (p == q || ip != q || iq != p) throw Error(LBM_ERR_INVALID, "periodic planes that do not point at each other");
+        lo[a] = p; hi[a] = q; C.periodic[a] = 1;
+    }
+    const int m[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+    std::vector<int32_t> f((size_t)m[0] * m[1] * m[2]);
+    for (int k = 0; k < m[2]; k++)
+        for (int j = 0; j < m[1]; j++)
+            for (int i = 0; i < m[0]; i++) {
+                const int32_t v = D.meshFluid[((size_t)(k + lo[2]) * n[1] + (j + lo[1])) * n[0] + (i + lo[0])];
+                f[((size_t)k * m[1] + j) * m[0] + i] = v == -3 ? 1 : v;
+            }
+    auto move = [&](auto& recs) {
+        size_t w = 0;
+        for (size_t e = 0; e < recs.size(); e++) {
+            auto r = recs[e];
+            int v[3] = {r.vertex.x - lo[0], r.vertex.y - lo[1], r.vertex.z - lo[2]};
+            if (v[0] < 0 || v[1] < 0 || v[2] < 0 || v[0] >= m[0] || v[1] >= m[1] || v[2] >= m[2]) continue;
+            r.vertex.x = v[0]; r.vertex.y = v[1]; r.vertex.z = v[2];
+            recs[w++] = r;
+        }
+        recs.resize(w);
+    };
+    move(D.meshBoundaryInlet);
+    move(D.meshBoundaryOutlet);
+    move(D.meshBoundarySymmetry);
+    D.meshBoundaryPeriodic.clear();
+    D.meshFluid.swap(f);
+    C.dimX_int = m[0]; C.dimY_int = m[1]; C.dimZ_int = m[2];
+}
 
 // preprocess/src/geometry/geometryHandlerOFF.h and geometryMesherOFF.h: the preprocessor's calls
 // (preprocess.cpp:60-72) over lbm_voxelize_off.  The handler reads the OFF/NOFF file and its bounding box

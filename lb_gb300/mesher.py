@@ -232,3 +232,47 @@ class geometryMesherOFF:
         if st:
             raise capi.LbmError(st, f"lbm_voxelize_off failed on {handler.path}")
         self.data["flags"] = flags
+
+
+def fold_periodic(flags, periodic_records, inlets=(), outlets=(), symmetry=()):
+    """A lattice made periodic the reference's way (Periodic.h: two planes of -3 nodes per axis whose
+    records point at each other, each copying the other's entering populations) as the index-wrapped
+    lattice the kernels run.  With the pair at planes p < q of axis a, planes p .. q-1 are kept (plane q
+    repeats plane p) and axis a wraps; the -3 flags become plain fluid (1) and the records move with the
+    planes.  Returns dict(flags, periodic, offset, inlets, outlets, symmetry); records on dropped planes
+    are dropped.  The ghost-plane and index-wrap forms step identically (tested on the oracle)."""
+    f = np.ascontiguousarray(flags, dtype=np.int32)
+    nz, ny, nx = f.shape
+    n = (nx, ny, nz)
+    pairs = {}
+    for r in periodic_records:
+        nrm = tuple(int(round(v)) for v in r.normal)
+        axes = [a for a in range(3) if nrm[a] != 0]
+        if len(axes) != 1:
+            raise ValueError("periodic record with a normal off the axes")
+        a = axes[0]
+        plane = (r.vertex.x, r.vertex.y, r.vertex.z)[a]
+        pairs.setdefault(a, set()).add((plane, int(r.periodic_index)))
+    lo, hi, periodic = [0, 0, 0], list(n), [0, 0, 0]
+    for a, ps in pairs.items():
+        if len(ps) != 2:
+            raise ValueError(f"axis {a}: expected two periodic planes pointing at each other, found {sorted(ps)}")
+        (p, pi), (q, qi) = sorted(ps)
+        if pi != q or qi != p or q <= p:
+            raise ValueError(f"axis {a}: planes {p} and {q} do not point at each other ({pi}, {qi})")
+        lo[a], hi[a], periodic[a] = p, q, 1
+    out = f[lo[2]:hi[2], lo[1]:hi[1], lo[0]:hi[0]].copy()
+    out[out == -3] = 1
+
+    def move(records, make):
+        kept = []
+        for r in records:
+            v = (r.vertex.x, r.vertex.y, r.vertex.z)
+            if all(lo[a] <= v[a] < hi[a] for a in range(3)):
+                kept.append(make(r, [v[a] - lo[a] for a in range(3)]))
+        return kept
+
+    return dict(flags=out, periodic=tuple(periodic), offset=tuple(lo),
+                inlets=move(inlets, lambda r, v: capi.make_inlet(*v, tuple(r.normal), tuple(r.velocity), r.regular)),
+                outlets=move(outlets, lambda r, v: capi.make_outlet(*v, tuple(r.normal), r.density, r.regular)),
+                symmetry=move(symmetry, lambda r, v: capi.make_symmetry(*v, tuple(r.normal), r.regular)))

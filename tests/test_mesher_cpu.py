@@ -272,3 +272,124 @@ int main(int argc, char** argv) {
     n = [int(v) for v in g["dims"]]
     assert out[:4] == [str(n[0]), str(n[1]), str(n[2]), str(n[0] * n[1] * n[2])]
     assert float(out[4]) == float("%.9g" % c["BBmin"][0]) and float(out[5]) == float("%.9g" % c["BBmax"][2])
+
+
+def test_fold_periodic_steps_like_the_ghost_planes(built_lib, oracle_lib):
+    """A lattice made periodic in x the reference's way (solid planes 0 and L+2, the mesher's periodic
+    pass on planes 1 and L+1 pointing at each other, as main.cu:176-177 builds it) folded by
+    fold_periodic steps like the ghost-plane form on the oracle (Periodic.h:43-138) to 1e-13."""
+    from oracle import oracle as O
+    from lb_gb300.mesher import fold_periodic
+    L, ny, nz = 9, 5, 4
+    X = L + 3
+    f = np.ones((nz, ny, X), np.int32)
+    f[:, :, 0] = 0
+    f[:, :, -1] = 0
+    frame = dict(resolution_factor=1.0, additional_factor=0.5, BBmin=(0.0, 0.0, 0.0))  # centres at integers
+    m = geometryMesherBoundary(frame, {"flags": f})
+    m.meshingBoundaryWall()
+    m.meshingBoundaryConditionPeriodic(geometryObjectCuboid((0.9, -1, -1), (1.1, 99, 99), (1.0, 99, -1), -3),
+                                       (-1, 0, 0), L + 1)
+    m.meshingBoundaryConditionPeriodic(geometryObjectCuboid((L + 0.9, -1, -1), (L + 1.1, 99, 99), (L + 1, -1, 99), -3),
+                                       (1, 0, 0), 1)
+    assert len(m.periodic) == 2 * ny * nz
+    fo = fold_periodic(f, m.periodic)
+    assert fo["periodic"] == (1, 0, 0) and fo["offset"] == (1, 0, 0)
+    assert np.array_equal(fo["flags"], np.ones((nz, ny, L), np.int32))
+    rng = np.random.default_rng(11)
+    rho = 1 + 0.01 * rng.standard_normal(L * ny * nz)
+    u = 0.03 * rng.standard_normal((3, L * ny * nz))
+    kw = dict(nu=0.02, collision=capi.LBM_COLLISION_CUMULANT2015, closure=capi.LBM_CLOSURE_SMAGORINSKY)
+    a = O.OracleSim(capi.make_config(L, ny, nz, periodic=(1, 1, 1), **kw), 64)
+    a.set_flags(fo["flags"])
+    a.set_bc()
+    a.init_fields(rho, u)
+    b = O.OracleSim(capi.make_config(X, ny, nz, periodic=(0, 1, 1), **kw), 64)
+    b.set_flags(f)
+    b.set_bc()
+    b.set_periodic_list([[r.vertex.x, r.vertex.y, r.vertex.z, *[int(v) for v in r.normal], r.periodic_index, r.regular]
+                         for r in m.periodic])
+    r3, u3 = rho.reshape(nz, ny, L), u.reshape(3, nz, ny, L)
+    rg, ug = np.ones((nz, ny, X)), np.zeros((3, nz, ny, X))
+    for p in range(1, L + 2):  # ghost plane p holds folded plane (p - 1) mod L
+        rg[:, :, p] = r3[:, :, (p - 1) % L]
+        ug[:, :, :, p] = u3[:, :, :, (p - 1) % L]
+    b.init_fields(rg.reshape(-1), ug.reshape(3, -1))
+    for _ in range(5):
+        a.step(1)
+        b.step(1)
+        ra, ua = a.moments()
+        rb, ub = b.moments()
+        assert np.abs(ra.reshape(nz, ny, L) - rb.reshape(nz, ny, X)[:, :, 1:L + 1]).max() < 1e-13
+        assert np.abs(ua.reshape(3, nz, ny, L) - ub.reshape(3, nz, ny, X)[:, :, :, 1:L + 1]).max() < 1e-13
+    with pytest.raises(ValueError):
+        fold_periodic(f, m.periodic[: ny * nz])  # one plane without its partner
+
+
+def test_cpp_fold_periodic_equals_python(built_lib):
+    import os
+    import subprocess
+    import tempfile
+    from lb_gb300.mesher import fold_periodic
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = r'''
+#include <cstdio>
+#include "lbm_solver.hpp"
+using namespace lbm_gb300;
+int main() {
+    LBMConstants C; LBMData D;
+    C.dimX_int = 12; C.dimY_int = 5; C.dimZ_int = 4;
+    D.meshFluid.assign(12 * 5 * 4, 1);
+    for (int k = 0; k < 4; k++) for (int j = 0; j < 5; j++) {
+        D.meshFluid[(k * 5 + j) * 12 + 0] = 0; D.meshFluid[(k * 5 + j) * 12 + 11] = 0;
+        if (j == 2) D.meshFluid[(k * 5 + j) * 12 + 6] = 0;
+    }
+    geometryMesherBoundary M(C, D);
+    M.meshingBoundaryWall(false);
+    const double a1[3] = {0.9, -1, -1}, a2[3] = {1.1, 99, 99}, a3[3] = {1.0, 99, -1};
+    const double b1[3] = {9.9, -1, -1}, b2[3] = {10.1, 99, 99}, b3[3] = {10.0, -1, 99};
+    const double c1[3] = {4.9, -1, -1}, c2[3] = {5.1, 99, 99}, c3[3] = {5.0, -1, 99};
+    const float nm[3] = {-1, 0, 0}, np_[3] = {1, 0, 0}, vin[3] = {0.04f, 0.f, 0.001f};
+    C.resolution_factor = 1.0; C.additional_factor = 0.5;
+    M.meshingBoundaryConditionPeriodic(geometryObjectCuboid(a1, a2, a3, -3), nm, 10, false);
+    M.meshingBoundaryConditionPeriodic(geometryObjectCuboid(b1, b2, b3, -3), np_, 1, false);
+    M.meshingBoundaryConditionInletUniform(geometryObjectCuboid(c1, c2, c3, -1), nm, vin, false);
+    foldPeriodic(C, D);
+    long long s = 0;
+    for (size_t q = 0; q < D.meshFluid.size(); q++) s += (long long)D.meshFluid[q] * (long long)(q + 1);
+    std::printf("%d %d %d %d %d %d %lld %zu", C.dimX_int, C.dimY_int, C.dimZ_int, C.periodic[0], C.periodic[1],
+                C.periodic[2], s, D.meshBoundaryInlet.size());
+    for (auto& r : D.meshBoundaryInlet) std::printf(" %d/%d/%d", r.vertex.x, r.vertex.y, r.vertex.z);
+    std::printf("\n");
+    return 0;
+}
+'''
+    with tempfile.TemporaryDirectory() as t:
+        p = os.path.join(t, "t.cpp")
+        exe = os.path.join(t, "t")
+        with open(p, "w") as fh:
+            fh.write(src)
+        lib = os.path.join(root, "lb_gb300")
+        r = subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(root, "include"), p, "-L", lib, "-llbm_gb300",
+                            "-Wl,-rpath," + lib, "-o", exe], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    f = np.ones((4, 5, 12), np.int32)
+    f[:, :, 0] = 0
+    f[:, :, 11] = 0
+    f[:, 2, 6] = 0
+    m = geometryMesherBoundary(dict(resolution_factor=1.0, additional_factor=0.5), {"flags": f})
+    m.meshingBoundaryWall()
+    m.meshingBoundaryConditionPeriodic(geometryObjectCuboid((0.9, -1, -1), (1.1, 99, 99), (1.0, 99, -1), -3),
+                                       (-1, 0, 0), 10)
+    m.meshingBoundaryConditionPeriodic(geometryObjectCuboid((9.9, -1, -1), (10.1, 99, 99), (10.0, -1, 99), -3),
+                                       (1, 0, 0), 1)
+    m.meshingBoundaryConditionInletUniform(geometryObjectCuboid((4.9, -1, -1), (5.1, 99, 99), (5.0, -1, 99), -1),
+                                           (-1, 0, 0), (0.04, 0.0, 0.001))
+    fo = fold_periodic(f, m.periodic, inlets=m.inlets)
+    g = fo["flags"]
+    s = int((g.reshape(-1).astype(np.int64) * np.arange(1, g.size + 1)).sum())
+    want = [str(v) for v in (g.shape[2], g.shape[1], g.shape[0], *fo["periodic"], s, len(fo["inlets"]))]
+    want += ["%d/%d/%d" % (r.vertex.x, r.vertex.y, r.vertex.z) for r in fo["inlets"]]
+    assert out == want
+    assert g.shape == (4, 5, 9) and (g == -1).sum() == 4 * 5
