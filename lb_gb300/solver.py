@@ -479,28 +479,92 @@ class SolverTurbulentLES:
         else:
             self.solver.init_equilibrium(rho0, u0)
 
+    _laminar_loop = False
+
     def runSimulation(self):
+        """The reference's loop (SolverTurbulentLES.h:179-268; SolverLaminar.h:127-204 for the laminar
+        solver) in batches of steps between events (step_schedule): the time average over the states after
+        step k > iterations - iterationsMomentAvg, the probe, the error (a NaN ends the loop) and, with a
+        results_dir, the VTK dumps and probe CSV under their reference names.  Returns [(k, error)]."""
+        from . import output
         c = self.C
         it = int(c["iterations"])
         navg = int(c.get("iterationsMomentAvg", 0))
-        err_every = int(c.get("err_every_it", 0))
-        errors = []
-        k = 0
-        while k < it:
-            if navg and k == it - navg:
+        rdir = c.get("results_dir") or ""
+        sched = step_schedule(it, navg, err_every=int(c.get("err_every_it", -1)),
+                              probe_every=int(c.get("probe_every_it", -1)),
+                              probe_iterations=int(c.get("probe_iterations", -1)),
+                              plot_every=int(c.get("plot_every_it", -1)) if rdir else -1, laminar=self._laminar_loop)
+        nx, ny, nz = self.solver.shape
+        grid = output.Grid((nx, ny, nz), resolution=c.get("resolution_factor", 1.0),
+                           additional=c.get("additional_factor", 0.5), bbmin=tuple(c.get("BBmin", (0.0, 0.0, 0.0))))
+        conv = {k: c.get(k, 1.0) for k in ("Crho", "Cpressure", "Cu")}
+        errors, probes = [], []
+        averaging = False
+        for begin, n, j, events in sched:
+            if begin:
                 self.solver.timeavg_begin()
-            n = it - k
-            if err_every:
-                n = min(n, err_every - (k % err_every) if k % err_every else err_every)
-            if navg and k < it - navg:
-                n = min(n, it - navg - k)
+                averaging = True
             self.solver.step(n)
-            k += n
-            if err_every and k % err_every == 0:
-                errors.append((k, self.solver.error_evaluation()))
-        if navg:
+            if "probe" in events:
+                sample = self.solver.probe(*c.get("ProbeLocationLat", (0, 0, 0)))
+                probes.append(sample)
+                if rdir:
+                    output.outputerVTK.probeWriteOut(os.path.join(rdir, "probeData.csv"), sample, conv,
+                                                     c.get("Ct", 1.0) * int(c["probe_every_it"]))
+            if "err" in events:
+                e = self.solver.error_evaluation()
+                errors.append((j, e))
+                if np.isnan(e):
+                    break
+            if "plot" in events:
+                rho, u = self.solver.moments()
+                step = j // int(c["plot_every_it"])
+                if self._laminar_loop:
+                    output.outputerVTK.variablesLatticeVTK(os.path.join(rdir, f"variablesLattice{step}.vtk"), grid,
+                                                           rho, u)
+                else:
+                    output.outputerVTK.variablesVTK(os.path.join(rdir, f"variables.{step}.vtk"), grid, rho, u, conv)
+        if averaging:
             self.solver.timeavg_end()
+            if rdir:
+                rm, um, _, _ = self.solver.timeavg_get()
+                output.outputerVTK.variablesTimeAvgVTK(os.path.join(rdir, "variablesTimeAvg.vtk"), grid, rm, um, conv)
+        self.probes = probes
         return errors
+
+
+def step_schedule(it, avg=0, err_every=-1, probe_every=-1, probe_iterations=-1, plot_every=-1, laminar=False):
+    """The reference loop's events grouped into runs of steps: [(begin_average, nsteps, j, events)], j the
+    0-based index of the batch's last step and events the subset of ("probe", "err", "plot") that the
+    reference runs after step j.  A state is averaged when its step k > it - avg (SolverTurbulentLES.h:216),
+    probed when k % probe_every == 0 within the last probe_iterations steps (:223; never in the laminar
+    loop), the error is taken when k % err_every == 0 and k != 0 (:228), and a dump is written when
+    k % plot_every == 0 and k != 0 (:243; from k = 0 on in the laminar loop, SolverLaminar.h:170)."""
+    avg_begin = it - avg + 1
+
+    def probe_after(k):
+        return not laminar and probe_every > 0 and k % probe_every == 0 and k >= it - probe_iterations
+
+    def err_after(k):
+        return err_every > 0 and k % err_every == 0 and k != 0
+
+    def plot_after(k):
+        return plot_every > 0 and k % plot_every == 0 and (k != 0 or laminar)
+
+    out, averaging, k = [], False, 0
+    while k < it:
+        begin = False
+        if avg > 0 and not averaging and k >= avg_begin:
+            begin = averaging = True
+        j = k
+        while j < it - 1 and not (probe_after(j) or err_after(j) or plot_after(j)) and \
+                not (avg > 0 and not averaging and j + 1 >= avg_begin):
+            j += 1
+        events = tuple(name for name, f in (("probe", probe_after), ("err", err_after), ("plot", plot_after)) if f(j))
+        out.append((begin, j - k + 1, j, events))
+        k = j + 1
+    return out
 
 
 class SolverLaminar(SolverTurbulentLES):
@@ -515,6 +579,8 @@ class SolverLaminar(SolverTurbulentLES):
                  NonDim=NonDimensiolnaliseFactorsVelocity, TimeAvg=MomentTimeAvg, *, constants, data):
         super().__init__(Model, Initialisation, Collision, Streaming, BounceBackWall, Symmetry, Periodic_, Inlet, Outlet,
                          Moments, OmegaNo, Error, NonDim, TimeAvg, constants=constants, data=data)
+
+    _laminar_loop = True
 
     def initializeSimulation(self, verbose=False):
         self.initializeSimulationData(verbose)

@@ -140,3 +140,40 @@ def test_laminar_solver_sets_up_like_the_reference():
     assert s.policies["Turbulence"] is OmegaNo
     with pytest.raises(ValueError, match="plot_every"):
         s.initializeSimulation()
+
+
+@pytest.mark.parametrize("laminar", [False, True])
+def test_step_schedule_replays_the_reference_loop(laminar):
+    """step_schedule (the Python mirror's runSimulation) against the reference loop run step by step
+    (SolverTurbulentLES.h:184-253, SolverLaminar.h:131-175): the same events after the same steps and the
+    same averaged states."""
+    from lb_gb300.solver import step_schedule
+    rng = np.random.default_rng(5)
+    for _ in range(300):
+        it = int(rng.integers(1, 60))
+        avg = int(rng.integers(0, it + 1))
+        kw = dict(err_every=int(rng.choice([-1, 1, 3, 10])), probe_every=int(rng.choice([-1, 1, 4])),
+                  probe_iterations=int(rng.integers(0, 70)), plot_every=int(rng.choice([-1, 1, 5, 7])))
+        naive_events, naive_avg = [], set()
+        for k in range(it):
+            if k > it - avg:
+                naive_avg.add(k)
+            ev = []
+            if not laminar and kw["probe_every"] > 0 and k % kw["probe_every"] == 0 and k >= it - kw["probe_iterations"]:
+                ev.append("probe")
+            if kw["err_every"] > 0 and k % kw["err_every"] == 0 and k != 0:
+                ev.append("err")
+            if kw["plot_every"] > 0 and k % kw["plot_every"] == 0 and (k != 0 or laminar):
+                ev.append("plot")
+            if ev:
+                naive_events.append((k, tuple(ev)))
+        sched = step_schedule(it, avg, laminar=laminar, **kw)
+        assert sum(n for _, n, _, _ in sched) == it
+        assert [(j, ev) for _, _, j, ev in sched if ev] == naive_events
+        averaged, on, done = set(), False, 0
+        for begin, n, j, _ in sched:
+            on = on or begin
+            if on:
+                averaged.update(range(done, done + n))
+            done += n
+        assert averaged == naive_avg, (it, avg)
