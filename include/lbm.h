@@ -110,6 +110,22 @@ typedef struct lbm_config {
     double  omega_dumping_high;  /* omegaDumpingHigh (LBMConstants.h:74-76, set in main.cu:137-138) */
 } lbm_config;
 
+/* The defaults the Python mirror uses: cumulant-2015, no closure, FP32, moving-wall inlet, density-
+ * interpolated outlet, nu = 1/6, cles = 0.173 (LBMConstants.h:70), rho0 = 1, s = 10, mlp_interval = 1,
+ * no sponge (-1), nothing periodic; the lattice size is left 0. */
+lbm_status lbm_config_defaults(lbm_config* cfg);
+/* A case file as text: one "key = value" (or "key value") per line, '#' to the end of a line is a
+ * comment.  Keys are the field names of lbm_config (periodic, force and omega_dumping take three, three
+ * and two numbers); collision, closure, storage, inlet and outlet take a number or a name: the
+ * reference's policy name (CollisionCumD3Q27Turbulent2015, OmegaLES, InletVelocityZouHe,
+ * OutletNeighbourEquilibriumOmega, ...) or srt, cumulant2015, cumulant2017, combined; none,
+ * smagorinsky, mlp; f64, f32, f16dev; moving_wall, equilibrium, zou_he; density_interpolated,
+ * neighbour_equilibrium, neighbour_equilibrium_omega, neighbour_equilibrium_omega_rf,
+ * density_equilibrium.  Fields not named keep their value in cfg.  LBM_ERR_INVALID on an unknown key
+ * or a bad value (cfg unchanged then; the reason in lbm_config_last_error). */
+lbm_status lbm_config_parse(const char* text, lbm_config* cfg);
+const char* lbm_config_last_error(void);
+
 /* implementation options */
 #define LBM_OPT_ROW_STAGING  1  /* FP16 storage: rows of bulk cells through the shared-memory row-staged step
                                    (identical results) */

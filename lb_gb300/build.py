@@ -19,7 +19,7 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-
 # extra nvcc flags for tuning experiments (e.g. LBM_NVCC_EXTRA="-DLBM_STEP2_MIN_BLOCKS=5")
 NVCC_FLAGS += os.environ.get("LBM_NVCC_EXTRA", "").split()
 UNITS = ["lbm_step_f64.cu", "lbm_step_f32.cu", "lbm_step_f16.cu", "lbm_capi.cu", "voxelizer.cu", "mlp.cu", "mesh_io.cu",
-         "mesher.cu", "vtk_io.cu"]
+         "mesher.cu", "vtk_io.cu", "config_io.cu"]
 
 
 def nvcc():

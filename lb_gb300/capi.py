@@ -136,6 +136,19 @@ def make_config(nx, ny, nz, periodic=(0, 0, 0), collision=LBM_COLLISION_CUMULANT
     return c
 
 
+def config_from_text(text, base=None):
+    """lbm_config_parse: a key = value case file over `base` (default: lbm_config_defaults)."""
+    c = LbmConfig()
+    if base is None:
+        lib().lbm_config_defaults(C.byref(c))
+    else:
+        C.memmove(C.byref(c), C.byref(base), C.sizeof(LbmConfig))
+    st = lib().lbm_config_parse(text.encode(), C.byref(c))
+    if st:
+        raise LbmError(st, lib().lbm_config_last_error().decode())
+    return c
+
+
 def make_inlet(x, y, z, normal, velocity, regular=1):
     r = LbmBcInlet()
     r.vertex = LbmVertex(int(x), int(y), int(z))
@@ -243,6 +256,9 @@ def lib():
         "lbm_mesher_periodic": ([C.POINTER(LbmMeshFrame), ip, C.POINTER(LbmCuboid), fp, i32, C.POINTER(LbmBcPeriodic),
                                  i64, C.POINTER(C.c_int64)], i32),
         "lbm_mesher_last_error": ([], C.c_char_p),
+        "lbm_config_defaults": ([C.POINTER(LbmConfig)], i32),
+        "lbm_config_parse": ([C.c_char_p, C.POINTER(LbmConfig)], i32),
+        "lbm_config_last_error": ([], C.c_char_p),
         "lbm_vtk_last_error": ([], C.c_char_p),
     }
     for name, (args, res) in sig.items():

@@ -85,3 +85,40 @@ def test_laminar_collisions_run_with_the_global_omega():
     for coll in (S.CollisionSRTTurbulent, S.CollisionCumD3Q27Turbulent2015, S.CollisionCumD3Q27Turbulent2017,
                  S.CollisionCumD3Q27TurbulentCombined):
         assert S.effective_closure(coll, S.OmegaLES, (0.0, 0.05)) == (S.OmegaLES, (0.0, 0.05))
+
+
+def test_case_file_fills_the_config(built_lib):
+    """lbm_config_parse: a case file with the reference's policy names and the field names of lbm_config
+    gives the config make_config builds from the same values; unknown keys and bad values are refused
+    with the line named and the config left as it was."""
+    text = """
+    # turbulent duct, as main.cu sets one up
+    nx = 96
+    ny 48
+    nz=48
+    periodic 0 1 1
+    collision = CollisionCumD3Q27Turbulent2017
+    closure = OmegaLES          # Smagorinsky
+    storage f16dev
+    inlet = InletVelocityZouHe
+    outlet = OutletNeighbourEquilibriumOmegaRF
+    nu = 0.002
+    cles 0.17
+    force 1e-7, 0, 0
+    omega_dumping 0.0 0.05
+    mlp_interval 16
+    """
+    c = capi.config_from_text(text)
+    want = capi.make_config(96, 48, 48, periodic=(0, 1, 1), collision=capi.LBM_COLLISION_CUMULANT2017,
+                            closure=capi.LBM_CLOSURE_SMAGORINSKY, storage=capi.LBM_STORAGE_F16DEV,
+                            inlet_kind=capi.LBM_INLET_ZOU_HE, nu=0.002, cles=0.17, force=(1e-7, 0, 0),
+                            outlet_kind=capi.LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA_RF, omega_dumping=(0.0, 0.05),
+                            mlp_interval=16)
+    assert bytes(c) == bytes(want)
+    d = capi.config_from_text("")
+    assert bytes(d) == bytes(capi.make_config(0, 0, 0))
+    assert capi.config_from_text("collision srt\nstorage 0", base=c).collision == capi.LBM_COLLISION_SRT
+    for bad in ("nx = 9x", "periodic 1 1", "colision srt", "closure smagorinski", "tau"):
+        with pytest.raises(capi.LbmError) as e:
+            capi.config_from_text("nx 8\n" + bad, base=c)
+        assert e.value.status == capi.LBM_ERR_INVALID and "line 2" in str(e.value)
