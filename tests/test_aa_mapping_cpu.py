@@ -6,7 +6,8 @@ lbm_capi.cu).  For every pair thread of small fully periodic lattices, on even a
     slot opp(v) of its own cells (even) or slot v of x + c_v (odd), with periodic wrap: the AA pattern;
   * the elements a thread writes are exactly the elements it read, so no other thread touches them;
   * the threads' element sets partition the 27 N elements of the population array.
-The velocity table is read from the kernels' own source."""
+The same for the row-staged kernel's shared segments, halo fill and fold (lbm_tma.cuh).  The velocity
+table is read from the kernels' own source."""
 import os
 import re
 
@@ -117,4 +118,64 @@ def test_pair_threads_follow_aa_and_partition_the_array(shape, odd):
                 tid = (z * ny + y) * nx + x0
                 assert (owner[ws] == -1).all()
                 owner[ws] = tid
+    assert (owner >= 0).all()
+
+
+def row_segment(nx, ny, nz, V, y, z, odd):
+    """Global element index of position 0 of segment V of row (y, z) (row_segment, lbm_tma.cuh)."""
+    N = nx * ny * nz
+    slot, yy, zz = V, y, z
+    if odd:
+        slot = opp(V)
+        yy = (y - CV[V][1]) % ny
+        zz = (z - CV[V][2]) % nz
+    return slot * N + (zz * ny + yy) * nx
+
+
+@pytest.mark.parametrize("shape", [(6, 3, 4), (8, 4, 3)])
+@pytest.mark.parametrize("odd", [False, True])
+def test_row_staged_segments_follow_aa(shape, odd):
+    """The row-staged kernel (lbm_tma.cuh row_from_stage): through its shared segments, periodic halo fill
+    and fold, every cell reads the AA element of each direction and every stored position receives the
+    post-collision value the AA pattern puts there; the 27 segments of a row are read and written back
+    whole, and the rows' segments partition the array."""
+    nx, ny, nz = shape
+    N = nx * ny * nz
+    owner = np.full(27 * N, -1, np.int64)
+    for z in range(nz):
+        for y in range(ny):
+            base = [row_segment(nx, ny, nz, V, y, z, odd) for V in range(27)]
+            for V in range(27):
+                seg = np.arange(base[V], base[V] + nx)
+                assert (owner[seg] == -1).all()
+                owner[seg] = z * ny + y
+            # stage[V][1 + pos], pos in [-1, nx]: element ids fetched (halo positions empty)
+            stage = [[None] + [base[V] + x for x in range(nx)] + [None] for V in range(27)]
+            if odd:  # halo fill
+                for V in range(27):
+                    if CV[V][0] > 0:
+                        stage[V][0] = stage[V][nx]
+                    elif CV[V][0] < 0:
+                        stage[V][nx + 1] = stage[V][1]
+            for x in range(nx):
+                for V in range(27):
+                    sh = -CV[V][0] if odd else 0
+                    r, _ = aa_expected(nx, ny, nz, x, y, z, V, odd)
+                    assert stage[V][1 + x + sh] == r, (x, y, z, V)
+            out = [[None] * (nx + 2) for _ in range(27)]
+            for x in range(nx):
+                for V in range(27):
+                    sh = CV[V][0] if odd else 0
+                    out[opp(V)][1 + x + sh] = (x, V)
+            if odd:  # halo fold
+                for V in range(27):
+                    if CV[V][0] < 0:
+                        out[V][1] = out[V][nx + 1]
+                    elif CV[V][0] > 0:
+                        out[V][nx] = out[V][0]
+            for V in range(27):
+                for x in range(nx):
+                    cell_x, v = out[V][1 + x]
+                    _, w = aa_expected(nx, ny, nz, cell_x, y, z, v, odd)
+                    assert w == base[V] + x, (x, y, z, V)
     assert (owner >= 0).all()
