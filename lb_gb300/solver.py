@@ -253,6 +253,19 @@ class Solver:
         self._ctx = C.c_void_p()
         check(lib().lbm_create(C.byref(self.cfg), C.byref(self._ctx)))
 
+    @classmethod
+    def from_config(cls, cfg):
+        """A solver for a ready lbm_config, e.g. capi.config_from_text(case_file_text).  The config is used
+        as given (no laminar-collision mapping: the case file names the closure itself)."""
+        s = cls.__new__(cls)
+        s.shape = (int(cfg.nx), int(cfg.ny), int(cfg.nz))
+        s.N = s.shape[0] * s.shape[1] * s.shape[2]
+        s.cfg = capi.LbmConfig()
+        C.memmove(C.byref(s.cfg), C.byref(cfg), C.sizeof(capi.LbmConfig))
+        s._ctx = C.c_void_p()
+        check(lib().lbm_create(C.byref(s.cfg), C.byref(s._ctx)))
+        return s
+
     # -- lifecycle
     def close(self):
         if self._ctx:

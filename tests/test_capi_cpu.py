@@ -118,6 +118,10 @@ def test_case_file_fills_the_config(built_lib):
     d = capi.config_from_text("")
     assert bytes(d) == bytes(capi.make_config(0, 0, 0))
     assert capi.config_from_text("collision srt\nstorage 0", base=c).collision == capi.LBM_COLLISION_SRT
+    from lb_gb300.solver import Solver
+    with pytest.raises(capi.LbmError) as e:  # refused by the set-up checks, before any device work
+        Solver.from_config(capi.config_from_text("nx 8\nny 8\nnz 8\ncollision 5"))
+    assert e.value.status == capi.LBM_ERR_UNSUPPORTED
     for bad in ("nx = 9x", "periodic 1 1", "colision srt", "closure smagorinski", "tau"):
         with pytest.raises(capi.LbmError) as e:
             capi.config_from_text("nx 8\n" + bad, base=c)
