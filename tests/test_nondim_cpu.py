@@ -177,3 +177,67 @@ def test_step_schedule_replays_the_reference_loop(laminar):
                 averaged.update(range(done, done + n))
             done += n
         assert averaged == naive_avg, (it, avg)
+
+
+class _FakeSolver:
+    """Stands in for the GPU Solver under SolverTurbulentLES.runSimulation: counts steps, records when
+    each call happens and returns fields that depend on the step count."""
+
+    def __init__(self, shape):
+        self.shape = shape
+        self.N = shape[0] * shape[1] * shape[2]
+        self.k = 0
+        self.calls = []
+
+    def step(self, n):
+        self.k += n
+
+    def timeavg_begin(self):
+        self.calls.append(("avg_begin", self.k))
+
+    def timeavg_end(self):
+        self.calls.append(("avg_end", self.k))
+
+    def timeavg_get(self):
+        return np.full(self.N, 1.0), np.zeros((3, self.N)), None, None
+
+    def probe(self, x, y, z):
+        self.calls.append(("probe", self.k, (x, y, z)))
+        return np.array([0.01, 0.0, 0.0, 1.0])
+
+    def error_evaluation(self):
+        self.calls.append(("err", self.k))
+        return 1.0 / self.k
+
+    def moments(self):
+        return np.full(self.N, 1.0 + 1e-3 * self.k), np.zeros((3, self.N))
+
+
+@pytest.mark.parametrize("laminar", [False, True])
+def test_python_run_loop_calls_and_files(tmp_path, laminar):
+    """SolverTurbulentLES.runSimulation (and SolverLaminar's) on a stand-in solver: the average starts
+    after it - avg + 1 steps, errors come after steps k = 10, 20 (k + 1 steps done), dumps and probe lines
+    land under results_dir with the reference's names."""
+    from lb_gb300.solver import SolverLaminar
+    shape = (4, 3, 2)
+    c = dict(nu=0.1, iterations=25, iterationsMomentAvg=5, err_every_it=10, plot_every_it=7, probe_every_it=4,
+             probe_iterations=9, ProbeLocationLat=(1, 1, 0), results_dir=str(tmp_path))
+    cls = SolverLaminar if laminar else SolverTurbulentLES
+    s = cls(constants=c, data={"flags": np.ones(shape[::-1], np.int32)})
+    s.solver = _FakeSolver(shape)
+    errors = s.runSimulation()
+    assert s.solver.k == 25
+    assert [e[0] for e in errors] == [10, 20]
+    calls = s.solver.calls
+    assert ("avg_begin", 21) in calls and calls[-1] == ("avg_end", 25)
+    assert [cl[1] for cl in calls if cl[0] == "err"] == [11, 21]
+    probes = [cl[1] for cl in calls if cl[0] == "probe"]
+    assert probes == ([] if laminar else [17, 21, 25])  # after steps k = 16, 20, 24 (k >= 25 - 9)
+    files = sorted(p.name for p in tmp_path.iterdir())
+    if laminar:
+        assert files == ["variablesLattice0.vtk", "variablesLattice1.vtk", "variablesLattice2.vtk",
+                         "variablesLattice3.vtk", "variablesTimeAvg.vtk"]
+    else:
+        assert files == ["probeData.csv", "variables.1.vtk", "variables.2.vtk", "variables.3.vtk",
+                         "variablesTimeAvg.vtk"]
+        assert len((tmp_path / "probeData.csv").read_text().splitlines()) == 2 + 3
