@@ -168,3 +168,95 @@ def test_driver_channel_profile_equals_python_api(built_lib):
     rxy = (uu[3] - um[0] * um[1]).mean(axis=(0, 2))
     assert np.allclose(prof[:, 1], mean_ux, rtol=1e-12, atol=1e-15)
     assert np.allclose(prof[:, 5], rxy, rtol=1e-9, atol=1e-15)
+
+
+STUB = r'''
+// stand-in for the library: records the calls SolverTurbulentLES makes (no GPU)
+#include <cstdio>
+#include <cstring>
+#include "lbm.h"
+static int g_k = 0;
+static lbm_ctx* const CTX = (lbm_ctx*)0x1;
+extern "C" {
+lbm_status lbm_create(const lbm_config*, lbm_ctx** c) { *c = CTX; return LBM_OK; }
+lbm_status lbm_destroy(lbm_ctx*) { return LBM_OK; }
+const char* lbm_last_error(const lbm_ctx*) { return ""; }
+const char* lbm_vtk_last_error(void) { return ""; }
+lbm_status lbm_set_flags(lbm_ctx*, const int32_t*) { return LBM_OK; }
+lbm_status lbm_set_bc(lbm_ctx*, const lbm_bc_inlet*, int32_t, const lbm_bc_outlet*, int32_t) { return LBM_OK; }
+lbm_status lbm_set_symmetry(lbm_ctx*, const lbm_bc_symmetry*, int32_t) { return LBM_OK; }
+lbm_status lbm_init_equilibrium(lbm_ctx*, double, const double*) { return LBM_OK; }
+lbm_status lbm_init_fields(lbm_ctx*, const double*, const double*) { return LBM_OK; }
+lbm_status lbm_vtk_read_variables(const char*, const int32_t*, double*, double*) { return LBM_OK; }
+lbm_status lbm_mlp_load(lbm_ctx*, const lbm_mlp_model*) { return LBM_OK; }
+lbm_status lbm_step(lbm_ctx*, int32_t n) { g_k += n; return LBM_OK; }
+lbm_status lbm_synchronize(lbm_ctx*) { return LBM_OK; }
+lbm_status lbm_timeavg_begin(lbm_ctx*) { std::printf("avg_begin %d\n", g_k); return LBM_OK; }
+lbm_status lbm_timeavg_end(lbm_ctx*) { std::printf("avg_end %d\n", g_k); return LBM_OK; }
+lbm_status lbm_timeavg_get(lbm_ctx*, double*, double*, double*, int64_t*) { return LBM_OK; }
+lbm_status lbm_probe(lbm_ctx*, int32_t, int32_t, int32_t, double out[4]) {
+    std::printf("probe %d\n", g_k); out[0] = out[1] = out[2] = 0; out[3] = 1; return LBM_OK; }
+lbm_status lbm_error_evaluation(lbm_ctx*, double* e) { std::printf("err %d\n", g_k); *e = 1.0; return LBM_OK; }
+lbm_status lbm_get_moments(lbm_ctx*, double*, double*) { return LBM_OK; }
+lbm_status lbm_vtk_write(const char* path, const char*, const int32_t*, double, double, const double*,
+                         const lbm_vtk_field*, int32_t) { std::printf("vtk %s %d\n", std::strrchr(path, '/') + 1, g_k);
+                                                          return LBM_OK; }
+lbm_status lbm_probe_csv_append(const char*, double, const double*, double, double, double) { return LBM_OK; }
+}
+'''
+
+
+@pytest.mark.parametrize("laminar", [False, True])
+def test_cpp_run_loop_matches_the_python_schedule(laminar):
+    """SolverTurbulentLES / SolverLaminar::runSimulation of include/lbm_solver.hpp, linked against a
+    stand-in library that records the calls: the average, probe, error and dump calls come after the same
+    steps as in step_schedule (the Python mirror's loop, itself checked against the reference loop)."""
+    from lb_gb300.solver import step_schedule
+    it, avg, err, plot, probe, probe_its = 25, 5, 10, 7, 4, 9
+    solver = ("SolverLaminar<D3Q27, InitializationEquilibriumConstVector, CollisionCumD3Q27Laminar, StreamingAB, "
+              "BounceBackWallHalf, NoSymmetry, NoPeriodic, InletVelocityMovingWall, OutletDensityInterpolated, "
+              "MomentDensityVelocityN27, ErrorQuadratic, NonDimensiolnaliseFactorsVelocity, MomentTimeAvg>"
+              if laminar else
+              "SolverTurbulentLES<D3Q27, InitializationEquilibriumConstVector, CollisionCumD3Q27Turbulent2015, "
+              "StreamingAB, BounceBackWallHalf, NoSymmetry, NoPeriodic, InletVelocityMovingWall, "
+              "OutletDensityInterpolated, MomentDensityVelocityN27, OmegaLES, ErrorQuadratic, "
+              "NonDimensiolnaliseFactorsVelocity, MomentTimeAvg>")
+    main = r'''
+#include "lbm_solver.hpp"
+using namespace lbm_gb300;
+int main() {
+    LBMConstants C; LBMData D;
+    C.dimX_int = 4; C.dimY_int = 3; C.dimZ_int = 2; D.meshFluid.assign(24, 1);
+    C.iterations = %d; C.iterationsMomentAvg = %d; C.err_every_it = %d; C.plot_every_it = %d;
+    C.probe_every_it = %d; C.probe_iterations = %d; C.results_dir = "out";
+    %s s(C, D);
+    s.initializeSimulation(false);
+    s.runSimulation();
+    return 0;
+}
+''' % (it, avg, err, plot, probe, probe_its, solver)
+    with tempfile.TemporaryDirectory() as d:
+        for name, text in (("stub.cpp", STUB), ("main.cpp", main)):
+            with open(os.path.join(d, name), "w") as fh:
+                fh.write(text)
+        exe = os.path.join(d, "t")
+        r = subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), os.path.join(d, "main.cpp"),
+                            os.path.join(d, "stub.cpp"), "-o", exe], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.splitlines()
+    want = []
+    for begin, n, j, events in step_schedule(it, avg, err_every=err, probe_every=probe, probe_iterations=probe_its,
+                                             plot_every=plot, laminar=laminar):
+        done = j + 1
+        if begin:
+            want.append(f"avg_begin {done - n}")
+        for e in events:
+            if e == "probe":
+                want.append(f"probe {done}")
+            elif e == "err":
+                want.append(f"err {done}")
+            else:
+                name = f"variablesLattice{j // plot}.vtk" if laminar else f"variables.{j // plot}.vtk"
+                want.append(f"vtk {name} {done}")
+    want += [f"avg_end {it}", f"vtk variablesTimeAvg.vtk {it}"]
+    assert out == want
