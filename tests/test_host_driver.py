@@ -260,3 +260,93 @@ int main() {
                 want.append(f"vtk {name} {done}")
     want += [f"avg_end {it}", f"vtk variablesTimeAvg.vtk {it}"]
     assert out == want
+
+
+SETUP_STUB = STUB.replace(
+    "lbm_status lbm_create(const lbm_config*, lbm_ctx** c) { *c = CTX; return LBM_OK; }",
+    "lbm_status lbm_create(const lbm_config* g, lbm_ctx** c) { *c = CTX; std::printf(\"cfg %d %d %d %d %.9g %.9g "
+    "%g %g %d%d%d\\n\", g->collision, g->closure, g->inlet_kind, g->outlet_kind, g->nu, g->tau, g->omega_dumping_low, "
+    "g->omega_dumping_high, g->periodic[0], g->periodic[1], g->periodic[2]); return LBM_OK; }").replace(
+    "lbm_status lbm_set_bc(lbm_ctx*, const lbm_bc_inlet*, int32_t, const lbm_bc_outlet*, int32_t) { return LBM_OK; }",
+    "lbm_status lbm_set_bc(lbm_ctx*, const lbm_bc_inlet* i, int32_t ni, const lbm_bc_outlet* o, int32_t no) { "
+    "for (int e = 0; e < ni; e++) std::printf(\"inlet %.9g\\n\", i[e].velocity[0]); "
+    "for (int e = 0; e < no; e++) std::printf(\"outlet %.9g\\n\", o[e].density); return LBM_OK; }").replace(
+    "lbm_status lbm_init_equilibrium(lbm_ctx*, double, const double*) { return LBM_OK; }",
+    "lbm_status lbm_init_equilibrium(lbm_ctx*, double r, const double* u) { std::printf(\"init %.9g %.9g\\n\", r, u[0]); "
+    "return LBM_OK; }").replace(
+    "lbm_status lbm_vtk_read_variables(const char*, const int32_t*, double*, double*) { return LBM_OK; }",
+    "lbm_status lbm_vtk_read_variables(const char* p, const int32_t*, double*, double*) { std::printf(\"read %s\\n\", p); "
+    "return LBM_OK; }").replace(
+    "lbm_status lbm_init_fields(lbm_ctx*, const double*, const double*) { return LBM_OK; }",
+    "lbm_status lbm_init_fields(lbm_ctx*, const double*, const double*) { std::printf(\"init_fields\\n\"); "
+    "return LBM_OK; }")
+
+
+def run_setup(solver, body):
+    main = r'''
+#include "lbm_solver.hpp"
+using namespace lbm_gb300;
+int main() {
+    LBMConstants C; LBMData D;
+    C.dimX_int = 4; C.dimY_int = 3; C.dimZ_int = 2; D.meshFluid.assign(24, 1);
+    C.periodic[0] = 1; C.omegaDumpingLow = 0.0; C.omegaDumpingHigh = 0.05;
+    lbm_bc_inlet in{}; in.velocity[0] = 4.0f; D.meshBoundaryInlet.push_back(in);
+    lbm_bc_outlet out{}; out.density = 1.293f; D.meshBoundaryOutlet.push_back(out);
+    %s
+    %s s(C, D);
+    s.convertToLattice(false);
+    s.initializeSimulation(false);
+    return 0;
+}
+''' % (body, solver)
+    with tempfile.TemporaryDirectory() as d:
+        for name, text in (("stub.cpp", SETUP_STUB), ("main.cpp", main)):
+            with open(os.path.join(d, name), "w") as fh:
+                fh.write(text)
+        exe = os.path.join(d, "t")
+        r = subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), os.path.join(d, "main.cpp"),
+                            os.path.join(d, "stub.cpp"), "-o", exe], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        return subprocess.run([exe], capture_output=True, text=True, check=True).stdout.splitlines()
+
+
+TAGS = ("D3Q27, {init}, {coll}, StreamingAB, BounceBackWallHalf, NoSymmetry, Periodic, InletVelocityEquilibrium, "
+        "OutletNeighbourEquilibriumOmega, MomentDensityVelocityN27, {turb}ErrorQuadratic, "
+        "NonDimensiolnaliseFactorsVelocity, MomentTimeAvg")
+
+
+def test_cpp_setup_converts_physical_inputs():
+    """convertToLattice + initializeSimulation of the C++ mirror (stand-in library): the config carries the
+    converted nu and tau, the inlet velocity is divided by Cu, the outlet density by Crho, and the initial
+    state is rho_fyz / Crho with VelocityInit / Cu (InitializationEquilibriumConstVector.h:79-82)."""
+    from lb_gb300.solver import NonDimensiolnaliseFactorsVelocity as ND
+    phys = ("C.ny_fyz = 2e-4; C.rho_fyz = 1.293; C.u_guess_fyz = 4.0; C.U_lb = 0.09; C.BBmax[0] = 1.0; "
+            "C.VelocityInit[0] = 2.0;")
+    out = run_setup("SolverTurbulentLES<%s>" % TAGS.format(init="InitializationEquilibriumConstVector",
+                                                          coll="CollisionCumD3Q27Turbulent2015", turb="OmegaLES, "),
+                    phys)
+    c = ND.nonDimensionalize(dict(BBmin=(0, 0, 0), BBmax=(1.0, 0, 0), u_guess_fyz=4.0, U_lb=0.09, rho_fyz=1.293,
+                                  ny_fyz=2e-4), 4)
+    cfg = out[0].split()
+    assert cfg[1:5] == ["1", "1", "1", "2"] and cfg[-1] == "100"
+    assert float(cfg[5]) == pytest.approx(c["nu"], rel=1e-7) and float(cfg[6]) == pytest.approx(c["tau"], rel=1e-7)
+    assert (cfg[7], cfg[8]) == ("0", "0.05")
+    assert float(out[1].split()[1]) == pytest.approx(4.0 / c["Cu"], rel=1e-6)
+    assert float(out[2].split()[1]) == pytest.approx(1.0, rel=1e-6)
+    init = out[3].split()
+    assert float(init[1]) == pytest.approx(1.0, rel=1e-6) and float(init[2]) == pytest.approx(2.0 / c["Cu"], rel=1e-6)
+
+
+def test_cpp_setup_laminar_and_restart_choices():
+    """A laminar collision runs without closure and sponge; SolverLaminar drops the periodic axes (its loop
+    has no periodic hook); InitializationEquilibriumVariables reads results/<InitFileName>."""
+    out = run_setup("SolverTurbulentLES<%s>" % TAGS.format(init="InitializationEquilibriumVariables",
+                                                          coll="CollisionSRTLaminar", turb="OmegaLES, "),
+                    'C.InitFileName = "variablesLattice3.vtk";')
+    cfg = out[0].split()
+    assert cfg[1:3] == ["0", "0"] and (cfg[7], cfg[8]) == ("0", "0") and cfg[-1] == "100"
+    assert out[1:] == ["inlet 4", "outlet 1.29299998", "read results/variablesLattice3.vtk", "init_fields"]
+    lam = TAGS.format(init="InitializationEquilibriumConstVector", coll="CollisionCumD3Q27Turbulent2015", turb="")
+    out = run_setup("SolverLaminar<%s>" % lam, "C.plot_every_it = 10; C.err_every_it = 10;")
+    cfg = out[0].split()
+    assert cfg[1:3] == ["1", "0"] and cfg[-1] == "000"
