@@ -122,6 +122,7 @@ struct LBMData {
     std::vector<double> rho, u;                // host copies after the run (u: ux[N], uy[N], uz[N])
     std::vector<double> rhoTimeAvg, uTimeAvg, uuTimeAvg;
     std::vector<double> probe;                 // u_x, u_y, u_z, rho per probe sample
+    std::vector<double> df;                    // populations [v][z][y][x] after readPopulations()
     std::vector<double> errors;                // ErrorQuadratic values, one per evaluation
 };
 
@@ -398,6 +399,16 @@ struct outputerVTK {
     }
     static void variablesTimeAvgLatticeVTK(const LBMData& D, const LBMConstants& C, bool /*verbose*/) {
         variables(dir(C) + "/variablesTimeAvg.vtk", C, D.rhoTimeAvg, D.uTimeAvg, "pressure", 1, 1, 1);
+    }
+    // :660-740: one population (reference velocity order) from D.df as "DFunciton_<velocity>", as the
+    // reference names the field (:690), in results/distributionFunction<velocity>.vtk
+    static void distributionFunctionVTK(const LBMData& D, const LBMConstants& C, int velocity, bool /*verbose*/) {
+        const size_t N = (size_t)C.dimX_int * C.dimY_int * C.dimZ_int;
+        if (velocity < 0 || velocity > 26 || D.df.size() != 27 * N)
+            throw Error(LBM_ERR_INVALID, "distributionFunctionVTK: velocity out of range or populations not read back");
+        const std::string name = "DFunciton_" + std::to_string(velocity);
+        const lbm_vtk_field f = {name.c_str(), 1, D.df.data() + (size_t)velocity * N, 1.0};
+        write(dir(C) + "/distributionFunction" + std::to_string(velocity) + ".vtk", "LBE variables", C, &f, 1);
     }
     // :824-851: one probe line appended to results/probeData.csv
     static void probeWriteOut(const LBMConstants& C, double velX, double velY, double velZ, double rho) {
@@ -724,6 +735,13 @@ public:
     }
 
     lbm_ctx* context() { return ctx; }
+
+    // the populations in the reference layout into Data.df (for distributionFunctionVTK)
+    void readPopulations() {
+        if (!ctx) throw Error(LBM_ERR_STATE, "readPopulations before initializeSimulation");
+        Data.df.resize((size_t)27 * Constants.dimX_int * Constants.dimY_int * Constants.dimZ_int);
+        check(lbm_get_populations(ctx, Data.df.data()), ctx, "lbm_get_populations");
+    }
 
     LBMConstants& Constants;
     LBMData& Data;

@@ -147,6 +147,8 @@ int main(int argc, char** argv) {
     }
     for (int q = 0; q < 36; q++) D.u.push_back(0.01 * (q - 17));
     D.rhoTimeAvg = D.rho; D.uTimeAvg = D.u;
+    for (int q = 0; q < 27 * 12; q++) D.df.push_back(0.001 * q - 0.1);
+    outputerVTK::distributionFunctionVTK(D, C, 13, false);
     outputerVTK::variablesVTK(D, C, 4, false);
     outputerVTK::variablesLatticeVTK(D, C, 4, false);
     outputerVTK::variablesTimeAvgVTK(D, C, false);
@@ -180,6 +182,9 @@ int main(int argc, char** argv) {
     output.outputerVTK.variablesLatticeVTK(py / "variablesLattice4.vtk", grid, rho, u)
     output.outputerVTK.variablesTimeAvgVTK(py / "variablesTimeAvg.vtk", grid, rho, u, conv)
     output.outputerVTK.MeshVTK(py / "meshIN.vtk", grid, flags, "meshIN")
+    output.outputerVTK.distributionFunctionVTK(py / "distributionFunction13.vtk", grid,
+                                               0.001 * np.arange(27 * N) - 0.1, 13)
     output.outputerVTK.probeWriteOut(py / "probeData.csv", [0.01, -0.02, 0.003, 1.001], conv, 1e-4 * 5)
-    for name in ("variables.4.vtk", "variablesLattice4.vtk", "variablesTimeAvg.vtk", "meshIN.vtk", "probeData.csv"):
+    for name in ("variables.4.vtk", "variablesLattice4.vtk", "variablesTimeAvg.vtk", "meshIN.vtk", "probeData.csv",
+                 "distributionFunction13.vtk"):
         assert (out / name).read_bytes() == (py / name).read_bytes(), name
