@@ -64,17 +64,20 @@ __global__ void __launch_bounds__(128, MODE == 2 ? step2_min_blocks(COLL) : LBM_
     F2 ri, ux, uy, uz, om_s;
     uint4 rowA = make_uint4(0, 0, 0, 0), rowB = rowA;
     bool inA = false, inB = false;
-    // populations decoded on load: taking the moments from the raw FP16 deviations (as step_pair does)
-    // measured 2 % slower here with the kept-viscosity steps and no faster with the network
+    // FP16 storage + cumulant-2015: the moments come from the raw deviations as in step_pair, so the
+    // Smagorinsky fallback rate and the collision see the same roundings as k_step2 (an all-fallback
+    // model then reproduces k_step2 bit for bit)
+    constexpr bool RAW = S::kind == 2 && COLL == 1;
     if (pair) {
         if (!yz_seam) {
-            load_pair<S, ODD>(p, q, k, f);
+            load_pair<S, ODD, RAW>(p, q, k, f);
         } else {
             PairRows w;
             make_pair_rows(p, x0, y, z, w);
-            load_pair_rows<S, ODD>(p, w, k, f);
+            load_pair_rows<S, ODD, RAW>(p, w, k, f);
         }
         mm = raw_moments(f);
+        if constexpr (RAW) mm = moments_from_raw(mm, p);
         ri = rcp(mm.rho);
         ux = mm.jx * ri; uy = mm.jy * ri; uz = mm.jz * ri;
         if (p.has_force) {
