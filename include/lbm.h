@@ -97,7 +97,7 @@ typedef struct lbm_config {
     int32_t inlet_kind;       /* LBM_INLET_* */
     double  nu;               /* lattice kinematic viscosity; tau = 3 nu + 1/2 */
     double  tau;              /* if > 0, overrides the tau derived from nu */
-    double  cles;             /* Smagorinsky constant; coefficient 18*cles (OmegaLES.h:347) */
+    double  cles;             /* Smagorinsky constant; coefficient 18*cles (OmegaLES.h:119) */
     double  force[3];         /* body force density (lattice units); no reference counterpart */
     double  rho0;             /* reference density of the FP16-deviation encoding */
     int32_t f16_scale_log2;   /* s of the FP16-deviation encoding (10 => 2^10) */
@@ -194,7 +194,7 @@ lbm_status lbm_set_bc(lbm_ctx* ctx, const lbm_bc_inlet* inlets, int32_t n_inlets
  * (which clears the list). */
 lbm_status lbm_set_symmetry(lbm_ctx* ctx, const lbm_bc_symmetry* records, int32_t n);
 
-/* ---- initialisation (InitializationEquilibriumConstVector.h:103-224) ---------- */
+/* ---- initialisation (InitializationEquilibriumConstVector.h:20-141) ---------- */
 lbm_status lbm_init_equilibrium(lbm_ctx* ctx, double rho0, const double u0[3]);
 /* rho: N doubles, u: 3*N doubles component-major (ux[N], uy[N], uz[N]) */
 lbm_status lbm_init_fields(lbm_ctx* ctx, const double* rho, const double* u);

@@ -567,7 +567,7 @@ public:
     }
 
     // the context, geometry, boundary records and the equilibrium initial state
-    // (SolverTurbulentLES.h:103-146; InitializationEquilibriumConstVector.h:103-224)
+    // (SolverTurbulentLES.h:103-146; InitializationEquilibriumConstVector.h:20-141)
     void initializeSimulation(bool verbose) {
         lbm_config c{};
         c.nx = Constants.dimX_int; c.ny = Constants.dimY_int; c.nz = Constants.dimZ_int;

@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(128) k_read(Params p, ReadOut o) {
         }
     }
     if (o.mode & READ_ERROR) {
-        // ErrorQuadratic.h:261-305: sum sqrt|u - u_prev|^2 and sqrt|u|^2 over flag == 1 cells
+        // ErrorQuadratic.h:33-78: sum sqrt|u - u_prev|^2 and sqrt|u|^2 over flag == 1 cells
         double e1 = 0, e2 = 0;
         if (live && (fl & BIT_REFBULK)) {
             const R px = (R)o.uerr[c.idx], py = (R)o.uerr[p.N + c.idx], pz = (R)o.uerr[2 * p.N + c.idx];
@@ -157,7 +157,7 @@ __global__ void k_probe(Params p, int x, int y, int z, double* out) {
     out[0] = ux; out[1] = uy; out[2] = uz; out[3] = rho;
 }
 
-// equilibrium initialisation (InitializationEquilibriumConstVector.h:157-218): state m = 0 in the
+// equilibrium initialisation (InitializationEquilibriumConstVector.h:111-126): state m = 0 in the
 // cells' own slots; side tables of the -1 nodes seeded so that the first steps see df_0 there.
 template <class S>
 __global__ void __launch_bounds__(128) k_init(Params p, const double* rho_f, const double* u_f, double rho0,

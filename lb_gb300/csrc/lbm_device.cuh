@@ -6,11 +6,11 @@
 // writes f*_v into A[x+c_v][v].  Every slot a thread reads is written only by that thread, so
 // one array serves in place with no race.  Boundaries are folded into the gather by the cell
 // class byte:
-//   half-way bounce-back from a solid neighbour x-c_v   (BounceBackWallHalf.h:114-125)
+//   half-way bounce-back from a solid neighbour x-c_v   (BounceBackWallHalf.h:38-49)
 //       even step reads A[x-c_v][opp v], odd step reads A[x][v]  (the swapped slot);
 //   moving-wall nodes (flag -1, InletVelocityMovingWall.h:31-55) keep their own 27-value state in
 //       a 3-level side table; neighbours stream their state of one step earlier (StreamingAB.h:62-65);
-//   equilibrium velocity-inlet nodes (InletVelocityEquilibrium.h:115-167) are not updated: their
+//   equilibrium velocity-inlet nodes (InletVelocityEquilibrium.h:51-103) are not updated: their
 //       neighbours rebuild f_eq(u_b, rho_b) from the moments that the two interior "probe" cells
 //       stored two steps earlier (3-level table);
 //   density-interpolated outlets (OutletDensityInterpolated.h:170-252) read the upstream cell's and
@@ -203,7 +203,7 @@ struct Codec<StF16> {
     }
 };
 
-// ---- equilibrium (second-order polynomial of the reference, e.g. OmegaLES.h:275-294) ----------
+// ---- equilibrium (second-order polynomial of the reference, e.g. OmegaLES.h:47-66) ----------
 template <int V, class R>
 LBM_D R feq(R r, R ux, R uy, R uz, R u2) {
     const R cu = V == 0 ? (R)0 : cdotu<V>(ux, uy, uz);
@@ -429,7 +429,7 @@ LBM_D void scatter(const Params& p, const Cell& c, const typename S::R (&f)[27])
 }
 
 // state df_m of an equilibrium-inlet node: f_eq(u_b, rho_b) with rho_b from the probe moments of
-// step m-1 (InletVelocityEquilibrium.h:148-160 run at the end of step m-1)
+// step m-1 (InletVelocityEquilibrium.h:71-97 run at the end of step m-1)
 template <class S>
 LBM_D void inlet_state(const Params& p, const Cell& c, typename S::R (&f)[27]) {
     using R = typename S::R;
@@ -446,7 +446,7 @@ LBM_D void inlet_state(const Params& p, const Cell& c, typename S::R (&f)[27]) {
 }
 
 // ---- moments of a gathered cell for the read-only kernels ------------------------------------------
-// rho and u as the reference's moment pass defines them (MomentDensityVelocityN27.h:212-228),
+// rho and u as the reference's moment pass defines them (MomentDensityVelocityN27.h:65-81),
 // with the half-force velocity shift
 template <class R>
 LBM_D void moments(const R (&f)[27], const Params& p, R& rho, R& jx, R& jy, R& jz, R& ux, R& uy, R& uz) {

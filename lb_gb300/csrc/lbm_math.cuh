@@ -142,7 +142,7 @@ LBM_D Mom<L> raw_moments(const L (&f)[27]) {
 }
 
 // ---- relaxation rate ----------------------------------------------------------------------------
-// Smagorinsky (OmegaLES.h:312-357): Pi = sum c c (f - f_eq) = M - rho (u u + I/3),
+// Smagorinsky (OmegaLES.h:84-129): Pi = sum c c (f - f_eq) = M - rho (u u + I/3),
 // tau_LES = tau/2 + sqrt(tau^2 + 18 CLES |Pi| / rho)/2
 template <class L>
 LBM_D L omega_smagorinsky(L tau, L cles18, L rho, L ri, L ux, L uy, L uz, const Mom<L>& m) {
@@ -157,7 +157,7 @@ LBM_D L omega_smagorinsky(L tau, L cles18, L rho, L ri, L ux, L uy, L uz, const 
     return rcp(tles);
 }
 
-// ---- SRT (CollisionSRTTurbulent.h:386-391) --------------------------------------------------------
+// ---- SRT (CollisionSRTTurbulent.h:63-68) --------------------------------------------------------
 template <class L>
 LBM_D void collide_srt(L (&f)[27], L rho, L ux, L uy, L uz, L om) {
     const L u2 = lfma(ux, ux, lfma(uy, uy, uz * uz));

@@ -136,7 +136,7 @@ struct Sim {
     inline int32_t mesh_at(int i, int j, int k) const { return inside(i, j, k) ? mesh[id(i, j, k)] : 0; }
 
     inline R feq(R ux, R uy, R uz, R r, int v) const {
-        // f_equilibrium lambdas, e.g. OmegaLES.h:275-294
+        // f_equilibrium lambdas, e.g. OmegaLES.h:47-66
         R uc = (R)C[v][0] * ux + (R)C[v][1] * uy + (R)C[v][2] * uz;
         R u2 = ux * ux + uy * uy + uz * uz;
         return w[v] * r * ((R)1 + (R)3 * uc + (R)4.5 * uc * uc - (R)1.5 * u2);
@@ -164,7 +164,7 @@ struct Sim {
             for (const Sym& sy : syms) walls.push_back({sy.x, sy.y, sy.z, 0});
     }
 
-    // ---- InitializationEquilibriumConstVector.h:103-224 (lattice units) ------------------
+    // ---- InitializationEquilibriumConstVector.h:20-141 (lattice units) ------------------
     void init_equilibrium(R r0, const R u0[3]) {
         a_count = 0; a_on = false;
 #pragma omp parallel for schedule(static)
@@ -194,7 +194,7 @@ struct Sim {
         }
     }
 
-    // ---- OmegaLES.h:297-359 ---------------------------------------------------------------
+    // ---- OmegaLES.h:69-131 ---------------------------------------------------------------
     void omega_les() {
 #pragma omp parallel for schedule(static)
         for (long long c = 0; c < (long long)N; c++) {
@@ -217,14 +217,14 @@ struct Sim {
             omega[c] = (R)1 / tles;
         }
     }
-    // ---- OmegaNo.h:404-412 ----------------------------------------------------------------
+    // ---- OmegaNo.h:34-42 ----------------------------------------------------------------
     void omega_no() {
 #pragma omp parallel for schedule(static)
         for (long long c = 0; c < (long long)N; c++)
             if (mesh[c] != 0) omega[c] = (R)1 / tau;
     }
 
-    // ---- CollisionSRTTurbulent.h:379-398 (+ Guo forcing extension) -------------------------
+    // ---- CollisionSRTTurbulent.h:56-75 (+ Guo forcing extension) -------------------------
     void collision_srt() {
         bool force = F[0] != 0 || F[1] != 0 || F[2] != 0;
 #pragma omp parallel for schedule(static)
@@ -465,7 +465,7 @@ struct Sim {
                 }
     }
 
-    // ---- BounceBackWallHalf.h:105-128 (+ momentum-exchange drag) ---------------------------
+    // ---- BounceBackWallHalf.h:29-52 (+ momentum-exchange drag) ---------------------------
     void bounce_back_wall() {
         double d0 = 0, d1 = 0, d2 = 0;
 #pragma omp parallel for reduction(+ : d0, d1, d2) schedule(static)
@@ -502,7 +502,7 @@ struct Sim {
         }
     }
 
-    // ---- InletVelocityEquilibrium.h:115-167 (x normals only, as the reference) ----------
+    // ---- InletVelocityEquilibrium.h:51-103 (x normals only, as the reference) ----------
     void inlet_equilibrium() {
 #pragma omp parallel for schedule(static)
         for (long long e = 0; e < (long long)inlets.size(); e++) {
@@ -705,7 +705,7 @@ struct Sim {
         }
     }
 
-    // ---- MomentDensityVelocityN27.h:182-229 (+ half-force velocity shift) ------------------
+    // ---- MomentDensityVelocityN27.h:27-83 (+ half-force velocity shift) ------------------
     void moment_update() {
 #pragma omp parallel for schedule(static)
         for (long long c = 0; c < (long long)N; c++) {
