@@ -12,7 +12,7 @@ and writes, next to this script:
 The mesh-matrix text format is the reference's outputerMesh::MeshMatrixOut
 (3D/preprocess/src/postprocesors/outputerMesh.h:19-56): a 9-line header, then the values
 with x fastest, one row per (y, z) and a blank line after every z slice.
-Run:  python tests/golden/make_golden.py [reference_root]
+Run:  python tests/golden/make_golden.py <reference_root>   (the reference checkout's top directory)
 """
 import hashlib
 import os
@@ -63,4 +63,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference_root>")
+    main(sys.argv[1])

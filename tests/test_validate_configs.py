@@ -1,8 +1,11 @@
-"""Validation runs of the benchmark configurations on the GPU (long; not collected by pytest).
+"""Validation runs of the benchmark configurations on the GPU: long, so skipped unless pytest is given
+--run-slow.  Each test writes its results as one JSON file into $LBM_VALIDATE_OUT (when set) and asserts
+the bounds stated beside it.
 
-    python -m tests.validate_configs c1 [--n 64 --steps 10000]
-    python -m tests.validate_configs c3 [--shape 512,256,256 --steps 20000 --avg 5000]
-    python -m tests.validate_configs c4 [--shape 384,192,192 --steps 4000]
+    python -m pytest tests/test_validate_configs.py --run-slow -m gpu -k c1      (64^3, 10k steps)
+    python -m pytest tests/test_validate_configs.py --run-slow -m gpu -k c3      (512x256x256, 20k steps)
+    python -m pytest tests/test_validate_configs.py --run-slow -m gpu -k c4      (384x192x192, 4k steps)
+    python -m pytest tests/test_validate_configs.py --run-slow -m gpu -k c5      (256^3 LES, 1024^3 fine run)
 
 c1: lid-driven cavity 64^3, FP64 cumulant on the GPU against the CPU oracle's FP64 run of the same case
     (parity of the whole 10k-step trajectory), FP32 against FP64; centre-line profiles.
@@ -12,15 +15,14 @@ c3: channel at 512x256x256 (laminar profile + 5 % seeded noise, Re_tau 180 forci
     against FP64.
 c4: flow past the voxelized seeded body at 384x192x192: GPU voxelizer against the CPU oracle (bit for
     bit), FP32 against FP64 drag (momentum exchange, FP64 sums).
-c5: periodic decaying turbulence, coarse n^3 (default 128; the configuration's 256 with --n 256) and a
-    4x-finer run of the same seeded random-phase field (E(k) ~ k^4 exp(-2 (k/k0)^2), k0 = 8,
-    divergence-free, u_rms = 0.04 per component).  A priori: the learned closure's and Smagorinsky's
-    subgrid-stress and dissipation errors on the filtered fine field.  A posteriori: coarse LES in
-    FP16-deviation storage with each closure from the filtered initial field, against the filtered
-    fine field after the same physical time.  Throughput of both closures on the coarse lattice.
-Each prints one JSON line.
+c5: periodic decaying turbulence, coarse 256^3 and a 4x-finer run of the same seeded random-phase field
+    (E(k) ~ k^4 exp(-2 (k/k0)^2), k0 = 8, divergence-free, u_rms = 0.04 per component).  A priori: the
+    learned closure's and Smagorinsky's subgrid-stress and dissipation errors on the filtered fine field.
+    A posteriori: coarse LES in FP16-deviation storage with each closure from the filtered initial
+    field, against the filtered fine field after the same physical time.  Throughput of both closures
+    on the coarse lattice.
+LBM_VALIDATE_SMALL=1 runs reduced sizes for a quick look (the bounds are then not asserted).
 """
-import argparse
 import json
 import os
 import sys
@@ -30,6 +32,8 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
+
+import pytest  # noqa: E402
 
 from lb_gb300 import cases  # noqa: E402
 from lb_gb300.solver import OmegaLES, OmegaNo, Solver, InletVelocityEquilibrium  # noqa: E402
@@ -237,33 +241,57 @@ def c5(n, steps, k, models):
     return out
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("which", choices=["c1", "c3", "c4", "c5"])
-    ap.add_argument("--interval", type=int, default=8)
-    ap.add_argument("--model", default=None, help="c5: evaluate this model file only")
-    ap.add_argument("--n", type=int, default=64)
-    ap.add_argument("--steps", type=int, default=None)
-    ap.add_argument("--avg", type=int, default=5000)
-    ap.add_argument("--shape", default=None)
-    a = ap.parse_args()
-    if a.which == "c1":
-        r = c1(a.n, a.steps or 10000)
-    elif a.which == "c3":
-        shape = tuple(int(x) for x in (a.shape or "512,256,256").split(","))
-        r = c3(shape, a.steps or 20000, a.avg)
-    elif a.which == "c4":
-        shape = tuple(int(x) for x in (a.shape or "384,192,192").split(","))
-        r = c4(shape, a.steps or 4000)
-    else:
-        data = os.path.join(ROOT, "lb_gb300", "data")
-        models = {"channel": os.path.join(data, "les_mlp_channel.npz"),
-                  "channel_decay": os.path.join(data, "les_mlp_channel_decay.npz")}
-        if a.model:
-            models = {"given": a.model}
-        r = c5(a.n if a.n != 64 else 128, a.steps or 200, a.interval, models)
+pytestmark = [pytest.mark.gpu, pytest.mark.slow]
+SMALL = os.environ.get("LBM_VALIDATE_SMALL") == "1"
+
+
+def _record(name, r):
+    out = os.environ.get("LBM_VALIDATE_OUT")
+    if out:
+        os.makedirs(out, exist_ok=True)
+        with open(os.path.join(out, f"validate_{name}.json"), "w") as fh:
+            json.dump(r, fh, indent=1)
     print(json.dumps(r))
 
 
-if __name__ == "__main__":
-    main()
+def test_c1_cavity(built_lib, oracle_lib):
+    r = c1(32 if SMALL else 64, 500 if SMALL else 10000)
+    _record("c1", r)
+    assert r["max_abs_du_over_ulid_gpu64_vs_oracle64"] <= 1e-12
+    assert r["max_abs_du_over_ulid_gpu32_vs_gpu64"] <= 1e-3
+
+
+def test_c3_channel_precision(built_lib):
+    shape = (128, 64, 64) if SMALL else (512, 256, 256)
+    steps, avg = (1000, 250) if SMALL else (20000, 5000)
+    r = c3(shape, steps, avg)
+    _record("c3", r)
+    for st in ("f32", "f16dev"):
+        assert r[f"{st}_nonfinite"] == 0
+    if SMALL:
+        return
+    assert r["f32_mean_velocity_rel_l2_vs_f64"] <= 1e-3
+    assert r["f16dev_mean_velocity_rel_l2_vs_f64"] <= 1e-3
+
+
+def test_c4_body(built_lib, oracle_lib):
+    shape = (192, 96, 96) if SMALL else (384, 192, 192)
+    r = c4(shape, 500 if SMALL else 4000)
+    _record("c4", r)
+    assert r["voxelizer_bit_exact"]
+    assert r["f64_nonfinite"] == 0 and r["f32_nonfinite"] == 0
+    if not SMALL:
+        assert r["drag_x_rel_diff_f32_vs_f64"] <= 1e-3
+
+
+def test_c5_learned_closure(built_lib):
+    data = os.path.join(ROOT, "lb_gb300", "data")
+    models = {"channel": os.path.join(data, "les_mlp_channel.npz"),
+              "channel_decay": os.path.join(data, "les_mlp_channel_decay.npz")}
+    r = c5(64 if SMALL else 256, 50 if SMALL else 200, 8, models)
+    _record("c5", r)
+    if SMALL:
+        return
+    post = r["a_posteriori_rel_l2_vs_filtered_fine"]
+    assert post["mlp_channel_decay"] < post["smagorinsky"]
+    assert post["mlp_channel_decay_every_8"] < post["smagorinsky"]
