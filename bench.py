@@ -181,6 +181,7 @@ def time_storage(shape, case, storage, steps, warmup, device, dist, with_clocks,
         sampler.__exit__()
     barrier(dist)
     d = s.reduce()
+    d.launches_per_step = s.step_launches()
     s.close()
     return ms, d, (sampler.summary() if sampler else None)
 
@@ -414,7 +415,7 @@ def main():
                                              (args.mlp_interval, cells / (ms16k * 1e-3) / 1e9) if ms16k else None),
             # one fused step kernel per step; the row-staged step adds the launch over the wall rows
             "collisions": colls,
-            "gpu_launches": args.steps * (2 if args.options & 1 else 1), "clocks": clk, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": args.steps * d16.launches_per_step, "clocks": clk, "cpu_baseline": cpu, "e2e": e2e,
             "check": {"f16_mass": d16.mass, "f32_mass": d32.mass,
                       "nonfinite": d16.nonfinite + d32.nonfinite + d16s.nonfinite}}
     print(json.dumps(line))

@@ -135,6 +135,10 @@ const char* lbm_config_last_error(void);
                                    body force, in expectation; reproducible: the random bits are a hash of
                                    the element and the step) */
 
+#define LBM_OPT_ONE_LAUNCH 4  /* FP32 / FP16 storage: one step launch over the whole lattice instead of the
+                                  default split (rows whose pairs all take the packed path, then the
+                                  remaining rows); identical results */
+
 /* boundary-condition records, mirroring LBMTraits.h:17-43 */
 typedef struct lbm_vertex { int32_t x, y, z; } lbm_vertex;
 
@@ -204,6 +208,10 @@ lbm_status lbm_step(lbm_ctx* ctx, int32_t nsteps);
 lbm_status lbm_synchronize(lbm_ctx* ctx);
 /* nsteps steps bracketed by CUDA events on the context's stream; *ms = elapsed device time */
 lbm_status lbm_step_timed(lbm_ctx* ctx, int32_t nsteps, double* ms);
+/* kernel launches one lbm_step step issues on this context (after initialisation): 1 or 2 (the split
+   step launches the plain rows and the remaining rows separately; a kind with no rows is not launched).
+   No reference counterpart (the reference runs one launch per hook) */
+lbm_status lbm_step_launches(const lbm_ctx* ctx, int32_t* per_step);
 
 /* ---- read-back (host copies, caller-owned) ----------------------------------- */
 /* moments of the current pre-collision state (MomentDensityVelocityN27.h:27-83) */

@@ -18,8 +18,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE]
 # extra nvcc flags for tuning experiments (e.g. LBM_NVCC_EXTRA="-DLBM_STEP2_MIN_BLOCKS=5")
 NVCC_FLAGS += os.environ.get("LBM_NVCC_EXTRA", "").split()
-UNITS = ["lbm_step_f64.cu", "lbm_step_f32.cu", "lbm_step_f16.cu", "lbm_capi.cu", "voxelizer.cu", "mlp.cu", "mesh_io.cu",
-         "mesher.cu", "vtk_io.cu", "config_io.cu"]
+STEP_UNITS = [f"lbm_step_{s}_{c}.cu" for s in ("f16", "f32", "f64") for c in ("srt", "cum15", "cum17", "comb")]
+UNITS = STEP_UNITS + ["lbm_step_f64.cu", "lbm_step_f32.cu", "lbm_step_f16.cu", "lbm_capi.cu", "voxelizer.cu", "mlp.cu",
+                      "mesh_io.cu", "mesher.cu", "vtk_io.cu", "config_io.cu"]
 
 
 def nvcc():
@@ -67,7 +68,7 @@ def build(force=False, verbose=False):
             print(r.stderr)
         return obj
 
-    with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=min(len(UNITS), max(4, os.cpu_count() or 4))) as ex:
         objs = list(ex.map(compile_one, UNITS))
     tmp = LIB + ".tmp"
     cmd = [exe] + ARCH + ["-shared", "-o", tmp] + objs

@@ -59,6 +59,7 @@ class LbmConfig(C.Structure):
 
 LBM_OPT_ROW_STAGING = 1
 LBM_OPT_F16_ROUND_NEAREST = 2
+LBM_OPT_ONE_LAUNCH = 4
 
 
 LBM_MLP_INPUTS = 7
@@ -213,6 +214,7 @@ def lib():
         "lbm_step": ([vp, i32], i32),
         "lbm_synchronize": ([vp], i32),
         "lbm_step_timed": ([vp, i32, dp], i32),
+        "lbm_step_launches": ([vp, ip], i32),
         "lbm_probe": ([vp, i32, i32, i32, dp], i32),
         "lbm_get_moments": ([vp, dp, dp], i32),
         "lbm_get_populations": ([vp, dp], i32),

@@ -23,9 +23,24 @@ struct ReadOut {
     double* f;     // 27N
     double* red;   // RED_COUNT
     double* uerr;  // 3N (error monitor's previous velocity)
+    double* part;  // READ_DIAG / READ_ERROR: per-block partial sums [RED_COUNT][blocks] (read_part_size)
     int mode;
     int ref_compat_err;  // reproduce the ErrorQuadratic z-term typo
 };
+
+// the reading kernels run one thread per x of a (y, kReadZ z-planes) column tile; the reductions keep
+// per-thread FP64 partial sums over the tile's cells, one partial per block in part[], and a second
+// kernel adds the partials in a fixed order: the result does not depend on scheduling (no atomics)
+constexpr int kReadZ = 4;
+inline dim3 read_grid(int nx, int ny, int nz) {
+    const int b = nx >= 128 ? 128 : ((nx + 31) / 32) * 32;
+    return dim3((unsigned)((nx + b - 1) / b), (unsigned)ny, (unsigned)((nz + kReadZ - 1) / kReadZ));
+}
+inline long long read_blocks(int nx, int ny, int nz) {
+    const dim3 g = read_grid(nx, ny, nz);
+    return (long long)g.x * g.y * g.z;
+}
+inline size_t read_part_size(int nx, int ny, int nz) { return (size_t)RED_COUNT * (size_t)read_blocks(nx, ny, nz); }
 
 LBM_D double warp_sum(double v) {
 #pragma unroll
@@ -38,102 +53,133 @@ LBM_D double warp_max(double v) {
     return v;
 }
 
-// one thread per cell; gathers df_m exactly as the step kernel would
+// block sum (max for RED_VMAX) of the quantities [q0, q1) in a fixed order, written as this block's
+// partial; every thread of the block calls it
+template <int Q0, int Q1>
+LBM_D void block_partials(double (&v)[RED_COUNT], double* part, long long nblk) {
+    __shared__ double sh[RED_COUNT][4];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int q = Q0; q < Q1; q++) {
+        const double s = q == RED_VMAX ? warp_max(v[q]) : warp_sum(v[q]);
+        if (lane == 0) sh[q][wid] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < Q1 - Q0) {
+        const int q = Q0 + threadIdx.x;
+        double s = sh[q][0];
+        for (int w = 1; w < nw; w++) s = q == RED_VMAX ? fmax(s, sh[q][w]) : s + sh[q][w];
+        const long long b = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
+        part[q * nblk + b] = s;
+    }
+}
+
+// one thread per x of a column tile of kReadZ cells along z; gathers df_m exactly as the step kernel
 template <class S, bool ODD>
 __global__ void __launch_bounds__(128) k_read(Params p, ReadOut o) {
     using R = typename S::R;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = x < p.nx;
-    Cell c;
-    make_cell(p, live ? x : 0, blockIdx.y, blockIdx.z, c);
-    const uint8_t fl = live ? p.cls[c.idx] : (uint8_t)0;
-    const int cl = fl & CLS_MASK;
-    R f[27];
-    R drag[3] = {0, 0, 0};
-    if (!live || cl == CLS_SOLID) {
+    double v[RED_COUNT];
 #pragma unroll
-        for (int v = 0; v < 27; v++) f[v] = (R)0;
-    } else if (cl == CLS_INLET) {
-        inlet_state<S>(p, c, f);
-    } else {
-        gather<S, ODD, true>(p, c, cl, f, drag);
-    }
-    R rho = 0, jx = 0, jy = 0, jz = 0, ux = 0, uy = 0, uz = 0;
-    if (live && cl != CLS_SOLID) moments(f, p, rho, jx, jy, jz, ux, uy, uz);
-    if (live && (o.mode & READ_MOMENTS)) {
-        o.rho[c.idx] = rho;
-        o.u[c.idx] = ux; o.u[p.N + c.idx] = uy; o.u[2 * p.N + c.idx] = uz;
-    }
-    if (live && (o.mode & READ_POPS)) {
+    for (int q = 0; q < RED_COUNT; q++) v[q] = 0.0;
+    long long nfluid = 0, nbad = 0;
+    for (int k = 0; k < kReadZ; k++) {
+        const int z = blockIdx.z * kReadZ + k;
+        if (z >= p.nz) break;
+        Cell c;
+        make_cell(p, live ? x : 0, blockIdx.y, z, c);
+        const uint8_t fl = live ? p.cls[c.idx] : (uint8_t)0;
+        const int cl = fl & CLS_MASK;
+        R f[27];
+        R drag[3] = {0, 0, 0};
+        if (!live || cl == CLS_SOLID) {
 #pragma unroll
-        for (int v = 0; v < 27; v++) o.f[v * p.N + c.idx] = f[v];
-    }
-    if (live && (o.mode & READ_ACC) && cl != CLS_SOLID) {
-        double* a = p.acc;
-        const long long N = p.N;
-        a[c.idx] += rho; a[N + c.idx] += ux; a[2 * N + c.idx] += uy; a[3 * N + c.idx] += uz;
-        a[4 * N + c.idx] += (double)ux * ux; a[5 * N + c.idx] += (double)uy * uy; a[6 * N + c.idx] += (double)uz * uz;
-        a[7 * N + c.idx] += (double)ux * uy; a[8 * N + c.idx] += (double)ux * uz; a[9 * N + c.idx] += (double)uy * uz;
-    }
-    if (o.mode & READ_DIAG) {
-        const bool tgt = live && (cl == CLS_BULK || cl == CLS_EDGE || cl == CLS_OUTLET || cl == CLS_SYM);
-        double v[RED_COUNT] = {0};
-        if (tgt) {
+            for (int q = 0; q < 27; q++) f[q] = (R)0;
+        } else if (cl == CLS_INLET) {
+            inlet_state<S>(p, c, f);
+        } else {
+            gather<S, ODD, true>(p, c, cl, f, drag);
+        }
+        R rho = 0, jx = 0, jy = 0, jz = 0, ux = 0, uy = 0, uz = 0;
+        if (live && cl != CLS_SOLID) moments(f, p, rho, jx, jy, jz, ux, uy, uz);
+        if (live && (o.mode & READ_MOMENTS)) {
+            o.rho[c.idx] = rho;
+            o.u[c.idx] = ux; o.u[p.N + c.idx] = uy; o.u[2 * p.N + c.idx] = uz;
+        }
+        if (live && (o.mode & READ_POPS)) {
+#pragma unroll
+            for (int q = 0; q < 27; q++) o.f[q * p.N + c.idx] = f[q];
+        }
+        if (live && (o.mode & READ_ACC) && cl != CLS_SOLID) {
+            double* a = p.acc;
+            const long long N = p.N;
+            a[c.idx] += rho; a[N + c.idx] += ux; a[2 * N + c.idx] += uy; a[3 * N + c.idx] += uz;
+            a[4 * N + c.idx] += (double)ux * ux; a[5 * N + c.idx] += (double)uy * uy; a[6 * N + c.idx] += (double)uz * uz;
+            a[7 * N + c.idx] += (double)ux * uy; a[8 * N + c.idx] += (double)ux * uz; a[9 * N + c.idx] += (double)uy * uz;
+        }
+        if ((o.mode & READ_DIAG) && live && (cl == CLS_BULK || cl == CLS_EDGE || cl == CLS_OUTLET || cl == CLS_SYM)) {
             bool ok = true;
 #pragma unroll
             for (int q = 0; q < 27; q++) ok = ok && isfinite((double)f[q]);
-            v[RED_MASS] = rho;
-            v[RED_MX] = (double)rho * ux; v[RED_MY] = (double)rho * uy; v[RED_MZ] = (double)rho * uz;
-            v[RED_DX] = drag[0]; v[RED_DY] = drag[1]; v[RED_DZ] = drag[2];
-            v[RED_VMAX] = sqrt((double)ux * ux + (double)uy * uy + (double)uz * uz);
-            if (!isfinite(v[RED_VMAX])) v[RED_VMAX] = 0;
-            v[RED_BAD] = ok ? 0.0 : 1.0;
-            v[RED_FLUID] = 1.0;
+            v[RED_MASS] += rho;
+            v[RED_MX] += (double)rho * ux; v[RED_MY] += (double)rho * uy; v[RED_MZ] += (double)rho * uz;
+            if (cl != CLS_BULK) {  // only cells beside a solid have momentum-exchange links
+                v[RED_DX] += drag[0]; v[RED_DY] += drag[1]; v[RED_DZ] += drag[2];
+            }
+            const R u2 = ux * ux + uy * uy + uz * uz;
+            if (isfinite((double)u2)) v[RED_VMAX] = fmax(v[RED_VMAX], (double)u2);
+            nbad += ok ? 0 : 1;
+            nfluid += 1;
         }
-        __shared__ double sh[RED_COUNT][4];
-        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-        for (int q = 0; q < RED_COUNT; q++) {
-            if (q == RED_ERR1 || q == RED_ERR2) continue;
-            double s = q == RED_VMAX ? warp_max(v[q]) : warp_sum(v[q]);
-            if (lane == 0) sh[q][wid] = s;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            for (int q = 0; q < RED_COUNT; q++) {
-                if (q == RED_ERR1 || q == RED_ERR2) continue;
-                double s = sh[q][0];
-                for (int w = 1; w < nw; w++) s = q == RED_VMAX ? fmax(s, sh[q][w]) : s + sh[q][w];
-                if (q == RED_VMAX) {
-                    // non-negative doubles order like their bit patterns
-                    atomicMax((unsigned long long*)&o.red[q], (unsigned long long)__double_as_longlong(s));
-                } else if (s != 0.0) {
-                    atomicAdd(&o.red[q], s);
-                }
+        if (o.mode & READ_ERROR) {
+            // ErrorQuadratic.h:33-78: sum sqrt|u - u_prev|^2 and sqrt|u|^2 over flag == 1 cells
+            if (live && (fl & BIT_REFBULK)) {
+                const R px = (R)o.uerr[c.idx], py = (R)o.uerr[p.N + c.idx], pz = (R)o.uerr[2 * p.N + c.idx];
+                const R dx = ux - px, dy = uy - py;
+                const R dz = o.ref_compat_err ? uy - pz : uz - pz;
+                const R a1 = dx * dx + dy * dy + dz * dz;
+                const R a2 = ux * ux + uy * uy + uz * uz;
+                v[RED_ERR1] += (double)sqrt(a1);
+                v[RED_ERR2] += (double)sqrt(a2);
+            }
+            if (live) {  // copy u -> u_error (:80-90), every cell
+                o.uerr[c.idx] = ux; o.uerr[p.N + c.idx] = uy; o.uerr[2 * p.N + c.idx] = uz;
             }
         }
     }
+    const long long nblk = (long long)gridDim.x * gridDim.y * gridDim.z;
+    if (o.mode & READ_DIAG) {
+        v[RED_BAD] = (double)nbad;
+        v[RED_FLUID] = (double)nfluid;
+        block_partials<RED_MASS, RED_ERR1>(v, o.part, nblk);
+    }
     if (o.mode & READ_ERROR) {
-        // ErrorQuadratic.h:33-78: sum sqrt|u - u_prev|^2 and sqrt|u|^2 over flag == 1 cells
-        double e1 = 0, e2 = 0;
-        if (live && (fl & BIT_REFBULK)) {
-            const R px = (R)o.uerr[c.idx], py = (R)o.uerr[p.N + c.idx], pz = (R)o.uerr[2 * p.N + c.idx];
-            const R dx = ux - px, dy = uy - py;
-            const R dz = o.ref_compat_err ? uy - pz : uz - pz;
-            const R a1 = dx * dx + dy * dy + dz * dz;
-            const R a2 = ux * ux + uy * uy + uz * uz;
-            e1 = (double)sqrt(a1);
-            e2 = (double)sqrt(a2);
+        if (o.mode & READ_DIAG) __syncthreads();
+        block_partials<RED_ERR1, RED_COUNT>(v, o.part, nblk);
+    }
+}
+
+// the partials of k_read added in a fixed order (per quantity: a strided pass per thread, then a tree
+// over the block's threads); RED_VMAX is the square root of the largest |u|^2
+constexpr int kFinalThreads = 512;
+template <class S>
+__global__ void __launch_bounds__(kFinalThreads) k_read_final(const double* part, long long nblk, int q0, int q1,
+                                                              double* red) {
+    __shared__ double sh[kFinalThreads];
+    for (int q = q0; q < q1; q++) {
+        const bool mx = q == RED_VMAX;
+        double s = 0.0;
+        for (long long b = threadIdx.x; b < nblk; b += kFinalThreads)
+            s = mx ? fmax(s, part[q * nblk + b]) : s + part[q * nblk + b];
+        sh[threadIdx.x] = s;
+        __syncthreads();
+        for (int w = kFinalThreads / 2; w > 0; w >>= 1) {
+            if (threadIdx.x < w) sh[threadIdx.x] = mx ? fmax(sh[threadIdx.x], sh[threadIdx.x + w]) : sh[threadIdx.x] + sh[threadIdx.x + w];
+            __syncthreads();
         }
-        if (live) {  // copy u -> u_error (:308-318), every cell
-            o.uerr[c.idx] = ux; o.uerr[p.N + c.idx] = uy; o.uerr[2 * p.N + c.idx] = uz;
-        }
-        e1 = warp_sum(e1);
-        e2 = warp_sum(e2);
-        if ((threadIdx.x & 31) == 0) {
-            if (e1 != 0.0) atomicAdd(&o.red[RED_ERR1], e1);
-            if (e2 != 0.0) atomicAdd(&o.red[RED_ERR2], e2);
-        }
+        if (threadIdx.x == 0) red[q] = mx ? sqrt(sh[0]) : sh[0];
+        __syncthreads();
     }
 }
 

@@ -16,7 +16,10 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
+#include <atomic>
 #include <string>
+#include <thread>
 #include <vector>
 
 using namespace lbm;
@@ -64,11 +67,16 @@ struct lbm_ctx {
     long long avg_begin = 0, avg_last = -1, avg_count = 0;
     double* d_uerr = nullptr;
     double* d_red = nullptr;
+    double* d_part = nullptr;  // per-block partial sums of the reductions (read_part_size doubles)
     double *d_rho_out = nullptr, *d_u_out = nullptr, *d_f_out = nullptr;
     double* d_probe = nullptr;
     int32_t* d_bulk_rows = nullptr;   // (y,z) rows whose cells are all bulk fluid
     int32_t* d_other_rows = nullptr;  // the remaining rows
     int n_bulk_rows = 0, n_other_rows = 0;
+    int32_t* d_plain_rows = nullptr;  // split step: rows whose pairs all take the packed path
+    int32_t* d_rest_rows = nullptr;   // split step: the remaining rows
+    int n_plain_rows = 0, n_rest_rows = 0;
+    bool split_ok = false;            // the step runs split by rows (FP32 / FP16 storage)
     int* d_err = nullptr;             // device error word
     bool rows_ok = false;             // the row-staged step applies to this lattice
     uint4* d_mlp_frag = nullptr;      // learned closure: fragment table
@@ -101,6 +109,19 @@ static lbm_status fail(lbm_ctx* c, lbm_status s, const char* fmt, ...) {
 
 static void dfree(void* p) { if (p) cudaFree(p); }
 
+// runs f(begin, end) over [0, n) split into contiguous chunks on the host cores (set-up loops over
+// the cells); each chunk writes only its own range
+template <class F>
+static void host_parallel(long long n, F&& f) {
+    const unsigned hw = std::thread::hardware_concurrency();
+    const long long nth = std::min<long long>(std::max(1u, std::min(hw, 32u)), std::max(1LL, n / 65536));
+    if (nth <= 1) { f(0LL, n); return; }
+    std::vector<std::thread> th;
+    for (long long t = 0; t < nth; t++)
+        th.emplace_back([&, t] { f(n * t / nth, n * (t + 1) / nth); });
+    for (auto& x : th) x.join();
+}
+
 static size_t real_size(const lbm_ctx* c) { return c->cfg.storage == LBM_STORAGE_F64 ? 8 : 4; }
 
 static Params make_params(const lbm_ctx* c) {
@@ -123,8 +144,10 @@ static Params make_params(const lbm_ctx* c) {
     p.has_force = (p.F[0] != 0.0 || p.F[1] != 0.0 || p.F[2] != 0.0) ? 1 : 0;
     p.rho0 = (float)c->cfg.rho0;
     p.f16_sr = (c->cfg.storage == LBM_STORAGE_F16DEV && !(c->cfg.options & LBM_OPT_F16_ROUND_NEAREST)) ? 1 : 0;
-    p.lcg_a = p.f16_sr ? kLcgA : 0u;
-    p.lcg_c = p.f16_sr ? kLcgC : kHalfStep2x;
+    p.lcg_a = kLcgA;
+    p.lcg_c = kLcgC;
+    p.sr_mix = p.f16_sr ? kSrMix : 0u;
+    p.sr_add = p.f16_sr ? 0u : kHalfStep2x;
     p.scale = std::ldexp(1.0f, c->cfg.f16_scale_log2);
     p.inv_scale = std::ldexp(1.0f, -c->cfg.f16_scale_log2);
     p.scale2 = make_float2(p.scale, p.scale);
@@ -172,10 +195,14 @@ static cudaError_t do_step(lbm_ctx* c, const Params& p) {
         c->cfg.storage == LBM_STORAGE_F16DEV)
         return launch_step_rows<StF16>(p, c->cfg.closure, c->d_bulk_rows, c->n_bulk_rows, c->d_other_rows,
                                        c->n_other_rows, c->st);
+    RowLists rl;
+    rl.plain = c->d_plain_rows; rl.n_plain = c->n_plain_rows;
+    rl.other = c->d_rest_rows; rl.n_other = c->n_rest_rows;
+    const RowLists* r = c->split_ok ? &rl : nullptr;
     switch (c->cfg.storage) {
-        case LBM_STORAGE_F64: return launch_step<StF64>(p, c->cfg.collision, c->cfg.closure, c->st);
-        case LBM_STORAGE_F32: return launch_step<StF32>(p, c->cfg.collision, c->cfg.closure, c->st);
-        default: return launch_step<StF16>(p, c->cfg.collision, c->cfg.closure, c->st);
+        case LBM_STORAGE_F64: return launch_step<StF64>(p, c->cfg.collision, c->cfg.closure, nullptr, c->st);
+        case LBM_STORAGE_F32: return launch_step<StF32>(p, c->cfg.collision, c->cfg.closure, r, c->st);
+        default: return launch_step<StF16>(p, c->cfg.collision, c->cfg.closure, r, c->st);
     }
 }
 static cudaError_t do_read(lbm_ctx* c, const Params& p, const ReadOut& o) {
@@ -297,9 +324,9 @@ lbm_status lbm_destroy(lbm_ctx* c) {
     if (c->st) cudaStreamSynchronize(c->st);
     dfree(c->d_f); dfree(c->d_cls); dfree(c->d_aux);
     free_side(c);
-    dfree(c->d_acc); dfree(c->d_uerr); dfree(c->d_red);
+    dfree(c->d_acc); dfree(c->d_uerr); dfree(c->d_red); dfree(c->d_part);
     dfree(c->d_rho_out); dfree(c->d_u_out); dfree(c->d_f_out); dfree(c->d_probe);
-    dfree(c->d_bulk_rows); dfree(c->d_other_rows); dfree(c->d_err); dfree(c->d_mlp_frag); dfree(c->d_nut);
+    dfree(c->d_bulk_rows); dfree(c->d_other_rows); dfree(c->d_plain_rows); dfree(c->d_rest_rows); dfree(c->d_err); dfree(c->d_mlp_frag); dfree(c->d_nut);
     if (c->st) cudaStreamDestroy(c->st);
     delete c;
     return LBM_OK;
@@ -360,16 +387,34 @@ static lbm_status build_geometry(lbm_ctx* c) {
         if (is_sym[id(i, j, k)]) return fail(c, LBM_ERR_INVALID, "two symmetry records for (%d,%d,%d)", i, j, k);
         is_sym[id(i, j, k)] = 1;
     }
+    // class byte of every cell, in contiguous chunks on the host cores (per-chunk counts and the first
+    // bad cell, combined afterwards)
     long long n_flag1 = 0, n_flag2 = 0;  // cells of flag -1 and -2 (each needs one record)
-    for (long long q = 0; q < N; q++) {
-        int32_t f = c->flags[q];
-        uint8_t k;
-        if (f == 0) k = CLS_SOLID;
-        else if (f == -1) { k = lid_kind ? CLS_LID : CLS_INLET; n_flag1++; }
-        else if (f == -2) { k = (!is_sym.empty() && is_sym[q]) ? CLS_SYM : CLS_OUTLET; n_flag2++; }
-        else if (f > 0 || f == -3) k = CLS_BULK;
-        else return fail(c, LBM_ERR_INVALID, "flag %d at cell %lld is not in the reference encoding", f, q);
-        cls[q] = k | (f == 1 ? BIT_REFBULK : 0);
+    {
+        struct Part { long long n1 = 0, n2 = 0, bad = -1; };
+        std::vector<Part> parts(64);
+        std::atomic<int> next{0};
+        host_parallel(N, [&](long long q0, long long q1) {
+            Part& pt = parts[(size_t)next.fetch_add(1)];
+            for (long long q = q0; q < q1; q++) {
+                const int32_t f = c->flags[q];
+                uint8_t k;
+                if (f == 0) k = CLS_SOLID;
+                else if (f == -1) { k = lid_kind ? CLS_LID : CLS_INLET; pt.n1++; }
+                else if (f == -2) { k = (!is_sym.empty() && is_sym[q]) ? CLS_SYM : CLS_OUTLET; pt.n2++; }
+                else if (f > 0 || f == -3) k = CLS_BULK;
+                else { if (pt.bad < 0) pt.bad = q; k = CLS_SOLID; }
+                cls[q] = k | (f == 1 ? BIT_REFBULK : 0);
+            }
+        });
+        long long bad = -1;
+        for (const Part& pt : parts) {
+            n_flag1 += pt.n1;
+            n_flag2 += pt.n2;
+            if (pt.bad >= 0 && (bad < 0 || pt.bad < bad)) bad = pt.bad;
+        }
+        if (bad >= 0)
+            return fail(c, LBM_ERR_INVALID, "flag %d at cell %lld is not in the reference encoding", c->flags[bad], bad);
     }
     // -1 records
     std::vector<float> lid_n, lid_u, in_u;
@@ -510,21 +555,26 @@ static lbm_status build_geometry(lbm_ctx* c) {
         }
     }
     // BULK/EDGE split: fluid cells next to a solid, moving-wall or inlet node stream through
-    // per-link rules (visit the 26-neighbourhood of those nodes only)
-    for (long long q = 0; q < N; q++) {
-        int k = cls[q] & CLS_MASK;
-        if (k != CLS_SOLID && k != CLS_LID && k != CLS_INLET) continue;
-        int i = (int)(q % nx), j = (int)((q / nx) % ny), kk = (int)(q / ((long long)nx * ny));
-        for (int dz = -1; dz <= 1; dz++)
-            for (int dy = -1; dy <= 1; dy++)
-                for (int dx = -1; dx <= 1; dx++) {
-                    bool ok = true;
-                    int a = wrapc(i + dx, nx, 0, ok), b = wrapc(j + dy, ny, 1, ok), e = wrapc(kk + dz, nz, 2, ok);
-                    if (!ok) continue;
-                    long long r = id(a, b, e);
-                    if ((cls[r] & CLS_MASK) == CLS_BULK) cls[r] = (uint8_t)((cls[r] & ~CLS_MASK) | CLS_EDGE);
-                }
-    }
+    // per-link rules (visit the 26-neighbourhood of those nodes only).  Chunks of cells on the host
+    // cores; a neighbour byte may be marked by two chunks, always from BULK to EDGE with its role bits
+    // kept, so the byte accesses are relaxed atomics and the result does not depend on the order
+    host_parallel(N, [&](long long q0, long long q1) {
+        for (long long q = q0; q < q1; q++) {
+            int k = __atomic_load_n(&cls[q], __ATOMIC_RELAXED) & CLS_MASK;
+            if (k != CLS_SOLID && k != CLS_LID && k != CLS_INLET) continue;
+            int i = (int)(q % nx), j = (int)((q / nx) % ny), kk = (int)(q / ((long long)nx * ny));
+            for (int dz = -1; dz <= 1; dz++)
+                for (int dy = -1; dy <= 1; dy++)
+                    for (int dx = -1; dx <= 1; dx++) {
+                        bool ok = true;
+                        int a = wrapc(i + dx, nx, 0, ok), b = wrapc(j + dy, ny, 1, ok), e = wrapc(kk + dz, nz, 2, ok);
+                        if (!ok) continue;
+                        uint8_t* cr = &cls[(size_t)id(a, b, e)];
+                        const uint8_t v = __atomic_load_n(cr, __ATOMIC_RELAXED);
+                        if ((v & CLS_MASK) == CLS_BULK) __atomic_store_n(cr, (uint8_t)((v & ~CLS_MASK) | CLS_EDGE), __ATOMIC_RELAXED);
+                    }
+        }
+    });
     // stream targets on a face of a non-periodic axis would stream from outside the lattice;
     // outlets may only do so on their interpolated links, and must not touch solid cells
     auto check_links = [&](long long q) -> lbm_status {
@@ -663,6 +713,42 @@ static lbm_status build_geometry(lbm_ctx* c) {
             }
         }
     }
+    // the step split by rows (FP32 and FP16-deviation storage): plain rows are off the periodic y/z seams
+    // with every cell a bulk fluid cell of the packed path (the combined collision packs reference-flag-1
+    // cells only); nx even.  LBM_OPT_ONE_LAUNCH keeps one launch over the lattice.
+    {
+        const long long nrow = (long long)ny * nz;
+        const bool comb = c->cfg.collision == LBM_COLLISION_CUMULANT_COMBINED;
+        const uint8_t keep = comb ? (uint8_t)0xff : (uint8_t)~BIT_REFBULK;
+        const uint8_t want = comb ? (uint8_t)(CLS_BULK | BIT_REFBULK) : (uint8_t)CLS_BULK;
+        c->split_ok = c->cfg.storage != LBM_STORAGE_F64 && !(c->cfg.options & LBM_OPT_ONE_LAUNCH) && nrow < (1LL << 31);
+        std::vector<uint8_t> plain(c->split_ok ? (size_t)nrow : 0, 0);
+        if (c->split_ok && !(nx & 1)) {
+            host_parallel(nrow, [&](long long r0, long long r1) {
+                for (long long r = r0; r < r1; r++) {
+                    const int y = (int)(r % ny), z = (int)(r / ny);
+                    if ((wrap[1] && (y == 0 || y == ny - 1)) || (wrap[2] && (z == 0 || z == nz - 1))) continue;
+                    bool all = true;
+                    for (int i = 0; i < nx && all; i++) all = (cls[(size_t)(r * nx + i)] & keep) == want;
+                    plain[(size_t)r] = all ? 1 : 0;
+                }
+            });
+        }
+        std::vector<int32_t> pr, rr;
+        for (long long r = 0; r < (long long)plain.size(); r++) (plain[(size_t)r] ? pr : rr).push_back((int32_t)r);
+        dfree(c->d_plain_rows); dfree(c->d_rest_rows);
+        c->d_plain_rows = c->d_rest_rows = nullptr;
+        c->n_plain_rows = (int)pr.size();
+        c->n_rest_rows = (int)rr.size();
+        if (c->split_ok && !pr.empty()) {
+            CU(c, cudaMalloc(&c->d_plain_rows, pr.size() * 4));
+            CU(c, cudaMemcpy(c->d_plain_rows, pr.data(), pr.size() * 4, cudaMemcpyHostToDevice));
+        }
+        if (c->split_ok && !rr.empty()) {
+            CU(c, cudaMalloc(&c->d_rest_rows, rr.size() * 4));
+            CU(c, cudaMemcpy(c->d_rest_rows, rr.data(), rr.size() * 4, cudaMemcpyHostToDevice));
+        }
+    }
     c->have_geom = true;
     return LBM_OK;
 }
@@ -765,6 +851,18 @@ lbm_status lbm_step_timed(lbm_ctx* c, int32_t n, double* ms) {
     return LBM_OK;
 }
 
+lbm_status lbm_step_launches(const lbm_ctx* c, int32_t* per_step) {
+    if (!c || !per_step) return fail(nullptr, LBM_ERR_INVALID, "lbm_step_launches: null argument");
+    if (!c->initialized) return fail(nullptr, LBM_ERR_STATE, "lbm_step_launches before initialisation");
+    if (c->rows_ok && c->cfg.collision == LBM_COLLISION_CUMULANT2015 && c->cfg.storage == LBM_STORAGE_F16DEV)
+        *per_step = (c->n_bulk_rows > 0 ? 1 : 0) + (c->n_other_rows > 0 ? 1 : 0);
+    else if (c->split_ok)
+        *per_step = (c->n_plain_rows > 0 ? 1 : 0) + (c->n_rest_rows > 0 ? 1 : 0);
+    else
+        *per_step = 1;
+    return LBM_OK;
+}
+
 lbm_status lbm_probe(lbm_ctx* c, int32_t x, int32_t y, int32_t z, double out[4]) {
     if (!c || !out) return fail(c, LBM_ERR_INVALID, "lbm_probe: null argument");
     if (x < 0 || y < 0 || z < 0 || x >= c->cfg.nx || y >= c->cfg.ny || z >= c->cfg.nz)
@@ -852,9 +950,9 @@ lbm_status lbm_reduce(lbm_ctx* c, lbm_diag* out) {
     if (!c || !out) return fail(c, LBM_ERR_INVALID, "lbm_reduce: null argument");
     if (!c->initialized) return fail(c, LBM_ERR_STATE, "lbm_reduce before initialisation");
     cudaSetDevice(c->cfg.device);
-    CU(c, cudaMemsetAsync(c->d_red, 0, RED_COUNT * sizeof(double), c->st));
+    if (!c->d_part) CU(c, cudaMalloc(&c->d_part, read_part_size(c->cfg.nx, c->cfg.ny, c->cfg.nz) * sizeof(double)));
     ReadOut o{};
-    o.red = c->d_red; o.mode = READ_DIAG;
+    o.red = c->d_red; o.part = c->d_part; o.mode = READ_DIAG;
     lbm_status s = run_read(c, o);
     if (s) return s;
     double h[RED_COUNT];
@@ -883,9 +981,9 @@ lbm_status lbm_error_evaluation(lbm_ctx* c, double* err) {
         CU(c, cudaMalloc(&c->d_uerr, 3 * N * 8));
         CU(c, cudaMemsetAsync(c->d_uerr, 0, 3 * N * 8, c->st));
     }
-    CU(c, cudaMemsetAsync(c->d_red, 0, RED_COUNT * sizeof(double), c->st));
+    if (!c->d_part) CU(c, cudaMalloc(&c->d_part, read_part_size(c->cfg.nx, c->cfg.ny, c->cfg.nz) * sizeof(double)));
     ReadOut o{};
-    o.red = c->d_red; o.uerr = c->d_uerr; o.mode = READ_ERROR;
+    o.red = c->d_red; o.part = c->d_part; o.uerr = c->d_uerr; o.mode = READ_ERROR;
     lbm_status s = run_read(c, o);
     if (s) return s;
     double h[RED_COUNT];

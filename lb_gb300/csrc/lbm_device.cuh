@@ -80,8 +80,8 @@ struct Params {
     int f16_sr;              // FP16 stores round stochastically (else to nearest)
     uint32_t sr_step_seed;   // step_seed(m)
     float raw_rho, raw_mdiag;  // sum_v w_v rho0 and sum_v w_v rho0 c_vx^2 of the FP16 codec's references
-    uint32_t lcg_a, lcg_c;   // the packed path's dither stream s -> a s + c: the LCG below when rounding
-                             // stochastically, a = 0 and c = the fixed half-step dither when to nearest
+    uint32_t lcg_a, lcg_c;   // the packed path's random stream s -> a s + c (the LCG below)
+    uint32_t sr_mix, sr_add; // packed FP16 stores: rbits = hi(s sr_mix) + sr_add (half2_sr)
     float wr[27];            // w_v rho0            (decode f = h 2^-s + w_v rho0)
     float nwrs[27];          // -w_v rho0 2^s       (encode h = f 2^s - w_v rho0 2^s)
     float2 wr2[27], nwrs2[27];  // the same as (x, x) pairs for the packed two-cell path
@@ -157,8 +157,7 @@ LBM_D uint32_t sr_seed(unsigned long long e, int m) {
 LBM_HD uint32_t step_seed(int m) { return mix32((uint32_t)m * 0x9E3779B9u); }
 LBM_D uint32_t sr_seed_pair(uint32_t e, const Params& p) { return mix32(e ^ p.sr_step_seed); }
 // next 32 random bits of a per-thread stream (32-bit LCG of Numerical Recipes, a = 1664525,
-// c = 1013904223; the high bits are used); a and c come from the parameters, so rounding to nearest
-// (a = 0, c = kHalfStep2x) takes the same instructions without a select
+// c = 1013904223)
 constexpr uint32_t kLcgA = 1664525u, kLcgC = 1013904223u;
 LBM_D uint32_t lcg_next(uint32_t& s, const Params& p) {
     s = s * p.lcg_a + p.lcg_c;
@@ -166,14 +165,20 @@ LBM_D uint32_t lcg_next(uint32_t& s, const Params& p) {
 }
 LBM_D __half half_sr(float v, uint32_t r13) { return __float2half_rz(__uint_as_float(__float_as_uint(v) + r13)); }
 // the same dither with a fixed half step instead of random bits rounds to nearest (ties away from zero)
-constexpr uint32_t kHalfStep13 = 0x1000u;                        // for half_sr
-constexpr uint32_t kHalfStep2x = (0x1000u << 19) | (0x1000u << 6);  // for half2_sr
-// two values from one 32-bit random: bits 19..31 for .x, bits 6..18 for .y
-LBM_D __half2 half2_sr(float2 v, uint32_t r) {
-    const float a = __uint_as_float(__float_as_uint(v.x) + (r >> 19));
-    const float b = __uint_as_float(__float_as_uint(v.y) + ((r >> 6) & 0x1FFFu));
+constexpr uint32_t kHalfStep13 = 0x1000u;  // for half_sr
+// Packed stores: cvt.rs.f16x2.f32 (sm_100 family) rounds both values stochastically in one instruction,
+// adding the 13-bit fields rbits[28:16] (upper half) and rbits[12:0] (lower half) below the FP16
+// mantissa of the FP32 patterns and truncating: the method of half_sr (the field layout was measured
+// on a GB300 against a software model, bit for bit on 65,536 inputs).  The LCG state's low bits are
+// weak (bit k has period 2^(k+1)), so rbits is the high word of the state times an odd constant,
+// rbits = hi(s * sr_mix) + sr_add: sr_mix = kSrMix, sr_add = 0 when rounding stochastically; sr_mix = 0,
+// sr_add = kHalfStep2x (a half step in both fields) rounds to nearest with the same instructions.
+constexpr uint32_t kSrMix = 0x9E3779B1u;
+constexpr uint32_t kHalfStep2x = (0x1000u << 16) | 0x1000u;
+LBM_D __half2 half2_sr(float2 v, uint32_t s, const Params& p) {
+    const uint32_t r = __umulhi(s, p.sr_mix) + p.sr_add;
     uint32_t h;
-    asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(h) : "f"(b), "f"(a));  // high half b, low half a
+    asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(h) : "f"(v.y), "f"(v.x), "r"(r));  // upper v.y, lower v.x
     return *reinterpret_cast<__half2*>(&h);
 }
 

@@ -9,49 +9,77 @@
 
 namespace lbm {
 
+using RowKernel = void (*)(Params, const int32_t*);
+
+// the learned-closure kernel for this step's parity and network mode (p.nut == nullptr: the network
+// runs every step; else p.mlp_run says whether it runs in this step)
+template <class S, int COLL, int ROWS>
+static RowKernel mlp_kernel(const Params& p) {
+    const bool odd = (p.m & 1) != 0;
+    if (!p.nut) return odd ? k_step2_mlp<S, COLL, true, 0, ROWS> : k_step2_mlp<S, COLL, false, 0, ROWS>;
+    if (p.mlp_run) return odd ? k_step2_mlp<S, COLL, true, 1, ROWS> : k_step2_mlp<S, COLL, false, 1, ROWS>;
+    return odd ? k_step2_mlp<S, COLL, true, 2, ROWS> : k_step2_mlp<S, COLL, false, 2, ROWS>;
+}
+
 template <class S, int COLL, int CLOS>
-static cudaError_t step_parity(const Params& p, cudaStream_t st) {
+static cudaError_t step_parity(const Params& p, const RowLists* rl, cudaStream_t st) {
+    const bool odd = (p.m & 1) != 0;
     if constexpr (S::kind == 0) {
         dim3 g = cell_grid(p.nx, p.ny, p.nz), b = cell_block(p.nx);
-        if (p.m & 1) k_step<S, COLL, CLOS, true><<<g, b, 0, st>>>(p);
-        else         k_step<S, COLL, CLOS, false><<<g, b, 0, st>>>(p);
+        if (odd) k_step<S, COLL, CLOS, true><<<g, b, 0, st>>>(p);
+        else     k_step<S, COLL, CLOS, false><<<g, b, 0, st>>>(p);
+    } else if (rl) {
+        // split step: the plain rows, then the remaining rows (one thread per x-pair)
+        const int half = (p.nx + 1) / 2;
+        const dim3 b = cell_block(half);
+        const unsigned xb = (unsigned)((half + (int)b.x - 1) / (int)b.x);
+        RowKernel kp, ko;
+        if constexpr (CLOS == 2) {
+            kp = mlp_kernel<S, COLL, 1>(p);
+            ko = mlp_kernel<S, COLL, 2>(p);
+        } else {
+            kp = odd ? k_step2_plain<S, COLL, CLOS, true> : k_step2_plain<S, COLL, CLOS, false>;
+            ko = odd ? k_step2_list<S, COLL, CLOS, true> : k_step2_list<S, COLL, CLOS, false>;
+        }
+        if (rl->n_plain > 0) {
+            kp<<<dim3((unsigned)rl->n_plain, xb), b, 0, st>>>(p, rl->plain);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+        }
+        if (rl->n_other > 0) ko<<<dim3((unsigned)rl->n_other, xb), b, 0, st>>>(p, rl->other);
     } else {
         const int half = (p.nx + 1) / 2;  // one thread per x-pair
         dim3 g = cell_grid(half, p.ny, p.nz), b = cell_block(half);
         if constexpr (CLOS == 2) {
-            // p.nut == nullptr: network every step; else mlp_run says whether it runs in this step
-            if (!p.nut) {
-                if (p.m & 1) k_step2_mlp<S, COLL, true, 0><<<g, b, 0, st>>>(p);
-                else         k_step2_mlp<S, COLL, false, 0><<<g, b, 0, st>>>(p);
-            } else if (p.mlp_run) {
-                if (p.m & 1) k_step2_mlp<S, COLL, true, 1><<<g, b, 0, st>>>(p);
-                else         k_step2_mlp<S, COLL, false, 1><<<g, b, 0, st>>>(p);
-            } else {
-                if (p.m & 1) k_step2_mlp<S, COLL, true, 2><<<g, b, 0, st>>>(p);
-                else         k_step2_mlp<S, COLL, false, 2><<<g, b, 0, st>>>(p);
-            }
+            mlp_kernel<S, COLL, 0>(p)<<<g, b, 0, st>>>(p, nullptr);
         } else {
-            if (p.m & 1) k_step2<S, COLL, CLOS, true><<<g, b, 0, st>>>(p);
-            else         k_step2<S, COLL, CLOS, false><<<g, b, 0, st>>>(p);
+            if (odd) k_step2<S, COLL, CLOS, true><<<g, b, 0, st>>>(p);
+            else     k_step2<S, COLL, CLOS, false><<<g, b, 0, st>>>(p);
         }
     }
     return cudaGetLastError();
 }
 
-// closure 2 (learned) runs on the packed path only: FP32 and FP16-deviation storage
-template <class S>
-cudaError_t launch_step(const Params& p, int collision, int closure, cudaStream_t st) {
+// one collision's step (instantiated per storage and collision in lbm_step_<storage>_<collision>.cu, so
+// the step kernels compile in parallel); closure 2 (learned) runs on the packed path only (FP32 and
+// FP16-deviation storage, SRT or cumulant-2015)
+template <class S, int COLL>
+cudaError_t launch_step_coll(const Params& p, int closure, const RowLists* rl, cudaStream_t st) {
     if (closure == 2) {
-        if constexpr (S::kind == 0) return cudaErrorInvalidValue;
-        else {
-            if (collision >= 2) return cudaErrorInvalidValue;  // learned closure: SRT or cumulant-2015
-            return collision == 0 ? step_parity<S, 0, 2>(p, st) : step_parity<S, 1, 2>(p, st);
-        }
+        if constexpr (S::kind == 0 || COLL >= 2) return cudaErrorInvalidValue;
+        else return step_parity<S, COLL, 2>(p, rl, st);
     }
-    if (collision == 0) return closure == 0 ? step_parity<S, 0, 0>(p, st) : step_parity<S, 0, 1>(p, st);
-    if (collision == 2) return closure == 0 ? step_parity<S, 2, 0>(p, st) : step_parity<S, 2, 1>(p, st);
-    if (collision == 3) return closure == 0 ? step_parity<S, 3, 0>(p, st) : step_parity<S, 3, 1>(p, st);
-    return closure == 0 ? step_parity<S, 1, 0>(p, st) : step_parity<S, 1, 1>(p, st);
+    return closure == 0 ? step_parity<S, COLL, 0>(p, rl, st) : step_parity<S, COLL, 1>(p, rl, st);
+}
+
+template <class S>
+cudaError_t launch_step(const Params& p, int collision, int closure, const RowLists* rl, cudaStream_t st) {
+    switch (collision) {
+        case 0: return launch_step_coll<S, 0>(p, closure, rl, st);
+        case 2: return launch_step_coll<S, 2>(p, closure, rl, st);
+        case 3: return launch_step_coll<S, 3>(p, closure, rl, st);
+        default: return launch_step_coll<S, 1>(p, closure, rl, st);
+    }
 }
 
 // row-staged step (cumulant collision, FP16-deviation storage); SW = shared elements per segment
@@ -115,9 +143,13 @@ cudaError_t launch_step_rows(const Params& p, int closure, const int32_t* bulk, 
 
 template <class S>
 cudaError_t launch_read(const Params& p, const ReadOut& o, cudaStream_t st) {
-    dim3 g = cell_grid(p.nx, p.ny, p.nz), b = cell_block(p.nx);
+    const dim3 g = read_grid(p.nx, p.ny, p.nz), b = cell_block(p.nx);
     if (p.m & 1) k_read<S, true><<<g, b, 0, st>>>(p, o);
     else         k_read<S, false><<<g, b, 0, st>>>(p, o);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !(o.mode & (READ_DIAG | READ_ERROR))) return e;
+    const int q0 = (o.mode & READ_DIAG) ? RED_MASS : RED_ERR1, q1 = (o.mode & READ_ERROR) ? RED_COUNT : RED_ERR1;
+    k_read_final<S><<<1, kFinalThreads, 0, st>>>(o.part, (long long)g.x * g.y * g.z, q0, q1, o.red);
     return cudaGetLastError();
 }
 
@@ -136,12 +168,20 @@ cudaError_t launch_probe(const Params& p, int x, int y, int z, double* out, cuda
     return cudaGetLastError();
 }
 
+// the launchers of one storage type except the step kernels (their collisions are compiled in their own
+// units: LBM_INSTANTIATE_COLL)
 #define LBM_INSTANTIATE(S)                                                                              \
-    template cudaError_t launch_step<S>(const Params&, int, int, cudaStream_t);                         \
+    extern template cudaError_t launch_step_coll<S, 0>(const Params&, int, const RowLists*, cudaStream_t); \
+    extern template cudaError_t launch_step_coll<S, 1>(const Params&, int, const RowLists*, cudaStream_t); \
+    extern template cudaError_t launch_step_coll<S, 2>(const Params&, int, const RowLists*, cudaStream_t); \
+    extern template cudaError_t launch_step_coll<S, 3>(const Params&, int, const RowLists*, cudaStream_t); \
+    template cudaError_t launch_step<S>(const Params&, int, int, const RowLists*, cudaStream_t);        \
     template cudaError_t launch_read<S>(const Params&, const ReadOut&, cudaStream_t);                   \
     template cudaError_t launch_init<S>(const Params&, const double*, const double*, double, const double*, \
-                                        const double*, cudaStream_t);                            \
-    template cudaError_t launch_probe<S>(const Params&, int, int, int, double*, cudaStream_t);                  \
+                                        const double*, cudaStream_t);                                   \
+    template cudaError_t launch_probe<S>(const Params&, int, int, int, double*, cudaStream_t);          \
     template cudaError_t launch_step_rows<S>(const Params&, int, const int32_t*, int, const int32_t*, int, cudaStream_t);
+#define LBM_INSTANTIATE_COLL(S, C) \
+    template cudaError_t launch_step_coll<S, C>(const Params&, int, const RowLists*, cudaStream_t);
 
 }  // namespace lbm

@@ -10,9 +10,21 @@ namespace lbm {
 struct Params;
 struct ReadOut;
 
-// returns cudaSuccess or the launch error
+// the step split by rows (FP32 and FP16-deviation storage): rows whose pairs all take the packed path
+// (every cell bulk fluid of the packed path, the row off the periodic y/z seams, nx even) and the
+// remaining rows; row r = y + ny z
+struct RowLists {
+    const int32_t* plain = nullptr;
+    int n_plain = 0;
+    const int32_t* other = nullptr;
+    int n_other = 0;
+};
+
+// returns cudaSuccess or the launch error; rl == nullptr: one launch over the lattice
 template <class S>
-cudaError_t launch_step(const Params& p, int collision, int closure, cudaStream_t st);
+cudaError_t launch_step(const Params& p, int collision, int closure, const RowLists* rl, cudaStream_t st);
+template <class S, int COLL>
+cudaError_t launch_step_coll(const Params& p, int closure, const RowLists* rl, cudaStream_t st);
 template <class S>
 cudaError_t launch_read(const Params& p, const ReadOut& o, cudaStream_t st);
 template <class S>

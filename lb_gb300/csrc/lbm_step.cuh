@@ -5,6 +5,8 @@
 //           plain bulk cells off the periodic seams, the pair is loaded with 64-bit (FP32) or 32-bit
 //           (FP16) accesses where the AA slot pair is aligned and collided in packed FP32 (F2 lanes:
 //           FADD2/FMUL2/FFMA2); otherwise each cell takes the scalar per-cell path.
+// k_step2_plain / k_step2_list : the same step split by rows (the default): the rows whose pairs all
+//           take the packed path, and the remaining rows.
 #pragma once
 
 #include "lbm_device.cuh"
@@ -306,7 +308,7 @@ LBM_D void store_pair(const Params& p, const PairIdx& q, const PairCodec& k, con
             else *(float2*)(a + q.e0) = f[V].v;
         } else {
             const F2 e = lfma(f[V], k.scale, k.nwrs[csq(V)]);
-            const __half2 h = half2_sr(e.v, lcg_next(rs, p));
+            const __half2 h = half2_sr(e.v, lcg_next(rs, p), p);
             if constexpr (split) { a[i0] = __low2half(h); a[i1] = __high2half(h); }
             else *(__half2*)(a + q.e0) = h;
         }
@@ -372,11 +374,52 @@ LBM_D void store_pair_rows(const Params& p, const PairRows& w, const PairCodec& 
             else *(float2*)(a + w.x0) = f[V].v;
         } else {
             const F2 e = lfma(f[V], k.scale, k.nwrs[csq(V)]);
-            const __half2 h = half2_sr(e.v, lcg_next(rs, p));
+            const __half2 h = half2_sr(e.v, lcg_next(rs, p), p);
             if constexpr (split) { a[i0] = __low2half(h); a[i1] = __high2half(h); }
             else *(__half2*)(a + w.x0) = h;
         }
     });
+}
+
+template <class S>
+LBM_D PairCodec make_codec(const Params& p) {
+    PairCodec k;
+    if constexpr (S::kind == 2) {
+        k.inv_scale = F2(p.inv_scale);
+        k.scale = F2(p.scale);
+        k.wr[0] = F2(p.wr[0]); k.wr[1] = F2(p.wr[1]); k.wr[2] = F2(p.wr[7]); k.wr[3] = F2(p.wr[19]);
+        k.nwrs[0] = F2(p.nwrs[0]); k.nwrs[1] = F2(p.nwrs[1]); k.nwrs[2] = F2(p.nwrs[7]); k.nwrs[3] = F2(p.nwrs[19]);
+    }
+    return k;
+}
+// element indices of the pair whose first cell is element e0 at x = x0 (x seams wrap through eL / eR)
+LBM_D PairIdx make_pair_idx(const Params& p, int e0, int x0) {
+    PairIdx q;
+    q.e0 = e0;
+    q.e1 = e0 + 1;
+    q.eL = (p.wrap[0] && x0 == 0) ? e0 + p.nx : e0;
+    q.eR = (p.wrap[0] && x0 + 2 == p.nx) ? q.e1 - p.nx : q.e1;
+    return q;
+}
+
+// the collision the packed path runs for the collision policy (the combined one packs only pairs of
+// reference-flag-1 cells, which both take the 2015 branch), and whether it takes its moments from the
+// raw FP16 deviations (FP16 + cumulant-2015)
+template <int COLL> LBM_HD constexpr int packed_coll() { return COLL == 3 ? 1 : COLL; }
+template <class S, int COLL> LBM_HD constexpr bool packed_raw() { return S::kind == 2 && packed_coll<COLL>() == 1; }
+
+// one packed pair of bulk cells in a row off the periodic y/z seams: every access is a per-direction
+// base address plus the element index
+template <class S, int COLL, int CLOS, bool ODD>
+LBM_D void step_pair_plain(const Params& p, int e0, int x0) {
+    constexpr int PC = packed_coll<COLL>();
+    constexpr bool RAW = packed_raw<S, COLL>();
+    const PairCodec k = make_codec<S>(p);
+    const PairIdx q = make_pair_idx(p, e0, x0);
+    F2 f[27];
+    load_pair<S, ODD, RAW>(p, q, k, f);
+    collide_pair<PC, CLOS, RAW>(p, f, e0);
+    store_pair<S, ODD>(p, q, k, f);
 }
 
 // one x-pair (x0 even): packed path for two bulk cells, else the per-cell path for each
@@ -385,11 +428,10 @@ LBM_D void step_pair(const Params& p, int x0, int y, int z) {
     static_assert(S::kind != 0, "packed pairs are FP32 arithmetic");
     const bool two = x0 + 1 < p.nx;
     const unsigned idx0 = (unsigned)x0 + (unsigned)p.nx * ((unsigned)y + (unsigned)p.ny * (unsigned)z);
-    // the combined collision packs only pairs of reference-flag-1 cells (both take the 2015 branch)
     constexpr uint8_t keep = COLL == 3 ? (uint8_t)0xff : (uint8_t)~BIT_REFBULK;
     constexpr uint8_t want = COLL == 3 ? (uint8_t)(CLS_BULK | BIT_REFBULK) : (uint8_t)CLS_BULK;
-    constexpr int PC = COLL == 3 ? 1 : COLL;
-    constexpr bool RAW = S::kind == 2 && PC == 1;  // FP16 + cumulant-2015: moments from the deviations
+    constexpr int PC = packed_coll<COLL>();
+    constexpr bool RAW = packed_raw<S, COLL>();
     const uint8_t f0 = p.cls[idx0] & keep;
     const uint8_t f1 = two ? (p.cls[idx0 + 1] & keep) : (uint8_t)0;
     const bool pair = two && f0 == want && f1 == want && (p.nx & 1) == 0;
@@ -398,27 +440,14 @@ LBM_D void step_pair(const Params& p, int x0, int y, int z) {
         if (two) step_cell_call<S, COLL, CLOS, ODD>(p, x0 + 1, y, z);
         return;
     }
-    PairCodec k;
-    if constexpr (S::kind == 2) {
-        k.inv_scale = F2(p.inv_scale);
-        k.scale = F2(p.scale);
-        k.wr[0] = F2(p.wr[0]); k.wr[1] = F2(p.wr[1]); k.wr[2] = F2(p.wr[7]); k.wr[3] = F2(p.wr[19]);
-        k.nwrs[0] = F2(p.nwrs[0]); k.nwrs[1] = F2(p.nwrs[1]); k.nwrs[2] = F2(p.nwrs[7]); k.nwrs[3] = F2(p.nwrs[19]);
-    }
     // rows on a periodic y or z seam (uniform per block) form their addresses from wrapped rows;
     // all other rows use the per-direction base addresses (x seams wrap through eL / eR)
     const bool yz_seam = (p.wrap[1] && (y == 0 || y == p.ny - 1)) || (p.wrap[2] && (z == 0 || z == p.nz - 1));
-    F2 f[27];
     if (!yz_seam) {
-        PairIdx q;
-        q.e0 = (int)idx0;
-        q.e1 = q.e0 + 1;
-        q.eL = (p.wrap[0] && x0 == 0) ? q.e0 + p.nx : q.e0;
-        q.eR = (p.wrap[0] && x0 + 2 == p.nx) ? q.e1 - p.nx : q.e1;
-        load_pair<S, ODD, RAW>(p, q, k, f);
-        collide_pair<PC, CLOS, RAW>(p, f, idx0);
-        store_pair<S, ODD>(p, q, k, f);
+        step_pair_plain<S, COLL, CLOS, ODD>(p, (int)idx0, x0);
     } else {
+        const PairCodec k = make_codec<S>(p);
+        F2 f[27];
         PairRows w;
         make_pair_rows(p, x0, y, z, w);
         load_pair_rows<S, ODD, RAW>(p, w, k, f);
@@ -458,6 +487,40 @@ __global__ void __launch_bounds__(128, step2_min_blocks(COLL)) k_step2(Params p)
     const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     if (x0 >= p.nx) return;
     step_pair<S, COLL, CLOS, ODD>(p, x0, blockIdx.y, blockIdx.z);
+}
+
+// ---- the step split by rows ------------------------------------------------------------------------
+// Set-up lists the plain rows (every cell a bulk fluid cell of the packed path, the row off the periodic
+// y/z seams, nx even) and the remaining rows.  k_step2_plain runs only the packed pair path over the
+// plain rows: no class byte, no per-cell fallback, so the register allocation is that of the packed
+// path alone.  k_step2_list runs the general pair step over the remaining rows.  Every population slot
+// is read and written by one thread only within a step (the AA argument), so running the two sets of
+// threads as two launches gives the same result as one launch over the lattice.
+// Grid: x = row in the list (up to 2^31 - 1 rows), y = block of 128 x-pairs within the row.
+#ifndef LBM_PLAIN_MIN_BLOCKS
+#define LBM_PLAIN_MIN_BLOCKS 6
+#endif
+#ifndef LBM_PLAIN_MIN_BLOCKS_SRT
+#define LBM_PLAIN_MIN_BLOCKS_SRT 4
+#endif
+#ifndef LBM_PLAIN_MIN_BLOCKS_CUM17
+#define LBM_PLAIN_MIN_BLOCKS_CUM17 4
+#endif
+constexpr int plain_min_blocks(int coll) {
+    return coll == 0 ? LBM_PLAIN_MIN_BLOCKS_SRT : coll == 2 ? LBM_PLAIN_MIN_BLOCKS_CUM17 : LBM_PLAIN_MIN_BLOCKS;
+}
+template <class S, int COLL, int CLOS, bool ODD>
+__global__ void __launch_bounds__(128, plain_min_blocks(COLL)) k_step2_plain(Params p, const int32_t* rows) {
+    const int x0 = 2 * (blockIdx.y * blockDim.x + threadIdx.x);
+    if (x0 >= p.nx) return;
+    step_pair_plain<S, COLL, CLOS, ODD>(p, rows[blockIdx.x] * p.nx + x0, x0);
+}
+template <class S, int COLL, int CLOS, bool ODD>
+__global__ void __launch_bounds__(128, step2_min_blocks(COLL)) k_step2_list(Params p, const int32_t* rows) {
+    const int x0 = 2 * (blockIdx.y * blockDim.x + threadIdx.x);
+    if (x0 >= p.nx) return;
+    const int r = rows[blockIdx.x];
+    step_pair<S, COLL, CLOS, ODD>(p, x0, r % p.ny, r / p.ny);
 }
 
 }  // namespace lbm

@@ -24,8 +24,18 @@ namespace lbm {
 #ifndef LBM_MLP_MIN_BLOCKS
 #define LBM_MLP_MIN_BLOCKS 0
 #endif
-template <class S, int COLL, bool ODD, int MODE>
-__global__ void __launch_bounds__(128, MODE == 2 ? step2_min_blocks(COLL) : LBM_MLP_MIN_BLOCKS) k_step2_mlp(Params p) {
+#ifndef LBM_MLP_PLAIN_MIN_BLOCKS
+#define LBM_MLP_PLAIN_MIN_BLOCKS LBM_MLP_MIN_BLOCKS
+#endif
+// ROWS: 0 one launch over the lattice (grid x = pair block, y, z); 1 the plain rows of the split step
+// (every pair a packed bulk pair off the y/z seams, lbm_step.cuh); 2 the remaining rows (grid x = row
+// in the list, y = pair block)
+constexpr int mlp_min_blocks(int mode, int rows, int coll) {
+    return mode == 2 ? (rows == 1 ? plain_min_blocks(coll) : step2_min_blocks(coll))
+                     : (rows == 1 ? LBM_MLP_PLAIN_MIN_BLOCKS : LBM_MLP_MIN_BLOCKS);
+}
+template <class S, int COLL, bool ODD, int MODE, int ROWS = 0>
+__global__ void __launch_bounds__(128, mlp_min_blocks(MODE, ROWS, COLL)) k_step2_mlp(Params p, const int32_t* rows) {
     static_assert(S::kind != 0, "the learned closure runs on the packed FP32 path");
     __shared__ uint4 wf[MODE == 2 ? 1 : kMlpFragRows][32];
     __shared__ uint4 stage[MODE == 2 ? 1 : 4][64];
@@ -34,28 +44,37 @@ __global__ void __launch_bounds__(128, MODE == 2 ? step2_min_blocks(COLL) : LBM_
         __syncthreads();
     }
 
-    const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
-    const int y = blockIdx.y, z = blockIdx.z;
+    int x0, y = 0, z = 0;
+    unsigned idx0;
+    const int r = ROWS == 0 ? 0 : rows[blockIdx.x];
+    if constexpr (ROWS == 0) {
+        x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+        y = blockIdx.y;
+        z = blockIdx.z;
+    } else {
+        x0 = 2 * (blockIdx.y * blockDim.x + threadIdx.x);
+        if constexpr (ROWS == 2) {
+            y = r % p.ny;
+            z = r / p.ny;
+        }
+    }
     const bool live = x0 < p.nx;
     const bool two = x0 + 1 < p.nx;
-    const unsigned idx0 = (unsigned)(live ? x0 : 0) + (unsigned)p.nx * ((unsigned)y + (unsigned)p.ny * (unsigned)z);
-    const uint8_t f0 = live ? (p.cls[idx0] & (uint8_t)~BIT_REFBULK) : (uint8_t)0;
-    const uint8_t f1 = two ? (p.cls[idx0 + 1] & (uint8_t)~BIT_REFBULK) : (uint8_t)0;
-    const bool pair = two && f0 == CLS_BULK && f1 == CLS_BULK && (p.nx & 1) == 0;
-
-    PairCodec k;
-    if constexpr (S::kind == 2) {
-        k.inv_scale = F2(p.inv_scale);
-        k.scale = F2(p.scale);
-        k.wr[0] = F2(p.wr[0]); k.wr[1] = F2(p.wr[1]); k.wr[2] = F2(p.wr[7]); k.wr[3] = F2(p.wr[19]);
-        k.nwrs[0] = F2(p.nwrs[0]); k.nwrs[1] = F2(p.nwrs[1]); k.nwrs[2] = F2(p.nwrs[7]); k.nwrs[3] = F2(p.nwrs[19]);
+    if constexpr (ROWS == 1) idx0 = (unsigned)(live ? x0 : 0) + (unsigned)p.nx * (unsigned)r;
+    else idx0 = (unsigned)(live ? x0 : 0) + (unsigned)p.nx * ((unsigned)y + (unsigned)p.ny * (unsigned)z);
+    bool pair;
+    if constexpr (ROWS == 1) {
+        pair = live;  // plain rows: nx even, every pair packed
+    } else {
+        const uint8_t f0 = live ? (p.cls[idx0] & (uint8_t)~BIT_REFBULK) : (uint8_t)0;
+        const uint8_t f1 = two ? (p.cls[idx0 + 1] & (uint8_t)~BIT_REFBULK) : (uint8_t)0;
+        pair = two && f0 == CLS_BULK && f1 == CLS_BULK && (p.nx & 1) == 0;
     }
-    const bool yz_seam = (p.wrap[1] && (y == 0 || y == p.ny - 1)) || (p.wrap[2] && (z == 0 || z == p.nz - 1));
-    PairIdx q;
-    q.e0 = (int)idx0;
-    q.e1 = q.e0 + 1;
-    q.eL = (p.wrap[0] && x0 == 0) ? q.e0 + p.nx : q.e0;
-    q.eR = (p.wrap[0] && x0 + 2 == p.nx) ? q.e1 - p.nx : q.e1;
+
+    const PairCodec k = make_codec<S>(p);
+    const bool yz_seam = ROWS != 1 &&
+        ((p.wrap[1] && (y == 0 || y == p.ny - 1)) || (p.wrap[2] && (z == 0 || z == p.nz - 1)));
+    const PairIdx q = make_pair_idx(p, (int)idx0, x0);
 
     float2 kept = make_float2(-1.f, -1.f);
     if (MODE == 2 && pair) kept = __half22float2(__ldg((const __half2*)(p.nut + idx0)));
@@ -130,9 +149,11 @@ __global__ void __launch_bounds__(128, MODE == 2 ? step2_min_blocks(COLL) : LBM_
             make_pair_rows(p, x0, y, z, w);
             store_pair_rows<S, ODD>(p, w, k, f);
         }
-    } else if (live) {
-        step_cell_call<S, COLL, 1, ODD>(p, x0, y, z);
-        if (two) step_cell_call<S, COLL, 1, ODD>(p, x0 + 1, y, z);
+    } else if constexpr (ROWS != 1) {
+        if (live) {
+            step_cell_call<S, COLL, 1, ODD>(p, x0, y, z);
+            if (two) step_cell_call<S, COLL, 1, ODD>(p, x0 + 1, y, z);
+        }
     }
 }
 

@@ -329,6 +329,12 @@ class Solver:
         self._check(lib().lbm_step_timed(self._ctx, int(n), C.byref(ms)))
         return ms.value
 
+    def step_launches(self):
+        """Kernel launches one step issues on this context (1, or 2 for the split step)."""
+        n = C.c_int32(0)
+        self._check(lib().lbm_step_launches(self._ctx, C.byref(n)))
+        return n.value
+
     def probe(self, x, y, z):
         """(u_x, u_y, u_z, rho) of one cell, copied to the host."""
         out = np.empty(4)

@@ -169,6 +169,63 @@ def test_row_staged_step_is_bit_identical_to_per_pair_path(built_lib, shape, cas
         assert np.array_equal(a, b)
 
 
+def _split_case(kind):
+    if kind == "channel":  # wall rows, x and z seams
+        return (64, 14, 12), cases.channel(64, 14, 12, re_tau=3.0, u_max=0.05, nu=0.01)
+    if kind == "box":  # fully periodic: every y/z seam row
+        rng = np.random.default_rng(11)
+        N = 64 * 8 * 6
+        return (64, 8, 6), {"flags": np.ones((6, 8, 64), np.int32), "inlets": [], "outlets": [], "nu": 0.004,
+                            "periodic": (1, 1, 1), "force": (0.0, 0.0, 0.0),
+                            "rho": 1 + 0.01 * rng.standard_normal(N), "u": 0.03 * rng.standard_normal((3, N))}
+    return (40, 16, 14), small_body_case()  # inlet, outlet and body rows beside plain rows
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16dev"])
+@pytest.mark.parametrize("coll,clos", [("cum", "smag"), ("srt", "smag"), ("cum17", "none"), ("comb", "smag"),
+                                       ("cum", "mlp"), ("cum", "mlp3")])
+@pytest.mark.parametrize("kind", ["channel", "box", "body"])
+def test_split_step_is_bit_identical_to_one_launch(built_lib, storage, coll, clos, kind):
+    """The default step runs the plain rows (every pair a packed bulk pair off the y/z seams) and the
+    remaining rows as two launches; LBM_OPT_ONE_LAUNCH runs one launch over the lattice.  Each slot is
+    read and written by one thread within a step, so the populations must agree bit for bit, on odd and
+    even steps, for every collision, the learned closure (every step and with a refresh interval of 3)
+    and the FP16 stochastic rounding."""
+    from lb_gb300 import les
+    from lb_gb300.solver import OmegaMLP
+    shape, c = _split_case(kind)
+    model = None
+    turb = CLOS.get(clos, OmegaLES)
+    interval = 1
+    if clos.startswith("mlp"):
+        model = les.MlpModel.load(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                               "lb_gb300", "data", "les_mlp_channel.npz"))
+        turb = OmegaMLP
+        interval = 3 if clos == "mlp3" else 1
+    inlet = InletVelocityEquilibrium if kind == "body" else InletVelocityMovingWall
+    runs = []
+    for opt in (0, capi.LBM_OPT_ONE_LAUNCH):
+        s = Solver(shape, collision=COLL[coll], turbulence=turb, inlet=inlet, storage=storage, nu=c["nu"],
+                   cles=0.17, periodic=c.get("periodic", (0, 0, 0)), force=c.get("force", (0, 0, 0)), options=opt,
+                   mlp_interval=interval)
+        s.set_flags(c["flags"])
+        s.set_bc(c.get("inlets", []), c.get("outlets", []))
+        if "rho" in c:
+            s.init_fields(c["rho"], c["u"])
+        else:
+            s.init_equilibrium(1.0, (0.04, 0.0, 0.0))
+        if model is not None:
+            s.load_mlp(model)
+        out = []
+        for n in (5, 4):
+            s.step(n)
+            out.append(s.populations())
+        runs.append(out)
+        s.close()
+    for a, b in zip(*runs):
+        assert np.array_equal(a, b)
+
+
 def test_channel_srt_force_fp64(built_lib, oracle_lib):
     nx, ny, nz = 16, 12, 10
     c = cases.channel(nx, ny, nz, re_tau=2.0, u_max=0.04, nu=0.02)  # u_tau = 0.008, F = 1.3e-5
@@ -380,3 +437,31 @@ def test_gpu_voxelizer_matches_oracle_on_seeded_body(built_lib, oracle_lib):
     ref, _ = O.voxelize_mesh(v, f, 1.0, 2.0, (-100.0, -90.0, -80.0))
     assert out.reshape(ref.shape).sum() > 100
     assert np.array_equal(out.reshape(ref.shape), ref)
+
+
+@pytest.mark.parametrize("storage", ["f64", "f32", "f16dev"])
+def test_reductions_are_deterministic_and_match_the_moments(built_lib, storage):
+    """lbm_reduce adds per-block FP64 partials in a fixed order: two calls give the same bits, the mass
+    equals the FP64 sum of the moments read back per cell, the momentum the sum of rho u, and the error
+    monitor repeats its value on an unchanged state."""
+    nx, ny, nz = 64, 34, 20
+    c = cases.channel(nx, ny, nz, re_tau=3.0, u_max=0.05, nu=0.01, amp=0.05)
+    s = Solver((nx, ny, nz), turbulence=OmegaLES, storage=storage, nu=c["nu"], cles=0.17, periodic=c["periodic"],
+               force=c["force"])
+    s.set_flags(c["flags"])
+    s.set_bc()
+    s.init_fields(c["rho"], c["u"])
+    s.step(7)
+    d1, d2 = s.reduce(), s.reduce()
+    assert (d1.mass, d1.momentum, d1.max_speed, d1.fluid_cells) == (d2.mass, d2.momentum, d2.max_speed, d2.fluid_cells)
+    rho, u = s.moments()
+    fl = c["flags"].reshape(-1) != 0
+    assert d1.fluid_cells == int(fl.sum())
+    assert abs(d1.mass - rho[fl].sum()) <= 1e-12 * rho[fl].sum()
+    ref = (rho[fl] * u[0, fl]).sum()
+    assert abs(d1.momentum[0] - ref) <= 1e-9 * abs(ref)
+    assert abs(d1.max_speed - np.sqrt((u[:, fl] ** 2).sum(axis=0)).max()) <= 1e-6 * d1.max_speed
+    e1 = s.error_evaluation()
+    e2 = s.error_evaluation()
+    assert np.isfinite(e1) and e2 == 0.0
+    s.close()
