@@ -372,9 +372,12 @@ lbm_status lbm_voxelize_mesh(const double* verts, int32_t nv, const int32_t* tri
  * device that loads the library until the process exits).  Limits: at most
  * LBM_VOXELIZE_NOALLOC_MAX_VERTICES vertices, LBM_VOXELIZE_NOALLOC_MAX_TRIANGLES triangles and
  * LBM_VOXELIZE_NOALLOC_MAX_DIM cells per axis; larger inputs return LBM_ERR_UNSUPPORTED before any
- * device work.  The first call on a device also looks up that array's device address, so make it
- * before capturing any CUDA stream.  All calls in a process share the array: calls that overlapped on
- * the GPU would race, so this function holds a lock and returns only after its kernels finished. */
+ * device work, as do triangle indices outside [0, nv) (LBM_ERR_INVALID, the output untouched).  Each
+ * call looks up that array's device address on `device`, so make the first call before capturing any
+ * CUDA stream.  All calls in a process share the array: calls that overlapped on the GPU would race,
+ * so this function holds a lock and returns only after its kernels finished.  Its copies and kernels
+ * run on the legacy default stream of `device`: a caller that wrote flags_out_device (or will read it)
+ * on a non-blocking stream must synchronise that stream first. */
 #define LBM_VOXELIZE_NOALLOC_MAX_VERTICES  32768
 #define LBM_VOXELIZE_NOALLOC_MAX_TRIANGLES 32768
 #define LBM_VOXELIZE_NOALLOC_MAX_DIM       4096

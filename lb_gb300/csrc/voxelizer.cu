@@ -234,7 +234,6 @@ static __device__ __align__(256) unsigned char g_vox_scratch[sizeof(VoxScratch)]
 
 constexpr int kMaxDevices = 64;
 std::mutex g_vox_mutex;                      // one call at a time per process
-VoxScratch* g_vox_addr[kMaxDevices] = {};    // device address of g_vox_scratch, per device
 
 // orient each triangle's (y, z) projection counter-clockwise, as the allocating path does on the
 // host; a triangle parallel to the rays gets NaN coordinates so that no column ever meets it
@@ -300,15 +299,18 @@ lbm_status lbm_voxelize_mesh_noalloc(const double* verts, int32_t nv, const int3
     if (nx > LBM_VOXELIZE_NOALLOC_MAX_DIM || ny > LBM_VOXELIZE_NOALLOC_MAX_DIM || nz > LBM_VOXELIZE_NOALLOC_MAX_DIM)
         return LBM_ERR_UNSUPPORTED;
 
+    // every triangle index must name a vertex: checked here, before any device work, so a bad mesh
+    // leaves the caller's buffer untouched (as lbm_voxelize_mesh does)
+    for (long long i = 0; i < 3LL * nt; i++)
+        if (tris[i] < 0 || tris[i] >= nv) return LBM_ERR_INVALID;
+
     std::lock_guard<std::mutex> lock(g_vox_mutex);
     if (cudaSetDevice(device) != cudaSuccess) return LBM_ERR_CUDA;
-    if (!g_vox_addr[device]) {
-        // first call on this device: find the device address of the scratch array
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_vox_scratch) != cudaSuccess || !p) return LBM_ERR_CUDA;
-        g_vox_addr[device] = (VoxScratch*)p;
-    }
-    VoxScratch* s = g_vox_addr[device];
+    // the scratch array's device address on this device, looked up on every call (a context torn
+    // down with cudaDeviceReset reloads the module at a new address)
+    void* sp = nullptr;
+    if (cudaGetSymbolAddress(&sp, g_vox_scratch) != cudaSuccess || !sp) return LBM_ERR_CUDA;
+    VoxScratch* s = (VoxScratch*)sp;
     // the status words start at zero; verts, tris, prepared and samples are overwritten for the
     // ranges this call reads
     if (cudaMemset(&s->overflow, 0, 2 * sizeof(int)) != cudaSuccess ||

@@ -71,3 +71,23 @@ def test_no_alloc_voxelizer_rejects_oversized_input(built_lib):
     dims = np.zeros(3, np.int32)
     rc = L.lbm_voxelize_mesh_noalloc(_dp(v), 3, _ip(t), len(t), 1.0, 1.0, C.c_void_p(1), _ip(dims), None, 0)
     assert rc == capi.LBM_ERR_UNSUPPORTED
+
+
+def test_no_alloc_voxelizer_rejects_a_bad_index_before_device_work(built_lib):
+    """A triangle naming a vertex outside [0, nv) is rejected on the host, before any copy or kernel:
+    the caller's device buffer keeps its contents."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    L = capi.lib()
+    v, t = cases.perturbed_icosphere(radius=6.0, subdiv=2, lmax=4, amp=0.10, seed=7)
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    t = np.ascontiguousarray(t, dtype=np.int32)
+    dims = np.zeros(3, np.int32)
+    assert L.lbm_voxelize_mesh_noalloc(_dp(v), len(v), _ip(t), len(t), 1.0, 1.0, None, _ip(dims), None, 0) == 0
+    t[len(t) // 2, 1] = len(v)
+    dev = torch.full((int(dims.prod()),), -7, dtype=torch.int32, device="cuda:0")
+    rc = L.lbm_voxelize_mesh_noalloc(_dp(v), len(v), _ip(t), len(t), 1.0, 1.0, C.c_void_p(dev.data_ptr()),
+                                     _ip(dims), None, 0)
+    assert rc == capi.LBM_ERR_INVALID
+    assert bool((dev == -7).all())
