@@ -239,6 +239,8 @@ def cpu_reference(shape, case, steps, warmup, budget_s, threads=None):
     boundary and moment passes) on the host cores; returns (seconds per step, steps timed, threads)."""
     from lb_gb300 import capi
     from oracle import oracle as O
+    if O._lib is None:
+        O.NATIVE = True  # the host-tuned build of the same sources (oracle/build.py)
     if threads:
         O.set_threads(threads)
     nth = O.max_threads()
@@ -259,6 +261,16 @@ def cpu_reference(shape, case, steps, warmup, budget_s, threads=None):
     dt = time.perf_counter() - t0
     o.close()
     return dt / n, n, nth
+
+
+def cpu_host_info():
+    """Compiler flags of the timed CPU baseline and the host's STREAM-triad bandwidth (all threads)."""
+    from oracle import build as obuild
+    from oracle import oracle as O
+    return {"flags": obuild.flags(native=True), "host_stream_gbs": round(O.host_stream_gbs(), 1),
+            "reference_pass_bytes_per_cell": 720,
+            "note": "reference pass structure (omega, collision, A-B streaming, boundary and moment passes) moves "
+                    "about 720 B per cell update in FP32"}
 
 
 def learned_block(path, model, glups_mlp, glups_smag, interval=None):
@@ -307,7 +319,7 @@ def main():
         if rank != 0:
             return
         from oracle import build as obuild
-        obuild.build()
+        obuild.build(native=True)
         case = channel_case(shape)
         sps, n, nth = cpu_reference(shape, case, args.steps, min(args.warmup, 1), budget_s=max(args.cpu_budget, 30.0))
         glups = N / sps / 1e9
@@ -316,8 +328,9 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": workload, "storage": "f32 (A-B, two population arrays)",
                            "impl_detail": "CPU restatement of the reference's per-hook passes (oracle/), OpenMP"},
-                "cpu_baseline": {"value": glups, "unit": "GLUPS", "cores": nth, "kind": "port",
-                                 "sample": f"{n} steps of the full {shape[0]}x{shape[1]}x{shape[2]} lattice"},
+                "cpu_baseline": dict({"value": glups, "unit": "GLUPS", "cores": nth, "kind": "port",
+                                      "sample": f"{n} steps of the full {shape[0]}x{shape[1]}x{shape[2]} lattice"},
+                                     **cpu_host_info()),
                 "e2e": {"value": glups, "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -390,12 +403,14 @@ def main():
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         from oracle import build as obuild
-        obuild.build()
+        obuild.build(native=True)
         cshape = (256, 128, 128)
         ccase = channel_case(cshape)
         sps, n, nth = cpu_reference(cshape, ccase, 50, 1, budget_s=args.cpu_budget)
-        cpu = {"value": cshape[0] * cshape[1] * cshape[2] / sps / 1e9, "unit": "GLUPS", "cores": nth, "kind": "port",
-               "sample": f"{n} steps of the 256x128x128 channel, FP32, reference pass structure (oracle/)"}
+        cpu = dict({"value": cshape[0] * cshape[1] * cshape[2] / sps / 1e9, "unit": "GLUPS", "cores": nth,
+                    "kind": "port",
+                    "sample": f"{n} steps of the 256x128x128 channel, FP32, reference pass structure (oracle/)"},
+                   **cpu_host_info())
     if rank != 0:
         return
     line = {"metric": METRIC, "value": glups16, "unit": "GLUPS", "n_gpus": ws, "steps": args.steps,

@@ -865,6 +865,23 @@ int orc_max_threads(void) {
     return 1;
 #endif
 }
+// host memory bandwidth (STREAM triad a = b + s c over n doubles per array, arrays first touched by the
+// threads that use them, best of `reps`), in GB/s counting 24 bytes per element; reported beside the
+// timed CPU baseline so its GLUPS can be read against the host's own roofline
+double orc_host_stream_gbs(long long n, int reps) {
+    std::vector<double> a((size_t)n), b((size_t)n), c((size_t)n);
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < n; i++) { a[i] = 0.0; b[i] = 1.0; c[i] = 2.0; }
+    double best = 0.0;
+    for (int r = 0; r < reps; r++) {
+        const double t0 = omp_get_wtime();
+#pragma omp parallel for schedule(static)
+        for (long long i = 0; i < n; i++) a[i] = b[i] + 3.0 * c[i];
+        const double dt = omp_get_wtime() - t0;
+        if (dt > 0) best = std::max(best, 24.0 * (double)n / dt / 1e9);
+    }
+    return best + 0.0 * a[(size_t)(n / 2)];
+}
 int orc_set_flags(void* p, const int32_t* flags) {
     Handle* h = (Handle*)p;
     DISPATCH(h, { std::memcpy(S->mesh.data(), flags, S->N * sizeof(int32_t)); S->build_wall_list(); });

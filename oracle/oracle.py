@@ -12,12 +12,15 @@ from . import build as _build
 from lb_gb300.capi import LbmConfig, LbmBcInlet, LbmBcOutlet, LbmBcSymmetry, LbmDiag  # plain ctypes structs
 
 _lib = None
+# LBM_ORACLE_NATIVE=1 (set before the first call) loads the host-tuned build; bench.py's timed CPU
+# baseline uses it, the parity tests keep the portable one
+NATIVE = os.environ.get("LBM_ORACLE_NATIVE") == "1"
 
 
 def lib():
     global _lib
     if _lib is None:
-        path = _build.build()
+        path = _build.build(native=NATIVE)
         L = C.CDLL(path)
         vp, i32, f64 = C.c_void_p, C.c_int, C.c_double
         dp = C.POINTER(C.c_double)
@@ -27,6 +30,8 @@ def lib():
         L.orc_destroy.argtypes = [vp]
         L.orc_set_threads.argtypes = [i32]
         L.orc_max_threads.restype = i32
+        L.orc_host_stream_gbs.restype = f64
+        L.orc_host_stream_gbs.argtypes = [C.c_longlong, i32]
         L.orc_set_flags.argtypes = [vp, ip]
         L.orc_set_bc.argtypes = [vp, C.POINTER(LbmBcInlet), i32, C.POINTER(LbmBcOutlet), i32]
         L.orc_set_periodic_list.argtypes = [vp, ip, i32]
@@ -174,6 +179,11 @@ def set_threads(n):
 
 def max_threads():
     return lib().orc_max_threads()
+
+
+def host_stream_gbs(n=1 << 26, reps=5):
+    """STREAM-triad bandwidth of the host's memory on all oracle threads (GB/s)."""
+    return lib().orc_host_stream_gbs(int(n), int(reps))
 
 
 def wall_pass(flags):
