@@ -144,10 +144,8 @@ static Params make_params(const lbm_ctx* c) {
     p.has_force = (p.F[0] != 0.0 || p.F[1] != 0.0 || p.F[2] != 0.0) ? 1 : 0;
     p.rho0 = (float)c->cfg.rho0;
     p.f16_sr = (c->cfg.storage == LBM_STORAGE_F16DEV && !(c->cfg.options & LBM_OPT_F16_ROUND_NEAREST)) ? 1 : 0;
-    p.lcg_a = kLcgA;
-    p.lcg_c = kLcgC;
-    p.sr_mix = p.f16_sr ? kSrMix : 0u;
-    p.sr_add = p.f16_sr ? 0u : kHalfStep2x;
+    p.lcg_a = p.f16_sr ? kLcgA : 0u;
+    p.lcg_c = p.f16_sr ? kLcgC : kHalfStepState;
     p.scale = std::ldexp(1.0f, c->cfg.f16_scale_log2);
     p.inv_scale = std::ldexp(1.0f, -c->cfg.f16_scale_log2);
     p.scale2 = make_float2(p.scale, p.scale);

@@ -80,8 +80,8 @@ struct Params {
     int f16_sr;              // FP16 stores round stochastically (else to nearest)
     uint32_t sr_step_seed;   // step_seed(m)
     float raw_rho, raw_mdiag;  // sum_v w_v rho0 and sum_v w_v rho0 c_vx^2 of the FP16 codec's references
-    uint32_t lcg_a, lcg_c;   // the packed path's random stream s -> a s + c (the LCG below)
-    uint32_t sr_mix, sr_add; // packed FP16 stores: rbits = hi(s sr_mix) + sr_add (half2_sr)
+    uint32_t lcg_a, lcg_c;   // the packed path's random stream s -> a s + c: the LCG below when rounding
+                             // stochastically, a = 0 and c = kHalfStepState when to nearest (half2_sr)
     float wr[27];            // w_v rho0            (decode f = h 2^-s + w_v rho0)
     float nwrs[27];          // -w_v rho0 2^s       (encode h = f 2^s - w_v rho0 2^s)
     float2 wr2[27], nwrs2[27];  // the same as (x, x) pairs for the packed two-cell path
@@ -169,14 +169,14 @@ constexpr uint32_t kHalfStep13 = 0x1000u;  // for half_sr
 // Packed stores: cvt.rs.f16x2.f32 (sm_100 family) rounds both values stochastically in one instruction,
 // adding the 13-bit fields rbits[28:16] (upper half) and rbits[12:0] (lower half) below the FP16
 // mantissa of the FP32 patterns and truncating: the method of half_sr (the field layout was measured
-// on a GB300 against a software model, bit for bit on 65,536 inputs).  The LCG state's low bits are
-// weak (bit k has period 2^(k+1)), so rbits is the high word of the state times an odd constant,
-// rbits = hi(s * sr_mix) + sr_add: sr_mix = kSrMix, sr_add = 0 when rounding stochastically; sr_mix = 0,
-// sr_add = kHalfStep2x (a half step in both fields) rounds to nearest with the same instructions.
-constexpr uint32_t kSrMix = 0x9E3779B1u;
-constexpr uint32_t kHalfStep2x = (0x1000u << 16) | 0x1000u;
-LBM_D __half2 half2_sr(float2 v, uint32_t s, const Params& p) {
-    const uint32_t r = __umulhi(s, p.sr_mix) + p.sr_add;
+// on a GB300 against a software model, bit for bit on 65,536 inputs).  Each field must be uniform for
+// the rounding to be unbiased.  rbits = s ^ (s >> 16) of the LCG state s: the upper field is s[28:16],
+// the lower s[12:0] ^ s[28:16] (the weak low LCG bits, bit k of period 2^(k+1), whitened by the high
+// ones).  The state's own transform gives round-to-nearest with the same instructions: a = 0,
+// c = kHalfStepState keeps s fixed at the value whose rbits is a half step in both fields.
+constexpr uint32_t kHalfStepState = 0x10000000u;  // rbits = 0x10001000
+LBM_D __half2 half2_sr(float2 v, uint32_t s) {
+    const uint32_t r = s ^ (s >> 16);
     uint32_t h;
     asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(h) : "f"(v.y), "f"(v.x), "r"(r));  // upper v.y, lower v.x
     return *reinterpret_cast<__half2*>(&h);

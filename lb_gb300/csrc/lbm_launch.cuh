@@ -29,7 +29,8 @@ static cudaError_t step_parity(const Params& p, const RowLists* rl, cudaStream_t
         if (odd) k_step<S, COLL, CLOS, true><<<g, b, 0, st>>>(p);
         else     k_step<S, COLL, CLOS, false><<<g, b, 0, st>>>(p);
     } else if (rl) {
-        // split step: the plain rows, then the remaining rows (one thread per x-pair)
+        // split step: the plain rows, then the remaining rows (one thread per x-pair; 1-D grid of
+        // rows x blocks, split by row_block)
         const int half = (p.nx + 1) / 2;
         const dim3 b = cell_block(half);
         const unsigned xb = (unsigned)((half + (int)b.x - 1) / (int)b.x);
@@ -42,11 +43,11 @@ static cudaError_t step_parity(const Params& p, const RowLists* rl, cudaStream_t
             ko = odd ? k_step2_list<S, COLL, CLOS, true> : k_step2_list<S, COLL, CLOS, false>;
         }
         if (rl->n_plain > 0) {
-            kp<<<dim3((unsigned)rl->n_plain, xb), b, 0, st>>>(p, rl->plain);
+            kp<<<(unsigned)rl->n_plain * xb, b, 0, st>>>(p, rl->plain);
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) return e;
         }
-        if (rl->n_other > 0) ko<<<dim3((unsigned)rl->n_other, xb), b, 0, st>>>(p, rl->other);
+        if (rl->n_other > 0) ko<<<(unsigned)rl->n_other * xb, b, 0, st>>>(p, rl->other);
     } else {
         const int half = (p.nx + 1) / 2;  // one thread per x-pair
         dim3 g = cell_grid(half, p.ny, p.nz), b = cell_block(half);

@@ -308,7 +308,7 @@ LBM_D void store_pair(const Params& p, const PairIdx& q, const PairCodec& k, con
             else *(float2*)(a + q.e0) = f[V].v;
         } else {
             const F2 e = lfma(f[V], k.scale, k.nwrs[csq(V)]);
-            const __half2 h = half2_sr(e.v, lcg_next(rs, p), p);
+            const __half2 h = half2_sr(e.v, lcg_next(rs, p));
             if constexpr (split) { a[i0] = __low2half(h); a[i1] = __high2half(h); }
             else *(__half2*)(a + q.e0) = h;
         }
@@ -374,7 +374,7 @@ LBM_D void store_pair_rows(const Params& p, const PairRows& w, const PairCodec& 
             else *(float2*)(a + w.x0) = f[V].v;
         } else {
             const F2 e = lfma(f[V], k.scale, k.nwrs[csq(V)]);
-            const __half2 h = half2_sr(e.v, lcg_next(rs, p), p);
+            const __half2 h = half2_sr(e.v, lcg_next(rs, p));
             if constexpr (split) { a[i0] = __low2half(h); a[i1] = __high2half(h); }
             else *(__half2*)(a + w.x0) = h;
         }
@@ -496,7 +496,8 @@ __global__ void __launch_bounds__(128, step2_min_blocks(COLL)) k_step2(Params p)
 // path alone.  k_step2_list runs the general pair step over the remaining rows.  Every population slot
 // is read and written by one thread only within a step (the AA argument), so running the two sets of
 // threads as two launches gives the same result as one launch over the lattice.
-// Grid: x = row in the list (up to 2^31 - 1 rows), y = block of 128 x-pairs within the row.
+// Grid: one dimension, rows x blocks of 128 x-pairs, the blocks of a row adjacent (as in the one-launch
+// grid, so neighbouring rows run together); row_block() splits the block index.
 #ifndef LBM_PLAIN_MIN_BLOCKS
 #define LBM_PLAIN_MIN_BLOCKS 6
 #endif
@@ -509,17 +510,25 @@ __global__ void __launch_bounds__(128, step2_min_blocks(COLL)) k_step2(Params p)
 constexpr int plain_min_blocks(int coll) {
     return coll == 0 ? LBM_PLAIN_MIN_BLOCKS_SRT : coll == 2 ? LBM_PLAIN_MIN_BLOCKS_CUM17 : LBM_PLAIN_MIN_BLOCKS;
 }
+// blocks of 128 x-pairs per row: blockIdx.x = list entry * xb + block within the row
+LBM_D void row_block(const Params& p, const int32_t* rows, int& r, int& x0) {
+    const unsigned xb = (((unsigned)p.nx + 1u) / 2u + blockDim.x - 1u) / blockDim.x;
+    const unsigned e = blockIdx.x / xb, bx = blockIdx.x - e * xb;
+    r = rows[e];
+    x0 = 2 * (int)(bx * blockDim.x + threadIdx.x);
+}
 template <class S, int COLL, int CLOS, bool ODD>
 __global__ void __launch_bounds__(128, plain_min_blocks(COLL)) k_step2_plain(Params p, const int32_t* rows) {
-    const int x0 = 2 * (blockIdx.y * blockDim.x + threadIdx.x);
+    int r, x0;
+    row_block(p, rows, r, x0);
     if (x0 >= p.nx) return;
-    step_pair_plain<S, COLL, CLOS, ODD>(p, rows[blockIdx.x] * p.nx + x0, x0);
+    step_pair_plain<S, COLL, CLOS, ODD>(p, r * p.nx + x0, x0);
 }
 template <class S, int COLL, int CLOS, bool ODD>
 __global__ void __launch_bounds__(128, step2_min_blocks(COLL)) k_step2_list(Params p, const int32_t* rows) {
-    const int x0 = 2 * (blockIdx.y * blockDim.x + threadIdx.x);
+    int r, x0;
+    row_block(p, rows, r, x0);
     if (x0 >= p.nx) return;
-    const int r = rows[blockIdx.x];
     step_pair<S, COLL, CLOS, ODD>(p, x0, r % p.ny, r / p.ny);
 }
 

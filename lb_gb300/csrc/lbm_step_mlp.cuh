@@ -28,8 +28,8 @@ namespace lbm {
 #define LBM_MLP_PLAIN_MIN_BLOCKS LBM_MLP_MIN_BLOCKS
 #endif
 // ROWS: 0 one launch over the lattice (grid x = pair block, y, z); 1 the plain rows of the split step
-// (every pair a packed bulk pair off the y/z seams, lbm_step.cuh); 2 the remaining rows (grid x = row
-// in the list, y = pair block)
+// (every pair a packed bulk pair off the y/z seams, lbm_step.cuh); 2 the remaining rows (1-D grid of
+// listed rows x pair blocks, row_block)
 constexpr int mlp_min_blocks(int mode, int rows, int coll) {
     return mode == 2 ? (rows == 1 ? plain_min_blocks(coll) : step2_min_blocks(coll))
                      : (rows == 1 ? LBM_MLP_PLAIN_MIN_BLOCKS : LBM_MLP_MIN_BLOCKS);
@@ -44,15 +44,14 @@ __global__ void __launch_bounds__(128, mlp_min_blocks(MODE, ROWS, COLL)) k_step2
         __syncthreads();
     }
 
-    int x0, y = 0, z = 0;
+    int x0, y = 0, z = 0, r = 0;
     unsigned idx0;
-    const int r = ROWS == 0 ? 0 : rows[blockIdx.x];
     if constexpr (ROWS == 0) {
         x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
         y = blockIdx.y;
         z = blockIdx.z;
     } else {
-        x0 = 2 * (blockIdx.y * blockDim.x + threadIdx.x);
+        row_block(p, rows, r, x0);
         if constexpr (ROWS == 2) {
             y = r % p.ny;
             z = r / p.ny;
