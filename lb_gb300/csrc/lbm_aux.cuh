@@ -98,6 +98,8 @@ __global__ void __launch_bounds__(128) k_read(Params p, ReadOut o) {
             for (int q = 0; q < 27; q++) f[q] = (R)0;
         } else if (cl == CLS_INLET) {
             inlet_state<S>(p, c, f);
+        } else if (cl == CLS_BULK && !on_seam(p, c.x, c.y, c.z)) {
+            load_fast<S, ODD>(p, (unsigned)c.idx, f);  // the step kernel's per-direction addresses
         } else {
             gather<S, ODD, true>(p, c, cl, f, drag);
         }
@@ -121,7 +123,7 @@ __global__ void __launch_bounds__(128) k_read(Params p, ReadOut o) {
         if ((o.mode & READ_DIAG) && live && (cl == CLS_BULK || cl == CLS_EDGE || cl == CLS_OUTLET || cl == CLS_SYM)) {
             bool ok = true;
 #pragma unroll
-            for (int q = 0; q < 27; q++) ok = ok && isfinite((double)f[q]);
+            for (int q = 0; q < 27; q++) ok = ok && isfinite(f[q]);
             v[RED_MASS] += rho;
             v[RED_MX] += (double)rho * ux; v[RED_MY] += (double)rho * uy; v[RED_MZ] += (double)rho * uz;
             if (cl != CLS_BULK) {  // only cells beside a solid have momentum-exchange links
@@ -160,27 +162,24 @@ __global__ void __launch_bounds__(128) k_read(Params p, ReadOut o) {
     }
 }
 
-// the partials of k_read added in a fixed order (per quantity: a strided pass per thread, then a tree
-// over the block's threads); RED_VMAX is the square root of the largest |u|^2
-constexpr int kFinalThreads = 512;
+// the partials of k_read added in a fixed order: one block per quantity q0 + blockIdx.x, a strided pass
+// per thread, then a tree over the block's threads; RED_VMAX is the square root of the largest |u|^2
+constexpr int kFinalThreads = 1024;
 template <class S>
-__global__ void __launch_bounds__(kFinalThreads) k_read_final(const double* part, long long nblk, int q0, int q1,
-                                                              double* red) {
+__global__ void __launch_bounds__(kFinalThreads) k_read_final(const double* part, long long nblk, int q0, double* red) {
     __shared__ double sh[kFinalThreads];
-    for (int q = q0; q < q1; q++) {
-        const bool mx = q == RED_VMAX;
-        double s = 0.0;
-        for (long long b = threadIdx.x; b < nblk; b += kFinalThreads)
-            s = mx ? fmax(s, part[q * nblk + b]) : s + part[q * nblk + b];
-        sh[threadIdx.x] = s;
-        __syncthreads();
-        for (int w = kFinalThreads / 2; w > 0; w >>= 1) {
-            if (threadIdx.x < w) sh[threadIdx.x] = mx ? fmax(sh[threadIdx.x], sh[threadIdx.x + w]) : sh[threadIdx.x] + sh[threadIdx.x + w];
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) red[q] = mx ? sqrt(sh[0]) : sh[0];
+    const int q = q0 + blockIdx.x;
+    const bool mx = q == RED_VMAX;
+    const double* a = part + q * nblk;
+    double s = 0.0;
+    for (long long b = threadIdx.x; b < nblk; b += kFinalThreads) s = mx ? fmax(s, a[b]) : s + a[b];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = kFinalThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] = mx ? fmax(sh[threadIdx.x], sh[threadIdx.x + w]) : sh[threadIdx.x] + sh[threadIdx.x + w];
         __syncthreads();
     }
+    if (threadIdx.x == 0) red[q] = mx ? sqrt(sh[0]) : sh[0];
 }
 
 // one cell's (u_x, u_y, u_z, rho), the reference's per-step probe (SolverTurbulentLES.h:150-177)
@@ -230,10 +229,23 @@ __global__ void __launch_bounds__(128) k_init(Params p, const double* rho_f, con
         constexpr int V = decltype(vc)::value;
         f[V] = cl == CLS_SOLID ? (R)0 : (pops ? (R)pops[V * N + c.idx] : feq<V>(r, ux, uy, uz, u2));
     });
-    sfor<0, 27>([&](auto vc) {
-        constexpr int V = decltype(vc)::value;
-        store_at<S, V>(p, V * N + c.idx, f[V]);
-    });
+    if constexpr (S::kind == 2) {
+        // FP16 deviations of the initial state: one random stream per cell (the packed stores' LCG and
+        // cvt.rs, lower field), a hash of the cell index and the step seed; sr_step_seed of this launch
+        uint32_t s = mix32((uint32_t)c.idx ^ p.sr_step_seed);
+        __half* A = (__half*)p.f;
+        sfor<0, 27>([&](auto vc) {
+            constexpr int V = decltype(vc)::value;
+            const float e = fmaf(f[V], p.scale, p.nwrs[V]);
+            const __half2 h = half2_sr(make_float2(e, 0.0f), lcg_next(s, p));
+            A[V * N + c.idx] = __low2half(h);
+        });
+    } else {
+        sfor<0, 27>([&](auto vc) {
+            constexpr int V = decltype(vc)::value;
+            store_at<S, V>(p, V * N + c.idx, f[V]);
+        });
+    }
     if (cl == CLS_LID) {
         const int id = p.aux[c.idx];
         R* st = (R*)p.lid_state;

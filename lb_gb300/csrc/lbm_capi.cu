@@ -33,6 +33,8 @@ static_assert(OUT_INTERPOLATED == LBM_OUTLET_DENSITY_INTERPOLATED && OUT_NEQ == 
 struct lbm_ctx {
     lbm_config cfg{};
     cudaStream_t st = nullptr;
+    cudaStream_t st_side = nullptr;    // split step: the remaining rows run here, beside the plain rows
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     long long N = 0;
     size_t esize = 0;  // bytes per stored population
     void* d_f = nullptr;
@@ -196,6 +198,7 @@ static cudaError_t do_step(lbm_ctx* c, const Params& p) {
     RowLists rl;
     rl.plain = c->d_plain_rows; rl.n_plain = c->n_plain_rows;
     rl.other = c->d_rest_rows; rl.n_other = c->n_rest_rows;
+    rl.side = c->st_side; rl.fork = c->ev_fork; rl.join = c->ev_join;
     const RowLists* r = c->split_ok ? &rl : nullptr;
     switch (c->cfg.storage) {
         case LBM_STORAGE_F64: return launch_step<StF64>(p, c->cfg.collision, c->cfg.closure, nullptr, c->st);
@@ -288,6 +291,9 @@ lbm_status lbm_create(const lbm_config* cfg, lbm_ctx** out) {
     lbm_status s = LBM_OK;
     if ((e = cudaSetDevice(cfg->device)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&c->st_side, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaMalloc(&c->d_f, 27 * (size_t)N * c->esize)) != cudaSuccess ||
         (e = cudaMalloc(&c->d_cls, (size_t)N)) != cudaSuccess ||
         (e = cudaMalloc(&c->d_aux, (size_t)N * 4)) != cudaSuccess ||
@@ -326,6 +332,9 @@ lbm_status lbm_destroy(lbm_ctx* c) {
     dfree(c->d_rho_out); dfree(c->d_u_out); dfree(c->d_f_out); dfree(c->d_probe);
     dfree(c->d_bulk_rows); dfree(c->d_other_rows); dfree(c->d_plain_rows); dfree(c->d_rest_rows); dfree(c->d_err); dfree(c->d_mlp_frag); dfree(c->d_nut);
     if (c->st) cudaStreamDestroy(c->st);
+    if (c->st_side) cudaStreamDestroy(c->st_side);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     delete c;
     return LBM_OK;
 }

@@ -42,12 +42,25 @@ static cudaError_t step_parity(const Params& p, const RowLists* rl, cudaStream_t
             kp = odd ? k_step2_plain<S, COLL, CLOS, true> : k_step2_plain<S, COLL, CLOS, false>;
             ko = odd ? k_step2_list<S, COLL, CLOS, true> : k_step2_list<S, COLL, CLOS, false>;
         }
-        if (rl->n_plain > 0) {
-            kp<<<(unsigned)rl->n_plain * xb, b, 0, st>>>(p, rl->plain);
+        const bool fork = rl->side && rl->n_other > 0 && rl->n_plain > 0;
+        cudaStream_t so = fork ? rl->side : st;
+        if (fork) {
+            cudaError_t e = cudaEventRecord(rl->fork, st);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(rl->side, rl->fork, 0);
+            if (e != cudaSuccess) return e;
+        }
+        if (rl->n_other > 0) {
+            ko<<<(unsigned)rl->n_other * xb, b, 0, so>>>(p, rl->other);
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) return e;
         }
-        if (rl->n_other > 0) ko<<<(unsigned)rl->n_other * xb, b, 0, st>>>(p, rl->other);
+        if (rl->n_plain > 0) kp<<<(unsigned)rl->n_plain * xb, b, 0, st>>>(p, rl->plain);
+        if (fork) {
+            cudaError_t e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaEventRecord(rl->join, rl->side);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(st, rl->join, 0);
+            if (e != cudaSuccess) return e;
+        }
     } else {
         const int half = (p.nx + 1) / 2;  // one thread per x-pair
         dim3 g = cell_grid(half, p.ny, p.nz), b = cell_block(half);
@@ -150,7 +163,7 @@ cudaError_t launch_read(const Params& p, const ReadOut& o, cudaStream_t st) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || !(o.mode & (READ_DIAG | READ_ERROR))) return e;
     const int q0 = (o.mode & READ_DIAG) ? RED_MASS : RED_ERR1, q1 = (o.mode & READ_ERROR) ? RED_COUNT : RED_ERR1;
-    k_read_final<S><<<1, kFinalThreads, 0, st>>>(o.part, (long long)g.x * g.y * g.z, q0, q1, o.red);
+    k_read_final<S><<<q1 - q0, kFinalThreads, 0, st>>>(o.part, (long long)g.x * g.y * g.z, q0, o.red);
     return cudaGetLastError();
 }
 

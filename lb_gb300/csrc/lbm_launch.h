@@ -18,6 +18,10 @@ struct RowLists {
     int n_plain = 0;
     const int32_t* other = nullptr;
     int n_other = 0;
+    // the remaining rows run on `side`, forked from and joined back into the step's stream, so their
+    // slow per-cell path overlaps the plain rows instead of trailing them (nullptr: same stream)
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
 };
 
 // returns cudaSuccess or the launch error; rl == nullptr: one launch over the lattice
