@@ -6,6 +6,7 @@ the bounds stated beside it.
     python -m pytest tests/test_validate_configs.py --run-slow -m gpu -k c3      (512x256x256, 20k steps)
     python -m pytest tests/test_validate_configs.py --run-slow -m gpu -k c4      (384x192x192, 4k steps)
     python -m pytest tests/test_validate_configs.py --run-slow -m gpu -k c5      (256^3 LES, 1024^3 fine run)
+    python -m pytest tests/test_validate_configs.py --run-slow -m gpu -k c2      (learned closure a priori)
 
 c1: lid-driven cavity 64^3, FP64 cumulant on the GPU against the CPU oracle's FP64 run of the same case
     (parity of the whole 10k-step trajectory), FP32 against FP64; centre-line profiles.
@@ -21,6 +22,10 @@ c5: periodic decaying turbulence, coarse 256^3 and a 4x-finer run of the same se
     A posteriori: coarse LES in FP16-deviation storage with each closure from the filtered initial
     field, against the filtered fine field after the same physical time.  Throughput of both closures
     on the coarse lattice.
+c2 a priori: the shipped channel model on a channel realisation with another seed (1024x256x256 FP32,
+    snapshots after 30k, 33k, 36k and 39k steps): subgrid-stress and dissipation errors per snapshot of
+    the network, of Smagorinsky with the training samples' fitted constant, with the snapshot's own
+    fitted constant and with CLES 0.17 (mean and spread over the snapshots).
 LBM_VALIDATE_SMALL=1 runs reduced sizes for a quick look (the bounds are then not asserted).
 """
 import json
@@ -173,6 +178,51 @@ def _box(f, w):
     return f.reshape(nz // w, w, ny // w, w, nx // w, w).mean(axis=(1, 3, 5))
 
 
+def c2_a_priori(fine, warmup, every, snapshots, seed, model_path):
+    """The shipped channel model on channel realisations it never saw: a run of the config-2 channel on the
+    fine lattice with another seed, filtered samples at several times; per snapshot the relative
+    subgrid-stress and dissipation errors of the network, of Smagorinsky with the constant fitted to the
+    model's training samples (lb_gb300/data/les_mlp_channel.json), with the constant fitted to that very
+    snapshot (the best any constant can do there) and with CLES 0.17."""
+    from lb_gb300 import les
+    model = les.MlpModel.load(model_path)
+    with open(model_path.replace(".npz", ".json")) as fh:
+        c_train = json.load(fh)["best_constant"]
+    c = cases.channel(*fine, re_tau=180.0, u_max=0.05, amp=0.05, modes=0.25, seed=seed)
+    s = Solver(fine, turbulence=OmegaLES, storage="f32", nu=c["nu"], cles=0.17, periodic=c["periodic"],
+               force=c["force"])
+    s.set_flags(c["flags"])
+    s.set_bc()
+    s.init_fields(c["rho"], c["u"])
+    s.step(warmup)
+    rows = []
+    for k in range(snapshots):
+        if k:
+            s.step(every)
+        smp = s.les_samples(4)
+        nu_net, ok = les.evaluate(model, smp[:, :7])
+        nu = np.where(ok, nu_net, les.smagorinsky_nu(smp, 0.17))
+        c_self = les.best_constant(smp)
+        rows.append({"step": warmup + k * every, "samples": int(smp.shape[0]), "in_range": float(ok.mean()),
+                     "sgs_mlp": les.sgs_error(nu, smp),
+                     "sgs_const_train": les.sgs_error(les.smagorinsky_nu(smp, c_train), smp),
+                     "sgs_const_self": les.sgs_error(les.smagorinsky_nu(smp, c_self), smp),
+                     "sgs_cles_0.17": les.sgs_error(les.smagorinsky_nu(smp, 0.17), smp),
+                     "diss_mlp": les.sgs_dissipation_error(nu, smp),
+                     "diss_const_train": les.sgs_dissipation_error(les.smagorinsky_nu(smp, c_train), smp),
+                     "diss_const_self": les.sgs_dissipation_error(les.smagorinsky_nu(smp, c_self), smp)})
+    s.close()
+    out = {"config": "C2 channel, learned closure a priori on unseen realisations", "fine": list(fine),
+           "seed": seed, "model": os.path.relpath(model_path, ROOT), "const_train": c_train, "snapshots": rows}
+    for key in ("sgs_mlp", "sgs_const_train", "sgs_const_self", "diss_mlp", "diss_const_train", "diss_const_self"):
+        v = np.array([r[key] for r in rows])
+        out[key + "_mean"] = float(v.mean())
+        out[key + "_min_max"] = [float(v.min()), float(v.max())]
+    gain = np.array([r["sgs_const_self"] - r["sgs_mlp"] for r in rows])
+    out["sgs_gain_over_self_fitted_constant_mean_std"] = [float(gain.mean()), float(gain.std())]
+    return out
+
+
 def c5(n, steps, k, models):
     """models: {name: path of an lb_gb300.les.MlpModel}."""
     from lb_gb300 import les
@@ -282,6 +332,18 @@ def test_c4_body(built_lib, oracle_lib):
     assert r["f64_nonfinite"] == 0 and r["f32_nonfinite"] == 0
     if not SMALL:
         assert r["drag_x_rel_diff_f32_vs_f64"] <= 1e-3
+
+
+def test_c2_learned_closure_a_priori(built_lib):
+    fine = (256, 64, 64) if SMALL else (1024, 256, 256)
+    warmup, every = (2000, 500) if SMALL else (30000, 3000)
+    r = c2_a_priori(fine, warmup, every, 4, cases.SEED + 2,
+                    os.path.join(ROOT, "lb_gb300", "data", "les_mlp_channel.npz"))
+    _record("c2_a_priori", r)
+    if SMALL:
+        return
+    assert r["sgs_mlp_mean"] < r["sgs_const_train_mean"]
+    assert r["diss_mlp_mean"] < r["diss_const_train_mean"]
 
 
 def test_c5_learned_closure(built_lib):
