@@ -230,14 +230,14 @@ __global__ void __launch_bounds__(128) k_init(Params p, const double* rho_f, con
         f[V] = cl == CLS_SOLID ? (R)0 : (pops ? (R)pops[V * N + c.idx] : feq<V>(r, ux, uy, uz, u2));
     });
     if constexpr (S::kind == 2) {
-        // FP16 deviations of the initial state: one random stream per cell (the packed stores' LCG and
-        // cvt.rs, lower field), a hash of the cell index and the step seed; sr_step_seed of this launch
-        uint32_t s = mix32((uint32_t)c.idx ^ p.sr_step_seed);
+        // FP16 deviations of the initial state: the packed stores' rounding (cvt.rs, lower field) with one
+        // seed per cell, a hash of the cell index and this launch's step seed
+        const uint32_t s = sr_seed_pair((uint32_t)c.idx, p);
         __half* A = (__half*)p.f;
         sfor<0, 27>([&](auto vc) {
             constexpr int V = decltype(vc)::value;
             const float e = fmaf(f[V], p.scale, p.nwrs[V]);
-            const __half2 h = half2_sr(make_float2(e, 0.0f), lcg_next(s, p));
+            const __half2 h = half2_sr(make_float2(e, 0.0f), s + p.sr_off[V]);
             A[V * N + c.idx] = __low2half(h);
         });
     } else {

@@ -146,8 +146,9 @@ static Params make_params(const lbm_ctx* c) {
     p.has_force = (p.F[0] != 0.0 || p.F[1] != 0.0 || p.F[2] != 0.0) ? 1 : 0;
     p.rho0 = (float)c->cfg.rho0;
     p.f16_sr = (c->cfg.storage == LBM_STORAGE_F16DEV && !(c->cfg.options & LBM_OPT_F16_ROUND_NEAREST)) ? 1 : 0;
-    p.lcg_a = p.f16_sr ? kLcgA : 0u;
-    p.lcg_c = p.f16_sr ? kLcgC : kHalfStepState;
+    p.sr_mul = p.f16_sr ? 1u : 0u;
+    p.sr_add = p.f16_sr ? 0u : kHalfStep2x;
+    for (int v = 0; v < 27; v++) p.sr_off[v] = p.f16_sr ? (uint32_t)v * kSrWeyl : 0u;
     p.scale = std::ldexp(1.0f, c->cfg.f16_scale_log2);
     p.inv_scale = std::ldexp(1.0f, -c->cfg.f16_scale_log2);
     p.scale2 = make_float2(p.scale, p.scale);
@@ -289,9 +290,12 @@ lbm_status lbm_create(const lbm_config* cfg, lbm_ctx** out) {
     c->N = N;
     c->esize = cfg->storage == LBM_STORAGE_F64 ? 8 : cfg->storage == LBM_STORAGE_F32 ? 4 : 2;
     lbm_status s = LBM_OK;
+    int lo_prio = 0, hi_prio = 0;  // the side stream of the split step runs at the highest priority, so
+                                   // its slow boundary rows start first and the plain rows fill around them
     if ((e = cudaSetDevice(cfg->device)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking)) != cudaSuccess ||
-        (e = cudaStreamCreateWithFlags(&c->st_side, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio)) != cudaSuccess ||
+        (e = cudaStreamCreateWithPriority(&c->st_side, cudaStreamNonBlocking, hi_prio)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaMalloc(&c->d_f, 27 * (size_t)N * c->esize)) != cudaSuccess ||

@@ -80,8 +80,9 @@ struct Params {
     int f16_sr;              // FP16 stores round stochastically (else to nearest)
     uint32_t sr_step_seed;   // step_seed(m)
     float raw_rho, raw_mdiag;  // sum_v w_v rho0 and sum_v w_v rho0 c_vx^2 of the FP16 codec's references
-    uint32_t lcg_a, lcg_c;   // the packed path's random stream s -> a s + c: the LCG below when rounding
-                             // stochastically, a = 0 and c = kHalfStepState when to nearest (half2_sr)
+    uint32_t sr_mul, sr_add; // packed FP16 stores: seed = hash * sr_mul + sr_add (sr_seed_pair)
+    uint32_t sr_off[27];     // packed FP16 stores: rounding bits of direction v = seed + sr_off[v]
+                             // (v kSrWeyl when rounding stochastically, 0 when to nearest)
     float wr[27];            // w_v rho0            (decode f = h 2^-s + w_v rho0)
     float nwrs[27];          // -w_v rho0 2^s       (encode h = f 2^s - w_v rho0 2^s)
     float2 wr2[27], nwrs2[27];  // the same as (x, x) pairs for the packed two-cell path
@@ -155,28 +156,23 @@ LBM_D uint32_t sr_seed(unsigned long long e, int m) {
 // the step's part of sr_seed for indices below 2^32 (the packed paths' pair indices), hashed once per
 // launch on the host: sr_seed(e, m) == mix32(e ^ step_seed(m)) for such e
 LBM_HD uint32_t step_seed(int m) { return mix32((uint32_t)m * 0x9E3779B9u); }
-LBM_D uint32_t sr_seed_pair(uint32_t e, const Params& p) { return mix32(e ^ p.sr_step_seed); }
-// next 32 random bits of a per-thread stream (32-bit LCG of Numerical Recipes, a = 1664525,
-// c = 1013904223)
-constexpr uint32_t kLcgA = 1664525u, kLcgC = 1013904223u;
-LBM_D uint32_t lcg_next(uint32_t& s, const Params& p) {
-    s = s * p.lcg_a + p.lcg_c;
-    return s;
-}
+// The packed paths draw one 32-bit seed per pair (or per cell) from this hash and give direction v the
+// bits seed + v K (K = kSrWeyl, a Weyl sequence: additions on the integer ALU pipe; an integer
+// multiply per direction would compete with the collision's FP32 work for the FMA pipe, which bounds
+// the FP16 step).  Every field of seed + v K is uniform when the seed is, so each rounding stays
+// unbiased; the 27 directions of a pair get evenly spread dithers.  Round-to-nearest takes the same
+// instructions: seed = hash * 0 + kHalfStep2x (Params::sr_mul, sr_add) and offsets sr_off[v] = 0.
+constexpr uint32_t kSrWeyl = 0x9E3779B9u;
+constexpr uint32_t kHalfStep2x = (0x1000u << 16) | 0x1000u;  // a half step in both cvt.rs fields
+LBM_D uint32_t sr_seed_pair(uint32_t e, const Params& p) { return mix32(e ^ p.sr_step_seed) * p.sr_mul + p.sr_add; }
 LBM_D __half half_sr(float v, uint32_t r13) { return __float2half_rz(__uint_as_float(__float_as_uint(v) + r13)); }
 // the same dither with a fixed half step instead of random bits rounds to nearest (ties away from zero)
 constexpr uint32_t kHalfStep13 = 0x1000u;  // for half_sr
 // Packed stores: cvt.rs.f16x2.f32 (sm_100 family) rounds both values stochastically in one instruction,
 // adding the 13-bit fields rbits[28:16] (upper half) and rbits[12:0] (lower half) below the FP16
 // mantissa of the FP32 patterns and truncating: the method of half_sr (the field layout was measured
-// on a GB300 against a software model, bit for bit on 65,536 inputs).  Each field must be uniform for
-// the rounding to be unbiased.  rbits = s ^ (s >> 16) of the LCG state s: the upper field is s[28:16],
-// the lower s[12:0] ^ s[28:16] (the weak low LCG bits, bit k of period 2^(k+1), whitened by the high
-// ones).  The state's own transform gives round-to-nearest with the same instructions: a = 0,
-// c = kHalfStepState keeps s fixed at the value whose rbits is a half step in both fields.
-constexpr uint32_t kHalfStepState = 0x10000000u;  // rbits = 0x10001000
-LBM_D __half2 half2_sr(float2 v, uint32_t s) {
-    const uint32_t r = s ^ (s >> 16);
+// on a GB300 against a software model, bit for bit on 65,536 inputs).
+LBM_D __half2 half2_sr(float2 v, uint32_t r) {
     uint32_t h;
     asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(h) : "f"(v.y), "f"(v.x), "r"(r));  // upper v.y, lower v.x
     return *reinterpret_cast<__half2*>(&h);

@@ -296,7 +296,7 @@ LBM_D void load_pair(const Params& p, const PairIdx& q, const PairCodec& k, F2 (
 template <class S, bool ODD>
 LBM_D void store_pair(const Params& p, const PairIdx& q, const PairCodec& k, const F2 (&f)[27]) {
     using T = typename S::T;
-    uint32_t rs = 0;  // stochastic-rounding stream of the pair (FP16)
+    uint32_t rs = 0;  // stochastic-rounding seed of the pair (FP16)
     if constexpr (S::kind == 2) rs = sr_seed_pair((uint32_t)q.e0, p);
     sfor<0, 27>([&](auto vc) {
         constexpr int V = decltype(vc)::value;
@@ -308,7 +308,7 @@ LBM_D void store_pair(const Params& p, const PairIdx& q, const PairCodec& k, con
             else *(float2*)(a + q.e0) = f[V].v;
         } else {
             const F2 e = lfma(f[V], k.scale, k.nwrs[csq(V)]);
-            const __half2 h = half2_sr(e.v, lcg_next(rs, p));
+            const __half2 h = half2_sr(e.v, rs + p.sr_off[V]);
             if constexpr (split) { a[i0] = __low2half(h); a[i1] = __high2half(h); }
             else *(__half2*)(a + q.e0) = h;
         }
@@ -360,7 +360,7 @@ template <class S, bool ODD>
 LBM_D void store_pair_rows(const Params& p, const PairRows& w, const PairCodec& k, const F2 (&f)[27]) {
     using T = typename S::T;
     T* A = (T*)p.f;
-    uint32_t rs = 0;  // stochastic-rounding stream of the pair (FP16), seeded by the pair's first cell
+    uint32_t rs = 0;  // stochastic-rounding seed of the pair (FP16), seeded by the pair's first cell
     if constexpr (S::kind == 2) rs = sr_seed_pair((uint32_t)(w.R[1][1] + w.x0), p);
     sfor<0, 27>([&](auto vc) {
         constexpr int V = decltype(vc)::value;
@@ -374,7 +374,7 @@ LBM_D void store_pair_rows(const Params& p, const PairRows& w, const PairCodec& 
             else *(float2*)(a + w.x0) = f[V].v;
         } else {
             const F2 e = lfma(f[V], k.scale, k.nwrs[csq(V)]);
-            const __half2 h = half2_sr(e.v, lcg_next(rs, p));
+            const __half2 h = half2_sr(e.v, rs + p.sr_off[V]);
             if constexpr (split) { a[i0] = __low2half(h); a[i1] = __high2half(h); }
             else *(__half2*)(a + w.x0) = h;
         }
@@ -498,8 +498,10 @@ __global__ void __launch_bounds__(128, step2_min_blocks(COLL)) k_step2(Params p)
 // threads as two launches gives the same result as one launch over the lattice.
 // Grid: one dimension, rows x blocks of 128 x-pairs, the blocks of a row adjacent (as in the one-launch
 // grid, so neighbouring rows run together); row_block() splits the block index.
+// resident CTAs per SM for the plain-row kernel (cumulant-2015), measured at 512x256x256 FP16: 7 (72
+// registers, 16 bytes spilled on odd steps) 42.5 GLUPS against 40.9 at 6 (80 registers) and less at 5
 #ifndef LBM_PLAIN_MIN_BLOCKS
-#define LBM_PLAIN_MIN_BLOCKS 6
+#define LBM_PLAIN_MIN_BLOCKS 7
 #endif
 #ifndef LBM_PLAIN_MIN_BLOCKS_SRT
 #define LBM_PLAIN_MIN_BLOCKS_SRT 4
@@ -507,8 +509,13 @@ __global__ void __launch_bounds__(128, step2_min_blocks(COLL)) k_step2(Params p)
 #ifndef LBM_PLAIN_MIN_BLOCKS_CUM17
 #define LBM_PLAIN_MIN_BLOCKS_CUM17 4
 #endif
-constexpr int plain_min_blocks(int coll) {
-    return coll == 0 ? LBM_PLAIN_MIN_BLOCKS_SRT : coll == 2 ? LBM_PLAIN_MIN_BLOCKS_CUM17 : LBM_PLAIN_MIN_BLOCKS;
+// FP32 storage (HBM-bound at 80 registers, no spill): as k_step2
+#ifndef LBM_PLAIN_MIN_BLOCKS_F32
+#define LBM_PLAIN_MIN_BLOCKS_F32 LBM_STEP2_MIN_BLOCKS
+#endif
+constexpr int plain_min_blocks(int coll, int kind = 2) {
+    return coll == 0 ? LBM_PLAIN_MIN_BLOCKS_SRT : coll == 2 ? LBM_PLAIN_MIN_BLOCKS_CUM17
+         : kind == 1 ? LBM_PLAIN_MIN_BLOCKS_F32 : LBM_PLAIN_MIN_BLOCKS;
 }
 // blocks of 128 x-pairs per row: blockIdx.x = list entry * xb + block within the row
 LBM_D void row_block(const Params& p, const int32_t* rows, int& r, int& x0) {
@@ -518,7 +525,7 @@ LBM_D void row_block(const Params& p, const int32_t* rows, int& r, int& x0) {
     x0 = 2 * (int)(bx * blockDim.x + threadIdx.x);
 }
 template <class S, int COLL, int CLOS, bool ODD>
-__global__ void __launch_bounds__(128, plain_min_blocks(COLL)) k_step2_plain(Params p, const int32_t* rows) {
+__global__ void __launch_bounds__(128, plain_min_blocks(COLL, S::kind)) k_step2_plain(Params p, const int32_t* rows) {
     int r, x0;
     row_block(p, rows, r, x0);
     if (x0 >= p.nx) return;

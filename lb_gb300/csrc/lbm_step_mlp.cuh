@@ -24,18 +24,20 @@ namespace lbm {
 #ifndef LBM_MLP_MIN_BLOCKS
 #define LBM_MLP_MIN_BLOCKS 0
 #endif
+// the plain-row kernel that runs the network: 6 (80 registers) measured 24.2 GLUPS against 23.2 with no
+// request (102 registers on odd steps) and 23.5 at 5
 #ifndef LBM_MLP_PLAIN_MIN_BLOCKS
-#define LBM_MLP_PLAIN_MIN_BLOCKS LBM_MLP_MIN_BLOCKS
+#define LBM_MLP_PLAIN_MIN_BLOCKS 6
 #endif
 // ROWS: 0 one launch over the lattice (grid x = pair block, y, z); 1 the plain rows of the split step
 // (every pair a packed bulk pair off the y/z seams, lbm_step.cuh); 2 the remaining rows (1-D grid of
 // listed rows x pair blocks, row_block)
-constexpr int mlp_min_blocks(int mode, int rows, int coll) {
-    return mode == 2 ? (rows == 1 ? plain_min_blocks(coll) : step2_min_blocks(coll))
+constexpr int mlp_min_blocks(int mode, int rows, int coll, int kind) {
+    return mode == 2 ? (rows == 1 ? plain_min_blocks(coll, kind) : step2_min_blocks(coll))
                      : (rows == 1 ? LBM_MLP_PLAIN_MIN_BLOCKS : LBM_MLP_MIN_BLOCKS);
 }
 template <class S, int COLL, bool ODD, int MODE, int ROWS = 0>
-__global__ void __launch_bounds__(128, mlp_min_blocks(MODE, ROWS, COLL)) k_step2_mlp(Params p, const int32_t* rows) {
+__global__ void __launch_bounds__(128, mlp_min_blocks(MODE, ROWS, COLL, S::kind)) k_step2_mlp(Params p, const int32_t* rows) {
     static_assert(S::kind != 0, "the learned closure runs on the packed FP32 path");
     __shared__ uint4 wf[MODE == 2 ? 1 : kMlpFragRows][32];
     __shared__ uint4 stage[MODE == 2 ? 1 : 4][64];

@@ -151,7 +151,7 @@ LBM_D void row_from_stage(const Params& p, typename S::T* buf, int y, int z, con
             else *(float2*)a = f[V].v;
         } else {
             const F2 e = lfma(f[V], k.scale, k.nwrs[csq(V)]);
-            const __half2 h = half2_sr(e.v, lcg_next(rs, p));
+            const __half2 h = half2_sr(e.v, rs + p.sr_off[V]);
             if constexpr (sh != 0) { a[0] = __low2half(h); a[1] = __high2half(h); }
             else *(__half2*)a = h;
         }
