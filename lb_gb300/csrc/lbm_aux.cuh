@@ -22,7 +22,7 @@ struct ReadOut {
     double* u;     // 3N
     double* f;     // 27N
     double* red;   // RED_COUNT
-    double* uerr;  // 3N (error monitor's previous velocity)
+    void* uerr;    // 3N of S::R (error monitor's previous velocity)
     double* part;  // READ_DIAG / READ_ERROR: per-block partial sums [RED_COUNT][blocks] (read_part_size)
     int mode;
     int ref_compat_err;  // reproduce the ErrorQuadratic z-term typo
@@ -53,15 +53,68 @@ LBM_D double warp_max(double v) {
     return v;
 }
 
-// block sum (max for RED_VMAX) of the quantities [q0, q1) in a fixed order, written as this block's
-// partial; every thread of the block calls it
-template <int Q0, int Q1>
-LBM_D void block_partials(double (&v)[RED_COUNT], double* part, long long nblk) {
+// per-thread partial sums of the reductions: FP64 for FP64 storage; for FP32 and FP16 storage a
+// compensated FP32 pair per quantity (GB300's FP64 pipe runs about one lane per cycle per SM, which
+// made the FP64 sums the read kernel's bound), converted to FP64 once per warp
+template <class R>
+struct RedAcc {
+    double v[RED_COUNT];
+    R vmax;
+    int nbad, nfluid;
+    LBM_D RedAcc() : vmax((R)0), nbad(0), nfluid(0) {
+#pragma unroll
+        for (int q = 0; q < RED_COUNT; q++) v[q] = 0.0;
+    }
+    LBM_D void add(int q, double x) { v[q] += x; }
+    LBM_D double warp_total(int q) const { return warp_sum(v[q]); }
+};
+template <>
+struct RedAcc<float> {
+    FSum v[RED_COUNT];
+    float vmax;
+    int nbad, nfluid;
+    LBM_D RedAcc() : vmax(0.0f), nbad(0), nfluid(0) {
+#pragma unroll
+        for (int q = 0; q < RED_COUNT; q++) v[q] = FSum{0.0f, 0.0f};
+    }
+    LBM_D void add(int q, float x) { fsum_add(v[q], x); }
+    LBM_D double warp_total(int q) const {
+        FSum s = v[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const FSum t{__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)};
+            fsum_merge(s, t);
+        }
+        return f2d(s.hi) + f2d(s.lo);
+    }
+};
+LBM_D double to_double(double x) { return x; }
+LBM_D double to_double(float x) { return f2d(x); }
+template <class R> LBM_D R to_real(double x) { if constexpr (std::is_same<R, float>::value) return d2f(x); else return x; }
+
+// block totals of the quantities [Q0, Q1) (the largest |u|^2 for RED_VMAX, counts exact in integers),
+// warp by warp and then over the block's warps in a fixed order, written as this block's partial;
+// every thread of the block calls it
+template <int Q0, int Q1, class R>
+LBM_D void block_partials(const RedAcc<R>& a, double* part, long long nblk) {
     __shared__ double sh[RED_COUNT][4];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
     for (int q = Q0; q < Q1; q++) {
-        const double s = q == RED_VMAX ? warp_max(v[q]) : warp_sum(v[q]);
+        double s;
+        if (q == RED_VMAX) {
+            R m = a.vmax;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const R t = __shfl_xor_sync(0xffffffffu, m, o);
+                m = t > m ? t : m;
+            }
+            s = to_double(m);
+        } else if (q == RED_BAD || q == RED_FLUID) {
+            s = (double)__reduce_add_sync(0xffffffffu, (unsigned)(q == RED_BAD ? a.nbad : a.nfluid));
+        } else {
+            s = a.warp_total(q);
+        }
         if (lane == 0) sh[q][wid] = s;
     }
     __syncthreads();
@@ -80,10 +133,8 @@ __global__ void __launch_bounds__(128) k_read(Params p, ReadOut o) {
     using R = typename S::R;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = x < p.nx;
-    double v[RED_COUNT];
-#pragma unroll
-    for (int q = 0; q < RED_COUNT; q++) v[q] = 0.0;
-    long long nfluid = 0, nbad = 0;
+    RedAcc<R> acc;
+    R* uerr = (R*)o.uerr;
     for (int k = 0; k < kReadZ; k++) {
         const int z = blockIdx.z * kReadZ + k;
         if (z >= p.nz) break;
@@ -106,12 +157,12 @@ __global__ void __launch_bounds__(128) k_read(Params p, ReadOut o) {
         R rho = 0, jx = 0, jy = 0, jz = 0, ux = 0, uy = 0, uz = 0;
         if (live && cl != CLS_SOLID) moments(f, p, rho, jx, jy, jz, ux, uy, uz);
         if (live && (o.mode & READ_MOMENTS)) {
-            o.rho[c.idx] = rho;
-            o.u[c.idx] = ux; o.u[p.N + c.idx] = uy; o.u[2 * p.N + c.idx] = uz;
+            o.rho[c.idx] = to_double(rho);
+            o.u[c.idx] = to_double(ux); o.u[p.N + c.idx] = to_double(uy); o.u[2 * p.N + c.idx] = to_double(uz);
         }
         if (live && (o.mode & READ_POPS)) {
 #pragma unroll
-            for (int q = 0; q < 27; q++) o.f[q * p.N + c.idx] = f[q];
+            for (int q = 0; q < 27; q++) o.f[q * p.N + c.idx] = to_double(f[q]);
         }
         if (live && (o.mode & READ_ACC) && cl != CLS_SOLID) {
             double* a = p.acc;
@@ -124,41 +175,37 @@ __global__ void __launch_bounds__(128) k_read(Params p, ReadOut o) {
             bool ok = true;
 #pragma unroll
             for (int q = 0; q < 27; q++) ok = ok && isfinite(f[q]);
-            v[RED_MASS] += rho;
-            v[RED_MX] += (double)rho * ux; v[RED_MY] += (double)rho * uy; v[RED_MZ] += (double)rho * uz;
+            acc.add(RED_MASS, rho);
+            acc.add(RED_MX, rho * ux); acc.add(RED_MY, rho * uy); acc.add(RED_MZ, rho * uz);
             if (cl != CLS_BULK) {  // only cells beside a solid have momentum-exchange links
-                v[RED_DX] += drag[0]; v[RED_DY] += drag[1]; v[RED_DZ] += drag[2];
+                acc.add(RED_DX, drag[0]); acc.add(RED_DY, drag[1]); acc.add(RED_DZ, drag[2]);
             }
             const R u2 = ux * ux + uy * uy + uz * uz;
-            if (isfinite((double)u2)) v[RED_VMAX] = fmax(v[RED_VMAX], (double)u2);
-            nbad += ok ? 0 : 1;
-            nfluid += 1;
+            if (isfinite(u2) && u2 > acc.vmax) acc.vmax = u2;
+            acc.nbad += ok ? 0 : 1;
+            acc.nfluid += 1;
         }
         if (o.mode & READ_ERROR) {
             // ErrorQuadratic.h:33-78: sum sqrt|u - u_prev|^2 and sqrt|u|^2 over flag == 1 cells
             if (live && (fl & BIT_REFBULK)) {
-                const R px = (R)o.uerr[c.idx], py = (R)o.uerr[p.N + c.idx], pz = (R)o.uerr[2 * p.N + c.idx];
+                const R px = uerr[c.idx], py = uerr[p.N + c.idx], pz = uerr[2 * p.N + c.idx];
                 const R dx = ux - px, dy = uy - py;
                 const R dz = o.ref_compat_err ? uy - pz : uz - pz;
                 const R a1 = dx * dx + dy * dy + dz * dz;
                 const R a2 = ux * ux + uy * uy + uz * uz;
-                v[RED_ERR1] += (double)sqrt(a1);
-                v[RED_ERR2] += (double)sqrt(a2);
+                acc.add(RED_ERR1, sqrt(a1));
+                acc.add(RED_ERR2, sqrt(a2));
             }
             if (live) {  // copy u -> u_error (:80-90), every cell
-                o.uerr[c.idx] = ux; o.uerr[p.N + c.idx] = uy; o.uerr[2 * p.N + c.idx] = uz;
+                uerr[c.idx] = ux; uerr[p.N + c.idx] = uy; uerr[2 * p.N + c.idx] = uz;
             }
         }
     }
     const long long nblk = (long long)gridDim.x * gridDim.y * gridDim.z;
-    if (o.mode & READ_DIAG) {
-        v[RED_BAD] = (double)nbad;
-        v[RED_FLUID] = (double)nfluid;
-        block_partials<RED_MASS, RED_ERR1>(v, o.part, nblk);
-    }
+    if (o.mode & READ_DIAG) block_partials<RED_MASS, RED_ERR1>(acc, o.part, nblk);
     if (o.mode & READ_ERROR) {
         if (o.mode & READ_DIAG) __syncthreads();
-        block_partials<RED_ERR1, RED_COUNT>(v, o.part, nblk);
+        block_partials<RED_ERR1, RED_COUNT>(acc, o.part, nblk);
     }
 }
 
@@ -214,8 +261,9 @@ __global__ void __launch_bounds__(128) k_init(Params p, const double* rho_f, con
     make_cell(p, x, blockIdx.y, blockIdx.z, c);
     const int cl = p.cls[c.idx] & CLS_MASK;
     const long long N = p.N;
-    R r = (R)rho0, ux = (R)u0x, uy = (R)u0y, uz = (R)u0z;
-    if (rho_f) { r = (R)rho_f[c.idx]; ux = (R)u_f[c.idx]; uy = (R)u_f[N + c.idx]; uz = (R)u_f[2 * N + c.idx]; }
+    R r, ux, uy, uz;
+    if (rho_f) { r = to_real<R>(rho_f[c.idx]); ux = to_real<R>(u_f[c.idx]); uy = to_real<R>(u_f[N + c.idx]); uz = to_real<R>(u_f[2 * N + c.idx]); }
+    else { r = to_real<R>(rho0); ux = to_real<R>(u0x); uy = to_real<R>(u0y); uz = to_real<R>(u0z); }
     if (cl == CLS_LID) {
         const int id = p.aux[c.idx];
         ux = p.lid_u[id]; uy = p.lid_u[p.n_lid + id]; uz = p.lid_u[2 * p.n_lid + id];
@@ -227,7 +275,7 @@ __global__ void __launch_bounds__(128) k_init(Params p, const double* rho_f, con
     const R u2 = ux * ux + uy * uy + uz * uz;
     sfor<0, 27>([&](auto vc) {
         constexpr int V = decltype(vc)::value;
-        f[V] = cl == CLS_SOLID ? (R)0 : (pops ? (R)pops[V * N + c.idx] : feq<V>(r, ux, uy, uz, u2));
+        f[V] = cl == CLS_SOLID ? (R)0 : (pops ? to_real<R>(pops[V * N + c.idx]) : feq<V>(r, ux, uy, uz, u2));
     });
     if constexpr (S::kind == 2) {
         // FP16 deviations of the initial state: the packed stores' rounding (cvt.rs, lower field) with one

@@ -67,7 +67,7 @@ struct lbm_ctx {
     double* d_acc = nullptr;
     bool avg_on = false;
     long long avg_begin = 0, avg_last = -1, avg_count = 0;
-    double* d_uerr = nullptr;
+    void* d_uerr = nullptr;     // error monitor's previous velocity, 3N of the storage's real type
     double* d_red = nullptr;
     double* d_part = nullptr;  // per-block partial sums of the reductions (read_part_size doubles)
     double *d_rho_out = nullptr, *d_u_out = nullptr, *d_f_out = nullptr;
@@ -796,7 +796,7 @@ static lbm_status init_common(lbm_ctx* c, const double* rho, const double* u, do
     if (c->d_out_save) CU(c, cudaMemset(c->d_out_save, 0, 2 * 18 * (size_t)c->n_out * real_size(c)));
     if (c->d_out_msave) CU(c, cudaMemset(c->d_out_msave, 0, 2 * 4 * (size_t)c->n_ms * real_size(c)));
     c->avg_on = false; c->avg_count = 0; c->avg_last = -1;
-    if (c->d_uerr) CU(c, cudaMemset(c->d_uerr, 0, 3 * N * 8));
+    if (c->d_uerr) CU(c, cudaMemset(c->d_uerr, 0, 3 * N * real_size(c)));
     c->initialized = true;
     return LBM_OK;
 }
@@ -989,8 +989,8 @@ lbm_status lbm_error_evaluation(lbm_ctx* c, double* err) {
     cudaSetDevice(c->cfg.device);
     const size_t N = (size_t)c->N;
     if (!c->d_uerr) {
-        CU(c, cudaMalloc(&c->d_uerr, 3 * N * 8));
-        CU(c, cudaMemsetAsync(c->d_uerr, 0, 3 * N * 8, c->st));
+        CU(c, cudaMalloc(&c->d_uerr, 3 * N * real_size(c)));
+        CU(c, cudaMemsetAsync(c->d_uerr, 0, 3 * N * real_size(c), c->st));
     }
     if (!c->d_part) CU(c, cudaMalloc(&c->d_part, read_part_size(c->cfg.nx, c->cfg.ny, c->cfg.nz) * sizeof(double)));
     ReadOut o{};

@@ -7,6 +7,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdint>
+
 #include <type_traits>
 
 namespace lbm {
@@ -80,6 +82,50 @@ LBM_D F2 rcp(F2 x) { return F2(__fdividef(1.0f, x.v.x), __fdividef(1.0f, x.v.y))
 LBM_D float sqrt_pos(float x) { x = fmaxf(x, 1e-30f); return x * rsqrtf(x); }
 LBM_D double sqrt_pos(double x) { return sqrt(x); }
 LBM_D F2 sqrt_pos(F2 x) { return F2(sqrt_pos(x.v.x), sqrt_pos(x.v.y)); }
+
+// ---- conversions between FP32 and FP64 on the integer pipe ---------------------------------------
+// GB300 executes FP64 instructions, conversions included, at about one lane per cycle per SM, so the
+// read and set-up kernels convert with integer operations: exact for every finite FP32 value, round to
+// nearest even for FP64 values in the FP32 normal range; zero keeps its sign; anything else (FP32
+// subnormal results, overflow, NaN) falls back to the hardware conversion.
+LBM_D double f2d(float x) {
+    const uint32_t b = __float_as_uint(x), e = (b >> 23) & 0xFFu;
+    if (e == 0u || e == 0xFFu) return (double)x;  // zero, subnormal, inf, NaN: exact either way
+    const uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7FFFFFu) >> 3);
+    const uint32_t lo = b << 29;
+    return __hiloint2double((int)hi, (int)lo);
+}
+LBM_D float d2f(double x) {
+    const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
+    const uint32_t e = (hi >> 20) & 0x7FFu;
+    if (e < 897u || e > 1149u) {  // zero or outside the FP32 normal range (2^-126 .. 2^127)
+        if (e == 0u && (hi & 0xFFFFFu) == 0u && lo == 0u) return __uint_as_float(hi & 0x80000000u);
+        return __double2float_rn(x);
+    }
+    // 23 kept mantissa bits, 29 dropped; round half to even; a carry moves into the exponent
+    uint32_t m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const uint32_t rem = lo & 0x1FFFFFFFu;
+    uint32_t b = (hi & 0x80000000u) | (((e - 896u) << 23) + m);
+    if (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) b += 1u;
+    return __uint_as_float(b);
+}
+
+// compensated FP32 sum (a float-float pair): TwoSum keeps each addition's rounding error in lo, so the
+// pair carries about 48 bits; used for the per-thread and per-warp partial sums of the reductions in
+// place of FP64 arithmetic
+struct FSum {
+    float hi, lo;
+};
+LBM_D void fsum_add(FSum& s, float x) {
+    const float t = s.hi + x;
+    const float bp = t - s.hi;
+    s.lo += (s.hi - (t - bp)) + (x - bp);
+    s.hi = t;
+}
+LBM_D void fsum_merge(FSum& s, const FSum& o) {
+    fsum_add(s, o.hi);
+    s.lo += o.lo;
+}
 
 // c . u with the zero components skipped at compile time
 template <int V, class L>

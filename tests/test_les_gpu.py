@@ -188,6 +188,10 @@ def test_trained_closure_beats_smagorinsky(built_lib):
 
 
 def test_fused_mlp_channel_is_stable_and_conserves_mass(built_lib):
+    """300 steps of the learned closure on a perturbed channel stay finite and keep the mass: to 2e-6 in
+    FP32; in FP16 storage every stored value carries an independent stochastic-rounding error (zero mean,
+    up to half an FP16 step, ~1e-5 in f here), so the mass does a random walk of about
+    sqrt(27 x 70k stores x 300 steps) x 5e-6 ~ 0.1 (1.5e-6 relative): the bound there is 1e-5 (~6 sigma)."""
     shape = (64, 34, 32)
     snaps, s, c = fine_channel(shape, 200, snapshots=(200,))
     s.close()
@@ -207,4 +211,4 @@ def test_fused_mlp_channel_is_stable_and_conserves_mass(built_lib):
         d1 = g.reduce()
         g.close()
         assert d1.nonfinite == 0
-        assert abs(d1.mass - d0.mass) <= 2e-6 * d0.mass
+        assert abs(d1.mass - d0.mass) <= (2e-6 if storage == "f32" else 1e-5) * d0.mass
