@@ -90,7 +90,8 @@ LBM_D F2 sqrt_pos(F2 x) { return F2(sqrt_pos(x.v.x), sqrt_pos(x.v.y)); }
 // subnormal results, overflow, NaN) falls back to the hardware conversion.
 LBM_D double f2d(float x) {
     const uint32_t b = __float_as_uint(x), e = (b >> 23) & 0xFFu;
-    if (e == 0u || e == 0xFFu) return (double)x;  // zero, subnormal, inf, NaN: exact either way
+    if ((b & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);  // signed zero
+    if (e == 0u || e == 0xFFu) return (double)x;  // subnormal, inf, NaN: exact either way
     const uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7FFFFFu) >> 3);
     const uint32_t lo = b << 29;
     return __hiloint2double((int)hi, (int)lo);
