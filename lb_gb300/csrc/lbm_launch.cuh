@@ -9,7 +9,14 @@
 
 namespace lbm {
 
-using RowKernel = void (*)(Params, const int32_t*);
+using RowKernel = void (*)(Params, const int32_t*, int);
+
+// grid of a row-list launch: x = blocks of 128 x-pairs per row, the n listed rows over y (at most
+// 65535) and z
+inline dim3 rows_grid(unsigned xb, int n) {
+    const unsigned gy = n < 65535 ? (unsigned)n : 65535u;
+    return dim3(xb, gy, ((unsigned)n + gy - 1u) / gy);
+}
 
 // the learned-closure kernel for this step's parity and network mode (p.nut == nullptr: the network
 // runs every step; else p.mlp_run says whether it runs in this step)
@@ -29,8 +36,7 @@ static cudaError_t step_parity(const Params& p, const RowLists* rl, cudaStream_t
         if (odd) k_step<S, COLL, CLOS, true><<<g, b, 0, st>>>(p);
         else     k_step<S, COLL, CLOS, false><<<g, b, 0, st>>>(p);
     } else if (rl) {
-        // split step: the plain rows, then the remaining rows (one thread per x-pair; 1-D grid of
-        // rows x blocks, split by row_block)
+        // split step: the remaining rows (side stream) and the plain rows, one thread per x-pair
         const int half = (p.nx + 1) / 2;
         const dim3 b = cell_block(half);
         const unsigned xb = (unsigned)((half + (int)b.x - 1) / (int)b.x);
@@ -50,11 +56,11 @@ static cudaError_t step_parity(const Params& p, const RowLists* rl, cudaStream_t
             if (e != cudaSuccess) return e;
         }
         if (rl->n_other > 0) {
-            ko<<<(unsigned)rl->n_other * xb, b, 0, so>>>(p, rl->other);
+            ko<<<rows_grid(xb, rl->n_other), b, 0, so>>>(p, rl->other, rl->n_other);
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) return e;
         }
-        if (rl->n_plain > 0) kp<<<(unsigned)rl->n_plain * xb, b, 0, st>>>(p, rl->plain);
+        if (rl->n_plain > 0) kp<<<rows_grid(xb, rl->n_plain), b, 0, st>>>(p, rl->plain, rl->n_plain);
         if (fork) {
             cudaError_t e = cudaGetLastError();
             if (e == cudaSuccess) e = cudaEventRecord(rl->join, rl->side);
@@ -65,7 +71,7 @@ static cudaError_t step_parity(const Params& p, const RowLists* rl, cudaStream_t
         const int half = (p.nx + 1) / 2;  // one thread per x-pair
         dim3 g = cell_grid(half, p.ny, p.nz), b = cell_block(half);
         if constexpr (CLOS == 2) {
-            mlp_kernel<S, COLL, 0>(p)<<<g, b, 0, st>>>(p, nullptr);
+            mlp_kernel<S, COLL, 0>(p)<<<g, b, 0, st>>>(p, nullptr, 0);
         } else {
             if (odd) k_step2<S, COLL, CLOS, true><<<g, b, 0, st>>>(p);
             else     k_step2<S, COLL, CLOS, false><<<g, b, 0, st>>>(p);

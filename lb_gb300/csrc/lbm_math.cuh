@@ -261,11 +261,13 @@ LBM_D Axis<L> make_axis(L u, L uu) {
     a.m2u = (L)-2.0f * u;
     return a;
 }
+// the three outputs add up to k0 (m + z + p = k0 for any u), so z = k0 - (m + p): two operations
+// instead of three
 template <class L>
 LBM_D void tri(L k0, L k1, L k2, const Axis<L>& a, L& m, L& z, L& p) {
     m = lfma(k0, a.A, lfma(k1, a.B, (L)0.5f * k2));
     p = m + lfma(k0, a.u, k1);
-    z = lfma(k0, a.C, lfma(a.m2u, k1, -k2));
+    z = k0 - (m + p);
 }
 template <class L>
 LBM_D void tri_k1zero(L k0, L k2, const Axis<L>& a, L& m, L& z, L& p) {  // k1 = 0

@@ -496,8 +496,8 @@ __global__ void __launch_bounds__(128, step2_min_blocks(COLL)) k_step2(Params p)
 // path alone.  k_step2_list runs the general pair step over the remaining rows.  Every population slot
 // is read and written by one thread only within a step (the AA argument), so running the two sets of
 // threads as two launches gives the same result as one launch over the lattice.
-// Grid: one dimension, rows x blocks of 128 x-pairs, the blocks of a row adjacent (as in the one-launch
-// grid, so neighbouring rows run together); row_block() splits the block index.
+// Grid: x = block of 128 x-pairs in the row, y and z = row in the list (rows_grid), so the blocks of a
+// row are adjacent and neighbouring rows run together, as in the one-launch grid.
 // resident CTAs per SM for the plain-row kernel (cumulant-2015), measured at 512x256x256 FP16: 7 (72
 // registers, 16 bytes spilled on odd steps) 42.5 GLUPS against 40.9 at 6 (80 registers) and less at 5
 #ifndef LBM_PLAIN_MIN_BLOCKS
@@ -517,25 +517,25 @@ constexpr int plain_min_blocks(int coll, int kind = 2) {
     return coll == 0 ? LBM_PLAIN_MIN_BLOCKS_SRT : coll == 2 ? LBM_PLAIN_MIN_BLOCKS_CUM17
          : kind == 1 ? LBM_PLAIN_MIN_BLOCKS_F32 : LBM_PLAIN_MIN_BLOCKS;
 }
-// blocks of 128 x-pairs per row: blockIdx.x = list entry * xb + block within the row
-LBM_D void row_block(const Params& p, const int32_t* rows, int& r, int& x0) {
-    const unsigned xb = (((unsigned)p.nx + 1u) / 2u + blockDim.x - 1u) / blockDim.x;
-    const unsigned e = blockIdx.x / xb, bx = blockIdx.x - e * xb;
+// blocks of 128 x-pairs per row: blockIdx.x = block within the row, list entry = blockIdx.y + gridDim.y
+// blockIdx.z (rows_grid); returns false for the tail blocks past the list
+LBM_D bool row_block(const int32_t* rows, int n, int& r, int& x0) {
+    const int e = (int)(blockIdx.y + gridDim.y * blockIdx.z);
+    if (e >= n) return false;
     r = rows[e];
-    x0 = 2 * (int)(bx * blockDim.x + threadIdx.x);
+    x0 = 2 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    return true;
 }
 template <class S, int COLL, int CLOS, bool ODD>
-__global__ void __launch_bounds__(128, plain_min_blocks(COLL, S::kind)) k_step2_plain(Params p, const int32_t* rows) {
+__global__ void __launch_bounds__(128, plain_min_blocks(COLL, S::kind)) k_step2_plain(Params p, const int32_t* rows, int n) {
     int r, x0;
-    row_block(p, rows, r, x0);
-    if (x0 >= p.nx) return;
+    if (!row_block(rows, n, r, x0) || x0 >= p.nx) return;
     step_pair_plain<S, COLL, CLOS, ODD>(p, r * p.nx + x0, x0);
 }
 template <class S, int COLL, int CLOS, bool ODD>
-__global__ void __launch_bounds__(128, step2_min_blocks(COLL)) k_step2_list(Params p, const int32_t* rows) {
+__global__ void __launch_bounds__(128, step2_min_blocks(COLL)) k_step2_list(Params p, const int32_t* rows, int n) {
     int r, x0;
-    row_block(p, rows, r, x0);
-    if (x0 >= p.nx) return;
+    if (!row_block(rows, n, r, x0) || x0 >= p.nx) return;
     step_pair<S, COLL, CLOS, ODD>(p, x0, r % p.ny, r / p.ny);
 }
 

@@ -37,7 +37,7 @@ constexpr int mlp_min_blocks(int mode, int rows, int coll, int kind) {
                      : (rows == 1 ? LBM_MLP_PLAIN_MIN_BLOCKS : LBM_MLP_MIN_BLOCKS);
 }
 template <class S, int COLL, bool ODD, int MODE, int ROWS = 0>
-__global__ void __launch_bounds__(128, mlp_min_blocks(MODE, ROWS, COLL, S::kind)) k_step2_mlp(Params p, const int32_t* rows) {
+__global__ void __launch_bounds__(128, mlp_min_blocks(MODE, ROWS, COLL, S::kind)) k_step2_mlp(Params p, const int32_t* rows, int nrows) {
     static_assert(S::kind != 0, "the learned closure runs on the packed FP32 path");
     __shared__ uint4 wf[MODE == 2 ? 1 : kMlpFragRows][32];
     __shared__ uint4 stage[MODE == 2 ? 1 : 4][64];
@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(128, mlp_min_blocks(MODE, ROWS, COLL, S::kind)
         y = blockIdx.y;
         z = blockIdx.z;
     } else {
-        row_block(p, rows, r, x0);
+        if (!row_block(rows, nrows, r, x0)) return;  // tail block past the list: the whole block leaves
         if constexpr (ROWS == 2) {
             y = r % p.ny;
             z = r / p.ny;
