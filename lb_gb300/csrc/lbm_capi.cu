@@ -18,6 +18,7 @@
 #include <cstring>
 #include <algorithm>
 #include <atomic>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -90,6 +91,12 @@ struct lbm_ctx {
 };
 
 static std::string g_err;
+
+// a[q[i]] = v[i] for the n listed cells (the side-table indices set at set-up)
+__global__ void k_scatter_aux(int32_t* a, const long long* q, const int32_t* v, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[q[i]] = v[i];
+}
 
 static lbm_status fail(lbm_ctx* c, lbm_status s, const char* fmt, ...) {
     char buf[512];
@@ -345,7 +352,9 @@ lbm_status lbm_destroy(lbm_ctx* c) {
 
 lbm_status lbm_set_flags(lbm_ctx* c, const int32_t* flags) {
     if (!c || !flags) return fail(c, LBM_ERR_INVALID, "lbm_set_flags: null argument");
-    c->flags.assign(flags, flags + c->N);
+    c->flags.resize((size_t)c->N);
+    int32_t* dst = c->flags.data();
+    host_parallel(c->N, [&](long long q0, long long q1) { std::memcpy(dst + q0, flags + q0, (size_t)(q1 - q0) * 4); });
     c->have_flags = true;
     c->have_geom = false;
     c->initialized = false;
@@ -381,8 +390,12 @@ static lbm_status build_geometry(lbm_ctx* c) {
         if (v < 0 || v >= n) { if (wrap[a]) v = (v + n) % n; else ok = false; }
         return v;
     };
-    std::vector<uint8_t> cls((size_t)N);
-    std::vector<int32_t> aux((size_t)N, -1);
+    // class byte and side-table index per cell (index -1: none), filled on the host cores
+    std::unique_ptr<uint8_t[]> cls_buf(new uint8_t[(size_t)N]);
+    std::unique_ptr<int32_t[]> aux_buf(new int32_t[(size_t)N]);
+    uint8_t* cls = cls_buf.get();
+    int32_t* aux = aux_buf.get();
+    host_parallel(N, [&](long long q0, long long q1) { std::fill(aux + q0, aux + q1, -1); });
     // moving-wall and Zou/He nodes share the 3-level side table: collided, never streamed into
     const bool lid_kind = c->cfg.inlet_kind == LBM_INLET_MOVING_WALL || c->cfg.inlet_kind == LBM_INLET_ZOU_HE;
     const int okind = c->cfg.outlet_kind;
@@ -651,8 +664,36 @@ static lbm_status build_geometry(lbm_ctx* c) {
     cudaSetDevice(c->cfg.device);
     free_side(c);
     c->sponge_axis = sp_axis; c->sponge_begin = sp_begin; c->sponge_slope = sp_slope;
-    CU(c, cudaMemcpyAsync(c->d_cls, cls.data(), (size_t)N, cudaMemcpyHostToDevice, c->st));
-    CU(c, cudaMemcpyAsync(c->d_aux, aux.data(), (size_t)N * 4, cudaMemcpyHostToDevice, c->st));
+    CU(c, cudaMemcpyAsync(c->d_cls, cls, (size_t)N, cudaMemcpyHostToDevice, c->st));
+    // side-table indices: -1 everywhere (every byte 0xff), then the few set entries scattered on the device
+    CU(c, cudaMemsetAsync(c->d_aux, 0xff, (size_t)N * 4, c->st));
+    {
+        std::vector<std::vector<long long>> part_q(64);
+        std::atomic<int> next{0};
+        host_parallel(N, [&](long long q0, long long q1) {
+            auto& v = part_q[(size_t)next.fetch_add(1)];
+            for (long long q = q0; q < q1; q++) if (aux[q] >= 0) v.push_back(q);
+        });
+        std::vector<long long> sq;
+        std::vector<int32_t> sv;
+        for (auto& v : part_q)
+            for (long long q : v) { sq.push_back(q); sv.push_back(aux[q]); }
+        if (!sq.empty()) {
+            long long* d_q = nullptr;
+            int32_t* d_v = nullptr;
+            CU(c, cudaMalloc(&d_q, sq.size() * sizeof(long long)));
+            CU(c, cudaMalloc(&d_v, sv.size() * sizeof(int32_t)));
+            CU(c, cudaMemcpyAsync(d_q, sq.data(), sq.size() * sizeof(long long), cudaMemcpyHostToDevice, c->st));
+            CU(c, cudaMemcpyAsync(d_v, sv.data(), sv.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c->st));
+            const long long n = (long long)sq.size();
+            k_scatter_aux<<<(unsigned)((n + 255) / 256), 256, 0, c->st>>>(c->d_aux, d_q, d_v, n);
+            cudaError_t e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+            cudaFree(d_q);
+            cudaFree(d_v);
+            if (e != cudaSuccess) return fail(c, LBM_ERR_CUDA, "side-table index upload: %s", cudaGetErrorString(e));
+        }
+    }
     const size_t rs = real_size(c);
     c->n_lid = n_lid; c->n_in = n_in; c->n_out = n_out;
     if (n_lid) {
