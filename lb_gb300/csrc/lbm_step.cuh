@@ -271,6 +271,20 @@ struct PairCodec {
     F2 inv_scale, scale, wr[4], nwrs[4];
 };
 
+// element i of a slot array of FP16 values as the slot's base address plus a zero-extended 32-bit
+// byte offset (i < 2^31, so 2 i fits): a 64-bit addition on the integer ALU instead of a wide integer
+// multiply-add on the FMA pipe, which bounds the FP16 step (measured 45.7 -> 47.3 GLUPS at 512x256x256)
+template <class T>
+LBM_D T* at32(T* base, int i) {
+    static_assert(sizeof(T) == 2, "32-bit byte offsets cover 2^31 elements of 2 bytes");
+    return (T*)((char*)base + (uint32_t)i * 2u);
+}
+template <class T>
+LBM_D const T* at32(const T* base, int i) {
+    static_assert(sizeof(T) == 2, "32-bit byte offsets cover 2^31 elements of 2 bytes");
+    return (const T*)((const char*)base + (uint32_t)i * 2u);
+}
+
 // RAW (FP16 storage): f[v] receives the stored deviation h_v itself (the caller then takes the moments of
 // f from those of h, moments_from_raw); else the population h_v 2^-s + w_v rho0
 template <class S, bool ODD, bool RAW = false>
@@ -285,9 +299,10 @@ LBM_D void load_pair(const Params& p, const PairIdx& q, const PairCodec& k, F2 (
             if constexpr (split) f[V] = F2(__ldg(a + i0), __ldg(a + i1));
             else f[V] = F2(__ldg((const float2*)(a + q.e0)));
         } else {
+            const T* b = (const T*)(ODD ? p.rd_odd[V] : p.rd_even[V]);
             float2 t;
-            if constexpr (split) t = make_float2(__half2float(__ldg(a + i0)), __half2float(__ldg(a + i1)));
-            else t = __half22float2(__ldg((const __half2*)(a + q.e0)));
+            if constexpr (split) t = make_float2(__half2float(__ldg(at32(b, i0))), __half2float(__ldg(at32(b, i1))));
+            else t = __half22float2(__ldg((const __half2*)at32(b, q.e0)));
             if constexpr (RAW) f[V] = F2(t);
             else f[V] = lfma(F2(t), k.inv_scale, k.wr[csq(V)]);
         }
@@ -309,8 +324,8 @@ LBM_D void store_pair(const Params& p, const PairIdx& q, const PairCodec& k, con
         } else {
             const F2 e = lfma(f[V], k.scale, k.nwrs[csq(V)]);
             const __half2 h = half2_sr(e.v, rs + p.sr_off[V]);
-            if constexpr (split) { a[i0] = __low2half(h); a[i1] = __high2half(h); }
-            else *(__half2*)(a + q.e0) = h;
+            if constexpr (split) { *at32(a, i0) = __low2half(h); *at32(a, i1) = __high2half(h); }
+            else *(__half2*)at32(a, q.e0) = h;
         }
     });
 }
