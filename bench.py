@@ -263,6 +263,43 @@ def cpu_reference(shape, case, steps, warmup, budget_s, threads=None):
     return dt / n, n, nth
 
 
+def voxelizer_block(reps=3):
+    """The OFF-mesh voxelizer on the C4 body (seeded perturbed icosphere, 20,480 triangles, radius 24
+    cells): lbm_voxelize_mesh through the C ABI (host mesh in, host flags out, best of `reps`) against the
+    CPU restatement of the reference's per-cell segment query (geometryMesherOFF.h:81-112) on all host
+    cores, and whether the two agree bit for bit."""
+    import ctypes as C
+    from lb_gb300 import capi, cases
+    from oracle import oracle as O
+    v, f = cases.perturbed_icosphere(radius=24.0)
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    f = np.ascontiguousarray(f, dtype=np.int32)
+    L = capi.lib()
+    dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int32)
+    dims = np.zeros(3, np.int32)
+    bbox = np.zeros(6)
+    args = (v.ctypes.data_as(dp), len(v), f.ctypes.data_as(ip), len(f), 1.0, 2.0)
+    capi.check(L.lbm_voxelize_mesh(*args, None, dims.ctypes.data_as(ip), bbox.ctypes.data_as(dp), 0))
+    g = np.zeros(int(dims.prod()), np.int32)
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        capi.check(L.lbm_voxelize_mesh(*args, g.ctypes.data_as(ip), dims.ctypes.data_as(ip), bbox.ctypes.data_as(dp), 0))
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    if O._lib is None:
+        O.NATIVE = True
+    t0 = time.perf_counter()
+    ref, _ = O.voxelize_mesh(v, f, 1.0, 2.0, (-300.0, -270.0, -240.0))
+    t_cpu = time.perf_counter() - t0
+    return {"mesh": "seeded perturbed icosphere, 20480 triangles, radius 24 cells (config 4 body)",
+            "dims": dims.tolist(), "cells": int(dims.prod()), "solid_cells": int(g.sum()),
+            "gpu_ms": best * 1e3, "gpu_includes": "lbm_voxelize_mesh: host mesh in, host flags out (best of %d)" % reps,
+            "cpu_s": t_cpu, "cpu_cores": O.max_threads(),
+            "cpu_impl": "oracle restatement of the reference's per-cell segment query, host-tuned build",
+            "bit_exact": bool(np.array_equal(g.reshape(ref.shape), ref)), "speedup": t_cpu / best}
+
+
 def cpu_host_info():
     """Compiler flags of the timed CPU baseline and the host's STREAM-triad bandwidth (all threads)."""
     from oracle import build as obuild
@@ -273,7 +310,7 @@ def cpu_host_info():
                     "about 720 B per cell update in FP32"}
 
 
-def learned_block(path, model, glups_mlp, glups_smag, interval=None):
+def learned_block(path, model, glups_mlp, glups_smag, interval=None, cost_table=None):
     if model is None:
         return {"model": None, "note": "no model file: headline ran the Smagorinsky closure"}
     rep = None
@@ -288,6 +325,10 @@ def learned_block(path, model, glups_mlp, glups_smag, interval=None):
         k, g = interval
         out["refresh_interval"] = {"k": k, "glups_f16_mlp": g, "throughput_cost": 1.0 - g / glups_smag,
                                    "note": "network every k-th step, nu_t kept per cell in FP16 in between"}
+    if cost_table:
+        out["cost_by_refresh_interval"] = {str(k): {"glups": g, "throughput_cost": 1.0 - g / glups_smag}
+                                           for k, g in sorted(cost_table.items())}
+        out["cost_by_refresh_interval"]["1"] = {"glups": glups_mlp, "throughput_cost": 1.0 - glups_mlp / glups_smag}
     return out
 
 
@@ -306,6 +347,9 @@ def main():
     ap.add_argument("--options", type=int, default=0, help="LBM_OPT_* bits passed to lbm_create")
     ap.add_argument("--mlp-interval", type=int, default=16,
                     help="also time the learned closure with nu_t refreshed every k-th step")
+    ap.add_argument("--mlp-intervals", default="2,4,8",
+                    help="further refresh intervals for the learned closure's cost table")
+    ap.add_argument("--no-voxelizer", action="store_true", help="skip the voxelizer line")
     ap.add_argument("--mlp", default=os.path.join(ROOT, "lb_gb300", "data", "les_mlp_channel.npz"),
                     help="learned-closure model (lb_gb300.les_train); the headline runs FP16 storage with it")
     args = ap.parse_args()
@@ -359,6 +403,14 @@ def main():
         ms16k, _, _ = time_storage(shape, case, "f16dev", args.steps, args.warmup, device, dist, False, args.options,
                                    model, args.mlp_interval)
         ms16k = dist_max(dist, ms16k)
+    cost_table = {}
+    if model:
+        for k in [int(v) for v in args.mlp_intervals.split(",") if v.strip()] + ([args.mlp_interval] if ms16k else []):
+            if k <= 1:
+                continue
+            msk = ms16k if k == args.mlp_interval else dist_max(dist, time_storage(
+                shape, case, "f16dev", args.steps, args.warmup, device, dist, False, args.options, model, k)[0])
+            cost_table[k] = dist_sum(dist, float(N) * args.steps) / (msk * 1e-3) / 1e9
     ms16 = dist_max(dist, ms16)
     ms16s = dist_max(dist, ms16s)
     ms32 = dist_max(dist, ms32)
@@ -411,6 +463,9 @@ def main():
                     "kind": "port",
                     "sample": f"{n} steps of the 256x128x128 channel, FP32, reference pass structure (oracle/)"},
                    **cpu_host_info())
+    vox = None
+    if rank == 0 and ws == 1 and not args.no_voxelizer:
+        vox = voxelizer_block()
     if rank != 0:
         return
     line = {"metric": METRIC, "value": glups16, "unit": "GLUPS", "n_gpus": ws, "steps": args.steps,
@@ -427,9 +482,11 @@ def main():
             "f16_smagorinsky": {"value": glups16s, "ms_per_step": ms16s / args.steps, "roofline": roof("f16dev", ms16s),
                                 "speedup_over_f32": glups16s / glups32},
             "learned_closure": learned_block(args.mlp, model, glups16, glups16s,
-                                             (args.mlp_interval, cells / (ms16k * 1e-3) / 1e9) if ms16k else None),
+                                             (args.mlp_interval, cells / (ms16k * 1e-3) / 1e9) if ms16k else None,
+                                             cost_table),
             # one fused step kernel per step; the row-staged step adds the launch over the wall rows
             "collisions": colls,
+            "voxelizer": vox,
             "gpu_launches": args.steps * d16.launches_per_step, "clocks": clk, "cpu_baseline": cpu, "e2e": e2e,
             "check": {"f16_mass": d16.mass, "f32_mass": d32.mass,
                       "nonfinite": d16.nonfinite + d32.nonfinite + d16s.nonfinite}}

@@ -181,7 +181,7 @@ def max_threads():
     return lib().orc_max_threads()
 
 
-def host_stream_gbs(n=1 << 26, reps=5):
+def host_stream_gbs(n=1 << 25, reps=4):
     """STREAM-triad bandwidth of the host's memory on all oracle threads (GB/s)."""
     return lib().orc_host_stream_gbs(int(n), int(reps))
 
