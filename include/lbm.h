@@ -412,6 +412,13 @@ typedef struct lbm_mlp_model {
  * the first lbm_step of such a context; may be replaced between steps */
 lbm_status lbm_mlp_load(lbm_ctx* ctx, const lbm_mlp_model* model);
 
+/* the eddy viscosity each cell keeps between network evaluations (contexts with mlp_interval > 1):
+ * nu[N] doubles, the value of the last step that ran the network (-1 where that cell's inputs were out
+ * of the training range and it relaxed with the Smagorinsky rate; NaN where it never ran the network:
+ * cells off the packed bulk path, or before the first network step).
+ * LBM_ERR_STATE without a kept value.  No reference counterpart (OmegaLES keeps omega, not nu_t). */
+lbm_status lbm_get_eddy_viscosity(lbm_ctx* ctx, double* nu);
+
 /* training samples from the current state of a run on a 4x-finer (generally width-x-finer) lattice:
  * box filter of `width` fine cells per coarse cell, strain rate of the filtered velocity by central
  * differences in coarse lattice units, filtered stress tau = <u u> - <u><u>.  A sample is

@@ -215,6 +215,7 @@ def lib():
         "lbm_synchronize": ([vp], i32),
         "lbm_step_timed": ([vp, i32, dp], i32),
         "lbm_step_launches": ([vp, ip], i32),
+        "lbm_get_eddy_viscosity": ([vp, dp], i32),
         "lbm_probe": ([vp, i32, i32, i32, dp], i32),
         "lbm_get_moments": ([vp, dp, dp], i32),
         "lbm_get_populations": ([vp, dp], i32),

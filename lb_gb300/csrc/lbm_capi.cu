@@ -1240,6 +1240,20 @@ lbm_status lbm_mlp_load(lbm_ctx* c, const lbm_mlp_model* m) {
     return LBM_OK;
 }
 
+lbm_status lbm_get_eddy_viscosity(lbm_ctx* c, double* nu) {
+    if (!c || !nu) return fail(c, LBM_ERR_INVALID, "lbm_get_eddy_viscosity: null argument");
+    if (!c->d_nut) return fail(c, LBM_ERR_STATE, "lbm_get_eddy_viscosity: the context keeps no eddy viscosity "
+                                                 "(learned closure with mlp_interval > 1 only)");
+    cudaSetDevice(c->cfg.device);
+    std::vector<__half> h((size_t)c->N);
+    CU(c, cudaMemcpyAsync(h.data(), c->d_nut, (size_t)c->N * sizeof(__half), cudaMemcpyDeviceToHost, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    host_parallel(c->N, [&](long long q0, long long q1) {
+        for (long long q = q0; q < q1; q++) nu[q] = (double)__half2float(h[(size_t)q]);
+    });
+    return LBM_OK;
+}
+
 lbm_status lbm_les_samples(lbm_ctx* c, int32_t w, float* out, int64_t capacity, int64_t* count) {
     if (!c || !count || w < 1 || capacity < 0 || (capacity > 0 && !out))
         return fail(c, LBM_ERR_INVALID, "lbm_les_samples: bad argument");

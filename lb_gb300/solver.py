@@ -329,6 +329,13 @@ class Solver:
         self._check(lib().lbm_step_timed(self._ctx, int(n), C.byref(ms)))
         return ms.value
 
+    def eddy_viscosity(self):
+        """The learned closure's kept nu_t per cell (mlp_interval > 1): -1 where the cell relaxed with
+        the Smagorinsky rate in the last network step."""
+        nu = np.empty(self.N, np.float64)
+        self._check(lib().lbm_get_eddy_viscosity(self._ctx, _dp(nu)))
+        return nu
+
     def step_launches(self):
         """Kernel launches one step issues on this context (1, or 2 for the split step)."""
         n = C.c_int32(0)

@@ -84,6 +84,10 @@ struct Sim {
 
     std::vector<int32_t> mesh;
     std::vector<R> df, dfp, rho, u[3], omega, uerr[3];
+    // a per-cell relaxation rate that replaces the closure pass of the next step (checking a closure
+    // computed outside the oracle, e.g. the learned eddy viscosity, against the GPU step that fuses it)
+    std::vector<R> omega_next;
+    bool use_omega_next = false;
     std::vector<double> a_rho, a_u[3], a_uu[6];
     int64_t a_count = 0;
     bool a_on = false;
@@ -740,7 +744,10 @@ struct Sim {
 
     // ---- SolverTurbulentLES::runSimulation loop body, SolverTurbulentLES.h:186-226 --------
     void step() {
-        if (closure == LBM_CLOSURE_SMAGORINSKY) omega_les(); else omega_no();
+        if (use_omega_next) {
+            for (size_t c = 0; c < N; c++) if (mesh[c] != 0) omega[c] = omega_next[c];
+            use_omega_next = false;
+        } else if (closure == LBM_CLOSURE_SMAGORINSKY) omega_les(); else omega_no();
         if (!outlets.empty() && (outlet_kind == LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA ||
                                  outlet_kind == LBM_OUTLET_NEIGHBOUR_EQUILIBRIUM_OMEGA_RF))
             outlet_omega();
@@ -996,6 +1003,15 @@ int orc_get_moments(void* p, double* rho, double* u) {
 int orc_get_omega(void* p, double* om) {
     Handle* h = (Handle*)p;
     DISPATCH(h, { for (size_t c = 0; c < S->N; c++) om[c] = S->omega[c]; });
+    return 0;
+}
+int orc_set_omega_next(void* p, const double* om) {
+    Handle* h = (Handle*)p;
+    DISPATCH(h, {
+        S->omega_next.resize(S->N);
+        for (size_t c = 0; c < S->N; c++) S->omega_next[c] = om[c];
+        S->use_omega_next = true;
+    });
     return 0;
 }
 int orc_get_df(void* p, double* f) {

@@ -43,6 +43,7 @@ def lib():
         L.orc_get_moments.argtypes = [vp, dp, dp]
         L.orc_get_omega.argtypes = [vp, dp]
         L.orc_get_df.argtypes = [vp, dp]
+        L.orc_set_omega_next.argtypes = [vp, dp]
         L.orc_set_df.argtypes = [vp, dp]
         L.orc_timeavg_begin.argtypes = [vp]
         L.orc_timeavg_end.argtypes = [vp]
@@ -135,6 +136,11 @@ class OracleSim:
         o = np.empty(self.N)
         lib().orc_get_omega(self.h, _d(o))
         return o
+
+    def set_omega_next(self, omega):
+        """Per-cell relaxation rate for the next step in place of the closure pass (one step)."""
+        a = np.ascontiguousarray(omega, dtype=np.float64).reshape(-1)
+        lib().orc_set_omega_next(self.h, _d(a))
 
     def populations(self):
         f = np.empty(27 * self.N)
