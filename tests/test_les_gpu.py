@@ -245,8 +245,9 @@ def test_fused_learned_step_matches_oracle_step(built_lib, oracle_lib, storage):
     """The headline kernel's learned path against the oracle: the GPU runs the network inside the
     collision kernel (k_step2_mlp, tensor-core FP16 network every step); the oracle runs the reference's
     cumulant step with, per cell and step, the relaxation rate of the same network restated on its own
-    FP64 state (oracle_learned_rate).  The model's normalisation comes from the oracle's inputs at step 0
-    and its range covers half of them, so both the network and the Smagorinsky fallback are exercised.
+    FP64 state (oracle_learned_rate), both from the oracle's state after 5 Smagorinsky steps.  The model's
+    normalisation comes from the oracle's inputs there and its range covers half of them, so both the
+    network and the Smagorinsky fallback are exercised.
     Bounds: FP32 moments within 5e-5 u_max of the FP64 oracle after 24 steps (the FP32 noise floor of the
     case is ~1e-5); FP16 storage 2e-3 relative L2 of u.  With a refresh interval of 2 (mode 1 on even
     steps) the kept nu_t read back from the GPU after a network step matches the oracle's nu_t of that
@@ -263,6 +264,7 @@ def test_fused_learned_step_matches_oracle_step(built_lib, oracle_lib, storage):
     o = O.OracleSim(cfg, 64)
     o.set_flags(c["flags"])
     o.init_fields(c["rho"], c["u"])
+    o.step(5)  # from the equilibrium start (Pi = 0 exactly) to a state with non-equilibrium stress
     tau = 3.0 * c["nu"] + 0.5
     fl = c["flags"].reshape(-1) != 0
     f0 = o.populations().reshape(27, -1)
@@ -280,7 +282,7 @@ def test_fused_learned_step_matches_oracle_step(built_lib, oracle_lib, storage):
                    cles=0.17, periodic=c["periodic"], force=c["force"], mlp_interval=interval)
         s.set_flags(c["flags"])
         s.set_bc()
-        s.init_fields(c["rho"], c["u"])
+        s.set_populations(f0)  # the oracle's state after its 5 Smagorinsky steps
         s.load_mlp(m)
         g[interval] = s
     steps = 24
