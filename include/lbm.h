@@ -139,6 +139,10 @@ const char* lbm_config_last_error(void);
                                   default split (rows whose pairs all take the packed path, then the
                                   remaining rows); identical results */
 
+#define LBM_OPT_NO_WALL_ROWS 8  /* FP32 / FP16 storage: rows beside a flat wall take the general per-cell path
+                                    instead of the packed wall kernel (the per-cell and packed paths round
+                                    differently; this keeps the split step bit-identical to one launch) */
+
 /* boundary-condition records, mirroring LBMTraits.h:17-43 */
 typedef struct lbm_vertex { int32_t x, y, z; } lbm_vertex;
 
@@ -208,8 +212,9 @@ lbm_status lbm_step(lbm_ctx* ctx, int32_t nsteps);
 lbm_status lbm_synchronize(lbm_ctx* ctx);
 /* nsteps steps bracketed by CUDA events on the context's stream; *ms = elapsed device time */
 lbm_status lbm_step_timed(lbm_ctx* ctx, int32_t nsteps, double* ms);
-/* kernel launches one lbm_step step issues on this context (after initialisation): 1 or 2 (the split
-   step launches the plain rows and the remaining rows separately; a kind with no rows is not launched).
+/* kernel launches one lbm_step step issues on this context (after initialisation): 1 to 3 (the split
+   step launches the plain rows, the rows beside flat walls and the remaining rows separately; a kind with
+   no rows is not launched).
    No reference counterpart (the reference runs one launch per hook) */
 lbm_status lbm_step_launches(const lbm_ctx* ctx, int32_t* per_step);
 

@@ -60,6 +60,7 @@ class LbmConfig(C.Structure):
 LBM_OPT_ROW_STAGING = 1
 LBM_OPT_F16_ROUND_NEAREST = 2
 LBM_OPT_ONE_LAUNCH = 4
+LBM_OPT_NO_WALL_ROWS = 8
 
 
 LBM_MLP_INPUTS = 7

@@ -77,8 +77,11 @@ struct lbm_ctx {
     int32_t* d_other_rows = nullptr;  // the remaining rows
     int n_bulk_rows = 0, n_other_rows = 0;
     int32_t* d_plain_rows = nullptr;  // split step: rows whose pairs all take the packed path
-    int32_t* d_rest_rows = nullptr;   // split step: the remaining rows
-    int n_plain_rows = 0, n_rest_rows = 0;
+    int32_t* d_rest_rows = nullptr;   // split step: the remaining rows that are not wall rows
+    int32_t* d_wall_rows = nullptr;   // split step: rows beside a flat wall (packed, bounce-back by mask)
+    uint32_t* d_wall_solid = nullptr; //   their solid-source masks
+    int32_t* d_rest_all = nullptr;    // split step: all non-plain rows (closures without the wall kernel)
+    int n_plain_rows = 0, n_rest_rows = 0, n_wall_rows = 0, n_rest_all = 0;
     bool split_ok = false;            // the step runs split by rows (FP32 / FP16 storage)
     int* d_err = nullptr;             // device error word
     bool rows_ok = false;             // the row-staged step applies to this lattice
@@ -206,6 +209,8 @@ static cudaError_t do_step(lbm_ctx* c, const Params& p) {
     RowLists rl;
     rl.plain = c->d_plain_rows; rl.n_plain = c->n_plain_rows;
     rl.other = c->d_rest_rows; rl.n_other = c->n_rest_rows;
+    rl.wall = c->d_wall_rows; rl.wall_solid = c->d_wall_solid; rl.n_wall = c->n_wall_rows;
+    rl.other_all = c->d_rest_all; rl.n_other_all = c->n_rest_all;
     rl.side = c->st_side; rl.fork = c->ev_fork; rl.join = c->ev_join;
     const RowLists* r = c->split_ok ? &rl : nullptr;
     switch (c->cfg.storage) {
@@ -341,7 +346,7 @@ lbm_status lbm_destroy(lbm_ctx* c) {
     free_side(c);
     dfree(c->d_acc); dfree(c->d_uerr); dfree(c->d_red); dfree(c->d_part);
     dfree(c->d_rho_out); dfree(c->d_u_out); dfree(c->d_f_out); dfree(c->d_probe);
-    dfree(c->d_bulk_rows); dfree(c->d_other_rows); dfree(c->d_plain_rows); dfree(c->d_rest_rows); dfree(c->d_err); dfree(c->d_mlp_frag); dfree(c->d_nut);
+    dfree(c->d_bulk_rows); dfree(c->d_other_rows); dfree(c->d_plain_rows); dfree(c->d_rest_rows); dfree(c->d_wall_rows); dfree(c->d_wall_solid); dfree(c->d_rest_all); dfree(c->d_err); dfree(c->d_mlp_frag); dfree(c->d_nut);
     if (c->st) cudaStreamDestroy(c->st);
     if (c->st_side) cudaStreamDestroy(c->st_side);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
@@ -786,20 +791,62 @@ static lbm_status build_geometry(lbm_ctx* c) {
                 }
             });
         }
-        std::vector<int32_t> pr, rr;
-        for (long long r = 0; r < (long long)plain.size(); r++) (plain[(size_t)r] ? pr : rr).push_back((int32_t)r);
-        dfree(c->d_plain_rows); dfree(c->d_rest_rows);
-        c->d_plain_rows = c->d_rest_rows = nullptr;
+        // rows beside a flat wall: every cell an edge cell (no role bit) whose 26 sources are solid or
+        // fluid cells of the packed kinds at the same offsets along the whole row, off the periodic y/z
+        // seams (the combined collision keeps them on the general path)
+        std::vector<uint32_t> wmask(plain.size(), 0);
+        std::vector<uint8_t> is_wall(plain.size(), 0);
+        if (c->split_ok && !(nx & 1) && !comb && !(c->cfg.options & LBM_OPT_NO_WALL_ROWS)) {
+            host_parallel(nrow, [&](long long r0, long long r1) {
+                for (long long r = r0; r < r1; r++) {
+                    if (plain[(size_t)r]) continue;
+                    const int y = (int)(r % ny), z = (int)(r / ny);
+                    if ((wrap[1] && (y == 0 || y == ny - 1)) || (wrap[2] && (z == 0 || z == nz - 1))) continue;
+                    bool ok = true;
+                    uint32_t mask = 0;
+                    for (int i = 0; i < nx && ok; i++) {
+                        if ((cls[(size_t)(r * nx + i)] & (uint8_t)~BIT_REFBULK) != CLS_EDGE) { ok = false; break; }
+                        uint32_t m = 0;
+                        for (int v = 1; v < 27 && ok; v++) {
+                            bool in = true;
+                            const int a = wrapc(i - cx(v), nx, 0, in), b = y - cy(v), e = z - cz(v);
+                            if (!in || b < 0 || b >= ny || e < 0 || e >= nz) { ok = false; break; }
+                            const int k = cls[(size_t)id(a, b, e)] & CLS_MASK;
+                            if (k == CLS_SOLID) m |= 1u << v;
+                            else if (k != CLS_BULK && k != CLS_EDGE) ok = false;
+                        }
+                        if (i == 0) mask = m;
+                        else if (m != mask) ok = false;
+                    }
+                    if (ok) { is_wall[(size_t)r] = 1; wmask[(size_t)r] = mask; }
+                }
+            });
+        }
+        std::vector<int32_t> pr, rr, wr, ra;
+        std::vector<uint32_t> wm;
+        for (long long r = 0; r < (long long)plain.size(); r++) {
+            if (plain[(size_t)r]) { pr.push_back((int32_t)r); continue; }
+            ra.push_back((int32_t)r);
+            if (is_wall[(size_t)r]) { wr.push_back((int32_t)r); wm.push_back(wmask[(size_t)r]); }
+            else rr.push_back((int32_t)r);
+        }
+        dfree(c->d_plain_rows); dfree(c->d_rest_rows); dfree(c->d_wall_rows); dfree(c->d_wall_solid); dfree(c->d_rest_all);
+        c->d_plain_rows = c->d_rest_rows = c->d_wall_rows = c->d_rest_all = nullptr;
+        c->d_wall_solid = nullptr;
         c->n_plain_rows = (int)pr.size();
         c->n_rest_rows = (int)rr.size();
-        if (c->split_ok && !pr.empty()) {
-            CU(c, cudaMalloc(&c->d_plain_rows, pr.size() * 4));
-            CU(c, cudaMemcpy(c->d_plain_rows, pr.data(), pr.size() * 4, cudaMemcpyHostToDevice));
-        }
-        if (c->split_ok && !rr.empty()) {
-            CU(c, cudaMalloc(&c->d_rest_rows, rr.size() * 4));
-            CU(c, cudaMemcpy(c->d_rest_rows, rr.data(), rr.size() * 4, cudaMemcpyHostToDevice));
-        }
+        c->n_wall_rows = (int)wr.size();
+        c->n_rest_all = (int)ra.size();
+        auto upload = [&](auto** dst, const auto& v) -> lbm_status {
+            if (!c->split_ok || v.empty()) return LBM_OK;
+            CU(c, cudaMalloc((void**)dst, v.size() * 4));
+            CU(c, cudaMemcpy(*dst, v.data(), v.size() * 4, cudaMemcpyHostToDevice));
+            return LBM_OK;
+        };
+        lbm_status us;
+        if ((us = upload(&c->d_plain_rows, pr)) || (us = upload(&c->d_rest_rows, rr)) ||
+            (us = upload(&c->d_wall_rows, wr)) || (us = upload(&c->d_wall_solid, wm)) || (us = upload(&c->d_rest_all, ra)))
+            return us;
     }
     c->have_geom = true;
     return LBM_OK;
@@ -908,8 +955,10 @@ lbm_status lbm_step_launches(const lbm_ctx* c, int32_t* per_step) {
     if (!c->initialized) return fail(nullptr, LBM_ERR_STATE, "lbm_step_launches before initialisation");
     if (c->rows_ok && c->cfg.collision == LBM_COLLISION_CUMULANT2015 && c->cfg.storage == LBM_STORAGE_F16DEV)
         *per_step = (c->n_bulk_rows > 0 ? 1 : 0) + (c->n_other_rows > 0 ? 1 : 0);
+    else if (c->split_ok && (c->cfg.closure == LBM_CLOSURE_MLP || c->cfg.collision == LBM_COLLISION_CUMULANT_COMBINED))
+        *per_step = (c->n_plain_rows > 0 ? 1 : 0) + (c->n_rest_all > 0 ? 1 : 0);
     else if (c->split_ok)
-        *per_step = (c->n_plain_rows > 0 ? 1 : 0) + (c->n_rest_rows > 0 ? 1 : 0);
+        *per_step = (c->n_plain_rows > 0 ? 1 : 0) + (c->n_rest_rows > 0 ? 1 : 0) + (c->n_wall_rows > 0 ? 1 : 0);
     else
         *per_step = 1;
     return LBM_OK;

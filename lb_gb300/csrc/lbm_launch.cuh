@@ -36,10 +36,17 @@ static cudaError_t step_parity(const Params& p, const RowLists* rl, cudaStream_t
         if (odd) k_step<S, COLL, CLOS, true><<<g, b, 0, st>>>(p);
         else     k_step<S, COLL, CLOS, false><<<g, b, 0, st>>>(p);
     } else if (rl) {
-        // split step: the remaining rows (side stream) and the plain rows, one thread per x-pair
+        // split step: the wall rows and the remaining rows (side stream) and the plain rows, one thread
+        // per x-pair
         const int half = (p.nx + 1) / 2;
         const dim3 b = cell_block(half);
         const unsigned xb = (unsigned)((half + (int)b.x - 1) / (int)b.x);
+        // the packed wall kernel serves the Smagorinsky and constant-rate closures of the collisions
+        // whose packed path is their own (not the combined one, which packs reference-flag-1 cells only)
+        constexpr bool WALL = CLOS != 2 && COLL != 3;
+        const int32_t* other = WALL ? rl->other : rl->other_all;
+        const int n_other = WALL ? rl->n_other : rl->n_other_all;
+        const int n_wall = WALL ? rl->n_wall : 0;
         RowKernel kp, ko;
         if constexpr (CLOS == 2) {
             kp = mlp_kernel<S, COLL, 1>(p);
@@ -48,17 +55,25 @@ static cudaError_t step_parity(const Params& p, const RowLists* rl, cudaStream_t
             kp = odd ? k_step2_plain<S, COLL, CLOS, true> : k_step2_plain<S, COLL, CLOS, false>;
             ko = odd ? k_step2_list<S, COLL, CLOS, true> : k_step2_list<S, COLL, CLOS, false>;
         }
-        const bool fork = rl->side && rl->n_other > 0 && rl->n_plain > 0;
+        const bool fork = rl->side && (n_other > 0 || n_wall > 0) && rl->n_plain > 0;
         cudaStream_t so = fork ? rl->side : st;
         if (fork) {
             cudaError_t e = cudaEventRecord(rl->fork, st);
             if (e == cudaSuccess) e = cudaStreamWaitEvent(rl->side, rl->fork, 0);
             if (e != cudaSuccess) return e;
         }
-        if (rl->n_other > 0) {
-            ko<<<rows_grid(xb, rl->n_other), b, 0, so>>>(p, rl->other, rl->n_other);
+        if (n_other > 0) {
+            ko<<<rows_grid(xb, n_other), b, 0, so>>>(p, other, n_other);
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) return e;
+        }
+        if constexpr (WALL) {
+            if (n_wall > 0) {
+                if (odd) k_step2_wall<S, COLL, CLOS, true><<<rows_grid(xb, n_wall), b, 0, so>>>(p, rl->wall, rl->wall_solid, n_wall);
+                else     k_step2_wall<S, COLL, CLOS, false><<<rows_grid(xb, n_wall), b, 0, so>>>(p, rl->wall, rl->wall_solid, n_wall);
+                cudaError_t e = cudaGetLastError();
+                if (e != cudaSuccess) return e;
+            }
         }
         if (rl->n_plain > 0) kp<<<rows_grid(xb, rl->n_plain), b, 0, st>>>(p, rl->plain, rl->n_plain);
         if (fork) {

@@ -18,6 +18,14 @@ struct RowLists {
     int n_plain = 0;
     const int32_t* other = nullptr;
     int n_other = 0;
+    // rows beside a flat wall (every cell an edge cell with the same solid-source mask, `wall_solid`),
+    // stepped by the packed wall kernel; closures without it take them with `other` (`other_all` lists
+    // both)
+    const int32_t* wall = nullptr;
+    const uint32_t* wall_solid = nullptr;
+    int n_wall = 0;
+    const int32_t* other_all = nullptr;
+    int n_other_all = 0;
     // the remaining rows run on `side`, forked from and joined back into the step's stream, so their
     // slow per-cell path overlaps the plain rows instead of trailing them (nullptr: same stream)
     cudaStream_t side = nullptr;

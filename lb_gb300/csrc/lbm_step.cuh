@@ -287,25 +287,43 @@ LBM_D const T* at32(const T* base, int i) {
 
 // RAW (FP16 storage): f[v] receives the stored deviation h_v itself (the caller then takes the moments of
 // f from those of h, moments_from_raw); else the population h_v 2^-s + w_v rho0
+// direction V of a pair through the address table of an odd (TODD) or even step: the odd table reads the
+// x-shifted pair of cell x - c_V's opposite slot, the even one the pair's own slot V
+template <class S, bool TODD, bool RAW, int V>
+LBM_D F2 load_dir(const Params& p, const PairIdx& q, const PairCodec& k) {
+    using T = typename S::T;
+    constexpr bool split = TODD && cx(V) != 0;
+    const int i0 = cx(V) > 0 ? q.eL : q.e0, i1 = cx(V) > 0 ? q.e1 : q.eR;
+    if constexpr (S::kind == 1) {
+        const T* a = (const T*)(TODD ? p.rd_odd[V] : p.rd_even[V]);
+        if constexpr (split) return F2(__ldg(a + i0), __ldg(a + i1));
+        else return F2(__ldg((const float2*)(a + q.e0)));
+    } else {
+        const T* b = (const T*)(TODD ? p.rd_odd[V] : p.rd_even[V]);
+        float2 t;
+        if constexpr (split) t = make_float2(__half2float(__ldg(at32(b, i0))), __half2float(__ldg(at32(b, i1))));
+        else t = __half22float2(__ldg((const __half2*)at32(b, q.e0)));
+        if constexpr (RAW) return F2(t);
+        else return lfma(F2(t), k.inv_scale, k.wr[csq(V)]);
+    }
+}
 template <class S, bool ODD, bool RAW = false>
 LBM_D void load_pair(const Params& p, const PairIdx& q, const PairCodec& k, F2 (&f)[27]) {
-    using T = typename S::T;
     sfor<0, 27>([&](auto vc) {
         constexpr int V = decltype(vc)::value;
-        const T* a = (const T*)(ODD ? p.rd_odd[V] : p.rd_even[V]);
-        constexpr bool split = ODD && cx(V) != 0;
-        const int i0 = cx(V) > 0 ? q.eL : q.e0, i1 = cx(V) > 0 ? q.e1 : q.eR;
-        if constexpr (S::kind == 1) {
-            if constexpr (split) f[V] = F2(__ldg(a + i0), __ldg(a + i1));
-            else f[V] = F2(__ldg((const float2*)(a + q.e0)));
-        } else {
-            const T* b = (const T*)(ODD ? p.rd_odd[V] : p.rd_even[V]);
-            float2 t;
-            if constexpr (split) t = make_float2(__half2float(__ldg(at32(b, i0))), __half2float(__ldg(at32(b, i1))));
-            else t = __half22float2(__ldg((const __half2*)at32(b, q.e0)));
-            if constexpr (RAW) f[V] = F2(t);
-            else f[V] = lfma(F2(t), k.inv_scale, k.wr[csq(V)]);
-        }
+        f[V] = load_dir<S, ODD, RAW, V>(p, q, k);
+    });
+}
+// a pair of a wall row: where bit V of `solid` is set, the source cell x - c_V is solid and the link
+// bounces back, f_V(x) = f*_{opp V}(x) of the previous step (BounceBackWallHalf.h:38-49).  In the AA
+// layout that value sits where the other parity's table points: after an odd step in the solid cell's
+// slot opp V (the odd table's address), after an even step in the cell's own slot V (the even table's)
+template <class S, bool ODD, bool RAW = false>
+LBM_D void load_pair_wall(const Params& p, const PairIdx& q, const PairCodec& k, uint32_t solid, F2 (&f)[27]) {
+    sfor<0, 27>([&](auto vc) {
+        constexpr int V = decltype(vc)::value;
+        if ((solid >> V) & 1u) f[V] = load_dir<S, !ODD, RAW, V>(p, q, k);
+        else f[V] = load_dir<S, ODD, RAW, V>(p, q, k);
     });
 }
 template <class S, bool ODD>
@@ -546,6 +564,25 @@ __global__ void __launch_bounds__(128, plain_min_blocks(COLL, S::kind)) k_step2_
     int r, x0;
     if (!row_block(rows, n, r, x0) || x0 >= p.nx) return;
     step_pair_plain<S, COLL, CLOS, ODD>(p, r * p.nx + x0, x0);
+}
+// rows beside a flat wall (set-up lists them with the row's solid-source mask): every cell an edge cell
+// whose solid neighbours lie at the same offsets, so the whole row takes the packed pair path with the
+// bounce-back links read through the other parity's address table (load_pair_wall)
+template <class S, int COLL, int CLOS, bool ODD>
+__global__ void __launch_bounds__(128, plain_min_blocks(COLL, S::kind)) k_step2_wall(Params p, const int32_t* rows,
+                                                                                   const uint32_t* solid, int n) {
+    int r, x0;
+    if (!row_block(rows, n, r, x0) || x0 >= p.nx) return;
+    const uint32_t m = solid[blockIdx.y + gridDim.y * blockIdx.z];
+    constexpr int PC = packed_coll<COLL>();
+    constexpr bool RAW = packed_raw<S, COLL>();
+    const int e0 = r * p.nx + x0;
+    const PairCodec k = make_codec<S>(p);
+    const PairIdx q = make_pair_idx(p, e0, x0);
+    F2 f[27];
+    load_pair_wall<S, ODD, RAW>(p, q, k, m, f);
+    collide_pair<PC, CLOS, RAW>(p, f, e0);
+    store_pair<S, ODD>(p, q, k, f);
 }
 template <class S, int COLL, int CLOS, bool ODD>
 __global__ void __launch_bounds__(128, step2_min_blocks(COLL)) k_step2_list(Params p, const int32_t* rows, int n) {

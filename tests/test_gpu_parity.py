@@ -204,7 +204,9 @@ def test_split_step_is_bit_identical_to_one_launch(built_lib, storage, coll, clo
         interval = 3 if clos == "mlp3" else 1
     inlet = InletVelocityEquilibrium if kind == "body" else InletVelocityMovingWall
     runs = []
-    for opt in (0, capi.LBM_OPT_ONE_LAUNCH):
+    # the packed wall-row kernel rounds like the packed path, the one-launch step takes those rows
+    # through the per-cell path: compare with it off (its own parity: test_wall_rows_match_oracle)
+    for opt in (capi.LBM_OPT_NO_WALL_ROWS, capi.LBM_OPT_ONE_LAUNCH):
         s = Solver(shape, collision=COLL[coll], turbulence=turb, inlet=inlet, storage=storage, nu=c["nu"],
                    cles=0.17, periodic=c.get("periodic", (0, 0, 0)), force=c.get("force", (0, 0, 0)), options=opt,
                    mlp_interval=interval)
@@ -224,6 +226,41 @@ def test_split_step_is_bit_identical_to_one_launch(built_lib, storage, coll, clo
         s.close()
     for a, b in zip(*runs):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16dev"])
+@pytest.mark.parametrize("coll,clos", [("cum", "smag"), ("srt", "smag"), ("cum17", "none")])
+def test_wall_rows_match_oracle(built_lib, oracle_lib, storage, coll, clos):
+    """Rows beside the channel walls take the packed wall kernel (bounce-back links read through the other
+    parity's address table).  Against the oracle on a channel whose edge rows are all wall rows: FP32
+    within 3e-5 of the FP32 oracle (fp32_parity); FP16 storage within 2e-3 relative L2 of FP64 after 100
+    steps; and against the same run with the wall kernel off (LBM_OPT_NO_WALL_ROWS): FP32 within 3e-5."""
+    nx, ny, nz = 32, 14, 12
+    c = cases.channel(nx, ny, nz, re_tau=3.0, u_max=0.05, nu=0.01)
+    g, o = pair((nx, ny, nz), c, coll, clos, storage, 32, force=c["force"])
+    _, o64 = pair((nx, ny, nz), c, coll, clos, "f64", 64, force=c["force"])
+    init_both(g, o, c)
+    assert g.step_launches() == 3  # plain rows, wall rows, the rest (solid rows and z-seam rows)
+    o64.init_fields(c["rho"], c["u"])
+    if storage == "f32":
+        fp32_parity(g, o, o64, 0.05, 100)
+        s = Solver((nx, ny, nz), collision=COLL[coll], turbulence=CLOS[clos], storage=storage, nu=c["nu"], cles=0.17,
+                   periodic=c["periodic"], force=c["force"], options=capi.LBM_OPT_NO_WALL_ROWS)
+        s.set_flags(c["flags"])
+        s.set_bc()
+        s.init_fields(c["rho"], c["u"])
+        s.step(100)
+        _, u0 = s.moments()
+        _, u1 = g.moments()
+        s.close()
+        assert np.abs(u1 - u0).max() <= 3e-5 * 0.05
+    else:
+        g.step(100)
+        o64.step(100)
+        _, ug = g.moments()
+        _, ut = o64.moments()
+        fl = c["flags"].reshape(-1) != 0
+        assert np.linalg.norm(ug[:, fl] - ut[:, fl]) / np.linalg.norm(ut[:, fl]) < 2e-3
 
 
 def test_channel_srt_force_fp64(built_lib, oracle_lib):
