@@ -285,10 +285,10 @@ LBM_D const T* at32(const T* base, int i) {
     return (const T*)((const char*)base + (uint32_t)i * 2u);
 }
 
-// RAW (FP16 storage): f[v] receives the stored deviation h_v itself (the caller then takes the moments of
-// f from those of h, moments_from_raw); else the population h_v 2^-s + w_v rho0
 // direction V of a pair through the address table of an odd (TODD) or even step: the odd table reads the
-// x-shifted pair of cell x - c_V's opposite slot, the even one the pair's own slot V
+// x-shifted pair of cell x - c_V's opposite slot, the even one the pair's own slot V.  RAW (FP16
+// storage): the stored deviation h_v itself (the caller then takes the moments of f from those of h,
+// moments_from_raw); else the population h_v 2^-s + w_v rho0
 template <class S, bool TODD, bool RAW, int V>
 LBM_D F2 load_dir(const Params& p, const PairIdx& q, const PairCodec& k) {
     using T = typename S::T;
@@ -573,7 +573,9 @@ __global__ void __launch_bounds__(128, plain_min_blocks(COLL, S::kind)) k_step2_
                                                                                    const uint32_t* solid, int n) {
     int r, x0;
     if (!row_block(rows, n, r, x0) || x0 >= p.nx) return;
-    const uint32_t m = solid[blockIdx.y + gridDim.y * blockIdx.z];
+    // at m = 0 every cell reads its own initial slots (there is no previous post-collision state to
+    // bounce back, and the solid cells' slots hold zeros): the gather rule of the per-cell path
+    const uint32_t m = p.m == 0 ? 0u : solid[blockIdx.y + gridDim.y * blockIdx.z];
     constexpr int PC = packed_coll<COLL>();
     constexpr bool RAW = packed_raw<S, COLL>();
     const int e0 = r * p.nx + x0;
