@@ -2,6 +2,7 @@
 #pragma once
 
 #include "lbm_device.cuh"
+#include "lbm_step.cuh"
 
 namespace lbm {
 
@@ -28,13 +29,18 @@ struct ReadOut {
     int ref_compat_err;  // reproduce the ErrorQuadratic z-term typo
 };
 
-// the reading kernels run one thread per x of a (y, kReadZ z-planes) column tile; the reductions keep
-// per-thread FP64 partial sums over the tile's cells, one partial per block in part[], and a second
-// kernel adds the partials in a fixed order: the result does not depend on scheduling (no atomics)
+// the reading kernels run one thread per x-pair of a (y, kReadZ z-planes) column tile (pairs of bulk
+// cells load both cells with the step kernel's packed accesses); the reductions keep per-thread partial
+// sums over the tile's cells, one partial per block in part[], and a second kernel adds the partials in
+// a fixed order: the result does not depend on scheduling (no atomics)
 constexpr int kReadZ = 4;
+inline int read_block(int nx) {
+    const int half = (nx + 1) / 2;
+    return half >= 128 ? 128 : ((half + 31) / 32) * 32;
+}
 inline dim3 read_grid(int nx, int ny, int nz) {
-    const int b = nx >= 128 ? 128 : ((nx + 31) / 32) * 32;
-    return dim3((unsigned)((nx + b - 1) / b), (unsigned)ny, (unsigned)((nz + kReadZ - 1) / kReadZ));
+    const int half = (nx + 1) / 2, b = read_block(nx);
+    return dim3((unsigned)((half + b - 1) / b), (unsigned)ny, (unsigned)((nz + kReadZ - 1) / kReadZ));
 }
 inline long long read_blocks(int nx, int ny, int nz) {
     const dim3 g = read_grid(nx, ny, nz);
@@ -127,79 +133,123 @@ LBM_D void block_partials(const RedAcc<R>& a, double* part, long long nblk) {
     }
 }
 
-// one thread per x of a column tile of kReadZ cells along z; gathers df_m exactly as the step kernel
-template <class S, bool ODD>
-// 6 resident CTAs per SM (80 registers): 1.08 ms against 1.27 ms per diagnostics call at 512x256x256
-__global__ void __launch_bounds__(128, 6) k_read(Params p, ReadOut o) {
+// one cell of the reading kernels: its populations f (gathered as the step kernel does) and drag links
+template <class S>
+LBM_D void read_cell(const Params& p, const ReadOut& o, RedAcc<typename S::R>& acc, long long idx, uint8_t fl,
+                     const typename S::R (&f)[27], const typename S::R (&drag)[3]) {
     using R = typename S::R;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool live = x < p.nx;
+    const int cl = fl & CLS_MASK;
+    R rho = 0, jx = 0, jy = 0, jz = 0, ux = 0, uy = 0, uz = 0;
+    if (cl != CLS_SOLID) moments(f, p, rho, jx, jy, jz, ux, uy, uz);
+    if (o.mode & READ_MOMENTS) {
+        o.rho[idx] = to_double(rho);
+        o.u[idx] = to_double(ux); o.u[p.N + idx] = to_double(uy); o.u[2 * p.N + idx] = to_double(uz);
+    }
+    if (o.mode & READ_POPS) {
+#pragma unroll
+        for (int q = 0; q < 27; q++) o.f[q * p.N + idx] = to_double(f[q]);
+    }
+    if ((o.mode & READ_ACC) && cl != CLS_SOLID) {
+        double* a = p.acc;
+        const long long N = p.N;
+        a[idx] += rho; a[N + idx] += ux; a[2 * N + idx] += uy; a[3 * N + idx] += uz;
+        a[4 * N + idx] += (double)ux * ux; a[5 * N + idx] += (double)uy * uy; a[6 * N + idx] += (double)uz * uz;
+        a[7 * N + idx] += (double)ux * uy; a[8 * N + idx] += (double)ux * uz; a[9 * N + idx] += (double)uy * uz;
+    }
+    if ((o.mode & READ_DIAG) && (cl == CLS_BULK || cl == CLS_EDGE || cl == CLS_OUTLET || cl == CLS_SYM)) {
+        // a non-finite population makes rho or the momentum non-finite (a NaN stays NaN, +-Inf
+        // give Inf or NaN), so the moments stand for the 27 values
+        const bool ok = isfinite(rho) && isfinite(jx) && isfinite(jy) && isfinite(jz);
+        acc.add(RED_MASS, rho);
+        acc.add(RED_MX, rho * ux); acc.add(RED_MY, rho * uy); acc.add(RED_MZ, rho * uz);
+        if (cl != CLS_BULK) {  // only cells beside a solid have momentum-exchange links
+            acc.add(RED_DX, drag[0]); acc.add(RED_DY, drag[1]); acc.add(RED_DZ, drag[2]);
+        }
+        const R u2 = ux * ux + uy * uy + uz * uz;
+        if (isfinite(u2) && u2 > acc.vmax) acc.vmax = u2;
+        acc.nbad += ok ? 0 : 1;
+        acc.nfluid += 1;
+    }
+    if (o.mode & READ_ERROR) {
+        // ErrorQuadratic.h:33-78: sum sqrt|u - u_prev|^2 and sqrt|u|^2 over flag == 1 cells
+        R* uerr = (R*)o.uerr;
+        if (fl & BIT_REFBULK) {
+            const R px = uerr[idx], py = uerr[p.N + idx], pz = uerr[2 * p.N + idx];
+            const R dx = ux - px, dy = uy - py;
+            const R dz = o.ref_compat_err ? uy - pz : uz - pz;
+            const R a1 = dx * dx + dy * dy + dz * dz;
+            const R a2 = ux * ux + uy * uy + uz * uz;
+            acc.add(RED_ERR1, sqrt(a1));
+            acc.add(RED_ERR2, sqrt(a2));
+        }
+        uerr[idx] = ux; uerr[p.N + idx] = uy; uerr[2 * p.N + idx] = uz;  // copy u -> u_error (:80-90), every cell
+    }
+}
+
+// a cell of a reading kernel through the general gather
+template <class S, bool ODD>
+LBM_D void read_cell_general(const Params& p, const ReadOut& o, RedAcc<typename S::R>& acc, int x, int y, int z) {
+    using R = typename S::R;
+    Cell c;
+    make_cell(p, x, y, z, c);
+    const uint8_t fl = p.cls[c.idx];
+    const int cl = fl & CLS_MASK;
+    R f[27];
+    R drag[3] = {0, 0, 0};
+    if (cl == CLS_SOLID) {
+#pragma unroll
+        for (int q = 0; q < 27; q++) f[q] = (R)0;
+    } else if (cl == CLS_INLET) {
+        inlet_state<S>(p, c, f);
+    } else if (cl == CLS_BULK && !on_seam(p, c.x, c.y, c.z)) {
+        load_fast<S, ODD>(p, (unsigned)c.idx, f);  // the step kernel's per-direction addresses
+    } else {
+        gather<S, ODD, true>(p, c, cl, f, drag);
+    }
+    read_cell<S>(p, o, acc, c.idx, fl, f, drag);
+}
+
+// one thread per x-pair of a column tile of kReadZ cells along z; gathers df_m exactly as the step kernel.
+// Pairs of bulk cells off the periodic y/z seams load through the packed pair accesses (one 32-bit FP16 /
+// 64-bit FP32 load per direction for both cells where the AA slot pair is aligned); other pairs cell by cell
+template <class S, bool ODD>
+__global__ void __launch_bounds__(128, 4) k_read(Params p, ReadOut o) {
+    using R = typename S::R;
+    const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = blockIdx.y;
     RedAcc<R> acc;
-    R* uerr = (R*)o.uerr;
-    for (int k = 0; k < kReadZ; k++) {
-        const int z = blockIdx.z * kReadZ + k;
-        if (z >= p.nz) break;
-        Cell c;
-        make_cell(p, live ? x : 0, blockIdx.y, z, c);
-        const uint8_t fl = live ? p.cls[c.idx] : (uint8_t)0;
-        const int cl = fl & CLS_MASK;
-        R f[27];
-        R drag[3] = {0, 0, 0};
-        if (!live || cl == CLS_SOLID) {
+    if (x0 < p.nx) {
+        const bool two = x0 + 1 < p.nx;
+        const bool yz_seam = (p.wrap[1] && (y == 0 || y == p.ny - 1));
+        for (int k = 0; k < kReadZ; k++) {
+            const int z = blockIdx.z * kReadZ + k;
+            if (z >= p.nz) break;
+            const long long idx0 = x0 + (long long)p.nx * (y + (long long)p.ny * z);
+            bool pair = false;
+            uint8_t f0 = 0, f1 = 0;
+            if constexpr (S::kind != 0) {
+                f0 = p.cls[idx0];
+                f1 = two ? p.cls[idx0 + 1] : (uint8_t)0;
+                pair = two && (p.nx & 1) == 0 && !yz_seam && !(p.wrap[2] && (z == 0 || z == p.nz - 1)) &&
+                       (f0 & (uint8_t)~BIT_REFBULK) == CLS_BULK && (f1 & (uint8_t)~BIT_REFBULK) == CLS_BULK;
+            }
+            if constexpr (S::kind != 0) {
+                if (pair) {
+                    const PairCodec kc = make_codec<S>(p);
+                    const PairIdx q = make_pair_idx(p, (int)idx0, x0);
+                    F2 f2[27];
+                    load_pair<S, ODD, false>(p, q, kc, f2);
+                    R fa[27], fb[27];
 #pragma unroll
-            for (int q = 0; q < 27; q++) f[q] = (R)0;
-        } else if (cl == CLS_INLET) {
-            inlet_state<S>(p, c, f);
-        } else if (cl == CLS_BULK && !on_seam(p, c.x, c.y, c.z)) {
-            load_fast<S, ODD>(p, (unsigned)c.idx, f);  // the step kernel's per-direction addresses
-        } else {
-            gather<S, ODD, true>(p, c, cl, f, drag);
-        }
-        R rho = 0, jx = 0, jy = 0, jz = 0, ux = 0, uy = 0, uz = 0;
-        if (live && cl != CLS_SOLID) moments(f, p, rho, jx, jy, jz, ux, uy, uz);
-        if (live && (o.mode & READ_MOMENTS)) {
-            o.rho[c.idx] = to_double(rho);
-            o.u[c.idx] = to_double(ux); o.u[p.N + c.idx] = to_double(uy); o.u[2 * p.N + c.idx] = to_double(uz);
-        }
-        if (live && (o.mode & READ_POPS)) {
-#pragma unroll
-            for (int q = 0; q < 27; q++) o.f[q * p.N + c.idx] = to_double(f[q]);
-        }
-        if (live && (o.mode & READ_ACC) && cl != CLS_SOLID) {
-            double* a = p.acc;
-            const long long N = p.N;
-            a[c.idx] += rho; a[N + c.idx] += ux; a[2 * N + c.idx] += uy; a[3 * N + c.idx] += uz;
-            a[4 * N + c.idx] += (double)ux * ux; a[5 * N + c.idx] += (double)uy * uy; a[6 * N + c.idx] += (double)uz * uz;
-            a[7 * N + c.idx] += (double)ux * uy; a[8 * N + c.idx] += (double)ux * uz; a[9 * N + c.idx] += (double)uy * uz;
-        }
-        if ((o.mode & READ_DIAG) && live && (cl == CLS_BULK || cl == CLS_EDGE || cl == CLS_OUTLET || cl == CLS_SYM)) {
-            // a non-finite population makes rho or the momentum non-finite (a NaN stays NaN, +-Inf
-            // give Inf or NaN), so the moments stand for the 27 values
-            const bool ok = isfinite(rho) && isfinite(jx) && isfinite(jy) && isfinite(jz);
-            acc.add(RED_MASS, rho);
-            acc.add(RED_MX, rho * ux); acc.add(RED_MY, rho * uy); acc.add(RED_MZ, rho * uz);
-            if (cl != CLS_BULK) {  // only cells beside a solid have momentum-exchange links
-                acc.add(RED_DX, drag[0]); acc.add(RED_DY, drag[1]); acc.add(RED_DZ, drag[2]);
+                    for (int v = 0; v < 27; v++) { fa[v] = f2[v].v.x; fb[v] = f2[v].v.y; }
+                    const R nod[3] = {0, 0, 0};
+                    read_cell<S>(p, o, acc, idx0, f0, fa, nod);
+                    read_cell<S>(p, o, acc, idx0 + 1, f1, fb, nod);
+                    continue;
+                }
             }
-            const R u2 = ux * ux + uy * uy + uz * uz;
-            if (isfinite(u2) && u2 > acc.vmax) acc.vmax = u2;
-            acc.nbad += ok ? 0 : 1;
-            acc.nfluid += 1;
-        }
-        if (o.mode & READ_ERROR) {
-            // ErrorQuadratic.h:33-78: sum sqrt|u - u_prev|^2 and sqrt|u|^2 over flag == 1 cells
-            if (live && (fl & BIT_REFBULK)) {
-                const R px = uerr[c.idx], py = uerr[p.N + c.idx], pz = uerr[2 * p.N + c.idx];
-                const R dx = ux - px, dy = uy - py;
-                const R dz = o.ref_compat_err ? uy - pz : uz - pz;
-                const R a1 = dx * dx + dy * dy + dz * dz;
-                const R a2 = ux * ux + uy * uy + uz * uz;
-                acc.add(RED_ERR1, sqrt(a1));
-                acc.add(RED_ERR2, sqrt(a2));
-            }
-            if (live) {  // copy u -> u_error (:80-90), every cell
-                uerr[c.idx] = ux; uerr[p.N + c.idx] = uy; uerr[2 * p.N + c.idx] = uz;
-            }
+            read_cell_general<S, ODD>(p, o, acc, x0, y, z);
+            if (two) read_cell_general<S, ODD>(p, o, acc, x0 + 1, y, z);
         }
     }
     const long long nblk = (long long)gridDim.x * gridDim.y * gridDim.z;

@@ -178,7 +178,7 @@ cudaError_t launch_step_rows(const Params& p, int closure, const int32_t* bulk, 
 
 template <class S>
 cudaError_t launch_read(const Params& p, const ReadOut& o, cudaStream_t st) {
-    const dim3 g = read_grid(p.nx, p.ny, p.nz), b = cell_block(p.nx);
+    const dim3 g = read_grid(p.nx, p.ny, p.nz), b((unsigned)read_block(p.nx));
     if (p.m & 1) k_read<S, true><<<g, b, 0, st>>>(p, o);
     else         k_read<S, false><<<g, b, 0, st>>>(p, o);
     cudaError_t e = cudaGetLastError();
