@@ -3,9 +3,10 @@
 // Replaces the reference preprocessor (3D/preprocess/src/geometry/geometryMesherOFF.h:45-112 with
 // geometryHandlerOFF.h:63-182), which asks a CGAL AABB tree, cell by cell on one host thread, for
 // the distinct intersection points of the segment [cell centre, outside point] and marks the cell
-// inside when their number is odd.  Here one GPU thread owns one (y, z) column of cells and casts a
-// +x ray through it: it collects the x of every triangle whose (y, z) projection contains the
-// column, and a cell is inside when an odd number of crossings lie before its x.  For a closed
+// inside when their number is odd.  Here every (y, z) column of cells casts a +x ray: the column
+// collects the x of every triangle whose (y, z) projection contains it, and a cell is inside when an
+// odd number of crossings lie before its x.  A CTA owns a 4 x 4 tile of columns and runs the exact
+// test only on the triangles whose bounding box meets the tile (k_columns).  For a closed
 // mesh and a cell not on the surface both counts have the same parity, so the flags agree with the
 // reference; the grid (dimensions, float-rounded bounding box and sample points) follows the
 // reference arithmetic exactly.  Ties (a column through an edge or a vertex of the projection) use
@@ -78,8 +79,40 @@ struct Tri {
     double y[3], z[3], x[3];
 };
 
-constexpr int kMaxCross = 256;
-constexpr int kTile = 256;
+constexpr int kMaxCross = 256;  // crossings kept per column
+constexpr int kTileJ = 4, kTileK = 4, kTileCols = kTileJ * kTileK;  // columns of one CTA (y x z)
+constexpr int kVoxThreads = 256;
+constexpr int kChunk = 2048;  // triangles filtered per pass of a CTA
+
+// the (y, z) bounding box of a prepared triangle's projection in float, rounded outwards, so that a
+// float sample point outside it is outside the exact box by at least one float step; NaN coordinates
+// (triangles parallel to the rays) give NaN bounds, which no comparison passes
+struct __align__(16) Box {
+    float y0, y1, z0, z1;
+};
+__host__ __device__ inline float round_down(double v) {
+    float f = (float)v;
+#ifdef __CUDA_ARCH__
+    if ((double)f > v) f = nextafterf(f, -INFINITY);
+#else
+    if ((double)f > v) f = std::nextafter(f, -INFINITY);
+#endif
+    return f;
+}
+__host__ __device__ inline float round_up(double v) {
+    float f = (float)v;
+#ifdef __CUDA_ARCH__
+    if ((double)f < v) f = nextafterf(f, INFINITY);
+#else
+    if ((double)f < v) f = std::nextafter(f, INFINITY);
+#endif
+    return f;
+}
+__host__ __device__ inline Box box_of(const Tri& r) {
+    const double y0 = fmin(r.y[0], fmin(r.y[1], r.y[2])), y1 = fmax(r.y[0], fmax(r.y[1], r.y[2]));
+    const double z0 = fmin(r.z[0], fmin(r.z[1], r.z[2])), z1 = fmax(r.z[0], fmax(r.z[1], r.z[2]));
+    return Box{round_down(y0), round_up(y1), round_down(z0), round_up(z1)};
+}
 
 // edge function of p against the edge (a -> b), evaluated on the canonically ordered endpoints so
 // that the reversed edge gives exactly the negated value
@@ -95,52 +128,77 @@ __device__ __forceinline__ double edge_fn(double ay, double az, double by, doubl
     return swap ? -e : e;
 }
 
-__global__ void k_columns(const Tri* tris, int nt, const float* ys, const float* zs, const float* xs, int nx,
-                          int ny, int nz, int32_t* flags, int* overflow) {
-    __shared__ Tri sh[kTile];
-    const int col = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool live = col < ny * nz;
-    const int j = live ? col % ny : 0, k = live ? col / ny : 0;
-    const double py = ys[j], pz = zs[k];
-    double cross[kMaxCross];
-    int nc = 0;
-    for (int base = 0; base < nt; base += kTile) {
+// x of the crossing of the +x ray through (py, pz) with triangle T, or NaN when the ray misses it
+__device__ __forceinline__ double crossing(const Tri& T, double py, double pz) {
+    bool i0, i1, i2;
+    const double e0 = edge_fn(T.y[1], T.z[1], T.y[2], T.z[2], py, pz, i0);  // opposite vertex 0
+    const double e1 = edge_fn(T.y[2], T.z[2], T.y[0], T.z[0], py, pz, i1);  // opposite vertex 1
+    const double e2 = edge_fn(T.y[0], T.z[0], T.y[1], T.z[1], py, pz, i2);  // opposite vertex 2
+    const bool in = (e0 > 0 || (e0 == 0 && i0)) && (e1 > 0 || (e1 == 0 && i1)) && (e2 > 0 || (e2 == 0 && i2));
+    const double area = e0 + e1 + e2;
+    if (!in || !(area > 0)) return NAN;
+    return (e0 * T.x[0] + e1 * T.x[1] + e2 * T.x[2]) / area;
+}
+
+// One CTA per tile of kTileJ x kTileK (y, z) columns.  Per chunk of triangles, the CTA keeps those
+// whose float box meets the tile's range of sample points (a conservative filter: the exact test can
+// only accept a point inside the exact box), then tests every (candidate, column) pair whose sample
+// lies in the candidate's box with the exact FP64 edge functions and appends the crossing x to the
+// column's list in shared memory.  Last, one warp per column writes the cells: a cell is inside when
+// an odd number of crossings lie before its x (the order of the list does not matter).
+__global__ void __launch_bounds__(kVoxThreads) k_columns(const Tri* tris, const Box* boxes, int nt, const float* ys,
+                                                         const float* zs, const float* xs, int nx, int ny, int nz,
+                                                         int32_t* flags, int* overflow) {
+    __shared__ double cross[kTileCols][kMaxCross];
+    __shared__ int ncross[kTileCols];
+    __shared__ int cand[kChunk];
+    __shared__ int ncand;
+    const int j0 = blockIdx.x * kTileJ, k0 = blockIdx.y * kTileK;
+    const int j1 = min(j0 + kTileJ, ny) - 1, k1 = min(k0 + kTileK, nz) - 1;
+    // sample coordinates increase with the index: the tile's samples lie in [ys[j0], ys[j1]] x [zs[k0], zs[k1]]
+    const float ty0 = ys[j0], ty1 = ys[j1], tz0 = zs[k0], tz1 = zs[k1];
+    if (threadIdx.x < kTileCols) ncross[threadIdx.x] = 0;
+    for (int base = 0; base < nt; base += kChunk) {
+        if (threadIdx.x == 0) ncand = 0;
         __syncthreads();
-        for (int t = threadIdx.x; t < kTile && base + t < nt; t += blockDim.x) sh[t] = tris[base + t];
+        const int cnt = min(kChunk, nt - base);
+        for (int t = threadIdx.x; t < cnt; t += kVoxThreads) {
+            const Box b = boxes[base + t];
+            if (b.y0 <= ty1 && b.y1 >= ty0 && b.z0 <= tz1 && b.z1 >= tz0) cand[atomicAdd(&ncand, 1)] = base + t;
+        }
         __syncthreads();
-        const int cnt = min(kTile, nt - base);
-        if (!live) continue;
-        for (int t = 0; t < cnt; t++) {
-            const Tri& T = sh[t];
-            bool i0, i1, i2;
-            const double e0 = edge_fn(T.y[1], T.z[1], T.y[2], T.z[2], py, pz, i0);  // opposite vertex 0
-            const double e1 = edge_fn(T.y[2], T.z[2], T.y[0], T.z[0], py, pz, i1);  // opposite vertex 1
-            const double e2 = edge_fn(T.y[0], T.z[0], T.y[1], T.z[1], py, pz, i2);  // opposite vertex 2
-            const bool in = (e0 > 0 || (e0 == 0 && i0)) && (e1 > 0 || (e1 == 0 && i1)) && (e2 > 0 || (e2 == 0 && i2));
-            if (!in) continue;
-            const double area = e0 + e1 + e2;
-            if (!(area > 0)) continue;
-            const double xc = (e0 * T.x[0] + e1 * T.x[1] + e2 * T.x[2]) / area;
-            if (nc < kMaxCross) cross[nc++] = xc;
+        const int nc = ncand;
+        for (int w = threadIdx.x; w < nc * kTileCols; w += kVoxThreads) {
+            const int c = w % kTileCols, ti = cand[w / kTileCols];
+            const int j = j0 + c % kTileJ, k = k0 + c / kTileJ;
+            if (j >= ny || k >= nz) continue;
+            const float fy = ys[j], fz = zs[k];
+            const Box b = boxes[ti];
+            if (!(fy >= b.y0 && fy <= b.y1 && fz >= b.z0 && fz <= b.z1)) continue;
+            const double xc = crossing(tris[ti], (double)fy, (double)fz);
+            if (xc != xc) continue;
+            const int slot = atomicAdd(&ncross[c], 1);
+            if (slot < kMaxCross) cross[c][slot] = xc;
             else atomicExch(overflow, 1);
         }
+        __syncthreads();  // the candidate list is refilled by the next chunk
     }
-    if (!live) return;
-    // insertion sort of the crossings, then parity along the column
-    for (int a = 1; a < nc; a++) {
-        double v = cross[a];
-        int b = a - 1;
-        while (b >= 0 && cross[b] > v) { cross[b + 1] = cross[b]; b--; }
-        cross[b + 1] = v;
-    }
-    int32_t* row = flags + (size_t)nx * ((size_t)j + (size_t)ny * k);
-    int q = 0;
-    for (int i = 0; i < nx; i++) {
-        const double px = xs[i];
-        while (q < nc && cross[q] < px) q++;
-        row[i] = q & 1;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int c = warp; c < kTileCols; c += kVoxThreads / 32) {
+        const int j = j0 + c % kTileJ, k = k0 + c / kTileJ;
+        if (j >= ny || k >= nz) continue;
+        const int n = min(ncross[c], kMaxCross);
+        int32_t* row = flags + (size_t)nx * ((size_t)j + (size_t)ny * k);
+        for (int i = lane; i < nx; i += 32) {
+            const double px = xs[i];
+            int q = 0;
+            for (int a = 0; a < n; a++) q += cross[c][a] < px;
+            row[i] = q & 1;
+        }
     }
 }
+
+dim3 column_grid(int ny, int nz) { return dim3((ny + kTileJ - 1) / kTileJ, (nz + kTileK - 1) / kTileK); }
 
 }  // namespace
 
@@ -170,6 +228,7 @@ lbm_status lbm_voxelize_mesh(const double* verts, int32_t nv, const int32_t* tri
     }
     // prepare triangles: drop index errors, orient projections counter-clockwise
     std::vector<Tri> T;
+    std::vector<Box> B;
     T.reserve(nt);
     for (int t = 0; t < nt; t++) {
         int i0 = tris[3 * t], i1 = tris[3 * t + 1], i2 = tris[3 * t + 2];
@@ -181,27 +240,30 @@ lbm_status lbm_voxelize_mesh(const double* verts, int32_t nv, const int32_t* tri
         if (ar == 0) continue;  // parallel to the rays: never crossed
         if (ar < 0) { std::swap(r.x[1], r.x[2]); std::swap(r.y[1], r.y[2]); std::swap(r.z[1], r.z[2]); }
         T.push_back(r);
+        B.push_back(box_of(r));
     }
     if (cudaSetDevice(device) != cudaSuccess) return LBM_ERR_CUDA;
     Tri* dT = nullptr;
+    Box* dB = nullptr;
     float *dy = nullptr, *dz = nullptr, *dx = nullptr;
     int32_t* dflags = nullptr;
     int* dovf = nullptr;
     const size_t ncell = (size_t)nx * ny * nz;
     lbm_status st = LBM_OK;
     if (cudaMalloc(&dT, std::max<size_t>(1, T.size()) * sizeof(Tri)) != cudaSuccess ||
+        cudaMalloc(&dB, std::max<size_t>(1, B.size()) * sizeof(Box)) != cudaSuccess ||
         cudaMalloc(&dx, nx * 4) != cudaSuccess || cudaMalloc(&dy, ny * 4) != cudaSuccess ||
         cudaMalloc(&dz, nz * 4) != cudaSuccess || cudaMalloc(&dflags, ncell * 4) != cudaSuccess ||
         cudaMalloc(&dovf, 4) != cudaSuccess) {
         st = LBM_ERR_OOM;
     } else {
         cudaMemcpy(dT, T.data(), T.size() * sizeof(Tri), cudaMemcpyHostToDevice);
+        cudaMemcpy(dB, B.data(), B.size() * sizeof(Box), cudaMemcpyHostToDevice);
         cudaMemcpy(dx, s[0].data(), nx * 4, cudaMemcpyHostToDevice);
         cudaMemcpy(dy, s[1].data(), ny * 4, cudaMemcpyHostToDevice);
         cudaMemcpy(dz, s[2].data(), nz * 4, cudaMemcpyHostToDevice);
         cudaMemset(dovf, 0, 4);
-        const int cols = ny * nz, bs = 128;
-        k_columns<<<(cols + bs - 1) / bs, bs>>>(dT, (int)T.size(), dy, dz, dx, nx, ny, nz, dflags, dovf);
+        k_columns<<<column_grid(ny, nz), kVoxThreads>>>(dT, dB, (int)T.size(), dy, dz, dx, nx, ny, nz, dflags, dovf);
         int ovf = 0;
         if (cudaGetLastError() != cudaSuccess || cudaMemcpy(&ovf, dovf, 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
             cudaMemcpy(flags_out, dflags, ncell * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
@@ -209,7 +271,7 @@ lbm_status lbm_voxelize_mesh(const double* verts, int32_t nv, const int32_t* tri
         else if (ovf)
             st = LBM_ERR_UNSUPPORTED;  // more than kMaxCross crossings on one column
     }
-    cudaFree(dT); cudaFree(dx); cudaFree(dy); cudaFree(dz); cudaFree(dflags); cudaFree(dovf);
+    cudaFree(dT); cudaFree(dB); cudaFree(dx); cudaFree(dy); cudaFree(dz); cudaFree(dflags); cudaFree(dovf);
     return st;
 }
 
@@ -225,6 +287,7 @@ struct VoxScratch {
     double verts[3 * LBM_VOXELIZE_NOALLOC_MAX_VERTICES];
     int32_t tris[3 * LBM_VOXELIZE_NOALLOC_MAX_TRIANGLES];
     Tri prepared[LBM_VOXELIZE_NOALLOC_MAX_TRIANGLES];
+    Box boxes[LBM_VOXELIZE_NOALLOC_MAX_TRIANGLES];
     float xs[LBM_VOXELIZE_NOALLOC_MAX_DIM], ys[LBM_VOXELIZE_NOALLOC_MAX_DIM], zs[LBM_VOXELIZE_NOALLOC_MAX_DIM];
     int overflow;   // a column met more crossings than the kernel keeps
     int bad_index;  // a triangle referenced a vertex outside [0, nv)
@@ -247,6 +310,7 @@ __global__ void k_prepare(VoxScratch* s, int nv, int nt) {
             s->bad_index = 1;
             for (int b = 0; b < 3; b++) r.x[b] = r.y[b] = r.z[b] = nan("");
             s->prepared[t] = r;
+            s->boxes[t] = box_of(r);
             return;
         }
         r.x[a] = s->verts[3 * id[a]];
@@ -264,6 +328,7 @@ __global__ void k_prepare(VoxScratch* s, int nv, int nt) {
         r.x[2] = tx; r.y[2] = ty; r.z[2] = tz;
     }
     s->prepared[t] = r;
+    s->boxes[t] = box_of(r);
 }
 
 // sample coordinates of geometryMesherOFF.h:94-96 (double arithmetic, stored as float)
@@ -321,9 +386,8 @@ lbm_status lbm_voxelize_mesh_noalloc(const double* verts, int32_t nv, const int3
     k_prepare<<<(nt + bs - 1) / bs, bs>>>(s, nv, nt);
     const int nmax = std::max(nx, std::max(ny, nz));
     k_samples<<<(nmax + bs - 1) / bs, bs>>>(s, nx, ny, nz, resf, addf, blo[0], blo[1], blo[2]);
-    const int cols = ny * nz;
-    k_columns<<<(cols + bs - 1) / bs, bs>>>(s->prepared, nt, s->ys, s->zs, s->xs, nx, ny, nz, flags_out_device,
-                                            &s->overflow);
+    k_columns<<<column_grid(ny, nz), kVoxThreads>>>(s->prepared, s->boxes, nt, s->ys, s->zs, s->xs, nx, ny, nz,
+                                                    flags_out_device, &s->overflow);
     int status[2] = {0, 0};
     if (cudaGetLastError() != cudaSuccess || cudaMemcpy(status, &s->overflow, sizeof(status), cudaMemcpyDeviceToHost) != cudaSuccess)
         return LBM_ERR_CUDA;
