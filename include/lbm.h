@@ -373,7 +373,7 @@ lbm_status lbm_voxelize_mesh(const double* verts, int32_t nv, const int32_t* tri
  * allocation's latency or failure is not acceptable.  This entry point gives the flags of
  * lbm_voxelize_mesh without allocating anything: the caller passes the output as device memory
  * (flags_out_device, dims[0]*dims[1]*dims[2] int32 on `device`; NULL queries dims and bbox only), and
- * the library's own scratch is one fixed array compiled into the library (about 3.6 MB, held on every
+ * the library's own scratch is one fixed array compiled into the library (about 4.1 MB, held on every
  * device that loads the library until the process exits).  Limits: at most
  * LBM_VOXELIZE_NOALLOC_MAX_VERTICES vertices, LBM_VOXELIZE_NOALLOC_MAX_TRIANGLES triangles and
  * LBM_VOXELIZE_NOALLOC_MAX_DIM cells per axis; larger inputs return LBM_ERR_UNSUPPORTED before any
@@ -392,8 +392,8 @@ lbm_status lbm_voxelize_mesh_noalloc(const double* verts, int32_t nv, const int3
 
 /* ---- learned LES closure (no reference counterpart; the reference has OmegaLES only) -----------
  * A per-cell MLP  x(7) -> 32 -> 32 -> 1  maps strain-rate invariants and density to the eddy
- * viscosity:  nu_t = out_scale * softplus(z).  Hidden activation: GELU in its sigmoid form
- * x * sigmoid(1.702 x).  Inputs, from the strain-rate tensor S (lattice units) and rho:
+ * viscosity:  nu_t = out_scale * softplus(z).  Hidden activation: ReLU.  Inputs, from the
+ * strain-rate tensor S (lattice units) and rho:
  *   0 tr S, 1 I2 = (tr^2 S - S:S)/2, 2 I3 = det S, 3 Lode parameter 3 sqrt(6) det(S_d)/|S_d|^3,
  *   4 S_d:S_d / S:S, 5 rho, 6 |S| = sqrt(2 S:S)        (S_d: deviatoric part)
  * normalised as (x - in_mean) / in_std before the first layer.  Training keeps FP32 parameters;

@@ -1,8 +1,8 @@
 // lbm_mlp.cuh - learned LES closure: strain-rate features, the per-warp tensor-core MLP evaluated
 // inside the step kernel, and the activation shared with the training kernels.
 //
-// Network: x(7) -> 32 -> 32 -> 1, GELU in its sigmoid form g(x) = x sigmoid(1.702 x) after both hidden
-// layers, nu_t = out_scale * softplus(z).  Inputs (order of lbm.h) from the strain rate S and rho:
+// Network: x(7) -> 32 -> 32 -> 1, ReLU after both hidden layers, nu_t = out_scale * softplus(z).
+// Inputs (order of lbm.h) from the strain rate S and rho:
 //   0 tr S   1 I2 = (tr^2 S - S:S)/2   2 I3 = det S   3 Lode parameter 3 sqrt(6) det(S_d) / |S_d|^3
 //   4 S_d:S_d / S:S   5 rho   6 |S| = sqrt(2 S:S)
 // normalised as (x - mean) / std.
@@ -11,10 +11,11 @@
 // cells of a warp (two per lane) are staged as 64 rows of 8 halves (7 inputs and a 1 that carries the
 // first bias) and loaded as A fragments with ldmatrix; layer 1 is mma.m16n8k8, layers 2 and 3
 // mma.m16n8k16.  The accumulator fragment of one layer (rows g, g+8, columns 2c, 2c+1 of each n-tile)
-// is the A fragment of the next after packing to f16x2, so no data moves between lanes.  The activation
-// is applied as z (1 + tanh z) with z = 0.851 x (g(x) = x/2 (1 + tanh(0.851 x)) exactly), the factors
-// 0.851 and 1/1.702 being folded into the FP16 weights on the host: one tanh.approx.f16x2 and one HFMA2
-// per two elements.
+// is the A fragment of the next after packing to f16x2, so no data moves between lanes.  The ReLU is
+// part of that pack (cvt.rn.relu.f16x2.f32): one instruction per two elements for the activation and
+// the conversion together.  (A GELU network of the same size measured 15 % slower in the fused step:
+// its tanh.approx.f16x2 and the HFMA2 around it per two elements were the single largest part of the
+// network's cost.)
 #pragma once
 
 #include <cuda_fp16.h>
@@ -27,7 +28,6 @@ namespace lbm {
 constexpr int kMlpIn = 7, kMlpHid = 32, kMlpParams = 1345, kMlpSample = 10;
 // offsets into the FP32 parameter vector: w1[32][7], b1[32], w2[32][32], b2[32], w3[32], b3
 constexpr int kMlpW1 = 0, kMlpB1 = 224, kMlpW2 = 256, kMlpB2 = 1280, kMlpW3 = 1312, kMlpB3 = 1344;
-constexpr float kGeluA = 1.702f;
 // uint4 rows of the fragment table: [0] W1, [1..4] W2 n-tiles, [5] W3, [6..7] b2 (as floats)
 constexpr int kMlpFragRows = 8;
 
@@ -67,13 +67,10 @@ LBM_D void mlp_features(const L (&s)[6], L rho, L (&x)[7]) {
     x[6] = sqrt_pos(s2 + s2);
 }
 
-// ---- training-side activations (FP32) -------------------------------------------------------------
+// ---- training-side activation (FP32) ---------------------------------------------------------------
 LBM_D float sigmoidf_(float x) { return 1.0f / (1.0f + expf(-x)); }
-LBM_D float gelu_s(float x) { return x * sigmoidf_(kGeluA * x); }
-LBM_D float gelu_s_grad(float x) {
-    const float s = sigmoidf_(kGeluA * x);
-    return s + kGeluA * x * s * (1.0f - s);
-}
+LBM_D float relu_f(float x) { return fmaxf(x, 0.0f); }
+LBM_D float relu_grad(float x) { return x > 0.0f ? 1.0f : 0.0f; }
 LBM_D float softplusf_(float z) { return fmaxf(z, 0.0f) + log1pf(expf(-fabsf(z))); }
 // the step kernel's softplus (fast exponential and logarithm)
 LBM_D float softplus_fast(float z) { return fmaxf(z, 0.0f) + __logf(1.0f + __expf(-fabsf(z))); }
@@ -82,12 +79,11 @@ LBM_D float softplus_fast(float z) { return fmaxf(z, 0.0f) + __logf(1.0f + __exp
 LBM_D uint32_t h2_bits(__half2 h) { return *reinterpret_cast<uint32_t*>(&h); }
 LBM_D __half2 bits_h2(uint32_t u) { return *reinterpret_cast<__half2*>(&u); }
 
-// z (1 + tanh z) on a packed pair of accumulators (z already carries the folded 0.851)
+// ReLU of a packed pair of accumulators, rounded to f16x2 (lo in the lower half)
 LBM_D uint32_t mlp_act(float lo, float hi) {
-    const __half2 z = __floats2half2_rn(lo, hi);
-    uint32_t t;
-    asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(h2_bits(z)));
-    return h2_bits(__hfma2(z, bits_h2(t), z));
+    uint32_t h;
+    asm("cvt.rn.relu.f16x2.f32 %0, %1, %2;" : "=r"(h) : "f"(hi), "f"(lo));
+    return h;
 }
 
 LBM_D void mma_k8(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t b0) {
@@ -102,6 +98,22 @@ LBM_D void mma_k16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_
         "{%0,%1,%2,%3};"
         : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
         : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+// the same with a separate accumulator input z in every element (zero here): the output registers are
+// not also the input, so no copy of a zero or bias quad precedes each product (fewer moves and spills;
+// the layer-2 bias is added after the product with one packed add per two elements)
+LBM_D void mma_k8_z(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t b0, float z) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5}, {%6}, {%7,%7,%7,%7};"
+        : "=f"(d[0]), "=f"(d[1]), "=f"(d[2]), "=f"(d[3])
+        : "r"(a0), "r"(a1), "r"(b0), "f"(z));
+}
+LBM_D void mma_k16_z(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0, uint32_t b1, float z) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%10,%10,%10,%10};"
+        : "=f"(d[0]), "=f"(d[1]), "=f"(d[2]), "=f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1), "f"(z));
 }
 LBM_D void ldmatrix_x4(uint32_t (&r)[4], const void* smem_row) {
     const unsigned a = (unsigned)__cvta_generic_to_shared(smem_row);
@@ -195,8 +207,8 @@ LBM_D float2 mlp_warp(uint4 rowA, uint4 rowB, uint4* stage, const uint4 (*wf)[32
         uint32_t h[4][2];
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            float d[4] = {0.f, 0.f, 0.f, 0.f};
-            mma_k8(d, a[2 * t], a[2 * t + 1], w1j[j]);
+            float d[4];
+            mma_k8_z(d, a[2 * t], a[2 * t + 1], w1j[j], 0.0f);
             h[j][0] = mlp_act(d[0], d[1]);
             h[j][1] = mlp_act(d[2], d[3]);
         }
@@ -205,14 +217,15 @@ LBM_D float2 mlp_warp(uint4 rowA, uint4 rowB, uint4* stage, const uint4 (*wf)[32
         for (int j = 0; j < 4; j++) {
             const uint4 w2 = lds128(&wf[1 + j][lane]);
             const float c0 = __uint_as_float(b2[j][0]), c1 = __uint_as_float(b2[j][1]);
-            float d[4] = {c0, c1, c0, c1};
-            mma_k16(d, h[0][0], h[0][1], h[1][0], h[1][1], w2.x, w2.y);
+            float d[4];
+            mma_k16_z(d, h[0][0], h[0][1], h[1][0], h[1][1], w2.x, w2.y, 0.0f);
             mma_k16(d, h[2][0], h[2][1], h[3][0], h[3][1], w2.z, w2.w);
-            h2[j][0] = mlp_act(d[0], d[1]);
-            h2[j][1] = mlp_act(d[2], d[3]);
+            const F2 e0 = F2(d[0], d[1]) + F2(c0, c1), e1 = F2(d[2], d[3]) + F2(c0, c1);
+            h2[j][0] = mlp_act(e0.v.x, e0.v.y);
+            h2[j][1] = mlp_act(e1.v.x, e1.v.y);
         }
-        float d[4] = {0.f, 0.f, 0.f, 0.f};
-        mma_k16(d, h2[0][0], h2[0][1], h2[1][0], h2[1][1], w3.x, w3.y);
+        float d[4];
+        mma_k16_z(d, h2[0][0], h2[0][1], h2[1][0], h2[1][1], w3.x, w3.y, 0.0f);
         mma_k16(d, h2[2][0], h2[2][1], h2[3][0], h2[3][1], w3.z, w3.w);
         if ((lane & 3) == 0) {  // column 0: rows g and g+8 of m-tile t
             out[16 * t + (lane >> 2)] = d[0];

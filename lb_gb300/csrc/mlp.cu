@@ -46,9 +46,9 @@ __global__ void __launch_bounds__(kBlk) k_mlp_grad(const float* __restrict__ sam
     extern __shared__ float sm[];
     float* W = sm;                          // parameters
     float* H1 = W + kSmW;                   // [kBlk][kPad] layer-1 activations
-    float* D1 = H1 + kBlk * kPad;           // gelu'(pre1), then delta1
+    float* D1 = H1 + kBlk * kPad;           // relu'(pre1), then delta1
     float* H2 = D1 + kBlk * kPad;           // layer-2 activations
-    float* D2 = H2 + kBlk * kPad;           // gelu'(pre2), then delta2
+    float* D2 = H2 + kBlk * kPad;           // relu'(pre2), then delta2
     float* X = D2 + kBlk * kPad;            // [kBlk][8] normalised inputs and 1
     float* DZ = X + kBlk * 8;               // dL/dz per sample
     float* LS = DZ + kBlk;                  // loss per sample
@@ -76,15 +76,15 @@ __global__ void __launch_bounds__(kBlk) k_mlp_grad(const float* __restrict__ sam
     for (int i = 0; i < 32; i++) {
         float pre = W[kMlpB1 + i];
         for (int k = 0; k < 7; k++) pre = fmaf(W[kMlpW1 + i * 7 + k], x[k], pre);
-        h1[i] = live ? gelu_s(pre) : 0.f;
-        d1[i] = live ? gelu_s_grad(pre) : 0.f;
+        h1[i] = live ? relu_f(pre) : 0.f;
+        d1[i] = live ? relu_grad(pre) : 0.f;
     }
     float zz = W[kMlpB3];
     for (int o = 0; o < 32; o++) {
         float pre = W[kMlpB2 + o];
         for (int i = 0; i < 32; i++) pre = fmaf(W[kMlpW2 + o * 32 + i], h1[i], pre);
-        h2[o] = live ? gelu_s(pre) : 0.f;
-        d2[o] = live ? gelu_s_grad(pre) : 0.f;
+        h2[o] = live ? relu_f(pre) : 0.f;
+        d2[o] = live ? relu_grad(pre) : 0.f;
         zz = fmaf(W[kMlpW3 + o], h2[o], zz);
     }
     float dz = 0.f, loss = 0.f;
@@ -308,12 +308,11 @@ uint64_t splitmix(uint64_t& s) {
 
 namespace lbm {
 
-// host: FP16 fragment table with the activation constants folded in, and the uniform normalisation
+// host: FP16 fragment table (the weights as trained) and the uniform normalisation
 void mlp_pack(const lbm_mlp_model& m, uint4* frag, MlpNorm& nm) {
-    const float h = 0.5f * kGeluA;  // z = 0.851 x
-    auto W1 = [&](int n, int k) { return h * (k < 7 ? m.params[kMlpW1 + n * 7 + k] : m.params[kMlpB1 + n]); };
-    auto W2 = [&](int n, int k) { return (h / kGeluA) * m.params[kMlpW2 + n * 32 + k]; };
-    auto W3 = [&](int k) { return m.params[kMlpW3 + k] / kGeluA; };
+    auto W1 = [&](int n, int k) { return k < 7 ? m.params[kMlpW1 + n * 7 + k] : m.params[kMlpB1 + n]; };
+    auto W2 = [&](int n, int k) { return m.params[kMlpW2 + n * 32 + k]; };
+    auto W3 = [&](int k) { return m.params[kMlpW3 + k]; };
     auto hb = [](float a, float b) {
         const __half2 v = __floats2half2_rn(a, b);
         uint32_t u;
@@ -341,7 +340,7 @@ void mlp_pack(const lbm_mlp_model& m, uint4* frag, MlpNorm& nm) {
                                              hb(W3(16 + 2 * c), W3(17 + 2 * c)), hb(W3(24 + 2 * c), W3(25 + 2 * c)));
         else
             frag[5 * 32 + lane] = make_uint4(0, 0, 0, 0);
-        auto B2 = [&](int n) { return fb(h * m.params[kMlpB2 + n]); };
+        auto B2 = [&](int n) { return fb(m.params[kMlpB2 + n]); };
         frag[6 * 32 + lane] = make_uint4(B2(2 * c), B2(2 * c + 1), B2(8 + 2 * c), B2(9 + 2 * c));
         frag[7 * 32 + lane] = make_uint4(B2(16 + 2 * c), B2(17 + 2 * c), B2(24 + 2 * c), B2(25 + 2 * c));
     }

@@ -137,13 +137,17 @@ def c4(shape, steps):
     L = capi.lib()
     args = (vv.ctypes.data_as(C.POINTER(C.c_double)), len(vv), ff.ctypes.data_as(C.POINTER(C.c_int32)), len(ff),
             1.0, 2.0)
-    t0 = time.time()
     capi.check(L.lbm_voxelize_mesh(*args, None, dims.ctypes.data_as(C.POINTER(C.c_int32)),
                                    bbox.ctypes.data_as(C.POINTER(C.c_double)), 0))
     g = np.zeros(int(np.prod(dims)), np.int32)
-    capi.check(L.lbm_voxelize_mesh(*args, g.ctypes.data_as(C.POINTER(C.c_int32)), dims.ctypes.data_as(C.POINTER(C.c_int32)),
-                                   bbox.ctypes.data_as(C.POINTER(C.c_double)), 0))
-    t_gpu = time.time() - t0
+    t_gpu = None
+    for _ in range(3):  # the first call also loads the kernel module: best of three calls
+        t0 = time.time()
+        capi.check(L.lbm_voxelize_mesh(*args, g.ctypes.data_as(C.POINTER(C.c_int32)),
+                                       dims.ctypes.data_as(C.POINTER(C.c_int32)),
+                                       bbox.ctypes.data_as(C.POINTER(C.c_double)), 0))
+        dt = time.time() - t0
+        t_gpu = dt if t_gpu is None else min(t_gpu, dt)
     t0 = time.time()
     ref, _ = O.voxelize_mesh(v, f, 1.0, 2.0, (-300.0, -270.0, -240.0))
     t_orc = time.time() - t0
@@ -279,8 +283,9 @@ def c5(n, steps, k, models):
         g.init_fields(np.ones(n ** 3), uc0.reshape(3, -1))
         if name:
             g.load_mlp(nets[name])
-        ms = g.step_timed(steps)
+        g.step(steps)
         u = g.moments()[1].reshape(3, n, n, n)
+        ms = g.step_timed(steps)  # throughput on warm kernels, after the compared state is read
         g.close()
         post[label] = float(np.linalg.norm(u - u_ref) / np.linalg.norm(u_ref))
         thr[label] = n ** 3 * steps / (ms * 1e-3) / 1e9
