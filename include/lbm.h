@@ -143,6 +143,11 @@ const char* lbm_config_last_error(void);
                                     instead of the packed wall kernel (the per-cell and packed paths round
                                     differently; this keeps the split step bit-identical to one launch) */
 
+#define LBM_OPT_MLP_TCGEN05 16  /* learned closure (LBM_CLOSURE_MLP): the network of the plain-row step
+                                   kernel runs on tcgen05.mma with TMEM accumulators (one CTA's 256 cells
+                                   per product) instead of warp-level mma.sync; same inputs, weights and
+                                   ReLU, FP32 accumulation in another order */
+
 /* boundary-condition records, mirroring LBMTraits.h:17-43 */
 typedef struct lbm_vertex { int32_t x, y, z; } lbm_vertex;
 
@@ -438,6 +443,14 @@ lbm_status lbm_les_samples(lbm_ctx* fine, int32_t width, float* out, int64_t cap
  * in_range (nullable) receives 1 where every input lies in [in_lo, in_hi] */
 lbm_status lbm_mlp_eval(const lbm_mlp_model* model, const float* x, int64_t n, float* nu,
                         int32_t* in_range, int32_t device);
+/* the same through a chosen product path: LBM_MLP_PATH_WARP_MMA (warp-level mma.sync, the default of
+ * the step kernel) or LBM_MLP_PATH_TCGEN05 (tcgen05.mma with TMEM accumulators, one CTA per 256 inputs;
+ * the path LBM_OPT_MLP_TCGEN05 selects in the step kernel).  LBM_ERR_TIMEOUT if a CTA gave up waiting
+ * for its products. */
+#define LBM_MLP_PATH_WARP_MMA 0
+#define LBM_MLP_PATH_TCGEN05  1
+lbm_status lbm_mlp_eval_path(const lbm_mlp_model* model, const float* x, int64_t n, float* nu,
+                             int32_t* in_range, int32_t path, int32_t device);
 
 /* GPU trainer: the samples (n * LBM_MLP_SAMPLE floats) are copied to the device once.  Loss of a set
  * of samples: the mean of (c + 4 nu_t a + 4 nu_t^2 b) / K with K the mean of c over all the trainer's

@@ -61,6 +61,8 @@ LBM_OPT_ROW_STAGING = 1
 LBM_OPT_F16_ROUND_NEAREST = 2
 LBM_OPT_ONE_LAUNCH = 4
 LBM_OPT_NO_WALL_ROWS = 8
+LBM_OPT_MLP_TCGEN05 = 16
+LBM_MLP_PATH_WARP_MMA, LBM_MLP_PATH_TCGEN05 = 0, 1
 
 
 LBM_MLP_INPUTS = 7
@@ -235,6 +237,7 @@ def lib():
         "lbm_mlp_load": ([vp, C.POINTER(LbmMlpModel)], i32),
         "lbm_les_samples": ([vp, i32, fp, i64, C.POINTER(i64)], i32),
         "lbm_mlp_eval": ([C.POINTER(LbmMlpModel), fp, i64, fp, ip, i32], i32),
+        "lbm_mlp_eval_path": ([C.POINTER(LbmMlpModel), fp, i64, fp, ip, i32, i32], i32),
         "lbm_mlp_trainer_create": ([fp, i64, i32, C.POINTER(vp)], i32),
         "lbm_mlp_trainer_destroy": ([vp], i32),
         "lbm_mlp_trainer_norm": ([vp], f64),

@@ -11,6 +11,7 @@
 #include "lbm_aux.cuh"
 #include "lbm_launch.h"
 #include "lbm_mlp_host.h"
+#include "lbm_sync.cuh"
 
 #include <cmath>
 #include <cstdarg>
@@ -196,6 +197,7 @@ static Params make_params(const lbm_ctx* c) {
     p.mlp = c->mlp_norm;
     p.nut = c->d_nut;
     p.mlp_run = 0;
+    p.mlp_tc = (c->cfg.options & LBM_OPT_MLP_TCGEN05) ? 1 : 0;
     p.acc = nullptr;
     p.err = c->d_err;
     return p;
@@ -991,7 +993,10 @@ static lbm_status check_device_error(lbm_ctx* c) {
     CU(c, cudaStreamSynchronize(c->st));
     if (h != 0) {
         CU(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
-        return fail(c, LBM_ERR_TIMEOUT, "a row-staged step gave up waiting for its bulk copies (code %d)", h);
+        return fail(c, LBM_ERR_TIMEOUT, "%s (code %d)",
+                    h == DEV_ERR_MMA_TIMEOUT ? "a step kernel gave up waiting for its tensor-core products"
+                                             : "a row-staged step gave up waiting for its bulk copies",
+                    h);
     }
     return LBM_OK;
 }
@@ -1272,7 +1277,7 @@ lbm_status lbm_mlp_load(lbm_ctx* c, const lbm_mlp_model* m) {
         return fail(c, LBM_ERR_STATE, "lbm_mlp_load: the context was not created with LBM_CLOSURE_MLP");
     if (!mlp_model_valid(m)) return fail(c, LBM_ERR_INVALID, "lbm_mlp_load: non-finite parameters or bad scales");
     cudaSetDevice(c->cfg.device);
-    std::vector<uint4> frag(kMlpFragRows * 32);
+    std::vector<uint4> frag(kMlpFragTotal);  // warp fragment table, then the tcgen05 weight image
     MlpNorm nm;
     mlp_pack(*m, frag.data(), nm);
     if (!c->d_mlp_frag) CU(c, cudaMalloc(&c->d_mlp_frag, frag.size() * sizeof(uint4)));

@@ -125,6 +125,7 @@ struct Params {
     MlpNorm mlp;
     __half* nut;             // per-cell nu_t of the last network evaluation (refresh interval > 1)
     int mlp_run;             // with nut: the network runs in this step
+    int mlp_tc;              // the plain-row kernel evaluates the network with tcgen05.mma (TMEM)
     // per-step options
     double* acc;             // time-average accumulators [10][N] (nullptr: off)
     int* err;                // device error word (bounded waits that gave up)

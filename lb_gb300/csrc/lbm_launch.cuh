@@ -23,6 +23,10 @@ inline dim3 rows_grid(unsigned xb, int n) {
 template <class S, int COLL, int ROWS>
 static RowKernel mlp_kernel(const Params& p) {
     const bool odd = (p.m & 1) != 0;
+    if constexpr (ROWS == 1) {  // the plain rows: the network on tcgen05 when the option asks for it
+        if (p.mlp_tc && !p.nut) return odd ? k_step2_mlp<S, COLL, true, 0, 1, true> : k_step2_mlp<S, COLL, false, 0, 1, true>;
+        if (p.mlp_tc && p.mlp_run) return odd ? k_step2_mlp<S, COLL, true, 1, 1, true> : k_step2_mlp<S, COLL, false, 1, 1, true>;
+    }
     if (!p.nut) return odd ? k_step2_mlp<S, COLL, true, 0, ROWS> : k_step2_mlp<S, COLL, false, 0, ROWS>;
     if (p.mlp_run) return odd ? k_step2_mlp<S, COLL, true, 1, ROWS> : k_step2_mlp<S, COLL, false, 1, ROWS>;
     return odd ? k_step2_mlp<S, COLL, true, 2, ROWS> : k_step2_mlp<S, COLL, false, 2, ROWS>;

@@ -28,8 +28,12 @@ namespace lbm {
 constexpr int kMlpIn = 7, kMlpHid = 32, kMlpParams = 1345, kMlpSample = 10;
 // offsets into the FP32 parameter vector: w1[32][7], b1[32], w2[32][32], b2[32], w3[32], b3
 constexpr int kMlpW1 = 0, kMlpB1 = 224, kMlpW2 = 256, kMlpB2 = 1280, kMlpW3 = 1312, kMlpB3 = 1344;
-// uint4 rows of the fragment table: [0] W1, [1..4] W2 n-tiles, [5] W3, [6..7] b2 (as floats)
+// uint4 rows of the fragment table: [0] W1, [1..4] W2 n-tiles, [5] W3, [6..7] b2 (as floats); the
+// device buffer holds the table ([kMlpFragRows][32]) followed by the tcgen05 weight image
+// (kMlpTcRows uint4, lbm_mlp_tc.cuh)
 constexpr int kMlpFragRows = 8;
+constexpr int kMlpTcRows = 256;
+constexpr int kMlpFragTotal = kMlpFragRows * 32 + kMlpTcRows;
 
 // ---- features -------------------------------------------------------------------------------------
 LBM_D float lmax(float a, float b) { return fmaxf(a, b); }
@@ -127,6 +131,7 @@ LBM_D void ldmatrix_x4(uint32_t (&r)[4], const void* smem_row) {
 struct MlpNorm {
     float isd[7], nmi[7], lo[7], hi[7];
     float b3, scale;
+    float b2[32];  // layer-2 bias (the tcgen05 path adds it after the accumulator load)
 };
 
 // normalised inputs of one cell as a row of 8 halves (input 7 = 1), and whether all lie in range

@@ -15,6 +15,7 @@
 #pragma once
 
 #include "lbm_mlp.cuh"
+#include "lbm_mlp_tc.cuh"
 #include "lbm_step.cuh"
 
 namespace lbm {
@@ -36,29 +37,13 @@ constexpr int mlp_min_blocks(int mode, int rows, int coll, int kind) {
     return mode == 2 ? (rows == 1 ? plain_min_blocks(coll, kind) : step2_min_blocks(coll))
                      : (rows == 1 ? LBM_MLP_PLAIN_MIN_BLOCKS : LBM_MLP_MIN_BLOCKS);
 }
-template <class S, int COLL, bool ODD, int MODE, int ROWS = 0>
-__global__ void __launch_bounds__(128, mlp_min_blocks(MODE, ROWS, COLL, S::kind)) k_step2_mlp(Params p, const int32_t* rows, int nrows) {
-    static_assert(S::kind != 0, "the learned closure runs on the packed FP32 path");
-    __shared__ uint4 wf[MODE == 2 ? 1 : kMlpFragRows][32];
-    __shared__ uint4 stage[MODE == 2 ? 1 : 4][64];
-    if constexpr (MODE != 2) {
-        for (int i = threadIdx.x; i < kMlpFragRows * 32; i += blockDim.x) (&wf[0][0])[i] = p.mlp_frag[i];
-        __syncthreads();
-    }
-
-    int x0, y = 0, z = 0, r = 0;
+// one x-pair of the learned-closure step (x0 even; y, z for ROWS 0 and 2, row r for ROWS 1).  Every
+// thread of the warp (TC: of the CTA) calls it, including threads without a pair, since the network runs
+// for the warp's (CTA's) cells together.
+template <class S, int COLL, bool ODD, int MODE, int ROWS, bool TC, class TS>
+LBM_D void mlp_pair(const Params& p, int x0, int y, int z, int r, const uint4 (*wf)[32], uint4* stage, TS& ts,
+                    uint32_t tm, unsigned parity) {
     unsigned idx0;
-    if constexpr (ROWS == 0) {
-        x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
-        y = blockIdx.y;
-        z = blockIdx.z;
-    } else {
-        if (!row_block(rows, nrows, r, x0)) return;  // tail block past the list: the whole block leaves
-        if constexpr (ROWS == 2) {
-            y = r % p.ny;
-            z = r / p.ny;
-        }
-    }
     const bool live = x0 < p.nx;
     const bool two = x0 + 1 < p.nx;
     if constexpr (ROWS == 1) idx0 = (unsigned)(live ? x0 : 0) + (unsigned)p.nx * (unsigned)r;
@@ -132,7 +117,9 @@ __global__ void __launch_bounds__(128, mlp_min_blocks(MODE, ROWS, COLL, S::kind)
     }
     float nuA = kept.x, nuB = kept.y;
     if constexpr (MODE != 2) {
-        const float2 zo = mlp_warp(rowA, rowB, stage[threadIdx.x >> 5], wf);
+        float2 zo;
+        if constexpr (TC) zo = tc_mlp(ts, tm, rowA, rowB, p.mlp, p.err, parity);
+        else zo = mlp_warp(rowA, rowB, stage, wf);
         nuA = inA ? mlp_nu(zo.x, p.mlp) : -1.0f;
         nuB = inB ? mlp_nu(zo.y, p.mlp) : -1.0f;
         if (MODE == 1 && pair) *(__half2*)(p.nut + idx0) = __floats2half2_rn(nuA, nuB);
@@ -156,6 +143,38 @@ __global__ void __launch_bounds__(128, mlp_min_blocks(MODE, ROWS, COLL, S::kind)
             if (two) step_cell_call<S, COLL, 1, ODD>(p, x0 + 1, y, z);
         }
     }
+}
+
+// TC (plain rows, network steps): the network on tcgen05.mma with TMEM accumulators for the CTA's cells
+// (lbm_mlp_tc.cuh) instead of the per-warp mma.sync evaluation
+template <class S, int COLL, bool ODD, int MODE, int ROWS = 0, bool TC = false>
+__global__ void __launch_bounds__(128, mlp_min_blocks(MODE, ROWS, COLL, S::kind)) k_step2_mlp(Params p, const int32_t* rows, int nrows) {
+    static_assert(S::kind != 0, "the learned closure runs on the packed FP32 path");
+    static_assert(!TC || (ROWS == 1 && MODE != 2), "the tcgen05 network serves the plain rows' network steps");
+    constexpr bool WARP = MODE != 2 && !TC;
+    __shared__ uint4 wf[WARP ? kMlpFragRows : 1][32];
+    __shared__ uint4 stage[WARP ? 4 : 1][64];
+    __shared__ typename std::conditional<TC, TcSmem, char>::type ts;
+    if constexpr (WARP) {
+        for (int i = threadIdx.x; i < kMlpFragRows * 32; i += blockDim.x) (&wf[0][0])[i] = p.mlp_frag[i];
+        __syncthreads();
+    }
+    int x0, y = 0, z = 0, r = 0;
+    if constexpr (ROWS == 0) {
+        x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+        y = blockIdx.y;
+        z = blockIdx.z;
+    } else {
+        if (!row_block(rows, nrows, r, x0)) return;  // tail block past the list: the whole block leaves
+        if constexpr (ROWS == 2) {
+            y = r % p.ny;
+            z = r / p.ny;
+        }
+    }
+    uint32_t tm = 0;
+    if constexpr (TC) tm = tc_setup(ts, p.mlp_frag + kMlpFragRows * 32);
+    mlp_pair<S, COLL, ODD, MODE, ROWS, TC>(p, x0, y, z, r, wf, stage[WARP ? threadIdx.x >> 5 : 0], ts, tm, 0u);
+    if constexpr (TC) tc_teardown(tm);
 }
 
 }  // namespace lbm

@@ -17,28 +17,13 @@
 #pragma once
 
 #include "lbm_step.cuh"
+#include "lbm_sync.cuh"
 
 namespace lbm {
 
-// ---- PTX: shared-memory barrier and bulk copies -------------------------------------------------------
-LBM_D unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-LBM_D void mbar_init(uint64_t* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-LBM_D void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// ---- PTX: bulk copies (the mbarrier helpers are in lbm_sync.cuh) ------------------------------------
 LBM_D void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-LBM_D bool mbar_try_wait(uint64_t* bar, unsigned parity) {
-    unsigned ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
 }
 // global -> shared, completion counted on the mbarrier (both addresses and the size 16-byte aligned)
 LBM_D void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
@@ -54,8 +39,6 @@ LBM_D void bulk_s2g(void* dst, const void* src, unsigned bytes) {
 }
 LBM_D void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 LBM_D void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
-// order this thread's shared-memory writes before later bulk (async-proxy) reads of them
-LBM_D void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // velocity table for the copy-issuing thread (runtime direction index)
 static __constant__ signed char kVel[27][3] = {
@@ -64,9 +47,6 @@ static __constant__ signed char kVel[27][3] = {
     {0, -1, 1},  {-1, 1, 0},  {1, -1, 0},  {0, 1, 1},   {0, -1, -1}, {-1, 1, -1}, {1, -1, 1},
     {-1, -1, 1}, {1, 1, -1},  {1, -1, -1}, {-1, 1, 1},  {-1, -1, -1}, {1, 1, 1}};
 
-enum : int { DEV_ERR_TMA_TIMEOUT = 1 };
-
-constexpr int kWaitLimit = 1 << 22;  // try_wait attempts before the CTA gives up
 
 // halo of one 16-byte unit on each side of a shared segment (keeps the bulk copies aligned)
 template <class S>

@@ -15,6 +15,7 @@
 #include "lbm_device.cuh"
 #include "lbm_launch.h"
 #include "lbm_mlp_host.h"
+#include "lbm_mlp_tc.cuh"
 
 #include <cmath>
 #include <cstring>
@@ -192,6 +193,30 @@ __global__ void __launch_bounds__(128) k_mlp_eval(const float* __restrict__ x, l
     if (sB < n) { nu[sB] = mlp_nu(z.y, nm); if (in_range) in_range[sB] = okB; }
 }
 
+// the same through the tcgen05 path: one CTA of 128 threads per 256 samples (thread t: samples 2t, 2t+1)
+__global__ void __launch_bounds__(128) k_mlp_eval_tc(const float* __restrict__ x, long long n, const uint4* __restrict__ img,
+                                                     MlpNorm nm, float* __restrict__ nu, int32_t* __restrict__ in_range,
+                                                     int* err) {
+    __shared__ TcSmem ts;
+    const uint32_t tm = tc_setup(ts, img);
+    const long long sA = (long long)blockIdx.x * 256 + 2 * threadIdx.x, sB = sA + 1;
+    uint4 rA = make_uint4(0, 0, 0, 0), rB = rA;
+    bool okA = false, okB = false;
+    float xr[7];
+    if (sA < n) {
+        for (int i = 0; i < 7; i++) xr[i] = x[sA * 7 + i];
+        rA = mlp_row(xr, nm, okA);
+    }
+    if (sB < n) {
+        for (int i = 0; i < 7; i++) xr[i] = x[sB * 7 + i];
+        rB = mlp_row(xr, nm, okB);
+    }
+    const float2 z = tc_mlp(ts, tm, rA, rB, nm, err, 0u);
+    tc_teardown(tm);
+    if (sA < n) { nu[sA] = mlp_nu(z.x, nm); if (in_range) in_range[sA] = okA; }
+    if (sB < n) { nu[sB] = mlp_nu(z.y, nm); if (in_range) in_range[sB] = okB; }
+}
+
 // ---- filtered samples -------------------------------------------------------------------------------
 // coarse cell = w^3 fine cells: mean rho and u, the filtered stress <u_i u_j> - <u_i><u_j> (FP64 sums,
 // the difference taken in FP64), and whether every fine cell is fluid.  cf: [11][Nc] =
@@ -352,6 +377,20 @@ void mlp_pack(const lbm_mlp_model& m, uint4* frag, MlpNorm& nm) {
     }
     nm.b3 = m.params[kMlpB3];
     nm.scale = m.out_scale;
+    for (int n = 0; n < 32; n++) nm.b2[n] = m.params[kMlpB2 + n];
+    // the tcgen05 weight image after the table: W1 (k 0..6 weights, k 7 = b1, 8..15 zero), W2, W3 (row
+    // 0 = w3), FP16, K-major core matrices of 8 rows x 8 halves (lbm_mlp_tc.cuh)
+    std::vector<__half> img(kTcWBytes / 2, __float2half(0.0f));
+    auto put = [&](int base, int KG, int n, int k, float v) {
+        img[(base + tc_off(n, k >> 3, KG)) / 2 + (k & 7)] = __float2half_rn(v);
+    };
+    for (int n = 0; n < 32; n++) {
+        for (int k = 0; k < 7; k++) put(kTcW1, 2, n, k, m.params[kMlpW1 + n * 7 + k]);
+        put(kTcW1, 2, n, 7, m.params[kMlpB1 + n]);
+        for (int k = 0; k < 32; k++) put(kTcW2, 4, n, k, m.params[kMlpW2 + n * 32 + k]);
+    }
+    for (int k = 0; k < 32; k++) put(kTcW3, 4, 0, k, m.params[kMlpW3 + k]);
+    std::memcpy(frag + kMlpFragRows * 32, img.data(), kTcWBytes);
 }
 
 bool mlp_model_valid(const lbm_mlp_model* m) { return model_ok(m); }
@@ -393,16 +432,25 @@ const char* lbm_mlp_last_error(void) { return g_mlp_err.c_str(); }
 
 lbm_status lbm_mlp_eval(const lbm_mlp_model* m, const float* x, int64_t n, float* nu, int32_t* in_range,
                         int32_t device) {
-    if (!model_ok(m) || n < 0 || (n > 0 && (!x || !nu))) return mfail(LBM_ERR_INVALID, "lbm_mlp_eval: bad arguments");
+    return lbm_mlp_eval_path(m, x, n, nu, in_range, LBM_MLP_PATH_WARP_MMA, device);
+}
+
+lbm_status lbm_mlp_eval_path(const lbm_mlp_model* m, const float* x, int64_t n, float* nu, int32_t* in_range,
+                             int32_t path, int32_t device) {
+    if (!model_ok(m) || n < 0 || (n > 0 && (!x || !nu)) || (path != LBM_MLP_PATH_WARP_MMA && path != LBM_MLP_PATH_TCGEN05))
+        return mfail(LBM_ERR_INVALID, "lbm_mlp_eval: bad arguments");
     if (n == 0) return LBM_OK;
     MCU(cudaSetDevice(device));
-    std::vector<uint4> frag(kMlpFragRows * 32);
+    std::vector<uint4> frag(kMlpFragTotal);
     MlpNorm nm;
     mlp_pack(*m, frag.data(), nm);
     uint4* d_frag = nullptr;
     float *d_x = nullptr, *d_nu = nullptr;
     int32_t* d_in = nullptr;
+    int* d_err = nullptr;
     cudaError_t e = cudaMalloc(&d_frag, frag.size() * sizeof(uint4));
+    if (e == cudaSuccess) e = cudaMalloc(&d_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(d_err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&d_x, (size_t)n * 7 * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&d_nu, (size_t)n * sizeof(float));
     if (e == cudaSuccess && in_range) e = cudaMalloc(&d_in, (size_t)n * sizeof(int32_t));
@@ -410,13 +458,19 @@ lbm_status lbm_mlp_eval(const lbm_mlp_model* m, const float* x, int64_t n, float
     if (e == cudaSuccess) e = cudaMemcpy(d_x, x, (size_t)n * 7 * sizeof(float), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
         const long long blocks = (n + 255) / 256;
-        k_mlp_eval<<<(unsigned)blocks, 128>>>(d_x, n, d_frag, nm, d_nu, d_in);
+        if (path == LBM_MLP_PATH_TCGEN05)
+            k_mlp_eval_tc<<<(unsigned)blocks, 128>>>(d_x, n, d_frag + kMlpFragRows * 32, nm, d_nu, d_in, d_err);
+        else
+            k_mlp_eval<<<(unsigned)blocks, 128>>>(d_x, n, d_frag, nm, d_nu, d_in);
         e = cudaGetLastError();
     }
+    int herr = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(nu, d_nu, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && in_range) e = cudaMemcpy(in_range, d_in, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost);
-    cudaFree(d_frag); cudaFree(d_x); cudaFree(d_nu); cudaFree(d_in);
+    cudaFree(d_frag); cudaFree(d_x); cudaFree(d_nu); cudaFree(d_in); cudaFree(d_err);
     if (e != cudaSuccess) return mfail(LBM_ERR_CUDA, std::string("lbm_mlp_eval: ") + cudaGetErrorString(e));
+    if (herr) return mfail(LBM_ERR_TIMEOUT, "lbm_mlp_eval: a CTA gave up waiting for its tensor-core products");
     return LBM_OK;
 }
 

@@ -94,15 +94,16 @@ class MlpModel:
         return cls(d["params"], d["in_mean"], d["in_std"], d["in_lo"], d["in_hi"], float(d["out_scale"]))
 
 
-def evaluate(model, x, device=0):
-    """nu_t and the in-range flag of raw inputs x (n x 7) on the GPU (FP16 tensor-core path)."""
+def evaluate(model, x, device=0, path=capi.LBM_MLP_PATH_WARP_MMA):
+    """nu_t and the in-range flag of raw inputs x (n x 7) on the GPU (FP16 tensor-core path: warp-level
+    mma.sync, or tcgen05.mma with TMEM accumulators for path=capi.LBM_MLP_PATH_TCGEN05)."""
     x = np.ascontiguousarray(x, np.float32).reshape(-1, NIN)
     n = x.shape[0]
     nu = np.zeros(n, np.float32)
     ok = np.zeros(n, np.int32)
     m = model.struct()
-    check(lib().lbm_mlp_eval(C.byref(m), _fp(x), n, _fp(nu), ok.ctypes.data_as(C.POINTER(C.c_int32)), device),
-          mlp=True)
+    check(lib().lbm_mlp_eval_path(C.byref(m), _fp(x), n, _fp(nu), ok.ctypes.data_as(C.POINTER(C.c_int32)), path,
+                                  device), mlp=True)
     return nu, ok.astype(bool)
 
 

@@ -79,7 +79,7 @@ def test_eval_matches_fp16_oracle(built_lib):
     nu, ok = les.evaluate(m, x)
     ref, ref_ok = lo.infer_fp16(m.params, x, m.in_mean, m.in_std, m.in_lo, m.in_hi, m.out_scale)
     assert np.array_equal(ok, ref_ok)
-    # tanh.approx.f16x2 against the exact tanh of the emulation, FP16 activations: 2 % of nu
+    # FP16 activations rounded after FP32 sums (float64 in the emulation): 2 % of nu
     rel = np.abs(nu - ref) / np.abs(ref)
     assert np.quantile(rel, 0.99) < 2e-2 and rel.max() < 5e-2, (np.quantile(rel, 0.99), rel.max())
     # inputs outside the range are flagged
@@ -89,8 +89,29 @@ def test_eval_matches_fp16_oracle(built_lib):
     assert not ok2[::2].any()
 
 
+def test_eval_tcgen05_matches_warp_path_and_oracle(built_lib):
+    """The network on tcgen05.mma (TMEM accumulators, one CTA per 256 inputs) against the warp-level
+    mma.sync path and the FP16 oracle: the same FP16 operands and ReLU, FP32 sums in another order, so
+    the two GPU paths agree to FP16 rounding of the hidden activations; 1,000 inputs (a partial last
+    CTA) and 300 (a CTA with unused rows)."""
+    m, s = _model_and_samples(seed=13)
+    m.params[:] = np.random.default_rng(7).standard_normal(les.NPAR).astype(np.float32) * 0.3
+    for n in (1000, 300):
+        x = s[:n, :7]
+        nu_w, ok_w = les.evaluate(m, x, path=capi.LBM_MLP_PATH_WARP_MMA)
+        nu_t, ok_t = les.evaluate(m, x, path=capi.LBM_MLP_PATH_TCGEN05)
+        assert np.array_equal(ok_w, ok_t)
+        assert np.all(np.isfinite(nu_t))
+        d = np.abs(nu_t - nu_w) / np.abs(nu_w)
+        assert np.quantile(d, 0.99) < 2e-3 and d.max() < 2e-2, (n, np.quantile(d, 0.99), d.max())
+        ref, _ = lo.infer_fp16(m.params, x, m.in_mean, m.in_std, m.in_lo, m.in_hi, m.out_scale)
+        rel = np.abs(nu_t - ref) / np.abs(ref)
+        assert np.quantile(rel, 0.99) < 2e-2 and rel.max() < 5e-2, (n, np.quantile(rel, 0.99), rel.max())
+
+
+@pytest.mark.parametrize("tc", [False, True])
 @pytest.mark.parametrize("storage", ["f32", "f16dev"])
-def test_fused_mlp_out_of_range_is_smagorinsky(built_lib, storage):
+def test_fused_mlp_out_of_range_is_smagorinsky(built_lib, storage, tc):
     """A model whose training range excludes every input relaxes every cell with the Smagorinsky rate:
     the populations equal those of the Smagorinsky kernel bit for bit."""
     shape = (64, 18, 12)
@@ -101,8 +122,9 @@ def test_fused_mlp_out_of_range_is_smagorinsky(built_lib, storage):
     out = []
     for clos in (OmegaLES, OmegaMLP):
         # the learned closure takes wall rows through the per-cell path: so does the Smagorinsky run here
+        opts = capi.LBM_OPT_NO_WALL_ROWS | (capi.LBM_OPT_MLP_TCGEN05 if tc else 0)
         s = Solver(shape, turbulence=clos, storage=storage, nu=c["nu"], cles=0.17, periodic=c["periodic"],
-                   options=capi.LBM_OPT_NO_WALL_ROWS, force=c["force"])
+                   options=opts, force=c["force"])
         s.set_flags(c["flags"])
         s.set_bc()
         s.init_fields(c["rho"], c["u"])
@@ -245,8 +267,9 @@ def oracle_learned_rate(f, force, tau, cles, m, smag_only=None):
     return om, nu, ok, x
 
 
+@pytest.mark.parametrize("tc", [False, True])
 @pytest.mark.parametrize("storage", ["f32", "f16dev"])
-def test_fused_learned_step_matches_oracle_step(built_lib, oracle_lib, storage):
+def test_fused_learned_step_matches_oracle_step(built_lib, oracle_lib, storage, tc):
     """The headline kernel's learned path against the oracle: the GPU runs the network inside the
     collision kernel (k_step2_mlp, tensor-core FP16 network every step); the oracle runs the reference's
     cumulant step with, per cell and step, the relaxation rate of the same network restated on its own
@@ -256,8 +279,9 @@ def test_fused_learned_step_matches_oracle_step(built_lib, oracle_lib, storage):
     Bounds: FP32 moments within 5e-5 u_max of the FP64 oracle after 24 steps (the FP32 noise floor of the
     case is ~1e-5); FP16 storage 2e-3 relative L2 of u.  With a refresh interval of 2 (mode 1 on even
     steps) the kept nu_t read back from the GPU after a network step matches the oracle's nu_t of that
-    step to 2 % at the 99th percentile (FP32; FP16 tanh.approx against the exact tanh), with the same
-    in-range decision on >= 99 % of the cells."""
+    step to 2 % at the 99th percentile (FP16 activations rounded after FP32 sums), with the same
+    in-range decision on >= 99 % of the cells.  tc: the network of the plain rows on tcgen05.mma
+    (LBM_OPT_MLP_TCGEN05), under the same bounds."""
     from lb_gb300 import capi
     from lb_gb300.solver import CollisionCumD3Q27Turbulent2015
     from oracle import oracle as O
@@ -291,7 +315,8 @@ def test_fused_learned_step_matches_oracle_step(built_lib, oracle_lib, storage):
     g = {}
     for interval in (1, 2):
         s = Solver(shape, collision=CollisionCumD3Q27Turbulent2015, turbulence=OmegaMLP, storage=storage, nu=c["nu"],
-                   cles=0.17, periodic=c["periodic"], force=c["force"], mlp_interval=interval)
+                   cles=0.17, periodic=c["periodic"], force=c["force"], mlp_interval=interval,
+                   options=capi.LBM_OPT_MLP_TCGEN05 if tc else 0)
         s.set_flags(c["flags"])
         s.set_bc()
         s.set_populations(f0)  # the oracle's state after its 5 Smagorinsky steps
