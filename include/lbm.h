@@ -396,7 +396,7 @@ lbm_status lbm_voxelize_mesh_noalloc(const double* verts, int32_t nv, const int3
                                      int32_t dims_out[3], double bbox_out[6], int32_t device);
 
 /* ---- learned LES closure (no reference counterpart; the reference has OmegaLES only) -----------
- * A per-cell MLP  x(7) -> 32 -> 32 -> 1  maps strain-rate invariants and density to the eddy
+ * A per-cell MLP  x(7) -> 16 -> 16 -> 1  maps strain-rate invariants and density to the eddy
  * viscosity:  nu_t = out_scale * softplus(z).  Hidden activation: ReLU.  Inputs, from the
  * strain-rate tensor S (lattice units) and rho:
  *   0 tr S, 1 I2 = (tr^2 S - S:S)/2, 2 I3 = det S, 3 Lode parameter 3 sqrt(6) det(S_d)/|S_d|^3,
@@ -408,8 +408,8 @@ lbm_status lbm_voxelize_mesh_noalloc(const double* verts, int32_t nv, const int3
  * outside [in_lo, in_hi] (the training range), or that is not a bulk cell, relaxes with tau_S.
  * params layout: w1[32][7], b1[32], w2[32][32], b2[32], w3[32], b3 (out x in, row-major). */
 #define LBM_MLP_INPUTS  7
-#define LBM_MLP_HIDDEN  32
-#define LBM_MLP_PARAMS  1345
+#define LBM_MLP_HIDDEN  16
+#define LBM_MLP_PARAMS  417   /* H^2 + 10 H + 1 for H = LBM_MLP_HIDDEN */
 #define LBM_MLP_SAMPLE  10   /* floats per training sample: x[7], a, b, c */
 typedef struct lbm_mlp_model {
     float params[LBM_MLP_PARAMS];

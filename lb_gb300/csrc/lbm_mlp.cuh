@@ -1,7 +1,8 @@
 // lbm_mlp.cuh - learned LES closure: strain-rate features, the per-warp tensor-core MLP evaluated
 // inside the step kernel, and the activation shared with the training kernels.
 //
-// Network: x(7) -> 32 -> 32 -> 1, ReLU after both hidden layers, nu_t = out_scale * softplus(z).
+// Network: x(7) -> H -> H -> 1 (H = kMlpHid = 16), ReLU after both hidden layers,
+// nu_t = out_scale * softplus(z).
 // Inputs (order of lbm.h) from the strain rate S and rho:
 //   0 tr S   1 I2 = (tr^2 S - S:S)/2   2 I3 = det S   3 Lode parameter 3 sqrt(6) det(S_d) / |S_d|^3
 //   4 S_d:S_d / S:S   5 rho   6 |S| = sqrt(2 S:S)
@@ -25,14 +26,20 @@
 
 namespace lbm {
 
-constexpr int kMlpIn = 7, kMlpHid = 32, kMlpParams = 1345, kMlpSample = 10;
-// offsets into the FP32 parameter vector: w1[32][7], b1[32], w2[32][32], b2[32], w3[32], b3
-constexpr int kMlpW1 = 0, kMlpB1 = 224, kMlpW2 = 256, kMlpB2 = 1280, kMlpW3 = 1312, kMlpB3 = 1344;
+constexpr int kMlpIn = 7, kMlpHid = 16, kMlpSample = 10;
+constexpr int kMlpParams = kMlpHid * kMlpHid + 10 * kMlpHid + 1;
+// offsets into the FP32 parameter vector: w1[H][7], b1[H], w2[H][H], b2[H], w3[H], b3
+constexpr int kMlpW1 = 0, kMlpB1 = 7 * kMlpHid, kMlpW2 = 8 * kMlpHid, kMlpB2 = kMlpW2 + kMlpHid * kMlpHid,
+              kMlpW3 = kMlpB2 + kMlpHid, kMlpB3 = kMlpW3 + kMlpHid;
+// warp evaluation: n-tiles of 8 hidden units, k16 steps over the hidden units
+constexpr int kMlpNT = kMlpHid / 8, kMlpKS = kMlpHid / 16;
+static_assert(kMlpHid == 16 || kMlpHid == 32, "the fragment table holds up to four n-tiles");
 // uint4 rows of the fragment table: [0] W1, [1..4] W2 n-tiles, [5] W3, [6..7] b2 (as floats); the
 // device buffer holds the table ([kMlpFragRows][32]) followed by the tcgen05 weight image
 // (kMlpTcRows uint4, lbm_mlp_tc.cuh)
 constexpr int kMlpFragRows = 8;
-constexpr int kMlpTcRows = 256;
+// tcgen05 image: W1 H x 16, W2 H x H, W3 16 x H halves
+constexpr int kMlpTcRows = (kMlpHid * 16 + kMlpHid * kMlpHid + 16 * kMlpHid) * 2 / 16;
 constexpr int kMlpFragTotal = kMlpFragRows * 32 + kMlpTcRows;
 
 // ---- features -------------------------------------------------------------------------------------
@@ -131,7 +138,7 @@ LBM_D void ldmatrix_x4(uint32_t (&r)[4], const void* smem_row) {
 struct MlpNorm {
     float isd[7], nmi[7], lo[7], hi[7];
     float b3, scale;
-    float b2[32];  // layer-2 bias (the tcgen05 path adds it after the accumulator load)
+    float b2[kMlpHid];  // layer-2 bias (the tcgen05 path adds it after the accumulator load)
 };
 
 // normalised inputs of one cell as a row of 8 halves (input 7 = 1), and whether all lie in range
@@ -206,32 +213,38 @@ LBM_D float2 mlp_warp(uint4 rowA, uint4 rowB, uint4* stage, const uint4 (*wf)[32
     const uint4 w3 = lds128(&wf[5][lane]);
     const uint4 bA = lds128(&wf[6][lane]), bB = lds128(&wf[7][lane]);
     const uint32_t w1j[4] = {w1.x, w1.y, w1.z, w1.w};
+    const uint32_t w3k[4] = {w3.x, w3.y, w3.z, w3.w};
     const uint32_t b2[4][2] = {{bA.x, bA.y}, {bA.z, bA.w}, {bB.x, bB.y}, {bB.z, bB.w}};
 #pragma unroll
     for (int t = 0; t < 4; t++) {
-        uint32_t h[4][2];
+        uint32_t h[kMlpNT][2];
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
+        for (int j = 0; j < kMlpNT; j++) {
             float d[4];
             mma_k8_z(d, a[2 * t], a[2 * t + 1], w1j[j], 0.0f);
             h[j][0] = mlp_act(d[0], d[1]);
             h[j][1] = mlp_act(d[2], d[3]);
         }
-        uint32_t h2[4][2];
+        uint32_t h2[kMlpNT][2];
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
+        for (int j = 0; j < kMlpNT; j++) {
             const uint4 w2 = lds128(&wf[1 + j][lane]);
+            const uint32_t w2k[4] = {w2.x, w2.y, w2.z, w2.w};
             const float c0 = __uint_as_float(b2[j][0]), c1 = __uint_as_float(b2[j][1]);
             float d[4];
-            mma_k16_z(d, h[0][0], h[0][1], h[1][0], h[1][1], w2.x, w2.y, 0.0f);
-            mma_k16(d, h[2][0], h[2][1], h[3][0], h[3][1], w2.z, w2.w);
+            mma_k16_z(d, h[0][0], h[0][1], h[1][0], h[1][1], w2k[0], w2k[1], 0.0f);
+#pragma unroll
+            for (int ks = 1; ks < kMlpKS; ks++)
+                mma_k16(d, h[2 * ks][0], h[2 * ks][1], h[2 * ks + 1][0], h[2 * ks + 1][1], w2k[2 * ks], w2k[2 * ks + 1]);
             const F2 e0 = F2(d[0], d[1]) + F2(c0, c1), e1 = F2(d[2], d[3]) + F2(c0, c1);
             h2[j][0] = mlp_act(e0.v.x, e0.v.y);
             h2[j][1] = mlp_act(e1.v.x, e1.v.y);
         }
         float d[4];
-        mma_k16_z(d, h2[0][0], h2[0][1], h2[1][0], h2[1][1], w3.x, w3.y, 0.0f);
-        mma_k16(d, h2[2][0], h2[2][1], h2[3][0], h2[3][1], w3.z, w3.w);
+        mma_k16_z(d, h2[0][0], h2[0][1], h2[1][0], h2[1][1], w3k[0], w3k[1], 0.0f);
+#pragma unroll
+        for (int ks = 1; ks < kMlpKS; ks++)
+            mma_k16(d, h2[2 * ks][0], h2[2 * ks][1], h2[2 * ks + 1][0], h2[2 * ks + 1][1], w3k[2 * ks], w3k[2 * ks + 1]);
         if ((lane & 3) == 0) {  // column 0: rows g and g+8 of m-tile t
             out[16 * t + (lane >> 2)] = d[0];
             out[16 * t + 8 + (lane >> 2)] = d[2];

@@ -10,10 +10,10 @@
 //   (cvt.rn.relu.f16x2.f32) and stores the next layer's A row.  (Alternating the two tiles, so that one
 //   tile's products run while the threads work on the other's accumulators, measured slower: two more
 //   CTA barriers per evaluation.)
-// Shapes (kind::f16, FP16 A and B, FP32 D): layer 1 M128 N32 K16 (7 inputs, a 1 that carries the first
-// bias, 8 zeros); layer 2 M128 N32 K32 (two MMAs, bias added after the load); layer 3 M128 N16 K32 (the
-// output in column 0; rows 1..15 of W3 are zero).  TMEM: 64 columns per CTA, the accumulators of the
-// two tiles at columns 0 and 32 (layer 3: 0 and 16).  Only thread 0 issues MMAs; the other threads'
+// Shapes (kind::f16, FP16 A and B, FP32 D; H = kMlpHid hidden units): layer 1 M128 NH K16 (7 inputs, a 1
+// that carries the first bias, 8 zeros); layer 2 M128 NH KH (H/16 MMAs, bias added after the load);
+// layer 3 M128 N16 KH (the output in column 0; rows 1..15 of W3 are zero).  TMEM: max(2H, 32) columns per
+// CTA, the accumulators of the two tiles at columns 0 and H (layer 3: 0 and 16).  Only thread 0 issues MMAs; the other threads'
 // instructions are the operand stores, the TMEM loads and the pack.
 // Shared-memory operands use the canonical K-major layout without swizzle: a core matrix of 8 rows x 8
 // halves is 128 contiguous bytes (row r at 16 r); core matrix (row group g, k group j) of a matrix with
@@ -29,13 +29,14 @@
 
 namespace lbm {
 
-// the weight image (host-packed, copied into shared memory by every CTA): W1 32 x 16, W2 32 x 32,
-// W3 16 x 32, each K-major in the layout above
-constexpr int kTcW1 = 0, kTcW2 = 1024, kTcW3 = 3072, kTcWBytes = 4096;
+// the weight image (host-packed, copied into shared memory by every CTA): W1 H x 16, W2 H x H, W3 16 x H,
+// each K-major in the layout above
+constexpr int kTcH = kMlpHid, kTcKG = kTcH / 8;  // hidden units; k groups of a hidden-layer operand
+constexpr int kTcW1 = 0, kTcW2 = kTcH * 16 * 2, kTcW3 = kTcW2 + kTcH * kTcH * 2, kTcWBytes = kTcW3 + 16 * kTcH * 2;
 constexpr int kTcWRows = kTcWBytes / 16;  // uint4 rows of the image
 static_assert(kTcWRows == kMlpTcRows, "the image's size in the model buffer");
-constexpr int kTcCols = 64;               // TMEM columns per CTA
-constexpr int kTcA1Bytes = 128 * 16 * 2, kTcA2Bytes = 128 * 32 * 2;
+constexpr int kTcCols = 2 * kTcH < 32 ? 32 : 2 * kTcH;  // TMEM columns per CTA (a power of two >= 32)
+constexpr int kTcA1Bytes = 128 * 16 * 2, kTcA2Bytes = 128 * kTcH * 2;
 
 // byte offset of element (row, k) group: row r, k group j, in a K-major matrix with KG k groups
 LBM_HD constexpr int tc_off(int row, int kg, int KG) { return (row >> 3) * KG * 128 + kg * 128 + (row & 7) * 16; }
@@ -140,15 +141,15 @@ LBM_D void tc_issue(TcSmem& s, uint32_t tm) {
 #pragma unroll
         for (int tile = 0; tile < 2; tile++) {
             if constexpr (LAYER == 1) {
-                tc_mma(tm + (uint32_t)(32 * tile), tc_desc(s.a1[tile], 256), tc_desc(w + kTcW1, 256), tc_idesc(32), 0);
+                tc_mma(tm + (uint32_t)(kTcH * tile), tc_desc(s.a1[tile], 256), tc_desc(w + kTcW1, 256), tc_idesc(kTcH), 0);
             } else {
-                constexpr int N = LAYER == 2 ? 32 : 16;
+                constexpr int N = LAYER == 2 ? kTcH : 16;
                 const char* wb = w + (LAYER == 2 ? kTcW2 : kTcW3);
                 const char* a = reinterpret_cast<const char*>(s.a2[tile]);
 #pragma unroll
-                for (int kk = 0; kk < 2; kk++)  // K = 32 as two K = 16 steps (two k groups each)
-                    tc_mma(tm + (uint32_t)(N * tile), tc_desc(a + kk * 256, 512), tc_desc(wb + kk * 256, 512),
-                           tc_idesc(N), (uint32_t)kk);
+                for (int kk = 0; kk < kTcH / 16; kk++)  // K = H as K = 16 steps (two k groups each)
+                    tc_mma(tm + (uint32_t)(N * tile), tc_desc(a + kk * 256, kTcKG * 128),
+                           tc_desc(wb + kk * 256, kTcKG * 128), tc_idesc(N), (uint32_t)kk);
             }
         }
         tc_commit(&s.bar);
@@ -178,13 +179,13 @@ LBM_D void tc_ld16(uint32_t taddr, uint32_t (&r)[16]) {
         : "memory");
 }
 
-// a layer's accumulators of this thread's row in one tile (32 columns at `col`) -> + bias -> ReLU ->
-// FP16 -> the next operand's row (k groups 0..3)
+// a layer's accumulators of this thread's row in one tile (H columns at `col`) -> + bias -> ReLU ->
+// FP16 -> the next operand's row (k groups 0 .. H/8 - 1)
 template <bool BIAS>
 LBM_D void tc_act_row(uint32_t lane_addr, int col, const float* bias, uint4* a2tile) {
     const int t = threadIdx.x;
 #pragma unroll
-    for (int half = 0; half < 2; half++) {
+    for (int half = 0; half < kTcH / 16; half++) {
         uint32_t r[16];
         tc_ld16(lane_addr + (uint32_t)(col + 16 * half), r);
 #pragma unroll
@@ -192,16 +193,16 @@ LBM_D void tc_act_row(uint32_t lane_addr, int col, const float* bias, uint4* a2t
             F2 v[4];
 #pragma unroll
             for (int i = 0; i < 4; i++) {
-                const int c = 16 * half + 8 * q + 2 * i;
-                v[i] = F2(__uint_as_float(r[c - 16 * half]), __uint_as_float(r[c + 1 - 16 * half]));
-                if constexpr (BIAS) v[i] = v[i] + F2(bias[c], bias[c + 1]);  // one packed add per two columns
+                const int c = 8 * q + 2 * i;  // column within the 16 loaded
+                v[i] = F2(__uint_as_float(r[c]), __uint_as_float(r[c + 1]));
+                if constexpr (BIAS) v[i] = v[i] + F2(bias[16 * half + c], bias[16 * half + c + 1]);  // one packed add per two columns
             }
             uint4 h;
             h.x = mlp_act(v[0].v.x, v[0].v.y);
             h.y = mlp_act(v[1].v.x, v[1].v.y);
             h.z = mlp_act(v[2].v.x, v[2].v.y);
             h.w = mlp_act(v[3].v.x, v[3].v.y);
-            a2tile[tc_off(t, 2 * half + q, 4) / 16] = h;
+            a2tile[tc_off(t, 2 * half + q, kTcKG) / 16] = h;
         }
     }
 }
@@ -217,11 +218,11 @@ LBM_D float2 tc_mlp(TcSmem& s, uint32_t tm, uint4 rowA, uint4 rowB, const MlpNor
     tc_issue<1>(s, tm);
     tc_wait(s, parity, err);
     tc_act_row<false>(lane_addr, 0, nullptr, s.a2[0]);
-    tc_act_row<false>(lane_addr, 32, nullptr, s.a2[1]);
+    tc_act_row<false>(lane_addr, kTcH, nullptr, s.a2[1]);
     tc_issue<2>(s, tm);
     tc_wait(s, parity ^ 1u, err);
     tc_act_row<true>(lane_addr, 0, nm.b2, s.a2[0]);
-    tc_act_row<true>(lane_addr, 32, nm.b2, s.a2[1]);
+    tc_act_row<true>(lane_addr, kTcH, nm.b2, s.a2[1]);
     tc_issue<3>(s, tm);
     tc_wait(s, parity, err);
     const float zA = __uint_as_float(tc_ld1(lane_addr + 0));

@@ -28,8 +28,8 @@ using namespace lbm;
 namespace {
 
 constexpr int kBlk = 128;   // samples per training block
-constexpr int kPad = 33;    // row stride of the per-sample hidden arrays in shared memory
-constexpr int kGradLen = kMlpParams + 1;  // 1345 gradients and the loss
+constexpr int kPad = kMlpHid + 1;  // row stride of the per-sample hidden arrays in shared memory
+constexpr int kGradLen = kMlpParams + 1;  // the gradients and the loss
 
 struct TrainNorm {
     float mu[7], isd[7];
@@ -74,16 +74,16 @@ __global__ void __launch_bounds__(kBlk) k_mlp_grad(const float* __restrict__ sam
     float* d1 = D1 + t * kPad;
     float* h2 = H2 + t * kPad;
     float* d2 = D2 + t * kPad;
-    for (int i = 0; i < 32; i++) {
+    for (int i = 0; i < kMlpHid; i++) {
         float pre = W[kMlpB1 + i];
         for (int k = 0; k < 7; k++) pre = fmaf(W[kMlpW1 + i * 7 + k], x[k], pre);
         h1[i] = live ? relu_f(pre) : 0.f;
         d1[i] = live ? relu_grad(pre) : 0.f;
     }
     float zz = W[kMlpB3];
-    for (int o = 0; o < 32; o++) {
+    for (int o = 0; o < kMlpHid; o++) {
         float pre = W[kMlpB2 + o];
-        for (int i = 0; i < 32; i++) pre = fmaf(W[kMlpW2 + o * 32 + i], h1[i], pre);
+        for (int i = 0; i < kMlpHid; i++) pre = fmaf(W[kMlpW2 + o * kMlpHid + i], h1[i], pre);
         h2[o] = live ? relu_f(pre) : 0.f;
         d2[o] = live ? relu_grad(pre) : 0.f;
         zz = fmaf(W[kMlpW3 + o], h2[o], zz);
@@ -97,29 +97,29 @@ __global__ void __launch_bounds__(kBlk) k_mlp_grad(const float* __restrict__ sam
     }
     DZ[t] = dz;
     LS[t] = loss;
-    for (int o = 0; o < 32; o++) d2[o] *= dz * W[kMlpW3 + o];
-    for (int i = 0; i < 32; i++) {
+    for (int o = 0; o < kMlpHid; o++) d2[o] *= dz * W[kMlpW3 + o];
+    for (int i = 0; i < kMlpHid; i++) {
         float s = 0.f;
-        for (int o = 0; o < 32; o++) s = fmaf(d2[o], W[kMlpW2 + o * 32 + i], s);
+        for (int o = 0; o < kMlpHid; o++) s = fmaf(d2[o], W[kMlpW2 + o * kMlpHid + i], s);
         d1[i] *= s;
     }
     __syncthreads();
     float* g = gpart + (size_t)blockIdx.x * kGradLen;
     // w2 [o][i] and b2 [o]
-    for (int q = t; q < 32 * 32 + 32; q += kBlk) {
+    for (int q = t; q < kMlpHid * kMlpHid + kMlpHid; q += kBlk) {
         float s = 0.f;
-        if (q < 1024) {
-            const int o = q >> 5, i = q & 31;
+        if (q < kMlpHid * kMlpHid) {
+            const int o = q / kMlpHid, i = q % kMlpHid;
             for (int n = 0; n < kBlk; n++) s = fmaf(D2[n * kPad + o], H1[n * kPad + i], s);
             g[kMlpW2 + q] = s;
         } else {
-            const int o = q - 1024;
+            const int o = q - kMlpHid * kMlpHid;
             for (int n = 0; n < kBlk; n++) s += D2[n * kPad + o];
             g[kMlpB2 + o] = s;
         }
     }
     // w1 [i][k] and b1 [i] (input 7 = 1)
-    for (int q = t; q < 32 * 8; q += kBlk) {
+    for (int q = t; q < kMlpHid * 8; q += kBlk) {
         const int i = q >> 3, k = q & 7;
         float s = 0.f;
         for (int n = 0; n < kBlk; n++) s = fmaf(D1[n * kPad + i], X[n * 8 + k], s);
@@ -127,15 +127,15 @@ __global__ void __launch_bounds__(kBlk) k_mlp_grad(const float* __restrict__ sam
         else g[kMlpB1 + i] = s;
     }
     // w3, b3, loss
-    if (t < 32) {
+    if (t < kMlpHid) {
         float s = 0.f;
         for (int n = 0; n < kBlk; n++) s = fmaf(DZ[n], H2[n * kPad + t], s);
         g[kMlpW3 + t] = s;
-    } else if (t == 32) {
+    } else if (t == kMlpHid) {
         float s = 0.f;
         for (int n = 0; n < kBlk; n++) s += DZ[n];
         g[kMlpB3] = s;
-    } else if (t == 33) {
+    } else if (t == kMlpHid + 1) {
         float s = 0.f;
         for (int n = 0; n < kBlk; n++) s += LS[n];
         g[kMlpParams] = s;
@@ -335,8 +335,9 @@ namespace lbm {
 
 // host: FP16 fragment table (the weights as trained) and the uniform normalisation
 void mlp_pack(const lbm_mlp_model& m, uint4* frag, MlpNorm& nm) {
+    constexpr int H = kMlpHid;
     auto W1 = [&](int n, int k) { return k < 7 ? m.params[kMlpW1 + n * 7 + k] : m.params[kMlpB1 + n]; };
-    auto W2 = [&](int n, int k) { return m.params[kMlpW2 + n * 32 + k]; };
+    auto W2 = [&](int n, int k) { return m.params[kMlpW2 + n * H + k]; };
     auto W3 = [&](int k) { return m.params[kMlpW3 + k]; };
     auto hb = [](float a, float b) {
         const __half2 v = __floats2half2_rn(a, b);
@@ -349,25 +350,37 @@ void mlp_pack(const lbm_mlp_model& m, uint4* frag, MlpNorm& nm) {
         std::memcpy(&u, &a, 4);
         return u;
     };
+    // warp fragment table: lane (g = lane / 4, c = lane % 4) holds, per n-tile j of 8 units, the B fragment
+    // of output unit 8 j + g at inputs (2c, 2c + 1) and (2c + 8, 2c + 9) of each k16 step; unused slots 0
+    for (int i = 0; i < kMlpFragRows * 32; i++) frag[i] = make_uint4(0, 0, 0, 0);
     for (int lane = 0; lane < 32; lane++) {
         const int g = lane >> 2, c = lane & 3;
-        uint32_t r[4];
-        for (int j = 0; j < 4; j++) r[j] = hb(W1(8 * j + g, 2 * c), W1(8 * j + g, 2 * c + 1));
+        uint32_t r[4] = {0, 0, 0, 0};
+        for (int j = 0; j < kMlpNT; j++) r[j] = hb(W1(8 * j + g, 2 * c), W1(8 * j + g, 2 * c + 1));
         frag[0 * 32 + lane] = make_uint4(r[0], r[1], r[2], r[3]);
-        for (int j = 0; j < 4; j++) {
+        for (int j = 0; j < kMlpNT; j++) {
             const int n = 8 * j + g;
-            frag[(1 + j) * 32 + lane] = make_uint4(hb(W2(n, 2 * c), W2(n, 2 * c + 1)), hb(W2(n, 2 * c + 8), W2(n, 2 * c + 9)),
-                                                   hb(W2(n, 16 + 2 * c), W2(n, 17 + 2 * c)),
-                                                   hb(W2(n, 24 + 2 * c), W2(n, 25 + 2 * c)));
+            uint32_t w[4] = {0, 0, 0, 0};
+            for (int ks = 0; ks < kMlpKS; ks++) {
+                w[2 * ks] = hb(W2(n, 16 * ks + 2 * c), W2(n, 16 * ks + 2 * c + 1));
+                w[2 * ks + 1] = hb(W2(n, 16 * ks + 2 * c + 8), W2(n, 16 * ks + 2 * c + 9));
+            }
+            frag[(1 + j) * 32 + lane] = make_uint4(w[0], w[1], w[2], w[3]);
         }
+        uint32_t w3[4] = {0, 0, 0, 0};
         if (g == 0)
-            frag[5 * 32 + lane] = make_uint4(hb(W3(2 * c), W3(2 * c + 1)), hb(W3(2 * c + 8), W3(2 * c + 9)),
-                                             hb(W3(16 + 2 * c), W3(17 + 2 * c)), hb(W3(24 + 2 * c), W3(25 + 2 * c)));
-        else
-            frag[5 * 32 + lane] = make_uint4(0, 0, 0, 0);
-        auto B2 = [&](int n) { return fb(m.params[kMlpB2 + n]); };
-        frag[6 * 32 + lane] = make_uint4(B2(2 * c), B2(2 * c + 1), B2(8 + 2 * c), B2(9 + 2 * c));
-        frag[7 * 32 + lane] = make_uint4(B2(16 + 2 * c), B2(17 + 2 * c), B2(24 + 2 * c), B2(25 + 2 * c));
+            for (int ks = 0; ks < kMlpKS; ks++) {
+                w3[2 * ks] = hb(W3(16 * ks + 2 * c), W3(16 * ks + 2 * c + 1));
+                w3[2 * ks + 1] = hb(W3(16 * ks + 2 * c + 8), W3(16 * ks + 2 * c + 9));
+            }
+        frag[5 * 32 + lane] = make_uint4(w3[0], w3[1], w3[2], w3[3]);
+        uint32_t b[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int j = 0; j < kMlpNT; j++) {
+            b[2 * j] = fb(m.params[kMlpB2 + 8 * j + 2 * c]);
+            b[2 * j + 1] = fb(m.params[kMlpB2 + 8 * j + 2 * c + 1]);
+        }
+        frag[6 * 32 + lane] = make_uint4(b[0], b[1], b[2], b[3]);
+        frag[7 * 32 + lane] = make_uint4(b[4], b[5], b[6], b[7]);
     }
     for (int i = 0; i < 7; i++) {
         nm.isd[i] = 1.0f / m.in_std[i];
@@ -377,19 +390,19 @@ void mlp_pack(const lbm_mlp_model& m, uint4* frag, MlpNorm& nm) {
     }
     nm.b3 = m.params[kMlpB3];
     nm.scale = m.out_scale;
-    for (int n = 0; n < 32; n++) nm.b2[n] = m.params[kMlpB2 + n];
+    for (int n = 0; n < H; n++) nm.b2[n] = m.params[kMlpB2 + n];
     // the tcgen05 weight image after the table: W1 (k 0..6 weights, k 7 = b1, 8..15 zero), W2, W3 (row
     // 0 = w3), FP16, K-major core matrices of 8 rows x 8 halves (lbm_mlp_tc.cuh)
     std::vector<__half> img(kTcWBytes / 2, __float2half(0.0f));
     auto put = [&](int base, int KG, int n, int k, float v) {
         img[(base + tc_off(n, k >> 3, KG)) / 2 + (k & 7)] = __float2half_rn(v);
     };
-    for (int n = 0; n < 32; n++) {
+    for (int n = 0; n < H; n++) {
         for (int k = 0; k < 7; k++) put(kTcW1, 2, n, k, m.params[kMlpW1 + n * 7 + k]);
         put(kTcW1, 2, n, 7, m.params[kMlpB1 + n]);
-        for (int k = 0; k < 32; k++) put(kTcW2, 4, n, k, m.params[kMlpW2 + n * 32 + k]);
+        for (int k = 0; k < H; k++) put(kTcW2, kTcKG, n, k, m.params[kMlpW2 + n * H + k]);
     }
-    for (int k = 0; k < 32; k++) put(kTcW3, 4, 0, k, m.params[kMlpW3 + k]);
+    for (int k = 0; k < H; k++) put(kTcW3, kTcKG, 0, k, m.params[kMlpW3 + k]);
     std::memcpy(frag + kMlpFragRows * 32, img.data(), kTcWBytes);
 }
 

@@ -16,8 +16,11 @@ from . import capi
 from .capi import check, lib
 
 NIN, NH, NPAR = capi.LBM_MLP_INPUTS, capi.LBM_MLP_HIDDEN, capi.LBM_MLP_PARAMS
-# offsets of the parameter vector (w1[32][7], b1, w2[32][32], b2, w3, b3)
-W1, B1, W2, B2, W3, B3 = 0, 224, 256, 1280, 1312, 1344
+# offsets of the parameter vector (w1[H][7], b1, w2[H][H], b2, w3, b3)
+W1, B1, W2 = 0, 7 * NH, 8 * NH
+B2 = W2 + NH * NH
+W3 = B2 + NH
+B3 = W3 + NH
 FEATURES = ("tr S", "I2", "I3 = det S", "Lode parameter", "S_d:S_d / S:S", "rho", "|S|")
 
 

@@ -16,8 +16,13 @@ central finite differences of the forward pass (tests/test_les_cpu.py).
 """
 import numpy as np
 
-NIN, NH, NPAR = 7, 32, 1345
-W1, B1, W2, B2, W3, B3 = 0, 224, 256, 1280, 1312, 1344
+NIN, NH = 7, 16
+NPAR = NH * NH + 10 * NH + 1
+# offsets of the parameter vector (w1[H][7], b1, w2[H][H], b2, w3, b3)
+W1, B1, W2 = 0, 7 * NH, 8 * NH
+B2 = W2 + NH * NH
+W3 = B2 + NH
+B3 = W3 + NH
 
 
 def features(S, rho):

