@@ -122,12 +122,13 @@ static lbm_status fail(lbm_ctx* c, lbm_status s, const char* fmt, ...) {
 
 static void dfree(void* p) { if (p) cudaFree(p); }
 
-// runs f(begin, end) over [0, n) split into contiguous chunks on the host cores (set-up loops over
-// the cells); each chunk writes only its own range
+// runs f(begin, end) over [0, n) split into contiguous chunks on the host cores (set-up loops), at
+// least `grain` items per chunk (65536 for loops over cells, 65536 / nx for loops over rows of cells);
+// each chunk writes only its own range
 template <class F>
-static void host_parallel(long long n, F&& f) {
+static void host_parallel(long long n, F&& f, long long grain = 65536) {
     const unsigned hw = std::thread::hardware_concurrency();
-    const long long nth = std::min<long long>(std::max(1u, std::min(hw, 32u)), std::max(1LL, n / 65536));
+    const long long nth = std::min<long long>(std::max(1u, std::min(hw, 32u)), std::max(1LL, n / std::max(1LL, grain)));
     if (nth <= 1) { f(0LL, n); return; }
     std::vector<std::thread> th;
     for (long long t = 0; t < nth; t++)
@@ -782,6 +783,7 @@ static lbm_status build_geometry(lbm_ctx* c) {
         const uint8_t want = comb ? (uint8_t)(CLS_BULK | BIT_REFBULK) : (uint8_t)CLS_BULK;
         c->split_ok = c->cfg.storage != LBM_STORAGE_F64 && !(c->cfg.options & LBM_OPT_ONE_LAUNCH) && nrow < (1LL << 31);
         std::vector<uint8_t> plain(c->split_ok ? (size_t)nrow : 0, 0);
+        const long long row_grain = std::max(1LL, 65536LL / nx);  // rows of nx cells per thread at least
         if (c->split_ok && !(nx & 1)) {
             host_parallel(nrow, [&](long long r0, long long r1) {
                 for (long long r = r0; r < r1; r++) {
@@ -791,7 +793,7 @@ static lbm_status build_geometry(lbm_ctx* c) {
                     for (int i = 0; i < nx && all; i++) all = (cls[(size_t)(r * nx + i)] & keep) == want;
                     plain[(size_t)r] = all ? 1 : 0;
                 }
-            });
+            }, row_grain);
         }
         // rows beside a flat wall: every cell an edge cell (no role bit) whose 26 sources are solid or
         // fluid cells of the packed kinds at the same offsets along the whole row, off the periodic y/z
@@ -822,7 +824,7 @@ static lbm_status build_geometry(lbm_ctx* c) {
                     }
                     if (ok) { is_wall[(size_t)r] = 1; wmask[(size_t)r] = mask; }
                 }
-            });
+            }, row_grain);
         }
         std::vector<int32_t> pr, rr, wr, ra;
         std::vector<uint32_t> wm;
@@ -864,22 +866,32 @@ static lbm_status init_common(lbm_ctx* c, const double* rho, const double* u, do
     cudaSetDevice(c->cfg.device);
     lbm_status s = ensure_geometry(c);
     if (s) return s;
-    double *dr = nullptr, *du = nullptr, *dp = nullptr;
+    double *dr = nullptr, *du = nullptr, *dp = nullptr;  // staging copies (pageable inputs)
     const size_t N = (size_t)c->N;
+    // a page-locked host array (cudaHostAlloc / cudaHostRegister) is read by the init kernel where it
+    // lies (its device view, over the host link); any other array is copied to a device buffer first
+    auto device_view = [&](const double* h, size_t bytes, double** staged, const double** view) -> cudaError_t {
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, h) == cudaSuccess && a.type == cudaMemoryTypeHost && a.devicePointer) {
+            *view = (const double*)a.devicePointer;
+            return cudaSuccess;
+        }
+        cudaGetLastError();  // a pointer the runtime does not know is not an error here
+        cudaError_t e = cudaMalloc(staged, bytes);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(*staged, h, bytes, cudaMemcpyHostToDevice, c->st);
+        *view = *staged;
+        return e;
+    };
+    const double *vr = nullptr, *vu = nullptr, *vp = nullptr;
     if (rho) {
-        CU(c, cudaMalloc(&dr, N * 8));
-        CU(c, cudaMalloc(&du, 3 * N * 8));
-        CU(c, cudaMemcpyAsync(dr, rho, N * 8, cudaMemcpyHostToDevice, c->st));
-        CU(c, cudaMemcpyAsync(du, u, 3 * N * 8, cudaMemcpyHostToDevice, c->st));
+        CU(c, device_view(rho, N * 8, &dr, &vr));
+        CU(c, device_view(u, 3 * N * 8, &du, &vu));
     }
-    if (pops) {
-        CU(c, cudaMalloc(&dp, 27 * N * 8));
-        CU(c, cudaMemcpyAsync(dp, pops, 27 * N * 8, cudaMemcpyHostToDevice, c->st));
-    }
+    if (pops) CU(c, device_view(pops, 27 * N * 8, &dp, &vp));
     c->m = 0;
     Params p = make_params(c);
     double z3[3] = {0, 0, 0};
-    cudaError_t e = do_init(c, p, dr, du, rho0, u0 ? u0 : z3, dp);
+    cudaError_t e = do_init(c, p, vr, vu, rho0, u0 ? u0 : z3, vp);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     dfree(dr); dfree(du); dfree(dp);
     if (e != cudaSuccess) return fail(c, LBM_ERR_CUDA, "init kernel: %s", cudaGetErrorString(e));

@@ -502,3 +502,30 @@ def test_reductions_are_deterministic_and_match_the_moments(built_lib, storage):
     e2 = s.error_evaluation()
     assert np.isfinite(e1) and e2 == 0.0
     s.close()
+
+
+def test_init_from_page_locked_fields_equals_pageable(built_lib):
+    """lbm_init_fields reads page-locked host arrays in place (the init kernel's device view of them) and
+    copies pageable ones to the device first: both give the same populations bit for bit."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    nx, ny, nz = 32, 18, 10
+    c = cases.channel(nx, ny, nz, re_tau=3.0, u_max=0.05, nu=0.01, amp=0.05)
+    out = []
+    for pinned in (False, True):
+        rho, u = c["rho"].astype(np.float64), c["u"].astype(np.float64)
+        if pinned:
+            tr = torch.empty(rho.size, dtype=torch.float64, pin_memory=True)
+            tu = torch.empty(u.size, dtype=torch.float64, pin_memory=True)
+            tr.numpy()[...] = rho.reshape(-1)
+            tu.numpy()[...] = u.reshape(-1)
+            rho, u = tr.numpy().reshape(c["rho"].shape), tu.numpy().reshape(c["u"].shape)
+        s = Solver((nx, ny, nz), turbulence=OmegaLES, storage="f32", nu=c["nu"], cles=0.17, periodic=c["periodic"],
+                   force=c["force"])
+        s.set_flags(c["flags"])
+        s.set_bc()
+        s.init_fields(rho, u)
+        out.append(s.populations())
+        s.close()
+    assert np.array_equal(out[0], out[1])
