@@ -22,6 +22,7 @@
 #include <memory>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 using namespace lbm;
@@ -398,12 +399,15 @@ static lbm_status build_geometry(lbm_ctx* c) {
         if (v < 0 || v >= n) { if (wrap[a]) v = (v + n) % n; else ok = false; }
         return v;
     };
-    // class byte and side-table index per cell (index -1: none), filled on the host cores
+    // class byte per cell, filled on the host cores; side-table index per cell (-1: none), kept sparse on
+    // the host (only boundary nodes and their helper cells have one)
     std::unique_ptr<uint8_t[]> cls_buf(new uint8_t[(size_t)N]);
-    std::unique_ptr<int32_t[]> aux_buf(new int32_t[(size_t)N]);
     uint8_t* cls = cls_buf.get();
-    int32_t* aux = aux_buf.get();
-    host_parallel(N, [&](long long q0, long long q1) { std::fill(aux + q0, aux + q1, -1); });
+    struct SparseIndex {
+        std::unordered_map<long long, int32_t> m;
+        int32_t operator[](long long q) const { auto it = m.find(q); return it == m.end() ? -1 : it->second; }
+        void set(long long q, int32_t v) { m[q] = v; }
+    } aux;
     // moving-wall and Zou/He nodes share the 3-level side table: collided, never streamed into
     const bool lid_kind = c->cfg.inlet_kind == LBM_INLET_MOVING_WALL || c->cfg.inlet_kind == LBM_INLET_ZOU_HE;
     const int okind = c->cfg.outlet_kind;
@@ -461,13 +465,13 @@ static lbm_status build_geometry(lbm_ctx* c) {
         if (c->flags[q] != -1) return fail(c, LBM_ERR_INVALID, "inlet record at (%d,%d,%d) is not a -1 cell", i, j, k);
         if (aux[q] >= 0) return fail(c, LBM_ERR_INVALID, "two inlet records for (%d,%d,%d)", i, j, k);
         if (lid_kind) {
-            aux[q] = n_lid++;
+            aux.set(q, n_lid++);
             for (int a = 0; a < 3; a++) { lid_n.push_back(r.normal[a]); lid_u.push_back(r.velocity[a]); }
         } else {
             int s = (r.normal[0] == 1.f && r.normal[1] == 0.f && r.normal[2] == 0.f) ? 1
                   : (r.normal[0] == -1.f && r.normal[1] == 0.f && r.normal[2] == 0.f) ? -1 : 0;
             if (!s) return fail(c, LBM_ERR_UNSUPPORTED, "equilibrium inlet at (%d,%d,%d): only +-x normals (as the reference)", i, j, k);
-            aux[q] = n_in++;
+            aux.set(q, n_in++);
             in_dir.push_back(s);
             for (int a = 0; a < 3; a++) in_u.push_back(r.velocity[a]);
         }
@@ -485,7 +489,7 @@ static lbm_status build_geometry(lbm_ctx* c) {
               : (r.normal[0] == -1.f && r.normal[1] == 0.f && r.normal[2] == 0.f) ? -1 : 0;
         if (!s) return fail(c, LBM_ERR_UNSUPPORTED, "outlet at (%d,%d,%d): only +-x normals (as the reference)", i, j, k);
         if (!(r.density > 0)) return fail(c, LBM_ERR_INVALID, "outlet density must be positive");
-        aux[q] = n_out++;
+        aux.set(q, n_out++);
         out_dir.push_back(s);
         out_rho.push_back(r.density);
     }
@@ -515,7 +519,7 @@ static lbm_status build_geometry(lbm_ctx* c) {
                 if (r.regular && fs == 0)
                     return fail(c, LBM_ERR_INVALID, "symmetry at (%d,%d,%d) is marked regular but has a solid in-plane neighbour", i, j, k);
             }
-        aux[q] = n_sym++;
+        aux.set(q, n_sym++);
         sym_dir.push_back(sg);
     }
     // every record names a distinct cell of its flag (checked above), so equal counts mean every -1 and
@@ -535,7 +539,7 @@ static lbm_status build_geometry(lbm_ctx* c) {
         if ((cls[q] & (BIT_PROBE1 | BIT_PROBE2 | BIT_OUTUP)) != 0)
             return fail(c, LBM_ERR_UNSUPPORTED, "cell %lld would serve two boundary nodes", q);
         cls[q] |= bit;
-        aux[q] = node;
+        aux.set(q, node);
         return LBM_OK;
     };
     std::vector<long long> bnodes;  // the inlet and outlet nodes, from their records
@@ -580,7 +584,7 @@ static lbm_status build_geometry(lbm_ctx* c) {
                         return fail(c, LBM_ERR_UNSUPPORTED, "cell %lld would serve two boundary nodes", r);
                     if (!(cls[r] & BIT_OUTUP)) {
                         cls[r] |= BIT_OUTUP;
-                        aux[r] = n_ms++;
+                        aux.set(r, n_ms++);
                     }
                     out_nb[(size_t)outlet_slot(vid(-s, dy, dz)) * n_out + aux[q]] = aux[r];
                 }
@@ -676,16 +680,9 @@ static lbm_status build_geometry(lbm_ctx* c) {
     // side-table indices: -1 everywhere (every byte 0xff), then the few set entries scattered on the device
     CU(c, cudaMemsetAsync(c->d_aux, 0xff, (size_t)N * 4, c->st));
     {
-        std::vector<std::vector<long long>> part_q(64);
-        std::atomic<int> next{0};
-        host_parallel(N, [&](long long q0, long long q1) {
-            auto& v = part_q[(size_t)next.fetch_add(1)];
-            for (long long q = q0; q < q1; q++) if (aux[q] >= 0) v.push_back(q);
-        });
         std::vector<long long> sq;
         std::vector<int32_t> sv;
-        for (auto& v : part_q)
-            for (long long q : v) { sq.push_back(q); sv.push_back(aux[q]); }
+        for (const auto& kv : aux.m) { sq.push_back(kv.first); sv.push_back(kv.second); }
         if (!sq.empty()) {
             long long* d_q = nullptr;
             int32_t* d_v = nullptr;
@@ -806,16 +803,24 @@ static lbm_status build_geometry(lbm_ctx* c) {
                     if (plain[(size_t)r]) continue;
                     const int y = (int)(r % ny), z = (int)(r / ny);
                     if ((wrap[1] && (y == 0 || y == ny - 1)) || (wrap[2] && (z == 0 || z == nz - 1))) continue;
-                    bool ok = true;
+                    bool ok = (cls[(size_t)(r * nx)] & (uint8_t)~BIT_REFBULK) == CLS_EDGE;  // cheap early exit
+                    // the nine source rows (y - c_y, z - c_z) of the row, inside the lattice (these rows are
+                    // off the periodic seams, so a y or z source outside it rules the row out)
+                    const uint8_t* src[27];
+                    for (int v = 1; v < 27 && ok; v++) {
+                        const int b = y - cy(v), e = z - cz(v);
+                        if (b < 0 || b >= ny || e < 0 || e >= nz) ok = false;
+                        else src[v] = cls + (size_t)id(0, b, e);
+                    }
+                    if (ok && !wrap[0]) ok = false;  // x sources wrap only on a periodic x axis
                     uint32_t mask = 0;
                     for (int i = 0; i < nx && ok; i++) {
                         if ((cls[(size_t)(r * nx + i)] & (uint8_t)~BIT_REFBULK) != CLS_EDGE) { ok = false; break; }
                         uint32_t m = 0;
-                        for (int v = 1; v < 27 && ok; v++) {
-                            bool in = true;
-                            const int a = wrapc(i - cx(v), nx, 0, in), b = y - cy(v), e = z - cz(v);
-                            if (!in || b < 0 || b >= ny || e < 0 || e >= nz) { ok = false; break; }
-                            const int k = cls[(size_t)id(a, b, e)] & CLS_MASK;
+                        for (int v = 1; v < 27; v++) {
+                            int a = i - cx(v);
+                            a = a < 0 ? a + nx : a >= nx ? a - nx : a;
+                            const int k = src[v][a] & CLS_MASK;
                             if (k == CLS_SOLID) m |= 1u << v;
                             else if (k != CLS_BULK && k != CLS_EDGE) ok = false;
                         }
