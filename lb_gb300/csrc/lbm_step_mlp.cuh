@@ -25,10 +25,10 @@ namespace lbm {
 #ifndef LBM_MLP_MIN_BLOCKS
 #define LBM_MLP_MIN_BLOCKS 0
 #endif
-// the plain-row kernel that runs the network: 6 (80 registers) measured 24.2 GLUPS against 23.2 with no
-// request (102 registers on odd steps) and 23.5 at 5
+// the plain-row kernel that runs the network: 7 CTAs per SM (72 registers) measured 36.4 GLUPS with the
+// 7-16-16-1 network against 35.5 at 6 (80 registers) and 33.8 at 5
 #ifndef LBM_MLP_PLAIN_MIN_BLOCKS
-#define LBM_MLP_PLAIN_MIN_BLOCKS 6
+#define LBM_MLP_PLAIN_MIN_BLOCKS 7
 #endif
 // ROWS: 0 one launch over the lattice (grid x = pair block, y, z); 1 the plain rows of the split step
 // (every pair a packed bulk pair off the y/z seams, lbm_step.cuh); 2 the remaining rows (1-D grid of
