@@ -6,7 +6,9 @@
 //   2. the Smagorinsky relaxation time tau_S (OmegaLES.h:117-124) and from it the strain-rate estimate
 //      S = -3 Pi / (2 rho tau_S), which is exact when the cell relaxed with tau_S (Pi = -2/3 rho tau S);
 //   3. the seven inputs of S and rho, normalised, as FP16 rows; the warp's 64 cells go through the
-//      tensor-core MLP together (mlp_warp), so every lane reaches it, including lanes without a pair;
+//      tensor-core MLP together (mlp_warp, warp-level mma.sync), so every lane reaches it, including
+//      lanes without a pair; with LBM_OPT_MLP_TCGEN05 the plain rows' CTA of 256 cells goes through
+//      tcgen05.mma with TMEM accumulators instead (tc_mlp, lbm_mlp_tc.cuh);
 //   4. tau = tau_0 + 3 nu_t for cells whose inputs lie in the training range, tau_S otherwise.
 // Cells that are not packed bulk pairs take the per-cell path with the Smagorinsky closure.
 // MODE 0: the network runs in this step.  MODE 1: it runs and its nu_t (or -1 for the fallback) is kept
