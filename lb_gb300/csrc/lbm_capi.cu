@@ -126,6 +126,15 @@ static void dfree(void* p) { if (p) cudaFree(p); }
 // runs f(begin, end) over [0, n) split into contiguous chunks on the host cores (set-up loops), at
 // least `grain` items per chunk (65536 for loops over cells, 65536 / nx for loops over rows of cells);
 // each chunk writes only its own range
+// compile-time loop over [B, E) for host code: f(std::integral_constant<int, v>) for each v
+template <int B, int E, class F>
+static inline void sfor_host(F&& f) {
+    if constexpr (B < E) {
+        f(std::integral_constant<int, B>{});
+        sfor_host<B + 1, E>(f);
+    }
+}
+
 template <class F>
 static void host_parallel(long long n, F&& f, long long grain = 65536) {
     const unsigned hw = std::thread::hardware_concurrency();
@@ -814,19 +823,28 @@ static lbm_status build_geometry(lbm_ctx* c) {
                     }
                     if (ok && !wrap[0]) ok = false;  // x sources wrap only on a periodic x axis
                     uint32_t mask = 0;
-                    for (int i = 0; i < nx && ok; i++) {
-                        if ((cls[(size_t)(r * nx + i)] & (uint8_t)~BIT_REFBULK) != CLS_EDGE) { ok = false; break; }
+                    // the solid-source mask of cell i, and whether a source is of a kind other than solid,
+                    // bulk or edge (a compile-time loop over the directions; x wraps only at the row ends)
+                    auto cell_mask = [&](int i, bool wrapx, uint32_t& other) {
                         uint32_t m = 0;
-                        for (int v = 1; v < 27; v++) {
+                        sfor_host<1, 27>([&](auto vc) {
+                            constexpr int v = decltype(vc)::value;
                             int a = i - cx(v);
-                            a = a < 0 ? a + nx : a >= nx ? a - nx : a;
+                            if (wrapx) a = a < 0 ? a + nx : a >= nx ? a - nx : a;
                             const int k = src[v][a] & CLS_MASK;
-                            if (k == CLS_SOLID) m |= 1u << v;
-                            else if (k != CLS_BULK && k != CLS_EDGE) ok = false;
-                        }
-                        if (i == 0) mask = m;
-                        else if (m != mask) ok = false;
+                            m |= (uint32_t)(k == CLS_SOLID) << v;
+                            other |= (uint32_t)(k != CLS_SOLID && k != CLS_BULK && k != CLS_EDGE);
+                        });
+                        return m;
+                    };
+                    const uint8_t* row = cls + (size_t)r * nx;
+                    uint32_t other = 0;
+                    if (ok) mask = cell_mask(0, true, other);
+                    for (int i = 1; i < nx && ok; i++) {
+                        if ((row[i] & (uint8_t)~BIT_REFBULK) != CLS_EDGE) { ok = false; break; }
+                        if (cell_mask(i, i == nx - 1, other) != mask) ok = false;
                     }
+                    if (other) ok = false;
                     if (ok) { is_wall[(size_t)r] = 1; wmask[(size_t)r] = mask; }
                 }
             }, row_grain);
