@@ -146,7 +146,7 @@ const char* lbm_config_last_error(void);
 #define LBM_OPT_MLP_TCGEN05 16  /* learned closure (LBM_CLOSURE_MLP): the network of the plain-row step
                                    kernel runs on tcgen05.mma with TMEM accumulators (one CTA's 256 cells
                                    per product) instead of warp-level mma.sync; same inputs, weights and
-                                   ReLU, FP32 accumulation in another order */
+                                   activation, FP32 accumulation in another order */
 
 /* boundary-condition records, mirroring LBMTraits.h:17-43 */
 typedef struct lbm_vertex { int32_t x, y, z; } lbm_vertex;
@@ -396,9 +396,9 @@ lbm_status lbm_voxelize_mesh_noalloc(const double* verts, int32_t nv, const int3
                                      int32_t dims_out[3], double bbox_out[6], int32_t device);
 
 /* ---- learned LES closure (no reference counterpart; the reference has OmegaLES only) -----------
- * A per-cell MLP  x(7) -> 16 -> 16 -> 1  maps strain-rate invariants and density to the eddy
- * viscosity:  nu_t = out_scale * softplus(z).  Hidden activation: ReLU.  Inputs, from the
- * strain-rate tensor S (lattice units) and rho:
+ * A per-cell MLP  x(7) -> 32 -> 32 -> 1  maps strain-rate invariants and density to the eddy
+ * viscosity:  nu_t = out_scale * softplus(z).  Hidden activation: GELU in its sigmoid form
+ * x * sigmoid(1.702 x).  Inputs, from the strain-rate tensor S (lattice units) and rho:
  *   0 tr S, 1 I2 = (tr^2 S - S:S)/2, 2 I3 = det S, 3 Lode parameter 3 sqrt(6) det(S_d)/|S_d|^3,
  *   4 S_d:S_d / S:S, 5 rho, 6 |S| = sqrt(2 S:S)        (S_d: deviatoric part)
  * normalised as (x - in_mean) / in_std before the first layer.  Training keeps FP32 parameters;
@@ -408,8 +408,8 @@ lbm_status lbm_voxelize_mesh_noalloc(const double* verts, int32_t nv, const int3
  * outside [in_lo, in_hi] (the training range), or that is not a bulk cell, relaxes with tau_S.
  * params layout: w1[32][7], b1[32], w2[32][32], b2[32], w3[32], b3 (out x in, row-major). */
 #define LBM_MLP_INPUTS  7
-#define LBM_MLP_HIDDEN  16
-#define LBM_MLP_PARAMS  417   /* H^2 + 10 H + 1 for H = LBM_MLP_HIDDEN */
+#define LBM_MLP_HIDDEN  32
+#define LBM_MLP_PARAMS  1345  /* H^2 + 10 H + 1 for H = LBM_MLP_HIDDEN */
 #define LBM_MLP_SAMPLE  10   /* floats per training sample: x[7], a, b, c */
 typedef struct lbm_mlp_model {
     float params[LBM_MLP_PARAMS];

@@ -66,7 +66,7 @@ LBM_MLP_PATH_WARP_MMA, LBM_MLP_PATH_TCGEN05 = 0, 1
 
 
 LBM_MLP_INPUTS = 7
-LBM_MLP_HIDDEN = 16
+LBM_MLP_HIDDEN = 32
 LBM_MLP_PARAMS = LBM_MLP_HIDDEN * LBM_MLP_HIDDEN + 10 * LBM_MLP_HIDDEN + 1
 LBM_MLP_SAMPLE = 10
 

@@ -1,9 +1,9 @@
 // lbm_mlp.cuh - learned LES closure: strain-rate features, the per-warp tensor-core MLP evaluated
 // inside the step kernel, and the activation shared with the training kernels.
 //
-// Network: x(7) -> H -> H -> 1 (H = kMlpHid = 16), ReLU after both hidden layers,
-// nu_t = out_scale * softplus(z).
-// Inputs (order of lbm.h) from the strain rate S and rho:
+// Network: x(7) -> H -> H -> 1 (H = kMlpHid = 32), GELU in its sigmoid form g(x) = x sigmoid(1.702 x)
+// after both hidden layers, nu_t = out_scale * softplus(z).  Inputs (order of lbm.h) from the strain
+// rate S and rho:
 //   0 tr S   1 I2 = (tr^2 S - S:S)/2   2 I3 = det S   3 Lode parameter 3 sqrt(6) det(S_d) / |S_d|^3
 //   4 S_d:S_d / S:S   5 rho   6 |S| = sqrt(2 S:S)
 // normalised as (x - mean) / std.
@@ -12,11 +12,10 @@
 // cells of a warp (two per lane) are staged as 64 rows of 8 halves (7 inputs and a 1 that carries the
 // first bias) and loaded as A fragments with ldmatrix; layer 1 is mma.m16n8k8, layers 2 and 3
 // mma.m16n8k16.  The accumulator fragment of one layer (rows g, g+8, columns 2c, 2c+1 of each n-tile)
-// is the A fragment of the next after packing to f16x2, so no data moves between lanes.  The ReLU is
-// part of that pack (cvt.rn.relu.f16x2.f32): one instruction per two elements for the activation and
-// the conversion together.  (A GELU network of the same size measured 15 % slower in the fused step:
-// its tanh.approx.f16x2 and the HFMA2 around it per two elements were the single largest part of the
-// network's cost.)
+// is the A fragment of the next after packing to f16x2, so no data moves between lanes.  The activation
+// is applied as z (1 + tanh z) with z = 0.851 x (g(x) = x/2 (1 + tanh(0.851 x)) exactly), the factors
+// 0.851 and 1/1.702 being folded into the FP16 weights on the host: one tanh.approx.f16x2 and one HFMA2
+// per two elements.
 #pragma once
 
 #include <cuda_fp16.h>
@@ -26,7 +25,8 @@
 
 namespace lbm {
 
-constexpr int kMlpIn = 7, kMlpHid = 16, kMlpSample = 10;
+constexpr int kMlpIn = 7, kMlpHid = 32, kMlpSample = 10;
+constexpr float kGeluA = 1.702f;
 constexpr int kMlpParams = kMlpHid * kMlpHid + 10 * kMlpHid + 1;
 // offsets into the FP32 parameter vector: w1[H][7], b1[H], w2[H][H], b2[H], w3[H], b3
 constexpr int kMlpW1 = 0, kMlpB1 = 7 * kMlpHid, kMlpW2 = 8 * kMlpHid, kMlpB2 = kMlpW2 + kMlpHid * kMlpHid,
@@ -78,10 +78,13 @@ LBM_D void mlp_features(const L (&s)[6], L rho, L (&x)[7]) {
     x[6] = sqrt_pos(s2 + s2);
 }
 
-// ---- training-side activation (FP32) ---------------------------------------------------------------
+// ---- training-side activations (FP32) -------------------------------------------------------------
 LBM_D float sigmoidf_(float x) { return 1.0f / (1.0f + expf(-x)); }
-LBM_D float relu_f(float x) { return fmaxf(x, 0.0f); }
-LBM_D float relu_grad(float x) { return x > 0.0f ? 1.0f : 0.0f; }
+LBM_D float gelu_s(float x) { return x * sigmoidf_(kGeluA * x); }
+LBM_D float gelu_s_grad(float x) {
+    const float s = sigmoidf_(kGeluA * x);
+    return s + kGeluA * x * s * (1.0f - s);
+}
 LBM_D float softplusf_(float z) { return fmaxf(z, 0.0f) + log1pf(expf(-fabsf(z))); }
 // the step kernel's softplus (fast exponential and logarithm)
 LBM_D float softplus_fast(float z) { return fmaxf(z, 0.0f) + __logf(1.0f + __expf(-fabsf(z))); }
@@ -90,11 +93,13 @@ LBM_D float softplus_fast(float z) { return fmaxf(z, 0.0f) + __logf(1.0f + __exp
 LBM_D uint32_t h2_bits(__half2 h) { return *reinterpret_cast<uint32_t*>(&h); }
 LBM_D __half2 bits_h2(uint32_t u) { return *reinterpret_cast<__half2*>(&u); }
 
-// ReLU of a packed pair of accumulators, rounded to f16x2 (lo in the lower half)
+// z (1 + tanh z) on a packed pair of accumulators (z already carries the folded 0.851), lo in the lower
+// half of the f16x2 result
 LBM_D uint32_t mlp_act(float lo, float hi) {
-    uint32_t h;
-    asm("cvt.rn.relu.f16x2.f32 %0, %1, %2;" : "=r"(h) : "f"(hi), "f"(lo));
-    return h;
+    const __half2 z = __floats2half2_rn(lo, hi);
+    uint32_t t;
+    asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(h2_bits(z)));
+    return h2_bits(__hfma2(z, bits_h2(t), z));
 }
 
 LBM_D void mma_k8(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t b0) {
@@ -138,7 +143,7 @@ LBM_D void ldmatrix_x4(uint32_t (&r)[4], const void* smem_row) {
 struct MlpNorm {
     float isd[7], nmi[7], lo[7], hi[7];
     float b3, scale;
-    float b2[kMlpHid];  // layer-2 bias (the tcgen05 path adds it after the accumulator load)
+    float b2[kMlpHid];  // layer-2 bias, 0.851 folded in (the tcgen05 path adds it after the accumulator load)
 };
 
 // normalised inputs of one cell as a row of 8 halves (input 7 = 1), and whether all lie in range

@@ -6,8 +6,8 @@
 //   every thread stores its rows of the A operands (FP16) in shared memory and fences them for the async
 //   proxy; the CTA synchronises; thread 0 issues the tcgen05.mma of both tiles (A and B from shared
 //   memory, FP32 accumulators in TMEM) and commits them to an mbarrier; every thread waits on it (bounded),
-//   loads its lane's accumulators with tcgen05.ld, adds the bias, applies the ReLU while packing to FP16
-//   (cvt.rn.relu.f16x2.f32) and stores the next layer's A row.  (Alternating the two tiles, so that one
+//   loads its lane's accumulators with tcgen05.ld, adds the bias, applies the activation while packing to
+//   FP16 (mlp_act, the same folded form as the warp path) and stores the next layer's A row.  (Alternating the two tiles, so that one
 //   tile's products run while the threads work on the other's accumulators, measured slower: two more
 //   CTA barriers per evaluation.)
 // Shapes (kind::f16, FP16 A and B, FP32 D; H = kMlpHid hidden units): layer 1 M128 NH K16 (7 inputs, a 1
@@ -179,7 +179,7 @@ LBM_D void tc_ld16(uint32_t taddr, uint32_t (&r)[16]) {
         : "memory");
 }
 
-// a layer's accumulators of this thread's row in one tile (H columns at `col`) -> + bias -> ReLU ->
+// a layer's accumulators of this thread's row in one tile (H columns at `col`) -> + bias -> activation ->
 // FP16 -> the next operand's row (k groups 0 .. H/8 - 1)
 template <bool BIAS>
 LBM_D void tc_act_row(uint32_t lane_addr, int col, const float* bias, uint4* a2tile) {

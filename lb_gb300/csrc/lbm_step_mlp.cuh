@@ -27,8 +27,8 @@ namespace lbm {
 #ifndef LBM_MLP_MIN_BLOCKS
 #define LBM_MLP_MIN_BLOCKS 0
 #endif
-// the plain-row kernel that runs the network: 7 CTAs per SM (72 registers) measured 36.4 GLUPS with the
-// 7-16-16-1 network against 35.5 at 6 (80 registers) and 33.8 at 5
+// the plain-row kernel that runs the network: 7 CTAs per SM (72 registers) measured 27.9 GLUPS against
+// 27.6 at 6 (80 registers) with the 7-32-32-1 GELU network
 #ifndef LBM_MLP_PLAIN_MIN_BLOCKS
 #define LBM_MLP_PLAIN_MIN_BLOCKS 7
 #endif

@@ -47,9 +47,9 @@ __global__ void __launch_bounds__(kBlk) k_mlp_grad(const float* __restrict__ sam
     extern __shared__ float sm[];
     float* W = sm;                          // parameters
     float* H1 = W + kSmW;                   // [kBlk][kPad] layer-1 activations
-    float* D1 = H1 + kBlk * kPad;           // relu'(pre1), then delta1
+    float* D1 = H1 + kBlk * kPad;           // gelu'(pre1), then delta1
     float* H2 = D1 + kBlk * kPad;           // layer-2 activations
-    float* D2 = H2 + kBlk * kPad;           // relu'(pre2), then delta2
+    float* D2 = H2 + kBlk * kPad;           // gelu'(pre2), then delta2
     float* X = D2 + kBlk * kPad;            // [kBlk][8] normalised inputs and 1
     float* DZ = X + kBlk * 8;               // dL/dz per sample
     float* LS = DZ + kBlk;                  // loss per sample
@@ -77,15 +77,15 @@ __global__ void __launch_bounds__(kBlk) k_mlp_grad(const float* __restrict__ sam
     for (int i = 0; i < kMlpHid; i++) {
         float pre = W[kMlpB1 + i];
         for (int k = 0; k < 7; k++) pre = fmaf(W[kMlpW1 + i * 7 + k], x[k], pre);
-        h1[i] = live ? relu_f(pre) : 0.f;
-        d1[i] = live ? relu_grad(pre) : 0.f;
+        h1[i] = live ? gelu_s(pre) : 0.f;
+        d1[i] = live ? gelu_s_grad(pre) : 0.f;
     }
     float zz = W[kMlpB3];
     for (int o = 0; o < kMlpHid; o++) {
         float pre = W[kMlpB2 + o];
         for (int i = 0; i < kMlpHid; i++) pre = fmaf(W[kMlpW2 + o * kMlpHid + i], h1[i], pre);
-        h2[o] = live ? relu_f(pre) : 0.f;
-        d2[o] = live ? relu_grad(pre) : 0.f;
+        h2[o] = live ? gelu_s(pre) : 0.f;
+        d2[o] = live ? gelu_s_grad(pre) : 0.f;
         zz = fmaf(W[kMlpW3 + o], h2[o], zz);
     }
     float dz = 0.f, loss = 0.f;
@@ -333,12 +333,15 @@ uint64_t splitmix(uint64_t& s) {
 
 namespace lbm {
 
-// host: FP16 fragment table (the weights as trained) and the uniform normalisation
+// host: FP16 fragment table with the activation constants folded in, and the uniform normalisation
 void mlp_pack(const lbm_mlp_model& m, uint4* frag, MlpNorm& nm) {
     constexpr int H = kMlpHid;
-    auto W1 = [&](int n, int k) { return k < 7 ? m.params[kMlpW1 + n * 7 + k] : m.params[kMlpB1 + n]; };
-    auto W2 = [&](int n, int k) { return m.params[kMlpW2 + n * H + k]; };
-    auto W3 = [&](int k) { return m.params[kMlpW3 + k]; };
+    // the activation constants folded into the weights: z = 0.851 x, the next layer takes g = z (1 + tanh z)
+    // / 1.702 (mlp_act returns z (1 + tanh z))
+    const float h = 0.5f * kGeluA;
+    auto W1 = [&](int n, int k) { return h * (k < 7 ? m.params[kMlpW1 + n * 7 + k] : m.params[kMlpB1 + n]); };
+    auto W2 = [&](int n, int k) { return (h / kGeluA) * m.params[kMlpW2 + n * H + k]; };
+    auto W3 = [&](int k) { return m.params[kMlpW3 + k] / kGeluA; };
     auto hb = [](float a, float b) {
         const __half2 v = __floats2half2_rn(a, b);
         uint32_t u;
@@ -376,8 +379,8 @@ void mlp_pack(const lbm_mlp_model& m, uint4* frag, MlpNorm& nm) {
         frag[5 * 32 + lane] = make_uint4(w3[0], w3[1], w3[2], w3[3]);
         uint32_t b[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (int j = 0; j < kMlpNT; j++) {
-            b[2 * j] = fb(m.params[kMlpB2 + 8 * j + 2 * c]);
-            b[2 * j + 1] = fb(m.params[kMlpB2 + 8 * j + 2 * c + 1]);
+            b[2 * j] = fb(h * m.params[kMlpB2 + 8 * j + 2 * c]);
+            b[2 * j + 1] = fb(h * m.params[kMlpB2 + 8 * j + 2 * c + 1]);
         }
         frag[6 * 32 + lane] = make_uint4(b[0], b[1], b[2], b[3]);
         frag[7 * 32 + lane] = make_uint4(b[4], b[5], b[6], b[7]);
@@ -390,19 +393,18 @@ void mlp_pack(const lbm_mlp_model& m, uint4* frag, MlpNorm& nm) {
     }
     nm.b3 = m.params[kMlpB3];
     nm.scale = m.out_scale;
-    for (int n = 0; n < H; n++) nm.b2[n] = m.params[kMlpB2 + n];
-    // the tcgen05 weight image after the table: W1 (k 0..6 weights, k 7 = b1, 8..15 zero), W2, W3 (row
-    // 0 = w3), FP16, K-major core matrices of 8 rows x 8 halves (lbm_mlp_tc.cuh)
+    for (int n = 0; n < H; n++) nm.b2[n] = h * m.params[kMlpB2 + n];
+    // the tcgen05 weight image after the table, with the same folded constants: W1 (k 0..6 weights, k 7 =
+    // b1, 8..15 zero), W2, W3 (row 0 = w3), FP16, K-major core matrices of 8 rows x 8 halves (lbm_mlp_tc.cuh)
     std::vector<__half> img(kTcWBytes / 2, __float2half(0.0f));
     auto put = [&](int base, int KG, int n, int k, float v) {
         img[(base + tc_off(n, k >> 3, KG)) / 2 + (k & 7)] = __float2half_rn(v);
     };
     for (int n = 0; n < H; n++) {
-        for (int k = 0; k < 7; k++) put(kTcW1, 2, n, k, m.params[kMlpW1 + n * 7 + k]);
-        put(kTcW1, 2, n, 7, m.params[kMlpB1 + n]);
-        for (int k = 0; k < H; k++) put(kTcW2, kTcKG, n, k, m.params[kMlpW2 + n * H + k]);
+        for (int k = 0; k < 8; k++) put(kTcW1, 2, n, k, W1(n, k));
+        for (int k = 0; k < H; k++) put(kTcW2, kTcKG, n, k, W2(n, k));
     }
-    for (int k = 0; k < H; k++) put(kTcW3, kTcKG, 0, k, m.params[kMlpW3 + k]);
+    for (int k = 0; k < H; k++) put(kTcW3, kTcKG, 0, k, W3(k));
     std::memcpy(frag + kMlpFragRows * 32, img.data(), kTcWBytes);
 }
 

@@ -41,7 +41,7 @@ class MlpModel:
 
     @classmethod
     def init_from_samples(cls, samples, seed=0x5EED2026, range_quantile=0.0):
-        """Seeded uniform weights (He into the ReLU layers, Glorot into the output); normalisation from the samples' inputs; training range =
+        """Seeded Glorot-uniform weights; normalisation from the samples' inputs; training range =
         [quantile, 1 - quantile] of each input; output scale = median least-squares nu of the samples."""
         x = samples[:, :NIN].astype(np.float64)
         mean, std = x.mean(0), x.std(0)
@@ -55,13 +55,13 @@ class MlpModel:
         rng = np.random.default_rng(seed)
         p = np.zeros(NPAR, np.float32)
 
-        def uniform(n_out, n_in, lim):
+        def glorot(n_out, n_in):
+            lim = np.sqrt(6.0 / (n_in + n_out))
             return rng.uniform(-lim, lim, size=(n_out, n_in)).astype(np.float32)
 
-        # He-uniform into the ReLU layers, Glorot-uniform into the output
-        p[W1:B1] = uniform(NH, NIN, np.sqrt(6.0 / NIN)).reshape(-1)
-        p[W2:B2] = uniform(NH, NH, np.sqrt(6.0 / NH)).reshape(-1)
-        p[W3:B3] = uniform(1, NH, np.sqrt(6.0 / (NH + 1))).reshape(-1)
+        p[W1:B1] = glorot(NH, NIN).reshape(-1)
+        p[W2:B2] = glorot(NH, NH).reshape(-1)
+        p[W3:B3] = glorot(1, NH).reshape(-1)
         return cls(p, mean, std, lo, hi, scale)
 
     def struct(self):
@@ -76,7 +76,7 @@ class MlpModel:
     def copy(self):
         return MlpModel(self.params, self.in_mean, self.in_std, self.in_lo, self.in_hi, self.out_scale)
 
-    ACTIVATION = "relu"  # hidden activation of the network the library evaluates
+    ACTIVATION = "gelu"  # hidden activation of the network the library evaluates (files without the key: gelu)
 
     def save(self, path):
         np.savez(path, params=self.params, in_mean=self.in_mean, in_std=self.in_std, in_lo=self.in_lo,

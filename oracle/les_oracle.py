@@ -9,14 +9,15 @@ what the CUDA library computes for the learned closure, so that the GPU kernels 
     filtered velocity, filtered stress and the error contractions (a, b, c);
   - loss_and_grad(): the training loss and its gradient w.r.t. the FP32 parameters (the forward and
     backward pass of the GPU training kernels, in float64);
-  - infer_fp16(): the step kernel's FP16 evaluation (FP16 weights and activations, FP32
-    accumulation, ReLU applied where each hidden layer is rounded to FP16).
+  - infer_fp16(): the step kernel's FP16 evaluation (folded activation constants, FP16 weights and
+    activations, FP32 accumulation), with an exact tanh in place of tanh.approx.f16x2.
 Parity of these with the GPU is "parity unpinned" by reference data; the backward pass is pinned by
 central finite differences of the forward pass (tests/test_les_cpu.py).
 """
 import numpy as np
 
-NIN, NH = 7, 16
+NIN, NH = 7, 32
+GELU_A = 1.702
 NPAR = NH * NH + 10 * NH + 1
 # offsets of the parameter vector (w1[H][7], b1, w2[H][H], b2, w3, b3)
 W1, B1, W2 = 0, 7 * NH, 8 * NH
@@ -105,12 +106,13 @@ def _sig(x):
     return 1.0 / (1.0 + np.exp(-x))
 
 
-def _relu(x):
-    return np.maximum(x, 0.0)
+def _gelu(x):
+    return x * _sig(GELU_A * x)
 
 
-def _relu_grad(x):
-    return (x > 0.0).astype(np.float64)
+def _gelu_grad(x):
+    s = _sig(GELU_A * x)
+    return s + GELU_A * x * s * (1.0 - s)
 
 
 def _softplus(z):
@@ -126,9 +128,9 @@ def forward(p, x, mean, std, scale):
     w1, b1, w2, b2, w3, b3 = unpack(p)
     xh = (np.asarray(x, np.float64) - mean) / std
     pre1 = xh @ w1.T + b1
-    h1 = _relu(pre1)
+    h1 = _gelu(pre1)
     pre2 = h1 @ w2.T + b2
-    h2 = _relu(pre2)
+    h2 = _gelu(pre2)
     z = h2 @ w3 + b3
     return scale * _softplus(z), (xh, pre1, h1, pre2, h2, z)
 
@@ -146,10 +148,10 @@ def loss_and_grad(p, samples, mean, std, scale, K):
     g = np.zeros(NPAR)
     g[W3:B3] = dz @ h2
     g[B3] = dz.sum()
-    d2 = (dz[:, None] * w3[None, :]) * _relu_grad(pre2)
+    d2 = (dz[:, None] * w3[None, :]) * _gelu_grad(pre2)
     g[W2:B2] = (d2.T @ h1).reshape(-1)
     g[B2:W3] = d2.sum(0)
-    d1 = (d2 @ w2) * _relu_grad(pre1)
+    d1 = (d2 @ w2) * _gelu_grad(pre1)
     g[W1:B1] = (d1.T @ xh).reshape(-1)
     g[B1:W2] = d1.sum(0)
     return loss, g
@@ -161,9 +163,11 @@ def _h(x):
 
 
 def infer_fp16(p, x, mean, std, lo, hi, scale):
-    """nu_t and in-range flags as the step kernel computes them: FP16 inputs and weights, float sums
-    (exact here), each hidden layer rounded to FP16 with the ReLU (cvt.rn.relu.f16x2.f32)."""
+    """nu_t and in-range flags as the step kernel computes them: FP16 inputs and folded FP16 weights
+    (z = 0.851 x, the activation z (1 + tanh z) with the 1/1.702 in the next layer's weights), sums in
+    float64, each activation rounded to FP16, with an exact tanh in place of tanh.approx.f16x2."""
     w1, b1, w2, b2, w3, b3 = unpack(p)
+    hA = 0.5 * GELU_A
     x = np.asarray(x, np.float64)
     # normalised input = fma(x, isd, nmi) in FP32: the product of two floats is exact in float64
     isd = (np.float32(1.0) / np.asarray(std, np.float32)).astype(np.float64)
@@ -176,13 +180,15 @@ def infer_fp16(p, x, mean, std, lo, hi, scale):
     lo_n, hi_n = fma32(lo), fma32(hi)
     ok = np.all((xn >= lo_n) & (xn <= hi_n), axis=1)
     xin = np.concatenate([_h(xn), np.ones((x.shape[0], 1))], axis=1)
-    W1e = _h(np.concatenate([w1.astype(np.float32), b1.astype(np.float32)[:, None]], axis=1))
-    W2e = _h(w2.astype(np.float32))
-    B2e = b2.astype(np.float32).astype(np.float64)
-    W3e = _h(w3.astype(np.float32))
+    W1e = _h(np.concatenate([(hA * w1).astype(np.float32), (hA * b1).astype(np.float32)[:, None]], axis=1))
+    W2e = _h((hA / GELU_A * w2).astype(np.float32))
+    B2e = (hA * b2).astype(np.float32).astype(np.float64)
+    W3e = _h((w3 / GELU_A).astype(np.float32))
 
     def act(v):
-        return np.maximum(_h(v), 0.0)
+        zq = _h(v)
+        t = _h(np.tanh(zq))
+        return _h(zq * t + zq)
 
     a1 = act(xin @ W1e.T)
     a2 = act(a1 @ W2e.T + B2e)

@@ -79,7 +79,7 @@ def test_eval_matches_fp16_oracle(built_lib):
     nu, ok = les.evaluate(m, x)
     ref, ref_ok = lo.infer_fp16(m.params, x, m.in_mean, m.in_std, m.in_lo, m.in_hi, m.out_scale)
     assert np.array_equal(ok, ref_ok)
-    # FP16 activations rounded after FP32 sums (float64 in the emulation): 2 % of nu
+    # tanh.approx.f16x2 against the exact tanh of the emulation, FP16 activations: 2 % of nu
     rel = np.abs(nu - ref) / np.abs(ref)
     assert np.quantile(rel, 0.99) < 2e-2 and rel.max() < 5e-2, (np.quantile(rel, 0.99), rel.max())
     # inputs outside the range are flagged
@@ -91,7 +91,7 @@ def test_eval_matches_fp16_oracle(built_lib):
 
 def test_eval_tcgen05_matches_warp_path_and_oracle(built_lib):
     """The network on tcgen05.mma (TMEM accumulators, one CTA per 256 inputs) against the warp-level
-    mma.sync path and the FP16 oracle: the same FP16 operands and ReLU, FP32 sums in another order, so
+    mma.sync path and the FP16 oracle: the same FP16 operands and activation, FP32 sums in another order, so
     the two GPU paths agree to FP16 rounding of the hidden activations; 1,000 inputs (a partial last
     CTA) and 300 (a CTA with unused rows)."""
     m, s = _model_and_samples(seed=13)
@@ -279,7 +279,7 @@ def test_fused_learned_step_matches_oracle_step(built_lib, oracle_lib, storage, 
     Bounds: FP32 moments within 5e-5 u_max of the FP64 oracle after 24 steps on 99.9 % of the cells (the
     FP32 noise floor of the case is ~1e-5), 5e-4 u_max on every cell; FP16 storage 2e-3 relative L2 of u.  With a refresh interval of 2 (mode 1 on even
     steps) the kept nu_t read back from the GPU after a network step matches the oracle's nu_t of that
-    step to 2 % at the 99th percentile (FP16 activations rounded after FP32 sums), with the same
+    step to 2 % at the 99th percentile (FP32; FP16 tanh.approx against the exact tanh), with the same
     in-range decision on >= 99 % of the cells.  tc: the network of the plain rows on tcgen05.mma
     (LBM_OPT_MLP_TCGEN05), under the same bounds."""
     from lb_gb300 import capi
