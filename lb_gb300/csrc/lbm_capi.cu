@@ -48,6 +48,8 @@ struct lbm_ctx {
     std::vector<lbm_bc_outlet> outlets;
     std::vector<lbm_bc_symmetry> syms;
     bool have_flags = false, have_geom = false, initialized = false;
+    bool rows_pending = false;                  // build_geometry left the row lists for finish_rows
+    std::unique_ptr<uint8_t[]> host_cls;        //   with the class bytes they are built from
     // side tables
     int n_lid = 0, n_in = 0, n_out = 0;
     void* d_lid_state = nullptr;
@@ -399,7 +401,140 @@ lbm_status lbm_set_symmetry(lbm_ctx* c, const lbm_bc_symmetry* recs, int32_t n) 
 }
 
 // ---- geometry: reference flags + BC records -> class byte, side-table indices, validation -------
-static lbm_status build_geometry(lbm_ctx* c) {
+// the row lists of the step kernels from the class bytes: the rows the row-staged step may take and the
+// split of the rows into plain, wall and remaining rows (host cores), uploaded to the device
+static lbm_status build_rows(lbm_ctx* c, const uint8_t* cls) {
+    const int nx = c->cfg.nx, ny = c->cfg.ny, nz = c->cfg.nz;
+    const int* wrap = c->cfg.periodic;
+    auto id = [&](int i, int j, int k) { return (long long)i + (long long)nx * ((long long)j + (long long)ny * k); };
+    // rows the row-staged step may take (FP16-deviation storage): every cell bulk fluid, x periodic,
+    // segments a multiple of 16 bytes, one thread per x-pair
+    {
+        const long long nrow = (long long)ny * nz;
+        std::vector<int32_t> bulk, other;
+        c->rows_ok = (c->cfg.options & LBM_OPT_ROW_STAGING) && c->cfg.closure != LBM_CLOSURE_MLP && c->cfg.storage == LBM_STORAGE_F16DEV && wrap[0] &&
+                     nx % 2 == 0 && nx >= 64 && nx <= 1024 &&
+                     ((size_t)nx * c->esize) % 16 == 0 && nrow < (1LL << 31);
+        for (long long r = 0; r < nrow && c->rows_ok; r++) {
+            bool all = true;
+            for (int i = 0; i < nx && all; i++) all = (cls[(size_t)(r * nx + i)] & (uint8_t)~BIT_REFBULK) == CLS_BULK;
+            (all ? bulk : other).push_back((int32_t)r);
+        }
+        if (bulk.empty()) c->rows_ok = false;
+        dfree(c->d_bulk_rows); dfree(c->d_other_rows);
+        c->d_bulk_rows = c->d_other_rows = nullptr;
+        c->n_bulk_rows = (int)bulk.size();
+        c->n_other_rows = (int)other.size();
+        if (c->rows_ok) {
+            CU(c, cudaMalloc(&c->d_bulk_rows, bulk.size() * 4));
+            CU(c, cudaMemcpy(c->d_bulk_rows, bulk.data(), bulk.size() * 4, cudaMemcpyHostToDevice));
+            if (!other.empty()) {
+                CU(c, cudaMalloc(&c->d_other_rows, other.size() * 4));
+                CU(c, cudaMemcpy(c->d_other_rows, other.data(), other.size() * 4, cudaMemcpyHostToDevice));
+            }
+        }
+    }
+    // the step split by rows (FP32 and FP16-deviation storage): plain rows are off the periodic y/z seams
+    // with every cell a bulk fluid cell of the packed path (the combined collision packs reference-flag-1
+    // cells only); nx even.  LBM_OPT_ONE_LAUNCH keeps one launch over the lattice.
+    {
+        const long long nrow = (long long)ny * nz;
+        const bool comb = c->cfg.collision == LBM_COLLISION_CUMULANT_COMBINED;
+        const uint8_t keep = comb ? (uint8_t)0xff : (uint8_t)~BIT_REFBULK;
+        const uint8_t want = comb ? (uint8_t)(CLS_BULK | BIT_REFBULK) : (uint8_t)CLS_BULK;
+        c->split_ok = c->cfg.storage != LBM_STORAGE_F64 && !(c->cfg.options & LBM_OPT_ONE_LAUNCH) && nrow < (1LL << 31);
+        std::vector<uint8_t> plain(c->split_ok ? (size_t)nrow : 0, 0);
+        const long long row_grain = std::max(1LL, 65536LL / nx);  // rows of nx cells per thread at least
+        if (c->split_ok && !(nx & 1)) {
+            host_parallel(nrow, [&](long long r0, long long r1) {
+                for (long long r = r0; r < r1; r++) {
+                    const int y = (int)(r % ny), z = (int)(r / ny);
+                    if ((wrap[1] && (y == 0 || y == ny - 1)) || (wrap[2] && (z == 0 || z == nz - 1))) continue;
+                    bool all = true;
+                    for (int i = 0; i < nx && all; i++) all = (cls[(size_t)(r * nx + i)] & keep) == want;
+                    plain[(size_t)r] = all ? 1 : 0;
+                }
+            }, row_grain);
+        }
+        // rows beside a flat wall: every cell an edge cell (no role bit) whose 26 sources are solid or
+        // fluid cells of the packed kinds at the same offsets along the whole row, off the periodic y/z
+        // seams (the combined collision keeps them on the general path)
+        std::vector<uint32_t> wmask(plain.size(), 0);
+        std::vector<uint8_t> is_wall(plain.size(), 0);
+        if (c->split_ok && !(nx & 1) && !comb && !(c->cfg.options & LBM_OPT_NO_WALL_ROWS)) {
+            host_parallel(nrow, [&](long long r0, long long r1) {
+                for (long long r = r0; r < r1; r++) {
+                    if (plain[(size_t)r]) continue;
+                    const int y = (int)(r % ny), z = (int)(r / ny);
+                    if ((wrap[1] && (y == 0 || y == ny - 1)) || (wrap[2] && (z == 0 || z == nz - 1))) continue;
+                    bool ok = (cls[(size_t)(r * nx)] & (uint8_t)~BIT_REFBULK) == CLS_EDGE;  // cheap early exit
+                    // the nine source rows (y - c_y, z - c_z) of the row, inside the lattice (these rows are
+                    // off the periodic seams, so a y or z source outside it rules the row out)
+                    const uint8_t* src[27];
+                    for (int v = 1; v < 27 && ok; v++) {
+                        const int b = y - cy(v), e = z - cz(v);
+                        if (b < 0 || b >= ny || e < 0 || e >= nz) ok = false;
+                        else src[v] = cls + (size_t)id(0, b, e);
+                    }
+                    if (ok && !wrap[0]) ok = false;  // x sources wrap only on a periodic x axis
+                    uint32_t mask = 0;
+                    // the solid-source mask of cell i, and whether a source is of a kind other than solid,
+                    // bulk or edge (a compile-time loop over the directions; x wraps only at the row ends)
+                    auto cell_mask = [&](int i, bool wrapx, uint32_t& other) {
+                        uint32_t m = 0;
+                        sfor_host<1, 27>([&](auto vc) {
+                            constexpr int v = decltype(vc)::value;
+                            int a = i - cx(v);
+                            if (wrapx) a = a < 0 ? a + nx : a >= nx ? a - nx : a;
+                            const int k = src[v][a] & CLS_MASK;
+                            m |= (uint32_t)(k == CLS_SOLID) << v;
+                            other |= (uint32_t)(k != CLS_SOLID && k != CLS_BULK && k != CLS_EDGE);
+                        });
+                        return m;
+                    };
+                    const uint8_t* row = cls + (size_t)r * nx;
+                    uint32_t other = 0;
+                    if (ok) mask = cell_mask(0, true, other);
+                    for (int i = 1; i < nx && ok; i++) {
+                        if ((row[i] & (uint8_t)~BIT_REFBULK) != CLS_EDGE) { ok = false; break; }
+                        if (cell_mask(i, i == nx - 1, other) != mask) ok = false;
+                    }
+                    if (other) ok = false;
+                    if (ok) { is_wall[(size_t)r] = 1; wmask[(size_t)r] = mask; }
+                }
+            }, row_grain);
+        }
+        std::vector<int32_t> pr, rr, wr, ra;
+        std::vector<uint32_t> wm;
+        for (long long r = 0; r < (long long)plain.size(); r++) {
+            if (plain[(size_t)r]) { pr.push_back((int32_t)r); continue; }
+            ra.push_back((int32_t)r);
+            if (is_wall[(size_t)r]) { wr.push_back((int32_t)r); wm.push_back(wmask[(size_t)r]); }
+            else rr.push_back((int32_t)r);
+        }
+        dfree(c->d_plain_rows); dfree(c->d_rest_rows); dfree(c->d_wall_rows); dfree(c->d_wall_solid); dfree(c->d_rest_all);
+        c->d_plain_rows = c->d_rest_rows = c->d_wall_rows = c->d_rest_all = nullptr;
+        c->d_wall_solid = nullptr;
+        c->n_plain_rows = (int)pr.size();
+        c->n_rest_rows = (int)rr.size();
+        c->n_wall_rows = (int)wr.size();
+        c->n_rest_all = (int)ra.size();
+        auto upload = [&](auto** dst, const auto& v) -> lbm_status {
+            if (!c->split_ok || v.empty()) return LBM_OK;
+            CU(c, cudaMalloc((void**)dst, v.size() * 4));
+            CU(c, cudaMemcpy(*dst, v.data(), v.size() * 4, cudaMemcpyHostToDevice));
+            return LBM_OK;
+        };
+        lbm_status us;
+        if ((us = upload(&c->d_plain_rows, pr)) || (us = upload(&c->d_rest_rows, rr)) ||
+            (us = upload(&c->d_wall_rows, wr)) || (us = upload(&c->d_wall_solid, wm)) || (us = upload(&c->d_rest_all, ra)))
+            return us;
+    }
+    return LBM_OK;
+}
+
+// defer_rows: leave the row lists for finish_rows (the class bytes stay on the host until then)
+static lbm_status build_geometry(lbm_ctx* c, bool defer_rows = false) {
     const int nx = c->cfg.nx, ny = c->cfg.ny, nz = c->cfg.nz;
     const long long N = c->N;
     const int* wrap = c->cfg.periodic;
@@ -752,142 +887,34 @@ static lbm_status build_geometry(lbm_ctx* c) {
         CU(c, cudaMemcpy(c->d_sym_dir, sym_dir.data(), (size_t)n_sym * 4, cudaMemcpyHostToDevice));
     }
     CU(c, cudaStreamSynchronize(c->st));
-    // rows the row-staged step may take (FP16-deviation storage): every cell bulk fluid, x periodic,
-    // segments a multiple of 16 bytes, one thread per x-pair
-    {
-        const long long nrow = (long long)ny * nz;
-        std::vector<int32_t> bulk, other;
-        c->rows_ok = (c->cfg.options & LBM_OPT_ROW_STAGING) && c->cfg.closure != LBM_CLOSURE_MLP && c->cfg.storage == LBM_STORAGE_F16DEV && wrap[0] &&
-                     nx % 2 == 0 && nx >= 64 && nx <= 1024 &&
-                     ((size_t)nx * c->esize) % 16 == 0 && nrow < (1LL << 31);
-        for (long long r = 0; r < nrow && c->rows_ok; r++) {
-            bool all = true;
-            for (int i = 0; i < nx && all; i++) all = (cls[(size_t)(r * nx + i)] & (uint8_t)~BIT_REFBULK) == CLS_BULK;
-            (all ? bulk : other).push_back((int32_t)r);
-        }
-        if (bulk.empty()) c->rows_ok = false;
-        dfree(c->d_bulk_rows); dfree(c->d_other_rows);
-        c->d_bulk_rows = c->d_other_rows = nullptr;
-        c->n_bulk_rows = (int)bulk.size();
-        c->n_other_rows = (int)other.size();
-        if (c->rows_ok) {
-            CU(c, cudaMalloc(&c->d_bulk_rows, bulk.size() * 4));
-            CU(c, cudaMemcpy(c->d_bulk_rows, bulk.data(), bulk.size() * 4, cudaMemcpyHostToDevice));
-            if (!other.empty()) {
-                CU(c, cudaMalloc(&c->d_other_rows, other.size() * 4));
-                CU(c, cudaMemcpy(c->d_other_rows, other.data(), other.size() * 4, cudaMemcpyHostToDevice));
-            }
-        }
-    }
-    // the step split by rows (FP32 and FP16-deviation storage): plain rows are off the periodic y/z seams
-    // with every cell a bulk fluid cell of the packed path (the combined collision packs reference-flag-1
-    // cells only); nx even.  LBM_OPT_ONE_LAUNCH keeps one launch over the lattice.
-    {
-        const long long nrow = (long long)ny * nz;
-        const bool comb = c->cfg.collision == LBM_COLLISION_CUMULANT_COMBINED;
-        const uint8_t keep = comb ? (uint8_t)0xff : (uint8_t)~BIT_REFBULK;
-        const uint8_t want = comb ? (uint8_t)(CLS_BULK | BIT_REFBULK) : (uint8_t)CLS_BULK;
-        c->split_ok = c->cfg.storage != LBM_STORAGE_F64 && !(c->cfg.options & LBM_OPT_ONE_LAUNCH) && nrow < (1LL << 31);
-        std::vector<uint8_t> plain(c->split_ok ? (size_t)nrow : 0, 0);
-        const long long row_grain = std::max(1LL, 65536LL / nx);  // rows of nx cells per thread at least
-        if (c->split_ok && !(nx & 1)) {
-            host_parallel(nrow, [&](long long r0, long long r1) {
-                for (long long r = r0; r < r1; r++) {
-                    const int y = (int)(r % ny), z = (int)(r / ny);
-                    if ((wrap[1] && (y == 0 || y == ny - 1)) || (wrap[2] && (z == 0 || z == nz - 1))) continue;
-                    bool all = true;
-                    for (int i = 0; i < nx && all; i++) all = (cls[(size_t)(r * nx + i)] & keep) == want;
-                    plain[(size_t)r] = all ? 1 : 0;
-                }
-            }, row_grain);
-        }
-        // rows beside a flat wall: every cell an edge cell (no role bit) whose 26 sources are solid or
-        // fluid cells of the packed kinds at the same offsets along the whole row, off the periodic y/z
-        // seams (the combined collision keeps them on the general path)
-        std::vector<uint32_t> wmask(plain.size(), 0);
-        std::vector<uint8_t> is_wall(plain.size(), 0);
-        if (c->split_ok && !(nx & 1) && !comb && !(c->cfg.options & LBM_OPT_NO_WALL_ROWS)) {
-            host_parallel(nrow, [&](long long r0, long long r1) {
-                for (long long r = r0; r < r1; r++) {
-                    if (plain[(size_t)r]) continue;
-                    const int y = (int)(r % ny), z = (int)(r / ny);
-                    if ((wrap[1] && (y == 0 || y == ny - 1)) || (wrap[2] && (z == 0 || z == nz - 1))) continue;
-                    bool ok = (cls[(size_t)(r * nx)] & (uint8_t)~BIT_REFBULK) == CLS_EDGE;  // cheap early exit
-                    // the nine source rows (y - c_y, z - c_z) of the row, inside the lattice (these rows are
-                    // off the periodic seams, so a y or z source outside it rules the row out)
-                    const uint8_t* src[27];
-                    for (int v = 1; v < 27 && ok; v++) {
-                        const int b = y - cy(v), e = z - cz(v);
-                        if (b < 0 || b >= ny || e < 0 || e >= nz) ok = false;
-                        else src[v] = cls + (size_t)id(0, b, e);
-                    }
-                    if (ok && !wrap[0]) ok = false;  // x sources wrap only on a periodic x axis
-                    uint32_t mask = 0;
-                    // the solid-source mask of cell i, and whether a source is of a kind other than solid,
-                    // bulk or edge (a compile-time loop over the directions; x wraps only at the row ends)
-                    auto cell_mask = [&](int i, bool wrapx, uint32_t& other) {
-                        uint32_t m = 0;
-                        sfor_host<1, 27>([&](auto vc) {
-                            constexpr int v = decltype(vc)::value;
-                            int a = i - cx(v);
-                            if (wrapx) a = a < 0 ? a + nx : a >= nx ? a - nx : a;
-                            const int k = src[v][a] & CLS_MASK;
-                            m |= (uint32_t)(k == CLS_SOLID) << v;
-                            other |= (uint32_t)(k != CLS_SOLID && k != CLS_BULK && k != CLS_EDGE);
-                        });
-                        return m;
-                    };
-                    const uint8_t* row = cls + (size_t)r * nx;
-                    uint32_t other = 0;
-                    if (ok) mask = cell_mask(0, true, other);
-                    for (int i = 1; i < nx && ok; i++) {
-                        if ((row[i] & (uint8_t)~BIT_REFBULK) != CLS_EDGE) { ok = false; break; }
-                        if (cell_mask(i, i == nx - 1, other) != mask) ok = false;
-                    }
-                    if (other) ok = false;
-                    if (ok) { is_wall[(size_t)r] = 1; wmask[(size_t)r] = mask; }
-                }
-            }, row_grain);
-        }
-        std::vector<int32_t> pr, rr, wr, ra;
-        std::vector<uint32_t> wm;
-        for (long long r = 0; r < (long long)plain.size(); r++) {
-            if (plain[(size_t)r]) { pr.push_back((int32_t)r); continue; }
-            ra.push_back((int32_t)r);
-            if (is_wall[(size_t)r]) { wr.push_back((int32_t)r); wm.push_back(wmask[(size_t)r]); }
-            else rr.push_back((int32_t)r);
-        }
-        dfree(c->d_plain_rows); dfree(c->d_rest_rows); dfree(c->d_wall_rows); dfree(c->d_wall_solid); dfree(c->d_rest_all);
-        c->d_plain_rows = c->d_rest_rows = c->d_wall_rows = c->d_rest_all = nullptr;
-        c->d_wall_solid = nullptr;
-        c->n_plain_rows = (int)pr.size();
-        c->n_rest_rows = (int)rr.size();
-        c->n_wall_rows = (int)wr.size();
-        c->n_rest_all = (int)ra.size();
-        auto upload = [&](auto** dst, const auto& v) -> lbm_status {
-            if (!c->split_ok || v.empty()) return LBM_OK;
-            CU(c, cudaMalloc((void**)dst, v.size() * 4));
-            CU(c, cudaMemcpy(*dst, v.data(), v.size() * 4, cudaMemcpyHostToDevice));
-            return LBM_OK;
-        };
-        lbm_status us;
-        if ((us = upload(&c->d_plain_rows, pr)) || (us = upload(&c->d_rest_rows, rr)) ||
-            (us = upload(&c->d_wall_rows, wr)) || (us = upload(&c->d_wall_solid, wm)) || (us = upload(&c->d_rest_all, ra)))
-            return us;
+    if (defer_rows) {  // the row lists follow in finish_rows, while the init kernel runs
+        c->host_cls = std::move(cls_buf);
+        c->rows_pending = true;
+    } else {
+        lbm_status rs = build_rows(c, cls);
+        if (rs) return rs;
     }
     c->have_geom = true;
     return LBM_OK;
 }
 
-static lbm_status ensure_geometry(lbm_ctx* c) {
+static lbm_status finish_rows(lbm_ctx* c) {
+    if (!c->rows_pending) return LBM_OK;
+    lbm_status s = build_rows(c, c->host_cls.get());
+    c->host_cls.reset();
+    c->rows_pending = false;
+    return s;
+}
+
+static lbm_status ensure_geometry(lbm_ctx* c, bool defer_rows = false) {
     if (c->have_geom) return LBM_OK;
-    return build_geometry(c);
+    return build_geometry(c, defer_rows);
 }
 
 static lbm_status init_common(lbm_ctx* c, const double* rho, const double* u, double rho0, const double* u0,
                               const double* pops) {
     cudaSetDevice(c->cfg.device);
-    lbm_status s = ensure_geometry(c);
+    lbm_status s = ensure_geometry(c, true);
     if (s) return s;
     double *dr = nullptr, *du = nullptr, *dp = nullptr;  // staging copies (pageable inputs)
     const size_t N = (size_t)c->N;
@@ -915,9 +942,11 @@ static lbm_status init_common(lbm_ctx* c, const double* rho, const double* u, do
     Params p = make_params(c);
     double z3[3] = {0, 0, 0};
     cudaError_t e = do_init(c, p, vr, vu, rho0, u0 ? u0 : z3, vp);
+    const lbm_status rs = finish_rows(c);  // host work while the init kernel runs
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     dfree(dr); dfree(du); dfree(dp);
     if (e != cudaSuccess) return fail(c, LBM_ERR_CUDA, "init kernel: %s", cudaGetErrorString(e));
+    if (rs) return rs;
     if (c->d_out_save) CU(c, cudaMemset(c->d_out_save, 0, 2 * 18 * (size_t)c->n_out * real_size(c)));
     if (c->d_out_msave) CU(c, cudaMemset(c->d_out_msave, 0, 2 * 4 * (size_t)c->n_ms * real_size(c)));
     c->avg_on = false; c->avg_count = 0; c->avg_last = -1;
