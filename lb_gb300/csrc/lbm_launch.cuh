@@ -29,7 +29,9 @@ static RowKernel mlp_kernel(const Params& p) {
     }
     if (!p.nut) return odd ? k_step2_mlp<S, COLL, true, 0, ROWS> : k_step2_mlp<S, COLL, false, 0, ROWS>;
     if (p.mlp_run) return odd ? k_step2_mlp<S, COLL, true, 1, ROWS> : k_step2_mlp<S, COLL, false, 1, ROWS>;
-    return odd ? k_step2_mlp<S, COLL, true, 2, ROWS> : k_step2_mlp<S, COLL, false, 2, ROWS>;
+    // the plain rows between network steps: the plain-row kernel with the kept nu_t's rate
+    if constexpr (ROWS == 1) return odd ? k_step2_plain<S, COLL, 2, true> : k_step2_plain<S, COLL, 2, false>;
+    else return odd ? k_step2_mlp<S, COLL, true, 2, ROWS> : k_step2_mlp<S, COLL, false, 2, ROWS>;
 }
 
 template <class S, int COLL, int CLOS>

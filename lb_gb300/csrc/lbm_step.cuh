@@ -233,9 +233,11 @@ LBM_D Mom<F2> moments_from_raw(const Mom<F2>& m, const Params& p) {
 
 // moments, relaxation rate and collision of a packed pair of bulk cells
 // (time-average accumulation of the two cells idx0, idx0+1 when p.acc is set).  RAW: f holds the FP16
-// deviations (the cumulant-2015 collision rebuilds every population from the moments)
+// deviations (the cumulant-2015 collision rebuilds every population from the moments).  CLOS 2 (the
+// learned closure in a step that reuses its kept nu_t): each cell relaxes with rate_kept of its kept
+// value, the Smagorinsky rate where that is the fallback mark
 template <int COLL, int CLOS, bool RAW = false>
-LBM_D void collide_pair(const Params& p, F2 (&f)[27], long long idx0) {
+LBM_D void collide_pair(const Params& p, F2 (&f)[27], long long idx0, float2 kept = make_float2(-1.f, -1.f)) {
     static_assert(!RAW || COLL == 1, "only the cumulant-2015 step needs no decoded populations");
     Mom<F2> mm = raw_moments(f);
     if constexpr (RAW) mm = moments_from_raw(mm, p);
@@ -250,8 +252,15 @@ LBM_D void collide_pair(const Params& p, F2 (&f)[27], long long idx0) {
         acc_add(p, idx0, mm.rho.v.x, ux.v.x, uy.v.x, uz.v.x);
         acc_add(p, idx0 + 1, mm.rho.v.y, ux.v.y, uy.v.y, uz.v.y);
     }
-    collide_lane<COLL, CLOS>(f, mm, ri, ux, uy, uz, F2(p.tauf), F2(p.cles18f), F2(p.omega0f), p.has_force != 0,
-                             F2(p.Ff[0]), F2(p.Ff[1]), F2(p.Ff[2]));
+    if constexpr (CLOS == 2) {
+        const F2 om_s = omega_smagorinsky(F2(p.tauf), F2(p.cles18f), mm.rho, ri, ux, uy, uz, mm);
+        const F2 om(rate_kept(kept.x, p.tauf, om_s.v.x), rate_kept(kept.y, p.tauf, om_s.v.y));
+        collide_with_rate<COLL>(f, mm, ri, ux, uy, uz, om, p.has_force != 0, F2(p.Ff[0]), F2(p.Ff[1]),
+                                F2(p.Ff[2]));
+    } else {
+        collide_lane<COLL, CLOS>(f, mm, ri, ux, uy, uz, F2(p.tauf), F2(p.cles18f), F2(p.omega0f),
+                                 p.has_force != 0, F2(p.Ff[0]), F2(p.Ff[1]), F2(p.Ff[2]));
+    }
 }
 
 // ---- x-pairs in packed FP32 ----------------------------------------------------------------------------
@@ -442,16 +451,19 @@ template <int COLL> LBM_HD constexpr int packed_coll() { return COLL == 3 ? 1 : 
 template <class S, int COLL> LBM_HD constexpr bool packed_raw() { return S::kind == 2 && packed_coll<COLL>() == 1; }
 
 // one packed pair of bulk cells in a row off the periodic y/z seams: every access is a per-direction
-// base address plus the element index
+// base address plus the element index.  CLOS 2: the learned closure's steps between network evaluations
+// (the pair's kept nu_t, Params::nut, fetched before the populations)
 template <class S, int COLL, int CLOS, bool ODD>
 LBM_D void step_pair_plain(const Params& p, int e0, int x0) {
     constexpr int PC = packed_coll<COLL>();
     constexpr bool RAW = packed_raw<S, COLL>();
     const PairCodec k = make_codec<S>(p);
     const PairIdx q = make_pair_idx(p, e0, x0);
+    float2 kept = make_float2(-1.f, -1.f);
+    if constexpr (CLOS == 2) kept = __half22float2(__ldg((const __half2*)(p.nut + e0)));
     F2 f[27];
     load_pair<S, ODD, RAW>(p, q, k, f);
-    collide_pair<PC, CLOS, RAW>(p, f, e0);
+    collide_pair<PC, CLOS, RAW>(p, f, e0, kept);
     store_pair<S, ODD>(p, q, k, f);
 }
 

@@ -14,6 +14,8 @@
 // MODE 0: the network runs in this step.  MODE 1: it runs and its nu_t (or -1 for the fallback) is kept
 // per cell in FP16 (Params::nut).  MODE 2: it does not run; each pair relaxes with the kept nu_t (the
 // Smagorinsky rate where the kept value is negative or not a number), fetched before the populations.
+// The plain rows' MODE 2 steps run k_step2_plain with closure 2 (step_pair_plain, the same rate), the
+// register allocation of the Smagorinsky plain-row kernel.
 #pragma once
 
 #include "lbm_mlp.cuh"
@@ -35,9 +37,8 @@ namespace lbm {
 // ROWS: 0 one launch over the lattice (grid x = pair block, y, z); 1 the plain rows of the split step
 // (every pair a packed bulk pair off the y/z seams, lbm_step.cuh); 2 the remaining rows (1-D grid of
 // listed rows x pair blocks, row_block)
-constexpr int mlp_min_blocks(int mode, int rows, int coll, int kind) {
-    return mode == 2 ? (rows == 1 ? plain_min_blocks(coll, kind) : step2_min_blocks(coll))
-                     : (rows == 1 ? LBM_MLP_PLAIN_MIN_BLOCKS : LBM_MLP_MIN_BLOCKS);
+constexpr int mlp_min_blocks(int mode, int rows, int coll) {
+    return mode == 2 ? step2_min_blocks(coll) : (rows == 1 ? LBM_MLP_PLAIN_MIN_BLOCKS : LBM_MLP_MIN_BLOCKS);
 }
 // one x-pair of the learned-closure step (x0 even; y, z for ROWS 0 and 2, row r for ROWS 1).  Every
 // thread of the warp (TC: of the CTA) calls it, including threads without a pair, since the network runs
@@ -150,9 +151,10 @@ LBM_D void mlp_pair(const Params& p, int x0, int y, int z, int r, const uint4 (*
 // TC (plain rows, network steps): the network on tcgen05.mma with TMEM accumulators for the CTA's cells
 // (lbm_mlp_tc.cuh) instead of the per-warp mma.sync evaluation
 template <class S, int COLL, bool ODD, int MODE, int ROWS = 0, bool TC = false>
-__global__ void __launch_bounds__(128, mlp_min_blocks(MODE, ROWS, COLL, S::kind)) k_step2_mlp(Params p, const int32_t* rows, int nrows) {
+__global__ void __launch_bounds__(128, mlp_min_blocks(MODE, ROWS, COLL)) k_step2_mlp(Params p, const int32_t* rows, int nrows) {
     static_assert(S::kind != 0, "the learned closure runs on the packed FP32 path");
     static_assert(!TC || (ROWS == 1 && MODE != 2), "the tcgen05 network serves the plain rows' network steps");
+    static_assert(MODE != 2 || ROWS != 1, "the plain rows' steps without the network run k_step2_plain");
     constexpr bool WARP = MODE != 2 && !TC;
     __shared__ uint4 wf[WARP ? kMlpFragRows : 1][32];
     __shared__ uint4 stage[WARP ? 4 : 1][64];
