@@ -227,8 +227,8 @@ def c2_a_priori(fine, warmup, every, snapshots, seed, model_path):
     return out
 
 
-def c5(n, steps, k, models):
-    """models: {name: path of an lb_gb300.les.MlpModel}."""
+def c5(n, steps, ks, models):
+    """models: {name: path of an lb_gb300.les.MlpModel}; ks: the refresh intervals run beside every step."""
     from lb_gb300 import les
     from lb_gb300.solver import OmegaMLP
     nf = 4 * n
@@ -273,7 +273,7 @@ def c5(n, steps, k, models):
     # a posteriori: coarse FP16 LES from the filtered initial field
     runs = [("smagorinsky", None, 1)]
     for name in nets:
-        runs += [(f"mlp_{name}", name, 1), (f"mlp_{name}_every_{k}", name, k)]
+        runs += [(f"mlp_{name}", name, 1)] + [(f"mlp_{name}_every_{k}", name, k) for k in ks]
     post, thr = {}, {}
     for label, name, interval in runs:
         g = Solver((n, n, n), turbulence=OmegaMLP if name else OmegaLES, storage="f16dev", nu=nu_c, cles=0.17,
@@ -357,10 +357,11 @@ def test_c5_learned_closure(built_lib):
     data = os.path.join(ROOT, "lb_gb300", "data")
     models = {"channel": os.path.join(data, "les_mlp_channel.npz"),
               "channel_decay": os.path.join(data, "les_mlp_channel_decay.npz")}
-    r = c5(64 if SMALL else 256, 50 if SMALL else 200, 8, models)
+    r = c5(64 if SMALL else 256, 50 if SMALL else 200, (8, 16), models)
     _record("c5", r)
     if SMALL:
         return
     post = r["a_posteriori_rel_l2_vs_filtered_fine"]
     assert post["mlp_channel_decay"] < post["smagorinsky"]
     assert post["mlp_channel_decay_every_8"] < post["smagorinsky"]
+    assert post["mlp_channel_decay_every_16"] < post["smagorinsky"]
