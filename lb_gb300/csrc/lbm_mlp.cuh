@@ -8,7 +8,8 @@
 //   4 S_d:S_d / S:S   5 rho   6 |S| = sqrt(2 S:S)
 // normalised as (x - mean) / std.
 //
-// Step-kernel evaluation (FP16 operands, FP32 accumulation, all in registers of one warp): the 64
+// Step-kernel evaluation (FP16 operands, all in registers of one warp; layer 1, eight products per sum,
+// accumulates in FP16, layers 2 and 3 in FP32): the 64
 // cells of a warp (two per lane) are staged as 64 rows of 8 halves (7 inputs and a 1 that carries the
 // first bias) and loaded as A fragments with ldmatrix; layer 1 is mma.m16n8k8, layers 2 and 3
 // mma.m16n8k16.  The accumulator fragment of one layer (rows g, g+8, columns 2c, 2c+1 of each n-tile)
@@ -100,6 +101,22 @@ LBM_D uint32_t mlp_act(float lo, float hi) {
     uint32_t t;
     asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(h2_bits(z)));
     return h2_bits(__hfma2(z, bits_h2(t), z));
+}
+
+// z (1 + tanh z) on a packed pair already in FP16
+LBM_D uint32_t mlp_act_h(uint32_t zb) {
+    uint32_t t;
+    asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(zb));
+    return h2_bits(__hfma2(bits_h2(zb), bits_h2(t), bits_h2(zb)));
+}
+
+// layer 1 (K = 8, the bias in the eighth column): FP16 accumulators from zero; the sums go to the
+// activation in FP16 either way, so no FP32-to-FP16 pack
+LBM_D void mma_k8_h(uint32_t (&d)[2], uint32_t a0, uint32_t a1, uint32_t b0) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f16.f16.f16.f16 {%0,%1}, {%2,%3}, {%4}, {%5,%5};"
+        : "=r"(d[0]), "=r"(d[1])
+        : "r"(a0), "r"(a1), "r"(b0), "r"(0u));
 }
 
 LBM_D void mma_k8(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t b0) {
@@ -225,10 +242,10 @@ LBM_D float2 mlp_warp(uint4 rowA, uint4 rowB, uint4* stage, const uint4 (*wf)[32
         uint32_t h[kMlpNT][2];
 #pragma unroll
         for (int j = 0; j < kMlpNT; j++) {
-            float d[4];
-            mma_k8_z(d, a[2 * t], a[2 * t + 1], w1j[j], 0.0f);
-            h[j][0] = mlp_act(d[0], d[1]);
-            h[j][1] = mlp_act(d[2], d[3]);
+            uint32_t d[2];
+            mma_k8_h(d, a[2 * t], a[2 * t + 1], w1j[j]);
+            h[j][0] = mlp_act_h(d[0]);
+            h[j][1] = mlp_act_h(d[1]);
         }
         uint32_t h2[kMlpNT][2];
 #pragma unroll
