@@ -1021,7 +1021,7 @@ lbm_status lbm_step_launches(const lbm_ctx* c, int32_t* per_step) {
     if (!c->initialized) return fail(nullptr, LBM_ERR_STATE, "lbm_step_launches before initialisation");
     if (c->rows_ok && c->cfg.collision == LBM_COLLISION_CUMULANT2015 && c->cfg.storage == LBM_STORAGE_F16DEV)
         *per_step = (c->n_bulk_rows > 0 ? 1 : 0) + (c->n_other_rows > 0 ? 1 : 0);
-    else if (c->split_ok && (c->cfg.closure == LBM_CLOSURE_MLP || c->cfg.collision == LBM_COLLISION_CUMULANT_COMBINED))
+    else if (c->split_ok && c->cfg.collision == LBM_COLLISION_CUMULANT_COMBINED)
         *per_step = (c->n_plain_rows > 0 ? 1 : 0) + (c->n_rest_all > 0 ? 1 : 0);
     else if (c->split_ok)
         *per_step = (c->n_plain_rows > 0 ? 1 : 0) + (c->n_rest_rows > 0 ? 1 : 0) + (c->n_wall_rows > 0 ? 1 : 0);

@@ -47,9 +47,11 @@ static cudaError_t step_parity(const Params& p, const RowLists* rl, cudaStream_t
         const int half = (p.nx + 1) / 2;
         const dim3 b = cell_block(half);
         const unsigned xb = (unsigned)((half + (int)b.x - 1) / (int)b.x);
-        // the packed wall kernel serves the Smagorinsky and constant-rate closures of the collisions
-        // whose packed path is their own (not the combined one, which packs reference-flag-1 cells only)
-        constexpr bool WALL = CLOS != 2 && COLL != 3;
+        // the packed wall kernel serves the collisions whose packed path is their own (not the combined
+        // one, which packs reference-flag-1 cells only); with the learned closure (CLOS 2) it runs the
+        // Smagorinsky closure, the rate the learned closure gives every cell off the bulk pairs
+        constexpr bool WALL = COLL != 3;
+        constexpr int WCLOS = CLOS == 2 ? 1 : CLOS;
         const int32_t* other = WALL ? rl->other : rl->other_all;
         const int n_other = WALL ? rl->n_other : rl->n_other_all;
         const int n_wall = WALL ? rl->n_wall : 0;
@@ -75,8 +77,8 @@ static cudaError_t step_parity(const Params& p, const RowLists* rl, cudaStream_t
         }
         if constexpr (WALL) {
             if (n_wall > 0) {
-                if (odd) k_step2_wall<S, COLL, CLOS, true><<<rows_grid(xb, n_wall), b, 0, so>>>(p, rl->wall, rl->wall_solid, n_wall);
-                else     k_step2_wall<S, COLL, CLOS, false><<<rows_grid(xb, n_wall), b, 0, so>>>(p, rl->wall, rl->wall_solid, n_wall);
+                if (odd) k_step2_wall<S, COLL, WCLOS, true><<<rows_grid(xb, n_wall), b, 0, so>>>(p, rl->wall, rl->wall_solid, n_wall);
+                else     k_step2_wall<S, COLL, WCLOS, false><<<rows_grid(xb, n_wall), b, 0, so>>>(p, rl->wall, rl->wall_solid, n_wall);
                 cudaError_t e = cudaGetLastError();
                 if (e != cudaSuccess) return e;
             }

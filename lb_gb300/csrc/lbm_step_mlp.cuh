@@ -10,7 +10,8 @@
 //      lanes without a pair; with LBM_OPT_MLP_TCGEN05 the plain rows' CTA of 256 cells goes through
 //      tcgen05.mma with TMEM accumulators instead (tc_mlp, lbm_mlp_tc.cuh);
 //   4. tau = tau_0 + 3 nu_t for cells whose inputs lie in the training range, tau_S otherwise.
-// Cells that are not packed bulk pairs take the per-cell path with the Smagorinsky closure.
+// Cells that are not packed bulk pairs take the per-cell path with the Smagorinsky closure; the rows beside
+// a flat wall (every cell such a cell) run the packed wall kernel with the Smagorinsky closure instead.
 // MODE 0: the network runs in this step.  MODE 1: it runs and its nu_t (or -1 for the fallback) is kept
 // per cell in FP16 (Params::nut).  MODE 2: it does not run; each pair relaxes with the kept nu_t (the
 // Smagorinsky rate where the kept value is negative or not a number), fetched before the populations.

@@ -113,27 +113,28 @@ def test_eval_tcgen05_matches_warp_path_and_oracle(built_lib):
 @pytest.mark.parametrize("storage", ["f32", "f16dev"])
 def test_fused_mlp_out_of_range_is_smagorinsky(built_lib, storage, tc):
     """A model whose training range excludes every input relaxes every cell with the Smagorinsky rate:
-    the populations equal those of the Smagorinsky kernel bit for bit."""
+    the populations equal those of the Smagorinsky kernel bit for bit, with the rows beside the walls on
+    the packed wall kernel (default) and on the per-cell path (LBM_OPT_NO_WALL_ROWS) in both runs."""
     shape = (64, 18, 12)
     c = cases.channel(*shape, re_tau=3.0, u_max=0.05, nu=0.01)
     m, _ = _model_and_samples()
     m.in_lo[:] = 1e30
     m.in_hi[:] = 2e30
-    out = []
-    for clos in (OmegaLES, OmegaMLP):
-        # the learned closure takes wall rows through the per-cell path: so does the Smagorinsky run here
-        opts = capi.LBM_OPT_NO_WALL_ROWS | (capi.LBM_OPT_MLP_TCGEN05 if tc else 0)
-        s = Solver(shape, turbulence=clos, storage=storage, nu=c["nu"], cles=0.17, periodic=c["periodic"],
-                   options=opts, force=c["force"])
-        s.set_flags(c["flags"])
-        s.set_bc()
-        s.init_fields(c["rho"], c["u"])
-        if clos is OmegaMLP:
-            s.load_mlp(m)
-        s.step(7)
-        out.append(s.populations())
-        s.close()
-    assert np.array_equal(out[0], out[1])
+    for wall_opt in (0, capi.LBM_OPT_NO_WALL_ROWS):
+        out = []
+        for clos in (OmegaLES, OmegaMLP):
+            opts = wall_opt | (capi.LBM_OPT_MLP_TCGEN05 if tc else 0)
+            s = Solver(shape, turbulence=clos, storage=storage, nu=c["nu"], cles=0.17, periodic=c["periodic"],
+                       options=opts, force=c["force"])
+            s.set_flags(c["flags"])
+            s.set_bc()
+            s.init_fields(c["rho"], c["u"])
+            if clos is OmegaMLP:
+                s.load_mlp(m)
+            s.step(7)
+            out.append(s.populations())
+            s.close()
+        assert np.array_equal(out[0], out[1]), wall_opt
 
 
 @pytest.mark.parametrize("storage", ["f32", "f16dev"])
@@ -145,20 +146,20 @@ def test_interval_out_of_range_is_smagorinsky(built_lib, storage):
     m, _ = _model_and_samples()
     m.in_lo[:] = 1e30
     m.in_hi[:] = 2e30
-    out = []
-    for clos in (OmegaLES, OmegaMLP):
-        # the learned closure takes wall rows through the per-cell path: so does the Smagorinsky run here
-        s = Solver(shape, turbulence=clos, storage=storage, nu=c["nu"], cles=0.17, periodic=c["periodic"],
-                   options=capi.LBM_OPT_NO_WALL_ROWS, force=c["force"], mlp_interval=3)
-        s.set_flags(c["flags"])
-        s.set_bc()
-        s.init_fields(c["rho"], c["u"])
-        if clos is OmegaMLP:
-            s.load_mlp(m)
-        s.step(8)
-        out.append(s.populations())
-        s.close()
-    assert np.array_equal(out[0], out[1])
+    for wall_opt in (0, capi.LBM_OPT_NO_WALL_ROWS):
+        out = []
+        for clos in (OmegaLES, OmegaMLP):
+            s = Solver(shape, turbulence=clos, storage=storage, nu=c["nu"], cles=0.17, periodic=c["periodic"],
+                       options=wall_opt, force=c["force"], mlp_interval=3)
+            s.set_flags(c["flags"])
+            s.set_bc()
+            s.init_fields(c["rho"], c["u"])
+            if clos is OmegaMLP:
+                s.load_mlp(m)
+            s.step(8)
+            out.append(s.populations())
+            s.close()
+        assert np.array_equal(out[0], out[1]), wall_opt
 
 
 def test_interval_tracks_every_step_evaluation(built_lib):
@@ -371,7 +372,7 @@ def test_fused_learned_step_matches_oracle_step(built_lib, oracle_lib, storage, 
             rel = np.linalg.norm(ug[:, fl] - uo[:, fl]) / np.linalg.norm(uo[:, fl])
             assert rel < 2e-3, (interval, rel)
     nu_o, ok_o, nu_g = nu_chk
-    kept = np.isfinite(nu_g)  # packed bulk cells (the wall rows take the per-cell Smagorinsky path)
+    kept = np.isfinite(nu_g)  # packed bulk cells (the rows beside the walls relax with the Smagorinsky rate)
     assert kept.mean() > 0.8
     in_g = nu_g[kept] >= 0
     assert (in_g == ok_o[kept]).mean() >= 0.99
