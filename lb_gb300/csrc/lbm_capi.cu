@@ -1050,13 +1050,17 @@ lbm_status lbm_probe(lbm_ctx* c, int32_t x, int32_t y, int32_t z, double out[4])
     return LBM_OK;
 }
 
-// a bounded device wait that gave up leaves a code in the error word
+// a bounded device wait that gave up, or a plain-row pair whose class bytes are not of the packed kind,
+// leaves a code in the error word
 static lbm_status check_device_error(lbm_ctx* c) {
     int h = 0;
     CU(c, cudaMemcpyAsync(&h, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->st));
     CU(c, cudaStreamSynchronize(c->st));
     if (h != 0) {
         CU(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
+        if (h == DEV_ERR_ROW_LIST)
+            return fail(c, LBM_ERR_STATE, "a plain-row pair is not a pair of bulk cells: the row lists do not "
+                        "match the cell classes (code %d)", h);
         return fail(c, LBM_ERR_TIMEOUT, "%s (code %d)",
                     h == DEV_ERR_MMA_TIMEOUT ? "a step kernel gave up waiting for its tensor-core products"
                                              : "a row-staged step gave up waiting for its bulk copies",

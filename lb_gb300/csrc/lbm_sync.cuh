@@ -8,8 +8,9 @@
 
 namespace lbm {
 
-// codes left in Params::err by a CTA that gave up waiting
-enum : int { DEV_ERR_TMA_TIMEOUT = 1, DEV_ERR_MMA_TIMEOUT = 2 };
+// codes left in Params::err by a CTA that gave up waiting, or by a plain-row thread whose pair is not of
+// the packed kind (the row lists no longer match the classes)
+enum : int { DEV_ERR_TMA_TIMEOUT = 1, DEV_ERR_MMA_TIMEOUT = 2, DEV_ERR_ROW_LIST = 3 };
 
 constexpr int kWaitLimit = 1 << 22;  // try_wait attempts before a CTA gives up
 
