@@ -466,8 +466,10 @@ LBM_D void step_pair_plain(const Params& p, int e0, int x0) {
     // cell), checked against the packed kind after the stores.  Measured at 512x256x256: the FP16
     // Smagorinsky step 49.6 GLUPS without the load, 51.3 with the check after the stores, 50.5 after
     // the collision, 49.3 before it; with the early load the long-scoreboard stalls per issue fall from
-    // 4.7 to 3.4 (even steps, ncu) and the even kernel no longer spills
-    constexpr bool CHECK = S::kind == 2 && CLOS != 2;
+    // 4.7 to 3.4 (even steps, ncu) and the even kernel no longer spills.  SRT 38.1 -> 40.1, combined
+    // 46.6 -> 48.3; cumulant-2017 36.3 -> 35.9, so it keeps no check (nor does the kept-rate step, whose
+    // kept nu_t is such an early load already)
+    constexpr bool CHECK = S::kind == 2 && CLOS != 2 && COLL != 2;
     uint32_t cls2 = 0;
     if constexpr (CHECK) cls2 = __ldg((const uint16_t*)(p.cls + e0));
     F2 f[27];
