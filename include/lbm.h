@@ -214,6 +214,9 @@ lbm_status lbm_init_fields(lbm_ctx* ctx, const double* rho, const double* u);
 
 /* ---- time stepping (SolverTurbulentLES::runSimulation body, :186-226) ---------- */
 lbm_status lbm_step(lbm_ctx* ctx, int32_t nsteps);
+/* waits for the context's stream; LBM_ERR_TIMEOUT when a bounded device wait gave up, LBM_ERR_STATE when
+ * an FP16 plain-row step met a pair whose class bytes are not of the packed kind (the row lists of the
+ * split step no longer match the cell classes; no sequence of calls of this header produces that) */
 lbm_status lbm_synchronize(lbm_ctx* ctx);
 /* nsteps steps bracketed by CUDA events on the context's stream; *ms = elapsed device time */
 lbm_status lbm_step_timed(lbm_ctx* ctx, int32_t nsteps, double* ms);
