@@ -553,8 +553,8 @@ __global__ void __launch_bounds__(128, step2_min_blocks(COLL)) k_step2(Params p)
 // ---- the step split by rows ------------------------------------------------------------------------
 // Set-up lists the plain rows (every cell a bulk fluid cell of the packed path, the row off the periodic
 // y/z seams, nx even) and the remaining rows.  k_step2_plain runs only the packed pair path over the
-// plain rows: no class byte, no per-cell fallback, so the register allocation is that of the packed
-// path alone.  k_step2_list runs the general pair step over the remaining rows.  Every population slot
+// plain rows: no class dispatch (FP16 loads the class bytes only to check them after the stores), no
+// per-cell fallback, so the register allocation is that of the packed path alone.  k_step2_list runs the general pair step over the remaining rows.  Every population slot
 // is read and written by one thread only within a step (the AA argument), so running the two sets of
 // threads as two launches gives the same result as one launch over the lattice.
 // Grid: x = block of 128 x-pairs in the row, y and z = row in the list (rows_grid), so the blocks of a
